@@ -1,0 +1,206 @@
+/*
+ * fipi.h — C ABI of the GB300-native FIPI step (sm_103a).
+ *
+ * This library replaces the per-step hot path of FIPI (Fast Interface
+ * Particle Interaction): a pseudo-spectral Cahn–Hilliard phase field coupled
+ * to a Stokes velocity by Leray projection, and overdamped spheres moved by
+ * interface-attachment and pair-contact forces whose contact forces are
+ * spread back onto the grid.
+ *
+ * The reference is host C++ (class `field`, `cluster`, `element`, `list`)
+ * with no FFI; every entry point below names the reference call it replaces
+ * (path:line inside the reference project).  All functions return a
+ * `fipi_status` (0 = FIPI_OK); the reference printed a message and called
+ * exit(0) instead.  The text of the last error of the calling thread is
+ * returned by fipi_last_error_string().
+ *
+ * Conventions
+ *  - Real grid fields are Nz*Ny*Nx doubles, x fastest: linear index
+ *    it = i + j*Nx + k*Nx*Ny, grid node i sits at x = i*dx
+ *    (field.cpp:88-92 of the reference).
+ *  - Vector grid fields are 3 such arrays back to back (component-major),
+ *    like field::v[d] (field.hpp:25).
+ *  - Particle vectors are n_p x 3 doubles, particle-major (x,y,z per
+ *    particle), like element::p (element.hpp:32).
+ *  - A context owns all device buffers and one CUDA stream.  It is not
+ *    thread-safe: use one host thread per context.
+ *  - Host pointers are copied in/out synchronously with respect to the
+ *    calling thread.
+ */
+#ifndef FIPI_H
+#define FIPI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FIPI_ABI_VERSION 1
+
+typedef enum fipi_status {
+    FIPI_OK = 0,
+    FIPI_ERR_BAD_PARAMS = 1,    /* parameters rejected by fipi_create         */
+    FIPI_ERR_BAD_ARG = 2,       /* NULL pointer, bad size or stage name       */
+    FIPI_ERR_CUDA = 3,          /* a CUDA runtime call failed                 */
+    FIPI_ERR_OUT_OF_RANGE = 4,  /* particle outside the sorting range:
+                                   cluster.cpp:238-257 printed and exit(0)    */
+    FIPI_ERR_NONFINITE = 5,     /* NaN/Inf detected in the state              */
+    FIPI_ERR_NO_DEVICE = 6,     /* no CUDA device visible                     */
+    FIPI_ERR_STATE = 7,         /* call out of order (e.g. step before state) */
+    FIPI_ERR_UNSUPPORTED = 8    /* configuration outside what is built        */
+} fipi_status;
+
+typedef enum fipi_precision {
+    FIPI_FP64 = 0,   /* plain FP64 everywhere (parity form)                   */
+    FIPI_MIXED = 1   /* FP32 grid/FFT/particle-force arithmetic; FP64 k=0
+                        mode, compensated reductions, particle positions      */
+} fipi_precision;
+
+/*
+ * Run-time replacement of the reference's compile-time constants
+ * (head.hpp:27-74, parameter.hpp:18-20).  fipi_params_reference() fills the
+ * values of the reference's head.hpp.
+ */
+typedef struct fipi_params {
+    int nx, ny, nz;            /* grid points, powers of two in [8, 512]      head.hpp:29-31 */
+    double lx, ly, lz;         /* periodic box lengths                         head.hpp:33-35 */
+    double dt;                 /* time step                                    head.hpp:41    */
+    int t_end;                 /* run length; enters ramp(t, 0.2 t_end) only   head.hpp:42    */
+    double pi;                 /* the reference uses pi = 3.1415926            head.hpp:27    */
+    double sigma;              /* surface tension                              head.hpp:45    */
+    double epsilon;            /* interface width                              head.hpp:46    */
+    double lambda;             /* gradient energy coefficient                  head.hpp:47    */
+    double mobility;           /* Cahn-Hilliard mobility M                     head.hpp:58    */
+    double mu;                 /* viscosity                                    head.hpp:54    */
+    double rho1, rho2;         /* fluid densities (buoyancy)                   head.hpp:52-53 */
+    double gravity;            /* z component of g                             head.hpp:51    */
+    double A;                  /* attachment force constant                    head.hpp:57    */
+    double k_n;                /* contact stiffness                            parameter.hpp:18 */
+    double margin;             /* cell-grid margin                             parameter.hpp:20 */
+    double r_p;                /* default particle radius                      head.hpp:59    */
+    double r_eq;               /* contact range                                head.hpp:64    */
+    double r_c;                /* cell-list cell size                          head.hpp:65    */
+    int n_p;                   /* number of particles (0 allowed)              head.hpp:63    */
+    int switch_particle;       /* head.hpp:72 */
+    int switch_ch;             /* head.hpp:73 */
+    int switch_ns;             /* head.hpp:74 */
+} fipi_params;
+
+typedef struct fipi_ctx fipi_ctx;
+
+/* ---------------------------------------------------------------- basics */
+int fipi_abi_version(void);
+const char* fipi_last_error_string(void);
+/* Values of the reference's head.hpp / parameter.hpp (64^3, Lx = 2 pi, ...). */
+fipi_status fipi_params_reference(fipi_params* out);
+/* Cell-grid geometry of cluster::cluster() (cluster.cpp:26-32):
+ * n_cell = floor(L/r_c + 2 margin/r_c), d_cell = fmod(L + 2 margin, r_c)/n_cell + r_c. */
+fipi_status fipi_cell_geometry(const fipi_params* p, int n_cell[3], double d_cell[3]);
+
+/* ------------------------------------------------------------- lifecycle */
+/* Allocates every device buffer of the step on `device`.  Replaces the field
+ * constructors of main.cpp:126-155 and cluster::cluster (cluster.cpp:21-40). */
+fipi_status fipi_create(const fipi_params* p, fipi_precision prec, int device, fipi_ctx** out);
+fipi_status fipi_destroy(fipi_ctx* ctx);
+/* Bytes of device memory held by the context. */
+fipi_status fipi_device_bytes(const fipi_ctx* ctx, size_t* out);
+
+/* ----------------------------------------------------------------- state */
+/* Initial phase field (field.cpp:85-99 drew it from rand()); resets t = 0
+ * and the SBDF2 history, like entering main.cpp:172 with t = 0. */
+fipi_status fipi_set_phase(fipi_ctx* ctx, const double* c);
+/* Velocity field u (3 x V).  The reference starts from u = 0 (main.cpp:146). */
+fipi_status fipi_set_velocity(fipi_ctx* ctx, const double* u);
+/* Particle state (cluster::distribute, cluster.cpp:53-92, drew p from rand()).
+ * p: n_p x 3 positions in [0, L).  r: n_p radii or NULL (= r_p, element.cpp:119).
+ * cos_theta: n_p wettabilities or NULL (= 0, the reference's 90 degree form).
+ * f_pp: n_p x 3 contact forces of the previous step or NULL (= 0); they are
+ * spread at the next step (cluster.cpp:452). */
+fipi_status fipi_set_particles(fipi_ctx* ctx, const double* p, const double* r,
+                               const double* cos_theta, const double* f_pp);
+fipi_status fipi_get_phase(fipi_ctx* ctx, double* c);
+fipi_status fipi_get_velocity(fipi_ctx* ctx, double* u);
+/* Any output pointer may be NULL.  f_pi is the attachment force of the last
+ * stage (element.cpp:169-191). */
+fipi_status fipi_get_particles(fipi_ctx* ctx, double* p, double* f_pp, double* f_pi);
+fipi_status fipi_get_time(const fipi_ctx* ctx, int* t);
+
+/* ------------------------------------------------------------------ step */
+/* Advances `nsteps` iterations of the loop body of main.cpp:172-316
+ * (Cahn-Hilliard, Stokes, two Heun particle stages). */
+fipi_status fipi_step(fipi_ctx* ctx, int nsteps);
+/* Enqueues the steps without waiting for them; errors raised on the device
+ * (particle out of range, non-finite state) are reported by the next
+ * fipi_sync, fipi_step or state read. */
+fipi_status fipi_step_async(fipi_ctx* ctx, int nsteps);
+fipi_status fipi_sync(fipi_ctx* ctx);
+/* The CUDA stream the context runs on (as a void*: cudaStream_t). */
+fipi_status fipi_stream(const fipi_ctx* ctx, void** stream);
+
+/* ------------------------------------------------------------ diagnostics */
+/* integral of phi: sum c dx dy dz.  FP64 form: compensated sum of the real
+ * field; mixed form: the FP64 k = 0 mode.  Not in the reference. */
+fipi_status fipi_mass(fipi_ctx* ctx, double* out);
+/* Total free energy sum lambda (0.5|grad c|^2 + 0.25/eps^2 (c^2-1)^2) dx^3
+ * (main.cpp:329 + field.cpp:507-516), compensated sum. */
+fipi_status fipi_free_energy(fipi_ctx* ctx, double* out);
+/* Packing energy tau of the last contact-force evaluation (cluster.cpp:283-353). */
+fipi_status fipi_packing_tau(fipi_ctx* ctx, double* out);
+
+/* ------------------------------------------ fine-grained parity entry points
+ * One call per reference function, on host arrays; they use the context's
+ * grid and particle count but do not touch its step state. */
+
+/* 3-D real-to-half-spectrum DFT, sign -1, unnormalised (field::fft,
+ * field.cpp:438-443, restricted to a real input).  Output layout:
+ * out[((kz*(nx/2+1)) + kx)*ny + ky] as (re, im) pairs, i.e. the half
+ * spectrum with kx in [0, nx/2], ky fastest. */
+fipi_status fipi_fft_r2c(fipi_ctx* ctx, const double* in, double* out);
+/* Inverse of the above, normalised by 1/V like field::ifft + normalize
+ * (field.cpp:446-455, primitive.cpp:137-145): real part of the inverse DFT
+ * of the Hermitian completion of the half spectrum. */
+fipi_status fipi_fft_c2r(fipi_ctx* ctx, const double* in, double* out);
+/* grad c = ifft(i k c_hat) with the Nyquist index of each component zeroed
+ * (field::grad, field.cpp:288-328, then ifft).  c: V reals, out: 3 x V. */
+fipi_status fipi_grad(fipi_ctx* ctx, const double* c, double* grad_out);
+/* cluster::sorting (cluster.cpp:210-263): cell key of every particle,
+ * particle ids sorted by (cell, id), cell offsets (n_cells + 1 entries).
+ * Any output may be NULL.  Returns FIPI_ERR_OUT_OF_RANGE like the reference's
+ * out-of-range exit. */
+fipi_status fipi_cells_build(fipi_ctx* ctx, const double* p, int* keys, int* sorted_ids,
+                             int* cell_offsets);
+/* cluster::compute_f_pp(t) (cluster.cpp:268-369): contact forces, n_p x 3.
+ * f_pi (n_p x 3, may be NULL = all zero) only feeds the packing energy tau. */
+fipi_status fipi_f_pp(fipi_ctx* ctx, const double* p, int t, const double* f_pi,
+                      double* f_pp, double* tau);
+/* The set of interacting pairs found by compute_f_pp (|d| < r_eq), as
+ * (i, j) with i < j, sorted; *n_pairs receives the count.  pairs may be
+ * NULL to query the count; max_pairs bounds what is written. */
+fipi_status fipi_pairs(fipi_ctx* ctx, const double* p, int* pairs, int max_pairs, int* n_pairs);
+/* element::get_local_c / get_local_dcdx via field::interpolate
+ * (element.cpp:149-165, field.cpp:223-248): trilinear values of `fields`
+ * (nfields x V reals) at the particles -> out (n_p x nfields). */
+fipi_status fipi_interpolate(fipi_ctx* ctx, const double* fields, int nfields, const double* p,
+                             double* out);
+/* element::get_f_pi (element.cpp:169-191) for every particle, with the
+ * contact-angle extension f_mag = -A pi (d - r cos_theta) sigma
+ * (cos_theta = 0 is the reference).  c_loc: n_p, dcdx: n_p x 3. */
+fipi_status fipi_f_pi(fipi_ctx* ctx, const double* c_loc, const double* dcdx, const double* r,
+                      const double* cos_theta, double* f_pi);
+/* element::advect (element.cpp:250-267) + element::enforce_bc
+ * (element.cpp:271-280).  stage 1: u_old = F/(6 pi mu r), p_old = p,
+ * p += dt u_old; stage 2: u = F/(6 pi mu r), p = p_old + dt/2 (u_old + u).
+ * p, p_old, u_old are updated in place (n_p x 3). */
+fipi_status fipi_advect(fipi_ctx* ctx, int stage, const double* f_pi, const double* f_pp,
+                        const double* r, double* p, double* p_old, double* u_old);
+/* cluster::compute_f_r (cluster.cpp:438-504): trilinear spreading of
+ * f_pp / (dx dy dz) onto the grid, out: 3 x V.  Deterministic: per grid
+ * node the contributions are summed in ascending particle id. */
+fipi_status fipi_spread(fipi_ctx* ctx, const double* p, const double* f_pp, double* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FIPI_H */

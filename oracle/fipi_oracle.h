@@ -1,0 +1,74 @@
+/*
+ * TEST INFRASTRUCTURE ONLY (oracle).  Only tests/, __graft_entry__.smoke()
+ * and bench.py's CPU-baseline leg may load this; the product never does.
+ *
+ * A plain-C, FP64 restatement of the reference FIPI step (main.cpp:172-316)
+ * and of the field / cluster / element calls it makes, using full complex
+ * C2C fields exactly as the reference does (field.cpp:41-46), so that it
+ * reproduces the reference's arithmetic, its Nyquist handling and its
+ * imaginary-part bookkeeping.  Every function cites the reference lines it
+ * follows.  Pinned against the reference itself (compiled in place by
+ * oracle/ref/) and against committed golden vectors (tests/golden/).
+ */
+#ifndef FIPI_ORACLE_H
+#define FIPI_ORACLE_H
+
+#include "../include/fipi.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct oracle oracle;
+
+/* NULL when the parameters are outside what the oracle restates
+ * (non power-of-two grid, fewer than 3 cells per axis with particles on). */
+oracle* oracle_create(const fipi_params* p);
+int oracle_params_ok(const fipi_params* p);
+/* cluster.cpp:120-126 */
+void oracle_cell_geometry(const fipi_params* p, int nc[3], double dc[3]);
+/* deterministic stand-in for the rand() separation of cluster.cpp:328-336 */
+void oracle_coincident_d(int a, int b, double r_p, double d[3]);
+void oracle_destroy(oracle* o);
+void oracle_set_threads(int n);
+
+/* state: c (V reals), u (3V reals), particles (n x 3), radii, cos_theta */
+int oracle_set_phase(oracle* o, const double* c);
+int oracle_set_velocity(oracle* o, const double* u);
+int oracle_set_particles(oracle* o, const double* p, const double* r, const double* cos_theta,
+                         const double* f_pp);
+void oracle_get_phase(const oracle* o, double* c);
+void oracle_get_phase_imag(const oracle* o, double* c_im);
+void oracle_get_velocity(const oracle* o, double* u);
+void oracle_get_grad(const oracle* o, double* g);
+void oracle_get_particles(const oracle* o, double* p, double* f_pp, double* f_pi);
+double oracle_tau(const oracle* o);
+int oracle_time(const oracle* o);
+
+/* One iteration of the main.cpp:172-316 loop body; returns FIPI_OK or
+ * FIPI_ERR_OUT_OF_RANGE (the reference's cluster.cpp:238-257 exit). */
+int oracle_step(oracle* o);
+
+/* Fine-grained restatements (stateless w.r.t. the step). */
+void oracle_fft3(const fipi_params* P, double* data, int sign); /* C2C, unnormalised */
+int oracle_sorting(const fipi_params* P, int n, const double* p, int* keys, int* sorted,
+                   int* offsets, int* it_mark);
+int oracle_f_pp(const fipi_params* P, int n, const double* p, int t, const double* f_pi,
+                double* f_pp, double* tau, int* pairs, int max_pairs, int* n_pairs);
+void oracle_interpolate(const fipi_params* P, const double* field, int n, const double* p,
+                        double* out);
+void oracle_f_pi(const fipi_params* P, int n, const double* c_loc, const double* dcdx,
+                 const double* r, const double* cos_theta, double* f_pi);
+void oracle_advect(const fipi_params* P, int n, int stage, const double* f_pi,
+                   const double* f_pp, const double* r, double* p, double* p_old,
+                   double* u_old);
+void oracle_enforce_bc(const fipi_params* P, int n, double* p);
+void oracle_spread(const fipi_params* P, int n, const double* p, const double* f_pp,
+                   double* out);
+double oracle_free_energy(const oracle* o);
+double oracle_mass(const oracle* o);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
