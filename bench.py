@@ -1,0 +1,419 @@
+#!/usr/bin/env python
+"""Benchmark of the FIPI step on GB300.
+
+Workload (default): 256^3 periodic grid with 20,000 spheres of radius 4 dx,
+phi0 = U(-0.05, 0.05), M = eps = sigma = mu = 1, dt = 1e-3 (seeded synthetic
+inputs of that shape).  A step is one iteration of the reference's loop body
+(Cahn-Hilliard, Stokes projection, two Heun particle stages).
+
+Printed JSON line (rank 0):
+  value        mixed-precision steps/s, inputs resident in HBM, CUDA events
+               on the library's stream, max over ranks (N replicas: sum)
+  e2e          the same metric through the C ABI with host buffers: every
+               step uploads the particle state and reads positions, forces
+               and the mass back
+  fp64         plain FP64 form steps/s and the mixed/FP64 ratio
+  error        mixed vs FP64 after `--err-steps` steps from the same state
+  roofline     dominant kernel: algorithmic bytes per launch / CUDA-event
+               duration against the measured HBM copy bandwidth
+  cpu_baseline the CPU oracle timed on this host on a bounded sample
+
+`--impl reference` times the reference's CPU path (the oracle) instead.
+Under torchrun every rank runs an independent replica (different seed).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+REPO = Path(__file__).resolve().parent
+sys.path.insert(0, str(REPO))
+
+METRIC = "steps/s 256³+20k particles, mixed vs FP64 at φ err≤1e-4; adjoint/forward ratio"
+
+
+def peaks():
+    try:
+        d = json.loads((REPO / "MEASURED_PEAKS.json").read_text())
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.device)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                out = ""
+            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in getattr(self, "lines", []):
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def seeded(w, seed):
+    import fipi_gb300 as F
+
+    P = w.params()
+    c = F.seed_phase(P, seed, w.phi_mean, w.phi_amp)
+    p, r, ct = F.seed_particles(P, seed + 1000, w.radius_range, w.theta_range_deg,
+                                allow_overlap=w.radius_range is not None)
+    return P, c, p, (r if w.radius_range else None), (ct if w.theta_range_deg else None)
+
+
+def timed_steps(sim, n, torch):
+    """Device time of n steps on the library's stream (CUDA events)."""
+    stream = torch.cuda.ExternalStream(sim.stream())
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    sim.sync()
+    e0.record(stream)
+    sim.step_async(n)
+    e1.record(stream)
+    sim.sync()
+    return e0.elapsed_time(e1) / 1e3
+
+
+def kernel_stats(sim):
+    import ctypes
+
+    lib = sim.lib
+    lib.fipi_kernel_stat_count.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
+    lib.fipi_kernel_stats.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_char_p, ctypes.c_int,
+                                      ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_double),
+                                      ctypes.POINTER(ctypes.c_double)]
+    n = ctypes.c_int()
+    lib.fipi_kernel_stat_count(sim.h, ctypes.byref(n))
+    out = []
+    for i in range(n.value):
+        name = ctypes.create_string_buffer(128)
+        la, ms, by = ctypes.c_longlong(), ctypes.c_double(), ctypes.c_double()
+        lib.fipi_kernel_stats(sim.h, i, name, 128, ctypes.byref(la), ctypes.byref(ms), ctypes.byref(by))
+        out.append({"name": name.value.decode(), "launches": la.value, "ms": ms.value, "bytes": by.value})
+    return out
+
+
+def launch_count(sim):
+    import ctypes
+
+    sim.lib.fipi_launch_count.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]
+    n = ctypes.c_longlong()
+    sim.lib.fipi_launch_count(sim.h, ctypes.byref(n))
+    return n.value
+
+
+def set_timing(sim, on):
+    import ctypes
+
+    sim.lib.fipi_set_kernel_timing.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    sim.lib.fipi_set_kernel_timing(sim.h, 1 if on else 0)
+
+
+def committed_traffic(kernel, workload):
+    """DRAM bytes per launch from the committed ncu summary, if it covers this kernel."""
+    try:
+        d = json.loads((REPO / "profiles" / "dram_traffic.json").read_text())
+        e = d.get(workload, {}).get(kernel)
+        return None if e is None else float(e)
+    except Exception:
+        return None
+
+
+def cpu_baseline(w, seed, steps=1):
+    """The CPU oracle (C restatement of the reference step) on the same workload."""
+    sys.path.insert(0, str(REPO / "oracle"))
+    import oracle as O
+
+    threads = os.cpu_count() or 1
+    P, c, p, r, ct = seeded(w, seed)
+    port = O.Port(P, threads=threads)
+    port.set_state(c, p, r, ct)
+    port.step(1)  # t = 0 (IMEX start) as warm-up
+    t0 = time.perf_counter()
+    port.step(steps)
+    dt = time.perf_counter() - t0
+    return {"value": steps / dt, "unit": "steps/s", "cores": threads, "kind": "port",
+            "sample": f"{steps} step(s) of the {w.name} workload after 1 warm-up step; C restatement "
+                      f"of the reference (full-complex C2C FFTs as the reference), {threads} OpenMP "
+                      f"threads in the transforms"}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    import fipi_gb300 as F
+
+    w = F.workload(args.workload)
+    warm = min(args.warmup, 1)
+    steps = max(1, min(args.steps, 2))
+    sys.path.insert(0, str(REPO / "oracle"))
+    import oracle as O
+
+    threads = os.cpu_count() or 1
+    P, c, p, r, ct = seeded(w, 1)
+    port = O.Port(P, threads=threads)
+    port.set_state(c, p, r, ct)
+    port.step(warm)
+    t0 = time.perf_counter()
+    port.step(steps)
+    dt = time.perf_counter() - t0
+    v = steps / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "steps/s", "n_gpus": 0,
+        "steps": steps, "warmup": warm, "ms_per_step": 1e3 * dt / steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": w.name, "grid": f"{w.nx}x{w.ny}x{w.nz}", "particles": w.n_p},
+        "cpu_baseline": {"value": v, "unit": "steps/s", "cores": threads, "kind": "port",
+                         "sample": f"{steps} timed step(s) after {warm} warm-up of the {w.name} workload "
+                                   f"(C restatement of the reference step; the reference's own build "
+                                   f"needs its sources, absent on this host)"},
+        "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_profile(args):
+    """Set-up, --warmup steps, then --profile steps of the --form form, nothing
+    else: the command ncu captures (launch counts are printed to stderr so the
+    capture's -s/-c can skip the set-up and warm-up)."""
+    import fipi_gb300 as F
+
+    w = F.workload(args.workload)
+    P, c, p, r, ct = seeded(w, 1)
+    sim = F.Simulation(P, args.form)
+    sim.set_phase(c)
+    sim.set_particles(p, r, ct)
+    sim.step(args.warmup)
+    n0 = launch_count(sim)
+    sim.step(args.profile)
+    n1 = launch_count(sim)
+    print(json.dumps({"profile": args.profile, "form": args.form, "workload": w.name,
+                      "launches_before": n0, "launches_per_step": (n1 - n0) / args.profile}),
+          file=sys.stderr, flush=True)
+    sim.close()
+    return 0
+
+
+def run_gpu(args):
+    import numpy as np
+    import torch
+
+    import fipi_gb300 as F
+
+    ws, rank, local = dist_env()
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(local)
+    w = F.workload(args.workload)
+    seed = 1 + rank
+    P, c, p, r, ct = seeded(w, seed)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+            torch.cuda.synchronize()
+
+    # ---- headline: mixed form, inputs resident
+    sim = F.Simulation(P, "mixed", device=local)
+    sim.set_phase(c)
+    sim.set_particles(p, r, ct)
+    sim.step(args.warmup)
+    barrier()
+    l0 = launch_count(sim)
+    with ClockSampler(local) as clk:
+        elapsed = timed_steps(sim, args.steps, torch)
+    launches = launch_count(sim) - l0
+    barrier()
+    if dist is not None:
+        t = torch.tensor([elapsed], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t.item())
+    value = ws * args.steps / elapsed
+
+    # ---- per-kernel CUDA-event timing (separate region; events add overhead)
+    set_timing(sim, True)
+    sim.step(args.kernel_steps)
+    ks = kernel_stats(sim)
+    set_timing(sim, False)
+
+    # ---- e2e through the C ABI with host buffers
+    pos, fpp, _ = sim.get_particles()
+    rr = r if r is not None else np.full(w.n_p, P.r_p)
+    cc = ct if ct is not None else np.zeros(w.n_p)
+    sim.sync()
+    e2e_steps = max(1, min(args.steps, args.e2e_steps))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        sim.set_particles(pos, rr, cc, fpp)
+        sim.step(1)
+        pos, fpp, fpi = sim.get_particles()
+        sim.mass()
+    e2e_dt = time.perf_counter() - t0
+    e2e_val = ws * e2e_steps / e2e_dt
+    h2d = w.n_p * 8 * (3 + 1 + 1 + 3)
+    d2h = w.n_p * 8 * 9 + 8
+    sim.close()
+
+    # ---- FP64 form and the mixed-vs-FP64 error from one state
+    res = {}
+    fp64_rate = None
+    for prec in ("fp64", "mixed"):
+        s = F.Simulation(P, prec, device=local)
+        s.set_phase(c)
+        s.set_particles(p, r, ct)
+        m0 = s.mass()
+        s.step(1)
+        el = timed_steps(s, args.err_steps - 1, torch)
+        if prec == "fp64":
+            fp64_rate = (args.err_steps - 1) / el
+        res[prec] = (s.get_phase(), s.get_velocity(), s.get_particles()[0], s.mass(), m0, s.free_energy())
+        s.close()
+    a, b = res["mixed"], res["fp64"]
+
+    def rl2(x, y):
+        return float(np.linalg.norm(x - y) / np.linalg.norm(y))
+
+    L = np.array([P.lx, P.ly, P.lz])
+    dpos = np.abs(a[2] - b[2]).reshape(-1, 3)
+    dpos = np.minimum(dpos, L - dpos)
+    err = {
+        "steps": args.err_steps,
+        "phi_rel_l2": rl2(a[0], b[0]),
+        "u_rel_l2": rl2(a[1], b[1]),
+        "pos_max_abs": float(dpos.max()),
+        "free_energy_rel": abs(a[5] - b[5]) / abs(b[5]),
+        "mass_drift_mixed": abs(a[3] - a[4]) / (np.abs(c).sum() * P.lx * P.ly * P.lz / w.V),
+        "mass_drift_fp64": abs(b[3] - b[4]) / (np.abs(c).sum() * P.lx * P.ly * P.lz / w.V),
+    }
+
+    # ---- roofline of the dominant kernel
+    hbm, src = peaks()
+    dom = max(ks, key=lambda k: k["ms"]) if ks else None
+    roof = None
+    if dom and dom["ms"] > 0:
+        per_launch_s = dom["ms"] / dom["launches"] / 1e3
+        ach = dom["bytes"] / per_launch_s / 1e9
+        roof = {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+                "traffic": committed_traffic(dom["name"], w.name), "kernel": dom["name"],
+                "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs)" if src == "measured" else src,
+                "alg_bytes_per_launch": dom["bytes"], "us_per_launch": per_launch_s * 1e6,
+                "share_of_step": dom["ms"] / sum(k["ms"] for k in ks)}
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(w, seed)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (k=0 mode, reductions, positions f64)",
+            "data": "synthetic (seeded phi0 = U(-0.05,0.05), random non-overlapping spheres)",
+            "config": {"workload": w.name, "grid": f"{w.nx}x{w.ny}x{w.nz}", "particles": w.n_p,
+                       "form": "mixed", "parallelism": f"replicas x{ws}",
+                       "l2": "working set > L2 (inputs larger than L2; no flush needed)"},
+            "particle_updates_per_s": value * w.n_p,
+            "fp64": {"steps_per_s": fp64_rate * ws, "mixed_over_fp64": value / (fp64_rate * ws)},
+            "error_mixed_vs_fp64": err,
+            "adjoint_over_forward": None,
+            "e2e": {"value": e2e_val, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches,
+            "roofline": roof,
+            "kernels": sorted([{"name": k["name"], "launches": k["launches"], "ms": round(k["ms"], 4),
+                                "gbs": (k["bytes"] * k["launches"] / (k["ms"] / 1e3) / 1e9) if k["ms"] > 0 else None}
+                               for k in ks], key=lambda k: -k["ms"]),
+            "clocks": clk.summary(),
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="cfg2_256")
+    ap.add_argument("--err-steps", type=int, default=1000)
+    ap.add_argument("--e2e-steps", type=int, default=50)
+    ap.add_argument("--kernel-steps", type=int, default=20)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", type=int, default=0, help="only run N steps (for ncu)")
+    ap.add_argument("--form", default="mixed", choices=["mixed", "fp64"])
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        return run_reference(args)
+    if args.profile > 0:
+        return run_profile(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

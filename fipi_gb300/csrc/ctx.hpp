@@ -1,0 +1,202 @@
+// Internal context of the FIPI GB300 library (not part of the C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/fipi.h"
+#include "fft.cuh"
+
+namespace fipi {
+
+// Device buffers of one precision form.  T = float (mixed) or double.
+struct FieldBufs {
+    void* twx = nullptr;  // exp(-2 pi i q / nx), q < nx     (cplx<T>)
+    void* twy = nullptr;  // exp(-2 pi i q / ny)
+    void* twz = nullptr;  // exp(-2 pi i q / nz)
+    void* kx = nullptr;   // wave numbers (T): kx[0..M], ky[0..ny), kz[0..nz)
+    void* ky = nullptr;
+    void* kz = nullptr;
+    // real fields (T, V each)
+    void* c = nullptr;       // phase field c^n
+    void* g[3] = {};         // grad c^n
+    void* fsp[3] = {};       // spread particle force density (cluster::compute_f_r)
+    void* ureal = nullptr;   // 3V, velocity materialised on demand
+    // spectral fields (cplx<T>, SH each)
+    void* chat = nullptr;
+    void* chat_old = nullptr;
+    void* fhat = nullptr;
+    void* fhat_old = nullptr;
+    void* Chat_old = nullptr;
+    void* uhat[3] = {};
+    void* S[4] = {};  // scratch
+};
+
+// Cell-list / sort scratch of the particle side.
+struct ParticleBufs {
+    int n = 0;
+    int ncell[3] = {0, 0, 0};
+    double dcell[3] = {0, 0, 0};
+    int ncells = 0;
+    // state, SoA, FP64
+    double* p = nullptr;      // 3 x n (x[n], y[n], z[n])
+    double* p_old = nullptr;  // 3 x n
+    double* u_old = nullptr;  // 3 x n
+    double* f_pp = nullptr;   // 3 x n
+    double* f_pi = nullptr;   // 3 x n
+    double* r = nullptr;      // n
+    double* cth = nullptr;    // n
+    // cell list
+    unsigned* keys = nullptr;      // n
+    unsigned* keys_alt = nullptr;  // n
+    unsigned* ids = nullptr;       // n (sorted particle ids)
+    unsigned* ids_alt = nullptr;   // n
+    int* cell_off = nullptr;       // ncells + 1
+    int* cell_cnt = nullptr;       // ncells
+    // spreading records (8 per particle)
+    unsigned* sp_keys = nullptr;      // 8n node index
+    unsigned* sp_keys_alt = nullptr;  // 8n
+    unsigned* sp_vals = nullptr;      // 8n record id = particle*8 + corner
+    unsigned* sp_vals_alt = nullptr;  // 8n
+    unsigned* sp_prev = nullptr;      // 8n nodes written by the previous spread
+    int sp_prev_valid = 0;
+    // radix sort scratch
+    unsigned* hist = nullptr;  // 256 * max_blocks
+    int hist_cap = 0;
+    // diagnostics
+    double* tau_part = nullptr;  // n, per-particle packing-energy terms
+    int* it_mark = nullptr;      // 1
+    double* tau = nullptr;       // 1
+};
+
+}  // namespace fipi
+
+namespace fipi {
+// Per-kernel-class instrumentation: launch counts always, CUDA-event
+// durations on the context stream when enabled.
+struct KernelStat {
+    std::string name;
+    long long launches = 0;
+    double ms = 0.0;
+    double bytes = 0.0;  // algorithmic bytes of one launch
+};
+struct KTimer {
+    bool enabled = false;
+    long long launches = 0;
+    std::vector<KernelStat> stats;
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
+    std::vector<cudaEvent_t> pool;
+};
+}  // namespace fipi
+
+struct fipi_ctx {
+    fipi_params P{};
+    fipi_precision prec = FIPI_FP64;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    fipi::Geom g{};
+    fipi::FieldBufs fb;
+    fipi::ParticleBufs pb;
+    double* k0 = nullptr;        // mixed form FP64 k=0 mode: [c0, c0_old, C0_old, C0_cur]
+    double* partials = nullptr;  // per-block FP64 partial sums
+    int n_partials = 0;
+    int* status = nullptr;       // device error word
+    double* scratch_d = nullptr; // small FP64 device scratch (reductions)
+    int t = 0;
+    bool have_phase = false;
+    bool track_tau = true;     // packing energy during the step (cluster.cpp:350-353)
+    size_t device_bytes = 0;
+    std::string last_error;
+    fipi::KTimer kt;
+};
+
+namespace fipi {
+
+// fields.cu
+fipi_status fields_alloc(fipi_ctx* ctx);
+void fields_free(fipi_ctx* ctx);
+// Set c^0 (host doubles) and derive c_hat, f_hat, grad c (t = 0 state).
+fipi_status fields_set_phase(fipi_ctx* ctx, const double* c_host);
+fipi_status fields_set_velocity(fipi_ctx* ctx, const double* u_host);
+fipi_status fields_get_phase(fipi_ctx* ctx, double* c_host);
+fipi_status fields_get_velocity(fipi_ctx* ctx, double* u_host);
+// The three grid sub-steps of one iteration (enqueue only).
+void fields_step_ch(fipi_ctx* ctx, int t);        // conv, CH update, c, f
+void fields_step_stokes(fipi_ctx* ctx);           // mu, grad c, force, projection
+fipi_status fields_mass(fipi_ctx* ctx, double* out);
+fipi_status fields_free_energy(fipi_ctx* ctx, double* out);
+// Fine-grained transforms on host arrays.
+fipi_status fields_fft_r2c(fipi_ctx* ctx, const double* in, double* out);
+fipi_status fields_fft_c2r(fipi_ctx* ctx, const double* in, double* out);
+fipi_status fields_grad(fipi_ctx* ctx, const double* c, double* out);
+// Device pointers of the real fields used by the particle side (T-typed).
+const void* fields_real_c(fipi_ctx* ctx);
+const void* fields_real_grad(fipi_ctx* ctx, int d);
+void* fields_spread_target(fipi_ctx* ctx, int d);
+
+// particles.cu
+fipi_status particles_alloc(fipi_ctx* ctx);
+void particles_free(fipi_ctx* ctx);
+// Spread f_pp at p onto the dense spread grid (enqueue).
+void particles_spread(fipi_ctx* ctx);
+// Two Heun stages (enqueue); t is the step index (ramp uses t + 1).
+void particles_step(fipi_ctx* ctx, int t);
+// Fine-grained parity entry points (synchronous, host arrays).
+fipi_status particles_cells_build(fipi_ctx* ctx, const double* p, int* keys, int* sorted,
+                                  int* offsets);
+fipi_status particles_f_pp(fipi_ctx* ctx, const double* p, int t, const double* f_pi,
+                           double* f_pp, double* tau);
+fipi_status particles_pairs(fipi_ctx* ctx, const double* p, int* pairs, int max_pairs,
+                            int* n_pairs);
+fipi_status particles_interpolate(fipi_ctx* ctx, const double* fields, int nfields,
+                                  const double* p, double* out);
+fipi_status particles_f_pi(fipi_ctx* ctx, const double* c_loc, const double* dcdx,
+                           const double* r, const double* cth, double* f_pi);
+fipi_status particles_advect(fipi_ctx* ctx, int stage, const double* f_pi, const double* f_pp,
+                             const double* r, double* p, double* p_old, double* u_old);
+fipi_status particles_spread_host(fipi_ctx* ctx, const double* p, const double* f_pp,
+                                  double* out);
+
+// Brackets one kernel launch: counts it and, when timing is on, records
+// events around it on the context stream (capi.cu).
+struct LaunchScope {
+    fipi_ctx* ctx;
+    int idx = -1;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    LaunchScope(fipi_ctx* c, const char* name, double bytes);
+    ~LaunchScope();
+};
+
+// capi.cu helpers
+fipi_status set_error(fipi_ctx* ctx, fipi_status st, const std::string& msg);
+fipi_status cuda_check(fipi_ctx* ctx, cudaError_t e, const char* what);
+
+}  // namespace fipi
+
+// Stream-ordered synchronous copies: the context stream is non-blocking, so
+// plain cudaMemcpy on the legacy stream would not order with its kernels.
+inline cudaError_t h2d(fipi_ctx* ctx, void* d, const void* h, size_t n) {
+    cudaError_t e = cudaMemcpyAsync(d, h, n, cudaMemcpyHostToDevice, ctx->stream);
+    return e != cudaSuccess ? e : cudaStreamSynchronize(ctx->stream);
+}
+inline cudaError_t d2h(fipi_ctx* ctx, void* h, const void* d, size_t n) {
+    cudaError_t e = cudaMemcpyAsync(h, d, n, cudaMemcpyDeviceToHost, ctx->stream);
+    return e != cudaSuccess ? e : cudaStreamSynchronize(ctx->stream);
+}
+// Raises a kernel's dynamic shared-memory limit to `bytes` when needed
+// (per kernel instantiation; `cur` remembers what was granted).
+template <class K> inline cudaError_t ensure_smem(K kern, size_t bytes, size_t& cur) {
+    if (bytes <= cur) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) cur = bytes;
+    return e;
+}
+
+#define FIPI_CUDA(ctx, call)                                                   \
+    do {                                                                       \
+        cudaError_t e_ = (call);                                               \
+        if (e_ != cudaSuccess) return fipi::cuda_check((ctx), e_, #call);      \
+    } while (0)

@@ -1,0 +1,1004 @@
+// Eulerian side of the FIPI step on sm_103a: the pseudo-spectral
+// Cahn-Hilliard update and the Stokes projection (main.cpp:176-278 of the
+// reference), as 3-pass R2C/C2R FFTs with the element-wise work fused into
+// the passes.  Per step (13 transforms):
+//
+//   A  u_hat -> u (3 inverse), conv = u . grad c, C_hat = R2C(conv)
+//      with the SBDF2 / IMEX update fused into the last forward Z pass
+//   B  c^{n+1} = C2R(c_hat), f = (lambda/eps^2)(c^3 - c) fused, f_hat = R2C(f)
+//   C  mu = C2R(lambda k^2 c_hat + f_hat), grad c = C2R(i k c_hat) (4 inverse),
+//      F = mu grad c + spread + buoyancy fused, F_hat = R2C(F) (3 forward)
+//      with the Leray projection fused into the last Z pass -> u_hat
+//
+// Template parameter T is the arithmetic type: double (plain FP64 form) or
+// float (mixed form, whose k = 0 mode of c lives in FP64 scalars).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <vector>
+
+#include "ctx.hpp"
+
+namespace fipi {
+
+// ------------------------------------------------------------ constants
+template <typename T> struct StepConsts {
+    T lam_eps;    // lambda/sqr(epsilon)              main.cpp:178
+    T lam;        // lambda
+    T dt;
+    T s1, s2;     // t = 0: dt*M, dt*M*lambda          main.cpp:203-210
+    T s4, s2m;    // t > 0: 4 dt M, 2 dt M             main.cpp:215-216
+    T s4c, s2c;   // 4 dt, 2 dt                        main.cpp:220-221
+    T s3;         // 2 dt M lambda                     main.cpp:224
+    T mu;
+    T rho1, rho2, gravity;
+    int ny2, nz2, m;  // Nyquist indices
+};
+
+template <typename T> StepConsts<T> make_consts(const fipi_ctx* ctx) {
+    const fipi_params& P = ctx->P;
+    StepConsts<T> k;
+    const double dt = P.dt, M = P.mobility, lam = P.lambda;
+    k.lam_eps = T(P.lambda / (P.epsilon * P.epsilon));
+    k.lam = T(lam);
+    k.dt = T(dt);
+    k.s1 = T(dt * M);
+    k.s2 = T(dt * M * lam);
+    k.s4 = T(4.0 * dt * M);
+    k.s2m = T(2.0 * dt * M);
+    k.s4c = T(4.0 * dt);
+    k.s2c = T(2.0 * dt);
+    k.s3 = T(2.0 * dt * M * lam);
+    k.mu = T(P.mu);
+    k.rho1 = T(P.rho1);
+    k.rho2 = T(P.rho2);
+    k.gravity = T(P.gravity);
+    k.ny2 = P.ny / 2;
+    k.nz2 = P.nz / 2;
+    k.m = P.nx / 2;
+    return k;
+}
+
+template <typename T> struct KTabs {
+    const T* kx;
+    const T* ky;
+    const T* kz;
+    __device__ __forceinline__ T k2(int ix, int iy, int iz) const {
+        const T a = kx[ix], b = ky[iy], c = kz[iz];
+        T s = a * a;
+        s += b * b;
+        s += c * c;
+        return s;
+    }
+};
+
+// ------------------------------------------------------------ block reduce
+__device__ __forceinline__ double block_sum(double v) {
+    __shared__ double red[32];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) red[w] = v;
+    __syncthreads();
+    double s = 0.0;
+    if (w == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+        s = lane < nw ? red[lane] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    }
+    return s;  // valid in thread 0
+}
+
+// ------------------------------------------------------------ X-pass ops
+// R2C of c and of f = (lambda/eps^2)(c^3 - c) from the real c (set-up).
+template <typename T> struct OpInitCF {
+    using C = cplx<T>;
+    const T* c;
+    C* o0;
+    C* o1;
+    T lam_eps;
+    int nx, ny;
+    __device__ C* out(int f) const { return f == 0 ? o0 : o1; }
+    __device__ const C* in(int) const { return nullptr; }
+    __device__ void point(int z, int y, int n, C* v) const {
+        const C cc = reinterpret_cast<const C*>(c + ((size_t)z * ny + y) * nx)[n];
+        v[0] = cc;
+        v[1] = mkc<C>((cc.x * cc.x * cc.x - cc.x) * lam_eps, (cc.y * cc.y * cc.y - cc.y) * lam_eps);
+    }
+};
+
+// R2C of one real field (fine-grained fipi_fft_r2c).
+template <typename T> struct OpR2C {
+    using C = cplx<T>;
+    const T* src;
+    C* o0;
+    int nx, ny;
+    __device__ C* out(int) const { return o0; }
+    __device__ const C* in(int) const { return nullptr; }
+    __device__ void point(int z, int y, int n, C* v) const {
+        v[0] = reinterpret_cast<const C*>(src + ((size_t)z * ny + y) * nx)[n];
+    }
+};
+
+// C2R of NIN fields into real arrays dst[f] (+ optional constant offset).
+template <typename T, int NIN> struct OpC2RStore {
+    using C = cplx<T>;
+    const C* src[NIN];
+    T* dst[NIN];
+    int nx, ny;
+    __device__ const C* in(int f) const { return src[f]; }
+    __device__ C* out(int) const { return nullptr; }
+    __device__ void point(int z, int y, int n, C* v) const {
+#pragma unroll
+        for (int f = 0; f < NIN; ++f) reinterpret_cast<C*>(dst[f] + ((size_t)z * ny + y) * nx)[n] = v[f];
+    }
+};
+
+// Step A: u (3 inverse) . grad c -> conv (1 forward).  main.cpp:188-189
+template <typename T, bool MIXED> struct OpConv {
+    using C = cplx<T>;
+    const C* uS[3];
+    const T* g[3];
+    C* o0;
+    double* partials;
+    int nx, ny;
+    __device__ const C* in(int f) const { return uS[f]; }
+    __device__ C* out(int) const { return o0; }
+    __device__ void point(int z, int y, int n, C* v, double& acc) const {
+        const size_t row = ((size_t)z * ny + y) * nx;
+        T s0 = T(0), s1 = T(0);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const C gg = reinterpret_cast<const C*>(g[d] + row)[n];
+            s0 += v[d].x * gg.x;
+            s1 += v[d].y * gg.y;
+        }
+        v[0] = mkc<C>(s0, s1);
+        if (MIXED) acc += (double)s0 + (double)s1;
+    }
+};
+
+// Step B: c = C2R(c_hat) (+ FP64 mean in the mixed form), f = (lambda/eps^2)(c^3 - c).
+template <typename T, bool MIXED> struct OpCF {
+    using C = cplx<T>;
+    const C* cS;
+    T* c;
+    C* o0;
+    const double* k0;  // mixed: k0[0] = c_hat(0) in FP64
+    double invV;
+    T lam_eps;
+    int nx, ny;
+    __device__ const C* in(int) const { return cS; }
+    __device__ C* out(int) const { return o0; }
+    __device__ void point(int z, int y, int n, C* v, double&) const {
+        C cc = v[0];
+        if (MIXED) {
+            const T cbar = T(k0[0] * invV);
+            cc.x += cbar;
+            cc.y += cbar;
+        }
+        reinterpret_cast<C*>(c + ((size_t)z * ny + y) * nx)[n] = cc;
+        v[0] = mkc<C>((cc.x * cc.x * cc.x - cc.x) * lam_eps, (cc.y * cc.y * cc.y - cc.y) * lam_eps);
+    }
+};
+
+// Step C: mu, grad c (4 inverse) -> F = mu grad c + spread + buoyancy (3 forward).
+// main.cpp:246-269; the spread term is cluster::compute_f_r.
+template <typename T> struct OpForce {
+    using C = cplx<T>;
+    const C* S[4];
+    T* g[3];
+    const T* c;
+    const T* fsp[3];
+    int spread;
+    T rho1, rho2, gravity;
+    int nx, ny;
+    __device__ const C* in(int f) const { return S[f]; }
+    __device__ C* out(int f) const { return const_cast<C*>(S[f]); }
+    __device__ void point(int z, int y, int n, C* v, double&) const {
+        const size_t row = ((size_t)z * ny + y) * nx;
+        const C mu = v[0];
+        const C cc = reinterpret_cast<const C*>(c + row)[n];
+        // buoyancy ((1+c)/2 rho1 + (1-c)/2 rho2) g, g = (0, 0, gravity)
+        const T b0 = ((cc.x + T(1)) / T(2)) * rho1 + ((cc.x * T(-1) + T(1)) / T(2)) * rho2;
+        const T b1 = ((cc.y + T(1)) / T(2)) * rho1 + ((cc.y * T(-1) + T(1)) / T(2)) * rho2;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const C gd = v[1 + d];
+            reinterpret_cast<C*>(g[d] + row)[n] = gd;
+            T f0 = mu.x * gd.x, f1 = mu.y * gd.y;
+            if (spread) {
+                const C sp = reinterpret_cast<const C*>(fsp[d] + row)[n];
+                f0 += sp.x;
+                f1 += sp.y;
+            }
+            const T gz = (d == 2) ? gravity : T(0);
+            f0 += b0 * gz;
+            f1 += b1 * gz;
+            v[d] = mkc<C>(f0, f1);
+        }
+    }
+};
+
+// Adapter giving point() an accumulator when the op does not take one.
+template <class Op> struct NoAcc {
+    Op op;
+    __device__ const auto* in(int f) const { return op.in(f); }
+    __device__ auto* out(int f) const { return op.out(f); }
+    template <class C> __device__ void point(int z, int y, int n, C* v, double&) const { op.point(z, y, n, v); }
+};
+
+// X pass with an FP64 per-block reduction of point()'s accumulator.
+template <typename T, int NIN, int NOUT, bool REDUCE, class Op>
+__global__ void __launch_bounds__(kThreads) k_xpass_acc(Geom g, const cplx<T>* __restrict__ twx, Op op,
+                                                      double* partials) {
+    using C = cplx<T>;
+    constexpr int TY = Tiles<T>::TY;
+    constexpr int NF = NIN > NOUT ? NIN : NOUT;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C* s = reinterpret_cast<C*>(smem_raw);
+    const int M = g.m, H = g.h, pitch = M + 1;
+    const int z = blockIdx.y, y0 = blockIdx.x * TY;
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    const int halfM = M / 2;
+    if constexpr (NIN > 0) {
+        for (int idx = tid; idx < NIN * H * TY; idx += nthr) {
+            const int ty = idx % TY;
+            const int rest = idx / TY;
+            const int kx = rest % H;
+            const int f = rest / H;
+            s[(f * TY + ty) * pitch + kx] = op.in(f)[((size_t)z * H + kx) * g.ny + y0 + ty];
+        }
+        __syncthreads();
+        for (int idx = tid; idx < NIN * TY * (halfM + 1); idx += nthr) {
+            const int k = idx % (halfM + 1);
+            C* r = s + (idx / (halfM + 1)) * pitch;
+            if (k == 0) {
+                const T a = r[0].x, c = r[M].x;
+                r[0] = mkc<C>(a + c, a - c);
+            } else {
+                const int km = M - k;
+                const C Xk = r[k], Xm = r[km];
+                const C Wk = twx[k], Wm = twx[km];
+                const C A = cadd(Xk, cconj(Xm)), B = csub(Xk, cconj(Xm));
+                const C A2 = cadd(Xm, cconj(Xk)), B2 = csub(Xm, cconj(Xk));
+                const C Zk = cadd(A, cmul_i(cmul(B, cconj(Wk)), +1));
+                const C Zm = cadd(A2, cmul_i(cmul(B2, cconj(Wm)), +1));
+                r[k] = Zk;
+                if (km != k) r[km] = Zm;
+            }
+        }
+        __syncthreads();
+        smem_fft<T>(s, M, g.lm, NIN * TY, pitch, twx, 2, +1);
+    }
+    const T invV = T(1) / T(g.V);
+    double acc = 0.0;
+    for (int idx = tid; idx < TY * M; idx += nthr) {
+        const int n = idx % M;
+        const int ty = idx / M;
+        C v[NF];
+#pragma unroll
+        for (int f = 0; f < NIN; ++f) v[f] = cscale(s[(f * TY + ty) * pitch + n], invV);
+        op.point(z, y0 + ty, n, v, acc);
+#pragma unroll
+        for (int f = 0; f < NOUT; ++f) s[(f * TY + ty) * pitch + n] = v[f];
+    }
+    if constexpr (REDUCE) {
+        const double bs = block_sum(acc);
+        if (tid == 0) partials[(size_t)blockIdx.y * gridDim.x + blockIdx.x] = bs;
+    }
+    __syncthreads();
+    if constexpr (NOUT > 0) {
+        smem_fft<T>(s, M, g.lm, NOUT * TY, pitch, twx, 2, -1);
+        for (int idx = tid; idx < NOUT * TY * (halfM + 1); idx += nthr) {
+            const int k = idx % (halfM + 1);
+            C* r = s + (idx / (halfM + 1)) * pitch;
+            if (k == 0) {
+                const C Z0 = r[0];
+                r[0] = mkc<C>(Z0.x + Z0.y, T(0));
+                r[M] = mkc<C>(Z0.x - Z0.y, T(0));
+            } else {
+                const int km = M - k;
+                const C Zk = r[k], Zm = r[km];
+                const C Wk = twx[k], Wm = twx[km];
+                const C E1 = cadd(Zk, cconj(Zm)), D1 = csub(Zk, cconj(Zm));
+                const C E2 = cadd(Zm, cconj(Zk)), D2 = csub(Zm, cconj(Zk));
+                const C Xk = cscale(csub(E1, cmul_i(cmul(Wk, D1), +1)), T(0.5));
+                const C Xm = cscale(csub(E2, cmul_i(cmul(Wm, D2), +1)), T(0.5));
+                r[k] = Xk;
+                if (km != k) r[km] = Xm;
+            }
+        }
+        __syncthreads();
+        for (int idx = tid; idx < NOUT * H * TY; idx += nthr) {
+            const int ty = idx % TY;
+            const int rest = idx / TY;
+            const int kx = rest % H;
+            const int f = rest / H;
+            op.out(f)[((size_t)z * H + kx) * g.ny + y0 + ty] = s[(f * TY + ty) * pitch + kx];
+        }
+    }
+}
+
+// ------------------------------------------------------------ Z-pass ops
+// Z forward with the Cahn-Hilliard update (main.cpp:192-235) fused.
+// The conv spectrum C^n is the transformed input; c_hat^{n+1} is written
+// over c_hat^{n-1} and C^n over C^{n-1} at the same index.
+template <typename T, bool MIXED> struct ZOpCH {
+    using C = cplx<T>;
+    const C* conv;
+    const C* chat;
+    C* chat_old;  // in: c^{n-1}; out: c^{n+1}
+    const C* fhat;
+    const C* fhat_old;
+    C* Chat_old;  // in: C^{n-1}; out: C^n
+    KTabs<T> kt;
+    StepConsts<T> k;
+    int first;  // t == 0
+    __device__ void load(int, int, int, size_t gi, C* v) const { v[0] = conv[gi]; }
+    __device__ void store(int ix, int iy, int iz, size_t gi, const C* v) const {
+        const C Cn = v[0];
+        const C c = chat[gi];
+        const C f = fhat[gi];
+        const T k2 = kt.k2(ix, iy, iz);
+        const T k4 = k2 * k2;
+        C out;
+        if (first) {
+            const T a = k2 * k.s1;
+            T re = c.x - a * f.x, im = c.y - a * f.y;
+            re -= Cn.x * k.dt;
+            im -= Cn.y * k.dt;
+            const T den = k4 * k.s2 + T(1);
+            out = mkc<C>(re / den, im / den);
+        } else {
+            const C co = chat_old[gi];
+            const C fo = fhat_old[gi];
+            const C Co = Chat_old[gi];
+            T re = c.x * T(4) - co.x, im = c.y * T(4) - co.y;
+            const T a4 = k2 * k.s4, a2 = k2 * k.s2m;
+            re -= a4 * f.x;
+            im -= a4 * f.y;
+            re += a2 * fo.x;
+            im += a2 * fo.y;
+            re -= Cn.x * k.s4c;
+            im -= Cn.y * k.s4c;
+            re += Co.x * k.s2c;
+            im += Co.y * k.s2c;
+            const T den = k4 * k.s3 + T(3);
+            out = mkc<C>(re / den, im / den);
+        }
+        if (MIXED && gi == 0) out = mkc<C>(T(0), T(0));  // k = 0 lives in FP64 scalars
+        chat_old[gi] = out;
+        Chat_old[gi] = Cn;
+    }
+};
+
+// Z inverse prologue: mu_hat = lambda k^2 c_hat + f_hat (main.cpp:254).
+template <typename T> struct ZOpMu {
+    using C = cplx<T>;
+    const C* chat;
+    const C* fhat;
+    C* out;
+    KTabs<T> kt;
+    T lam;
+    __device__ void load(int ix, int iy, int iz, size_t gi, C* v) const {
+        const T a = kt.k2(ix, iy, iz) * lam;
+        const C c = chat[gi], f = fhat[gi];
+        v[0] = mkc<C>(a * c.x + f.x, a * c.y + f.y);
+    }
+    __device__ void store(int, int, int, size_t gi, const C* v) const { out[gi] = v[0]; }
+};
+
+// Z inverse prologue: i k_d c_hat, zero at the Nyquist index of d (field.cpp:288-328).
+template <typename T> struct ZOpGrad {
+    using C = cplx<T>;
+    const C* chat;
+    C* out[3];
+    KTabs<T> kt;
+    int m, ny2, nz2;
+    __device__ void load(int ix, int iy, int iz, size_t gi, C* v) const {
+        const C c = chat[gi];
+        const T kx = kt.kx[ix], ky = kt.ky[iy], kz = kt.kz[iz];
+        v[0] = (ix == m) ? mkc<C>(T(0), T(0)) : mkc<C>(-kx * c.y, kx * c.x);
+        v[1] = (iy == ny2) ? mkc<C>(T(0), T(0)) : mkc<C>(-ky * c.y, ky * c.x);
+        v[2] = (iz == nz2) ? mkc<C>(T(0), T(0)) : mkc<C>(-kz * c.y, kz * c.x);
+    }
+    __device__ void store(int, int, int, size_t gi, const C* v) const {
+        out[0][gi] = v[0];
+        out[1][gi] = v[1];
+        out[2][gi] = v[2];
+    }
+};
+
+// Z forward with the Leray projection (main.cpp:274-275) fused:
+// u_hat = (F - k (k.F)/k^2) / (mu k^2), 0 at k = 0.  At modes with a Nyquist
+// index the reference's C2C inverse keeps only the real part of a
+// non-Hermitian spectrum; that equals the inverse of the average of the
+// projections with k and with the Nyquist components of k negated, which is
+// what is stored here (a Hermitian half spectrum).
+template <typename T> struct ZOpProj {
+    using C = cplx<T>;
+    const C* in[3];
+    C* out[3];
+    KTabs<T> kt;
+    T mu;
+    int m, ny2, nz2;
+    __device__ void load(int, int, int, size_t gi, C* v) const {
+        v[0] = in[0][gi];
+        v[1] = in[1][gi];
+        v[2] = in[2][gi];
+    }
+    __device__ static void project(const T* kv, T k2, T mk2, const C* F, C* u) {
+        T dre = T(0), dim = T(0);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            dre += kv[d] * F[d].x;
+            dim += kv[d] * F[d].y;
+        }
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const T qre = (kv[d] * dre) / k2, qim = (kv[d] * dim) / k2;
+            u[d] = mkc<C>((F[d].x - qre) / mk2, (F[d].y - qim) / mk2);
+        }
+    }
+    __device__ void store(int ix, int iy, int iz, size_t gi, const C* F) const {
+        const T kv[3] = {kt.kx[ix], kt.ky[iy], kt.kz[iz]};
+        const T k2 = kt.k2(ix, iy, iz);
+        C u[3];
+        if (k2 == T(0)) {
+            u[0] = u[1] = u[2] = mkc<C>(T(0), T(0));
+        } else {
+            const T mk2 = k2 * mu;
+            project(kv, k2, mk2, F, u);
+            const bool nx_ = ix == m, ny_ = iy == ny2, nz_ = iz == nz2;
+            if (nx_ || ny_ || nz_) {
+                const T ks[3] = {nx_ ? -kv[0] : kv[0], ny_ ? -kv[1] : kv[1], nz_ ? -kv[2] : kv[2]};
+                C u2[3];
+                project(ks, k2, mk2, F, u2);
+#pragma unroll
+                for (int d = 0; d < 3; ++d)
+                    u[d] = mkc<C>(T(0.5) * (u[d].x + u2[d].x), T(0.5) * (u[d].y + u2[d].y));
+            }
+        }
+        out[0][gi] = u[0];
+        out[1][gi] = u[1];
+        out[2][gi] = u[2];
+    }
+};
+
+// Z forward plain store; in the mixed form the k = 0 entry of c_hat is held
+// in FP64 and zeroed in the FP32 array.
+template <typename T, int NF> struct ZOpStore {
+    using C = cplx<T>;
+    const C* in[NF];
+    C* out[NF];
+    int zero_k0_mask;
+    __device__ void load(int, int, int, size_t gi, C* v) const {
+#pragma unroll
+        for (int f = 0; f < NF; ++f) v[f] = in[f][gi];
+    }
+    __device__ void store(int, int, int, size_t gi, const C* v) const {
+#pragma unroll
+        for (int f = 0; f < NF; ++f)
+            out[f][gi] = (gi == 0 && ((zero_k0_mask >> f) & 1)) ? mkc<C>(T(0), T(0)) : v[f];
+    }
+};
+
+// FP64 k = 0 update of the mixed form: c_hat(0) follows the same IMEX /
+// SBDF2 recurrence with k = 0 (the f terms vanish), C(0) from the FP64
+// per-block sums of conv.  k0 = [c0, c0_old, C0_old, C0_cur].
+__global__ void k_k0_update(double* k0, const double* partials, int np, int first, double dt) {
+    double s = 0.0;
+    for (int i = threadIdx.x; i < np; i += blockDim.x) s += partials[i];
+    s = block_sum(s);
+    if (threadIdx.x == 0) {
+        const double c0 = k0[0], c0o = k0[1], C0o = k0[2];
+        double nw;
+        if (first) {
+            nw = c0 - s * dt;
+        } else {
+            double re = c0 * 4.0 - c0o;
+            re -= s * (4.0 * dt);
+            re += C0o * (2.0 * dt);
+            nw = re / 3.0;
+        }
+        k0[1] = c0;
+        k0[0] = nw;
+        k0[2] = s;
+        k0[3] = s;
+    }
+}
+
+template <typename Tin, typename Tout>
+__global__ void k_convert(const Tin* __restrict__ a, Tout* __restrict__ b, size_t n) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        b[i] = (Tout)a[i];
+}
+
+// FP64 per-block sums for mass and free energy (main.cpp:329, field.cpp:507-516).
+template <typename T>
+__global__ void k_diag(const T* __restrict__ c, const T* __restrict__ g0, const T* __restrict__ g1,
+                       const T* __restrict__ g2, size_t V, double lam, double e2, double dv,
+                       double* partials, int mode) {
+    double s = 0.0;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < V; i += (size_t)gridDim.x * blockDim.x) {
+        const double cr = (double)c[i];
+        if (mode == 0) {
+            s += cr;
+        } else {
+            const double a = g0[i], b = g1[i], d = g2[i];
+            double g2s = a * a;
+            g2s += b * b;
+            g2s += d * d;
+            const double w = cr * cr - 1.0;
+            const double fe = (g2s * 0.5 + (w * w) * e2) * lam;
+            s += fe * dv;
+        }
+    }
+    s = block_sum(s);
+    if (threadIdx.x == 0) partials[blockIdx.x] = s;
+}
+
+// ------------------------------------------------------------ launch glue
+template <typename T> struct F {
+    using C = cplx<T>;
+    static C* S(fipi_ctx* ctx, int i) { return (C*)ctx->fb.S[i]; }
+    static C* sp(void* p) { return (C*)p; }
+    static T* re(void* p) { return (T*)p; }
+    static const C* tw(void* p) { return (const C*)p; }
+    static KTabs<T> ktabs(fipi_ctx* ctx) {
+        return KTabs<T>{(const T*)ctx->fb.kx, (const T*)ctx->fb.ky, (const T*)ctx->fb.kz};
+    }
+};
+
+// nreal: real (V-sized) arrays the fused point operation reads or writes.
+template <typename T, int NIN, int NOUT, bool REDUCE, class Op>
+void launch_x(fipi_ctx* ctx, const char* name, int nreal, const Op& op, double* partials = nullptr) {
+    const Geom& g = ctx->g;
+    LaunchScope ls(ctx, name,
+                   (double)(NIN + NOUT) * g.SH * sizeof(cplx<T>) + (double)nreal * g.V * sizeof(T));
+    constexpr int NF = NIN > NOUT ? NIN : NOUT;
+    const size_t smem = (size_t)NF * Tiles<T>::TY * (g.m + 1) * sizeof(cplx<T>);
+    auto kern = k_xpass_acc<T, NIN, NOUT, REDUCE, Op>;
+    static size_t granted = 48 * 1024;
+    ensure_smem(kern, smem, granted);
+    dim3 grid(g.ny / Tiles<T>::TY, g.nz);
+    kern<<<grid, kThreads, smem, ctx->stream>>>(g, (const cplx<T>*)ctx->fb.twx, op, partials);
+}
+
+template <typename T> void launch_y(fipi_ctx* ctx, int nf, void* const* in, void* const* out, int dir) {
+    const Geom& g = ctx->g;
+    static const char* names[9] = {"Y pass x0", "Y pass x1", "Y pass x2", "Y pass x3", "Y pass x4",
+                                   "Y pass x5", "Y pass x6", "Y pass x7", "Y pass x8"};
+    LaunchScope ls(ctx, names[nf], 2.0 * nf * g.SH * sizeof(cplx<T>));
+    FieldPtrs<T> fp{};
+    for (int f = 0; f < nf; ++f) {
+        fp.in[f] = (cplx<T>*)in[f];
+        fp.out[f] = (cplx<T>*)out[f];
+    }
+    int rows = (4 * kThreads) / g.ny;
+    if (rows < 1) rows = 1;
+    const long long total = (long long)g.nz * g.h;
+    dim3 grid((unsigned)((total + rows - 1) / rows), nf);
+    const size_t smem = (size_t)rows * g.ny * sizeof(cplx<T>);
+    static size_t granted = 48 * 1024;
+    ensure_smem(k_ypass<T>, smem, granted);
+    k_ypass<T><<<grid, kThreads, smem, ctx->stream>>>(g, (const cplx<T>*)ctx->fb.twy, dir, fp, rows);
+}
+
+// nspec: spectral arrays the pass and its fused operation read or write.
+template <typename T, int NF, class Op> void launch_z(fipi_ctx* ctx, const char* name, int nspec, const Op& op, int dir) {
+    const Geom& g = ctx->g;
+    LaunchScope ls(ctx, name, (double)nspec * g.SH * sizeof(cplx<T>));
+    const size_t smem = (size_t)NF * Tiles<T>::TZ * (g.nz + 1) * sizeof(cplx<T>);
+    auto kern = k_zpass<T, NF, Op>;
+    static size_t granted = 48 * 1024;
+    ensure_smem(kern, smem, granted);
+    dim3 grid(g.h, g.ny / Tiles<T>::TZ);
+    kern<<<grid, kThreads, smem, ctx->stream>>>(g, (const cplx<T>*)ctx->fb.twz, dir, op);
+}
+
+// grad c (real, 3 fields) from c_hat.
+template <typename T> void grad_from_chat(fipi_ctx* ctx, const cplx<T>* chat, T* const g3[3]) {
+    using C = cplx<T>;
+    const Geom& g = ctx->g;
+    ZOpGrad<T> zg{chat, {F<T>::S(ctx, 1), F<T>::S(ctx, 2), F<T>::S(ctx, 3)}, F<T>::ktabs(ctx), g.m,
+                  g.ny / 2, g.nz / 2};
+    launch_z<T, 3>(ctx, "Z inverse grad", 4, zg, +1);
+    void* sp[3] = {ctx->fb.S[1], ctx->fb.S[2], ctx->fb.S[3]};
+    launch_y<T>(ctx, 3, sp, sp, +1);
+    OpC2RStore<T, 3> op{{F<T>::S(ctx, 1), F<T>::S(ctx, 2), F<T>::S(ctx, 3)}, {g3[0], g3[1], g3[2]}, g.nx, g.ny};
+    launch_x<T, 3, 0, false>(ctx, "X inverse store", 3, NoAcc<OpC2RStore<T, 3>>{op});
+    (void)sizeof(C);
+}
+
+// ------------------------------------------------------------ allocation
+template <typename T> static fipi_status alloc_fields_t(fipi_ctx* ctx) {
+    using C = cplx<T>;
+    const Geom& g = ctx->g;
+    FieldBufs& b = ctx->fb;
+    const size_t V = (size_t)g.V, SH = (size_t)g.SH;
+    auto A = [&](void** p, size_t bytes) -> cudaError_t {
+        cudaError_t e = cudaMalloc(p, bytes);
+        if (e == cudaSuccess) ctx->device_bytes += bytes;
+        return e;
+    };
+    FIPI_CUDA(ctx, A(&b.twx, sizeof(C) * g.nx));
+    FIPI_CUDA(ctx, A(&b.twy, sizeof(C) * g.ny));
+    FIPI_CUDA(ctx, A(&b.twz, sizeof(C) * g.nz));
+    FIPI_CUDA(ctx, A(&b.kx, sizeof(T) * (g.m + 1)));
+    FIPI_CUDA(ctx, A(&b.ky, sizeof(T) * g.ny));
+    FIPI_CUDA(ctx, A(&b.kz, sizeof(T) * g.nz));
+    FIPI_CUDA(ctx, A(&b.c, sizeof(T) * V));
+    for (int d = 0; d < 3; ++d) {
+        FIPI_CUDA(ctx, A(&b.g[d], sizeof(T) * V));
+        FIPI_CUDA(ctx, A(&b.fsp[d], sizeof(T) * V));
+        FIPI_CUDA(ctx, cudaMemsetAsync(b.fsp[d], 0, sizeof(T) * V, ctx->stream));
+        FIPI_CUDA(ctx, A(&b.uhat[d], sizeof(C) * SH));
+        FIPI_CUDA(ctx, cudaMemsetAsync(b.uhat[d], 0, sizeof(C) * SH, ctx->stream));
+    }
+    FIPI_CUDA(ctx, A(&b.ureal, sizeof(T) * V * 3));
+    void** specs[] = {&b.chat, &b.chat_old, &b.fhat, &b.fhat_old, &b.Chat_old, &b.S[0], &b.S[1], &b.S[2], &b.S[3]};
+    for (void** p : specs) {
+        FIPI_CUDA(ctx, A(p, sizeof(C) * SH));
+        FIPI_CUDA(ctx, cudaMemsetAsync(*p, 0, sizeof(C) * SH, ctx->stream));
+    }
+    // twiddles and wave numbers, computed in extended precision on the host
+    auto twiddles = [&](int n) {
+        std::vector<C> t(n);
+        const long double two_pi = 6.283185307179586476925286766559005768L;
+        for (int q = 0; q < n; ++q) {
+            const long double a = two_pi * (long double)q / (long double)n;
+            t[q].x = (T)cosl(a);
+            t[q].y = (T)(-sinl(a));
+        }
+        return t;
+    };
+    auto tx = twiddles(g.nx), ty = twiddles(g.ny), tz = twiddles(g.nz);
+    FIPI_CUDA(ctx, h2d(ctx, b.twx, tx.data(), sizeof(C) * g.nx));
+    FIPI_CUDA(ctx, h2d(ctx, b.twy, ty.data(), sizeof(C) * g.ny));
+    FIPI_CUDA(ctx, h2d(ctx, b.twz, tz.data(), sizeof(C) * g.nz));
+    // field.cpp:100-121: i*2.0*pi/L for i <= N/2 else (i - N)*2.0*pi/L
+    const fipi_params& P = ctx->P;
+    auto waves = [&](int n, int count, double L) {
+        std::vector<T> k(count);
+        for (int i = 0; i < count; ++i) k[i] = (T)((i <= n / 2) ? i * 2.0 * P.pi / L : (i - n) * 2.0 * P.pi / L);
+        return k;
+    };
+    auto kx = waves(g.nx, g.m + 1, P.lx), ky = waves(g.ny, g.ny, P.ly), kz = waves(g.nz, g.nz, P.lz);
+    FIPI_CUDA(ctx, h2d(ctx, b.kx, kx.data(), sizeof(T) * (g.m + 1)));
+    FIPI_CUDA(ctx, h2d(ctx, b.ky, ky.data(), sizeof(T) * g.ny));
+    FIPI_CUDA(ctx, h2d(ctx, b.kz, kz.data(), sizeof(T) * g.nz));
+    return FIPI_OK;
+}
+
+fipi_status fields_alloc(fipi_ctx* ctx) {
+    const fipi_params& P = ctx->P;
+    Geom& g = ctx->g;
+    g.nx = P.nx;
+    g.ny = P.ny;
+    g.nz = P.nz;
+    g.m = P.nx / 2;
+    g.h = P.nx / 2 + 1;
+    g.lm = ilog2i(g.m);
+    g.ly = ilog2i(g.ny);
+    g.lz = ilog2i(g.nz);
+    g.V = (long long)P.nx * P.ny * P.nz;
+    g.SH = (long long)P.nz * g.h * P.ny;
+    fipi_status st = (ctx->prec == FIPI_MIXED) ? alloc_fields_t<float>(ctx) : alloc_fields_t<double>(ctx);
+    if (st != FIPI_OK) return st;
+    ctx->n_partials = (g.ny / 8) * g.nz;  // upper bound of X-pass blocks (TY >= 8)
+    if (ctx->n_partials < 1024) ctx->n_partials = 1024;
+    FIPI_CUDA(ctx, cudaMalloc(&ctx->partials, sizeof(double) * ctx->n_partials));
+    FIPI_CUDA(ctx, cudaMalloc(&ctx->k0, sizeof(double) * 4));
+    FIPI_CUDA(ctx, cudaMemsetAsync(ctx->k0, 0, sizeof(double) * 4, ctx->stream));
+    ctx->device_bytes += sizeof(double) * (ctx->n_partials + 4);
+    return FIPI_OK;
+}
+
+void fields_free(fipi_ctx* ctx) {
+    FieldBufs& b = ctx->fb;
+    void* all[] = {b.twx, b.twy, b.twz, b.kx, b.ky, b.kz, b.c, b.ureal, b.chat, b.chat_old, b.fhat,
+                   b.fhat_old, b.Chat_old, b.S[0], b.S[1], b.S[2], b.S[3], b.g[0], b.g[1], b.g[2],
+                   b.fsp[0], b.fsp[1], b.fsp[2], b.uhat[0], b.uhat[1], b.uhat[2], ctx->partials, ctx->k0};
+    for (void* p : all)
+        if (p) cudaFree(p);
+    b = FieldBufs{};
+    ctx->partials = nullptr;
+    ctx->k0 = nullptr;
+}
+
+// ------------------------------------------------------------ state I/O
+// Copies host doubles into a T device array through a staging buffer.
+template <typename T> static fipi_status upload(fipi_ctx* ctx, const double* h, T* d, size_t n) {
+    if (sizeof(T) == sizeof(double)) {
+        FIPI_CUDA(ctx, cudaMemcpyAsync(d, h, n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+        return FIPI_OK;
+    }
+    double* stage = nullptr;
+    FIPI_CUDA(ctx, cudaMallocAsync((void**)&stage, n * sizeof(double), ctx->stream));
+    FIPI_CUDA(ctx, cudaMemcpyAsync(stage, h, n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    { LaunchScope ls(ctx, "convert", 0.0); k_convert<double, T><<<1024, 256, 0, ctx->stream>>>(stage, d, n); }
+    FIPI_CUDA(ctx, cudaFreeAsync(stage, ctx->stream));
+    return FIPI_OK;
+}
+
+template <typename T> static fipi_status download(fipi_ctx* ctx, const T* d, double* h, size_t n) {
+    if (sizeof(T) == sizeof(double)) {
+        FIPI_CUDA(ctx, cudaMemcpyAsync(h, d, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        FIPI_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        return FIPI_OK;
+    }
+    double* stage = nullptr;
+    FIPI_CUDA(ctx, cudaMallocAsync((void**)&stage, n * sizeof(double), ctx->stream));
+    { LaunchScope ls(ctx, "convert", 0.0); k_convert<T, double><<<1024, 256, 0, ctx->stream>>>(d, stage, n); }
+    FIPI_CUDA(ctx, cudaMemcpyAsync(h, stage, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    FIPI_CUDA(ctx, cudaFreeAsync(stage, ctx->stream));
+    FIPI_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return FIPI_OK;
+}
+
+// t = 0 state: c, c_hat, f_hat, grad c (everything main.cpp:178-189 needs).
+template <typename T> static fipi_status set_phase_t(fipi_ctx* ctx, const double* c_host) {
+    const Geom& g = ctx->g;
+    const bool mixed = ctx->prec == FIPI_MIXED;
+    fipi_status st = upload<T>(ctx, c_host, (T*)ctx->fb.c, (size_t)g.V);
+    if (st != FIPI_OK) return st;
+    if (mixed) {
+        // FP64 k = 0 mode: sum of c (Neumaier)
+        double s = 0.0, comp = 0.0;
+        for (long long i = 0; i < g.V; ++i) {
+            const double x = c_host[i];
+            const double t = s + x;
+            comp += (fabs(s) >= fabs(x)) ? (s - t) + x : (x - t) + s;
+            s = t;
+        }
+        const double k0h[4] = {s + comp, s + comp, 0.0, 0.0};
+        FIPI_CUDA(ctx, cudaMemcpyAsync(ctx->k0, k0h, sizeof(k0h), cudaMemcpyHostToDevice, ctx->stream));
+    }
+    const StepConsts<T> k = make_consts<T>(ctx);
+    OpInitCF<T> op{(const T*)ctx->fb.c, F<T>::S(ctx, 0), F<T>::S(ctx, 1), k.lam_eps, g.nx, g.ny};
+    launch_x<T, 0, 2, false>(ctx, "X forward c,f", 1, NoAcc<OpInitCF<T>>{op});
+    void* sp[2] = {ctx->fb.S[0], ctx->fb.S[1]};
+    launch_y<T>(ctx, 2, sp, sp, -1);
+    ZOpStore<T, 2> zs{{F<T>::S(ctx, 0), F<T>::S(ctx, 1)}, {F<T>::sp(ctx->fb.chat), F<T>::sp(ctx->fb.fhat)}, mixed ? 1 : 0};
+    launch_z<T, 2>(ctx, "Z forward store", 4, zs, -1);
+    T* g3[3] = {(T*)ctx->fb.g[0], (T*)ctx->fb.g[1], (T*)ctx->fb.g[2]};
+    grad_from_chat<T>(ctx, F<T>::sp(ctx->fb.chat), g3);
+    FIPI_CUDA(ctx, cudaGetLastError());
+    return FIPI_OK;
+}
+
+fipi_status fields_set_phase(fipi_ctx* ctx, const double* c_host) {
+    return ctx->prec == FIPI_MIXED ? set_phase_t<float>(ctx, c_host) : set_phase_t<double>(ctx, c_host);
+}
+
+// u_hat = R2C(u): the step only needs the spectrum of the velocity.
+template <typename T> static fipi_status set_velocity_t(fipi_ctx* ctx, const double* u_host) {
+    const Geom& g = ctx->g;
+    for (int d = 0; d < 3; ++d) {
+        T* tmp = (T*)ctx->fb.ureal + (size_t)d * g.V;
+        fipi_status st = upload<T>(ctx, u_host + (size_t)d * g.V, tmp, (size_t)g.V);
+        if (st != FIPI_OK) return st;
+        OpR2C<T> op{tmp, F<T>::S(ctx, 0), g.nx, g.ny};
+        launch_x<T, 0, 1, false>(ctx, "X forward", 1, NoAcc<OpR2C<T>>{op});
+        void* sp[1] = {ctx->fb.S[0]};
+        launch_y<T>(ctx, 1, sp, sp, -1);
+        ZOpStore<T, 1> zs{{F<T>::S(ctx, 0)}, {F<T>::sp(ctx->fb.uhat[d])}, 0};
+        launch_z<T, 1>(ctx, "Z forward store", 2, zs, -1);
+    }
+    FIPI_CUDA(ctx, cudaGetLastError());
+    return FIPI_OK;
+}
+
+fipi_status fields_set_velocity(fipi_ctx* ctx, const double* u_host) {
+    return ctx->prec == FIPI_MIXED ? set_velocity_t<float>(ctx, u_host) : set_velocity_t<double>(ctx, u_host);
+}
+
+fipi_status fields_get_phase(fipi_ctx* ctx, double* c_host) {
+    if (ctx->prec == FIPI_MIXED) return download<float>(ctx, (const float*)ctx->fb.c, c_host, (size_t)ctx->g.V);
+    return download<double>(ctx, (const double*)ctx->fb.c, c_host, (size_t)ctx->g.V);
+}
+
+template <typename T> static fipi_status get_velocity_t(fipi_ctx* ctx, double* u_host) {
+    const Geom& g = ctx->g;
+    ZOpStore<T, 3> zs{{F<T>::sp(ctx->fb.uhat[0]), F<T>::sp(ctx->fb.uhat[1]), F<T>::sp(ctx->fb.uhat[2])},
+                      {F<T>::S(ctx, 0), F<T>::S(ctx, 1), F<T>::S(ctx, 2)}, 0};
+    launch_z<T, 3>(ctx, "Z inverse copy", 6, zs, +1);
+    void* sp[3] = {ctx->fb.S[0], ctx->fb.S[1], ctx->fb.S[2]};
+    launch_y<T>(ctx, 3, sp, sp, +1);
+    T* ur = (T*)ctx->fb.ureal;
+    OpC2RStore<T, 3> op{{F<T>::S(ctx, 0), F<T>::S(ctx, 1), F<T>::S(ctx, 2)}, {ur, ur + g.V, ur + 2 * g.V}, g.nx, g.ny};
+    launch_x<T, 3, 0, false>(ctx, "X inverse store", 3, NoAcc<OpC2RStore<T, 3>>{op});
+    FIPI_CUDA(ctx, cudaGetLastError());
+    return download<T>(ctx, ur, u_host, (size_t)g.V * 3);
+}
+
+fipi_status fields_get_velocity(fipi_ctx* ctx, double* u_host) {
+    return ctx->prec == FIPI_MIXED ? get_velocity_t<float>(ctx, u_host) : get_velocity_t<double>(ctx, u_host);
+}
+
+// ------------------------------------------------------------ the step
+template <typename T, bool MIXED> static void step_ch_t(fipi_ctx* ctx, int t) {
+    using C = cplx<T>;
+    const Geom& g = ctx->g;
+    FieldBufs& b = ctx->fb;
+    const StepConsts<T> k = make_consts<T>(ctx);
+    // A: u_hat -> u (Z, Y inverse; X inverse fused with conv and its R2C)
+    ZOpStore<T, 3> zu{{F<T>::sp(b.uhat[0]), F<T>::sp(b.uhat[1]), F<T>::sp(b.uhat[2])},
+                      {F<T>::S(ctx, 0), F<T>::S(ctx, 1), F<T>::S(ctx, 2)}, 0};
+    launch_z<T, 3>(ctx, "Z inverse copy", 6, zu, +1);
+    void* s3[3] = {b.S[0], b.S[1], b.S[2]};
+    launch_y<T>(ctx, 3, s3, s3, +1);
+    OpConv<T, MIXED> oc{{F<T>::S(ctx, 0), F<T>::S(ctx, 1), F<T>::S(ctx, 2)},
+                        {(const T*)b.g[0], (const T*)b.g[1], (const T*)b.g[2]}, F<T>::S(ctx, 3), ctx->partials,
+                        g.nx, g.ny};
+    launch_x<T, 3, 1, MIXED>(ctx, "X inverse u, conv, forward", 3, oc, ctx->partials);
+    void* s1[1] = {b.S[3]};
+    launch_y<T>(ctx, 1, s1, s1, -1);
+    if (MIXED) {
+        const int nblk = (g.ny / Tiles<T>::TY) * g.nz;
+        LaunchScope ls(ctx, "k0 update", 0.0);
+        k_k0_update<<<1, 256, 0, ctx->stream>>>(ctx->k0, ctx->partials, nblk, t == 0, ctx->P.dt);
+    }
+    ZOpCH<T, MIXED> zc{F<T>::S(ctx, 3), F<T>::sp(b.chat), F<T>::sp(b.chat_old), F<T>::sp(b.fhat),
+                       F<T>::sp(b.fhat_old), F<T>::sp(b.Chat_old), F<T>::ktabs(ctx), k, t == 0 ? 1 : 0};
+    launch_z<T, 1>(ctx, t == 0 ? "Z forward + IMEX update" : "Z forward + SBDF2 update", t == 0 ? 5 : 8, zc, -1);
+    std::swap(b.chat, b.chat_old);  // chat = c^{n+1}, chat_old = c^n
+    // B: c^{n+1} = C2R(c_hat), f fused, f_hat = R2C(f)
+    ZOpStore<T, 1> zc2{{F<T>::sp(b.chat)}, {F<T>::S(ctx, 0)}, 0};
+    launch_z<T, 1>(ctx, "Z inverse copy", 2, zc2, +1);
+    void* s0[1] = {b.S[0]};
+    launch_y<T>(ctx, 1, s0, s0, +1);
+    OpCF<T, MIXED> ocf{F<T>::S(ctx, 0), (T*)b.c, F<T>::S(ctx, 1), ctx->k0, 1.0 / (double)g.V, k.lam_eps, g.nx, g.ny};
+    launch_x<T, 1, 1, false>(ctx, "X inverse c, f, forward", 1, ocf);
+    void* s1b[1] = {b.S[1]};
+    launch_y<T>(ctx, 1, s1b, s1b, -1);
+    ZOpStore<T, 1> zf{{F<T>::S(ctx, 1)}, {F<T>::sp(b.fhat_old)}, 0};
+    launch_z<T, 1>(ctx, "Z forward store", 2, zf, -1);
+    std::swap(b.fhat, b.fhat_old);  // fhat = f^{n+1}, fhat_old = f^n
+    (void)sizeof(C);
+}
+
+void fields_step_ch(fipi_ctx* ctx, int t) {
+    if (ctx->prec == FIPI_MIXED) step_ch_t<float, true>(ctx, t);
+    else step_ch_t<double, false>(ctx, t);
+}
+
+template <typename T> static void step_stokes_t(fipi_ctx* ctx) {
+    const Geom& g = ctx->g;
+    FieldBufs& b = ctx->fb;
+    const StepConsts<T> k = make_consts<T>(ctx);
+    const KTabs<T> kt = F<T>::ktabs(ctx);
+    ZOpMu<T> zm{F<T>::sp(b.chat), F<T>::sp(b.fhat), F<T>::S(ctx, 0), kt, k.lam};
+    launch_z<T, 1>(ctx, "Z inverse mu", 3, zm, +1);
+    ZOpGrad<T> zg{F<T>::sp(b.chat), {F<T>::S(ctx, 1), F<T>::S(ctx, 2), F<T>::S(ctx, 3)}, kt, g.m, g.ny / 2, g.nz / 2};
+    launch_z<T, 3>(ctx, "Z inverse grad", 4, zg, +1);
+    void* s4[4] = {b.S[0], b.S[1], b.S[2], b.S[3]};
+    launch_y<T>(ctx, 4, s4, s4, +1);
+    OpForce<T> of{{F<T>::S(ctx, 0), F<T>::S(ctx, 1), F<T>::S(ctx, 2), F<T>::S(ctx, 3)},
+                  {(T*)b.g[0], (T*)b.g[1], (T*)b.g[2]},
+                  (const T*)b.c,
+                  {(const T*)b.fsp[0], (const T*)b.fsp[1], (const T*)b.fsp[2]},
+                  (ctx->P.switch_particle && ctx->P.n_p > 0) ? 1 : 0,
+                  k.rho1, k.rho2, k.gravity, g.nx, g.ny};
+    launch_x<T, 4, 3, false>(ctx, "X inverse mu,grad, force, forward", (of.spread ? 7 : 4), of);
+    void* s3[3] = {b.S[0], b.S[1], b.S[2]};
+    launch_y<T>(ctx, 3, s3, s3, -1);
+    ZOpProj<T> zp{{F<T>::S(ctx, 0), F<T>::S(ctx, 1), F<T>::S(ctx, 2)},
+                  {F<T>::sp(b.uhat[0]), F<T>::sp(b.uhat[1]), F<T>::sp(b.uhat[2])}, kt, k.mu, g.m, g.ny / 2, g.nz / 2};
+    launch_z<T, 3>(ctx, "Z forward + projection", 6, zp, -1);
+}
+
+void fields_step_stokes(fipi_ctx* ctx) {
+    if (ctx->prec == FIPI_MIXED) step_stokes_t<float>(ctx);
+    else step_stokes_t<double>(ctx);
+}
+
+// ------------------------------------------------------------ diagnostics
+template <typename T> static fipi_status diag_t(fipi_ctx* ctx, int mode, double* out) {
+    const Geom& g = ctx->g;
+    const fipi_params& P = ctx->P;
+    const int nb = 1024;
+    const double dx = P.lx / P.nx, dy = P.ly / P.ny, dz = P.lz / P.nz;
+    const double dv = (mode == 0) ? dx * dy * dz : dx * dx * dx;  // field.cpp:512 uses cubic(dx)
+    LaunchScope ls(ctx, "diagnostic reduce", (mode == 0 ? 1.0 : 4.0) * g.V * sizeof(T));
+    k_diag<T><<<nb, 256, 0, ctx->stream>>>((const T*)ctx->fb.c, (const T*)ctx->fb.g[0], (const T*)ctx->fb.g[1],
+                                           (const T*)ctx->fb.g[2], (size_t)g.V, P.lambda,
+                                           0.25 / (P.epsilon * P.epsilon), dv, ctx->partials, mode);
+    std::vector<double> h(nb);
+    FIPI_CUDA(ctx, cudaMemcpyAsync(h.data(), ctx->partials, sizeof(double) * nb, cudaMemcpyDeviceToHost, ctx->stream));
+    FIPI_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    double s = 0.0, comp = 0.0;
+    for (double x : h) {
+        const double t = s + x;
+        comp += (fabs(s) >= fabs(x)) ? (s - t) + x : (x - t) + s;
+        s = t;
+    }
+    *out = (mode == 0) ? (s + comp) * dv : (s + comp);  // mass: sum(c) dx dy dz; energy: dv inside
+    return FIPI_OK;
+}
+
+fipi_status fields_mass(fipi_ctx* ctx, double* out) {
+    if (ctx->prec == FIPI_MIXED) {
+        double k0h[4];
+        FIPI_CUDA(ctx, cudaMemcpyAsync(k0h, ctx->k0, sizeof(k0h), cudaMemcpyDeviceToHost, ctx->stream));
+        FIPI_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        const fipi_params& P = ctx->P;
+        *out = k0h[0] * ((P.lx / P.nx) * (P.ly / P.ny) * (P.lz / P.nz));
+        return FIPI_OK;
+    }
+    return diag_t<double>(ctx, 0, out);
+}
+
+fipi_status fields_free_energy(fipi_ctx* ctx, double* out) {
+    return ctx->prec == FIPI_MIXED ? diag_t<float>(ctx, 1, out) : diag_t<double>(ctx, 1, out);
+}
+
+// ------------------------------------------------------------ fine-grained
+template <typename T> static fipi_status r2c_t(fipi_ctx* ctx, const double* in, double* out) {
+    using C = cplx<T>;
+    const Geom& g = ctx->g;
+    T* tmp = (T*)ctx->fb.ureal;
+    fipi_status st = upload<T>(ctx, in, tmp, (size_t)g.V);
+    if (st != FIPI_OK) return st;
+    OpR2C<T> op{tmp, F<T>::S(ctx, 0), g.nx, g.ny};
+    launch_x<T, 0, 1, false>(ctx, "X forward", 1, NoAcc<OpR2C<T>>{op});
+    void* sp[1] = {ctx->fb.S[0]};
+    launch_y<T>(ctx, 1, sp, sp, -1);
+    ZOpStore<T, 1> zs{{F<T>::S(ctx, 0)}, {F<T>::S(ctx, 1)}, 0};
+    launch_z<T, 1>(ctx, "Z forward store", 2, zs, -1);
+    FIPI_CUDA(ctx, cudaGetLastError());
+    return download<T>(ctx, (const T*)F<T>::S(ctx, 1), out, (size_t)g.SH * 2);
+    (void)sizeof(C);
+}
+
+fipi_status fields_fft_r2c(fipi_ctx* ctx, const double* in, double* out) {
+    return ctx->prec == FIPI_MIXED ? r2c_t<float>(ctx, in, out) : r2c_t<double>(ctx, in, out);
+}
+
+template <typename T> static fipi_status c2r_t(fipi_ctx* ctx, const double* in, double* out) {
+    const Geom& g = ctx->g;
+    fipi_status st = upload<T>(ctx, in, (T*)F<T>::S(ctx, 0), (size_t)g.SH * 2);
+    if (st != FIPI_OK) return st;
+    ZOpStore<T, 1> zs{{F<T>::S(ctx, 0)}, {F<T>::S(ctx, 1)}, 0};
+    launch_z<T, 1>(ctx, "Z inverse copy", 2, zs, +1);
+    void* sp[1] = {ctx->fb.S[1]};
+    launch_y<T>(ctx, 1, sp, sp, +1);
+    T* dst = (T*)ctx->fb.ureal;
+    OpC2RStore<T, 1> op{{F<T>::S(ctx, 1)}, {dst}, g.nx, g.ny};
+    launch_x<T, 1, 0, false>(ctx, "X inverse store", 1, NoAcc<OpC2RStore<T, 1>>{op});
+    FIPI_CUDA(ctx, cudaGetLastError());
+    return download<T>(ctx, dst, out, (size_t)g.V);
+}
+
+fipi_status fields_fft_c2r(fipi_ctx* ctx, const double* in, double* out) {
+    return ctx->prec == FIPI_MIXED ? c2r_t<float>(ctx, in, out) : c2r_t<double>(ctx, in, out);
+}
+
+template <typename T> static fipi_status grad_t(fipi_ctx* ctx, const double* c, double* out) {
+    const Geom& g = ctx->g;
+    T* tmp = (T*)ctx->fb.ureal;
+    fipi_status st = upload<T>(ctx, c, tmp, (size_t)g.V);
+    if (st != FIPI_OK) return st;
+    OpR2C<T> op{tmp, F<T>::S(ctx, 0), g.nx, g.ny};
+    launch_x<T, 0, 1, false>(ctx, "X forward", 1, NoAcc<OpR2C<T>>{op});
+    void* sp[1] = {ctx->fb.S[0]};
+    launch_y<T>(ctx, 1, sp, sp, -1);
+    ZOpStore<T, 1> zs{{F<T>::S(ctx, 0)}, {F<T>::S(ctx, 0)}, 0};
+    launch_z<T, 1>(ctx, "Z forward store", 2, zs, -1);
+    T* g3[3] = {tmp, tmp + g.V, tmp + 2 * g.V};
+    grad_from_chat<T>(ctx, F<T>::S(ctx, 0), g3);
+    FIPI_CUDA(ctx, cudaGetLastError());
+    return download<T>(ctx, tmp, out, (size_t)g.V * 3);
+}
+
+fipi_status fields_grad(fipi_ctx* ctx, const double* c, double* out) {
+    return ctx->prec == FIPI_MIXED ? grad_t<float>(ctx, c, out) : grad_t<double>(ctx, c, out);
+}
+
+const void* fields_real_c(fipi_ctx* ctx) { return ctx->fb.c; }
+const void* fields_real_grad(fipi_ctx* ctx, int d) { return ctx->fb.g[d]; }
+void* fields_spread_target(fipi_ctx* ctx, int d) { return ctx->fb.fsp[d]; }
+
+}  // namespace fipi

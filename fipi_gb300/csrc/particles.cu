@@ -1,0 +1,1010 @@
+// Lagrangian side of the FIPI step on sm_103a (main.cpp:283-316 and
+// cluster.cpp / element.cpp of the reference).
+//
+//  - cell list: key = i + j n + k n^2 with i = floor(p/d_cell + margin/d_cell)
+//    (cluster.cpp:234-259), a stable LSD radix sort of (key, particle id) and
+//    offsets by binary search; ids inside a cell are ascending, which is the
+//    order the reference's linked lists hold them in (linked_list.cpp:30-43);
+//  - contact forces one warp per home cell (cluster.cpp:268-369): each lane
+//    owns one particle of the cell and walks the 27 neighbour cells in the
+//    reference's (k, j, i) order; every pair is evaluated from the lower id's
+//    side exactly as the reference does and the result is applied with the
+//    reference's sign, so forces are deterministic and atomic-free;
+//  - interpolation, attachment force, Heun advection and periodic wrap per
+//    particle (field.cpp:223-248, element.cpp:149-280);
+//  - spreading (cluster.cpp:438-504) as a sorted segmented reduction: the
+//    8 corner records of every particle are radix-sorted by grid node,
+//    stable in particle id, and each node sums its records in ascending id,
+//    the order in which the reference's loop adds them.
+//
+// Positions are FP64 in every form.  This file is compiled with
+// -fmad=false so its FP64 expressions round exactly as the reference's.
+// TA is the arithmetic type of interpolation, contact forces and spreading
+// weights: double in the plain form, float in the mixed form.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "ctx.hpp"
+
+namespace fipi {
+
+struct PC {
+    int n;
+    int nc[3];
+    double dc[3];
+    double margin;
+    double L[3];
+    double r_eq, k_n, r_p, A, sigma, epsilon, pi, mu, dt;
+    double dx, dy, dz;
+    int N[3];
+    double tanh2;  // tanh(2.0), element.cpp:178
+};
+
+static PC make_pc(const fipi_ctx* ctx) {
+    const fipi_params& P = ctx->P;
+    PC c;
+    c.n = P.n_p;
+    for (int a = 0; a < 3; ++a) {
+        c.nc[a] = ctx->pb.ncell[a];
+        c.dc[a] = ctx->pb.dcell[a];
+    }
+    c.margin = P.margin;
+    c.L[0] = P.lx;
+    c.L[1] = P.ly;
+    c.L[2] = P.lz;
+    c.r_eq = P.r_eq;
+    c.k_n = P.k_n;
+    c.r_p = P.r_p;
+    c.A = P.A;
+    c.sigma = P.sigma;
+    c.epsilon = P.epsilon;
+    c.pi = P.pi;
+    c.mu = P.mu;
+    c.dt = P.dt;
+    c.dx = P.lx / P.nx;
+    c.dy = P.ly / P.ny;
+    c.dz = P.lz / P.nz;
+    c.N[0] = P.nx;
+    c.N[1] = P.ny;
+    c.N[2] = P.nz;
+    c.tanh2 = std::tanh(2.0);
+    return c;
+}
+
+// ramp (primitive.cpp:205-212)
+static double ramp(double t, double thr) {
+    if (t < 0) return 0.0;
+    if (t >= 0 && t < thr) return t / thr;
+    return 1.0;
+}
+
+// ------------------------------------------------------------ radix sort
+// Stable LSD radix sort of (key, value) pairs, 8-bit digits.
+constexpr int RS_T = 256;
+constexpr int RS_TILE = 2048;
+
+__global__ void k_rs_hist(const unsigned* __restrict__ keys, int n, int shift, unsigned* hist, int nblk) {
+    __shared__ unsigned cnt[256];
+    cnt[threadIdx.x] = 0;
+    __syncthreads();
+    const int base = blockIdx.x * RS_TILE;
+    for (int i = threadIdx.x; i < RS_TILE; i += RS_T) {
+        const int s = base + i;
+        if (s < n) atomicAdd(&cnt[(keys[s] >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    hist[threadIdx.x * nblk + blockIdx.x] = cnt[threadIdx.x];
+}
+
+// Exclusive scan of `total` entries in one block of 1024 threads.
+__global__ void k_scan_excl(unsigned* a, int total) {
+    __shared__ unsigned part[1024];
+    const int t = threadIdx.x;
+    const int chunk = (total + 1023) / 1024;
+    const int b = t * chunk, e = min(total, b + chunk);
+    unsigned s = 0;
+    for (int i = b; i < e; ++i) s += a[i];
+    part[t] = s;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {
+        unsigned v = (t >= off) ? part[t - off] : 0u;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    unsigned run = part[t] - s;
+    for (int i = b; i < e; ++i) {
+        const unsigned x = a[i];
+        a[i] = run;
+        run += x;
+    }
+}
+
+__global__ void k_rs_scatter(const unsigned* __restrict__ kin, const unsigned* __restrict__ vin,
+                             unsigned* __restrict__ kout, unsigned* __restrict__ vout, int n, int shift,
+                             const unsigned* __restrict__ hist, int nblk) {
+    __shared__ unsigned base[256];
+    __shared__ unsigned wcnt[RS_T / 32][256];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    base[tid] = hist[tid * nblk + blockIdx.x];
+    for (int w = 0; w < RS_T / 32; ++w) wcnt[w][tid] = 0;
+    __syncthreads();
+    const unsigned lt = (1u << lane) - 1u;
+    for (int r = 0; r < RS_TILE; r += RS_T) {
+        const int s = blockIdx.x * RS_TILE + r + tid;
+        const bool valid = s < n;
+        unsigned key = 0, val = 0, d = 256;
+        if (valid) {
+            key = kin[s];
+            val = vin[s];
+            d = (key >> shift) & 255u;
+        }
+        const unsigned peers = __match_any_sync(0xffffffffu, d);
+        const unsigned rank = __popc(peers & lt);
+        if (valid && rank == 0) wcnt[warp][d] = __popc(peers);
+        __syncthreads();
+        {
+            unsigned run = base[tid];
+            for (int w = 0; w < RS_T / 32; ++w) {
+                const unsigned c = wcnt[w][tid];
+                wcnt[w][tid] = run;
+                run += c;
+            }
+            base[tid] = run;
+        }
+        __syncthreads();
+        if (valid) {
+            const unsigned pos = wcnt[warp][d] + rank;
+            kout[pos] = key;
+            vout[pos] = val;
+        }
+        __syncthreads();
+        for (int w = 0; w < RS_T / 32; ++w) wcnt[w][tid] = 0;
+        __syncthreads();
+    }
+}
+
+// Sorts (k, v) by the low `bits` bits of k; results end in (k, v).
+static void radix_sort(fipi_ctx* ctx, unsigned*& k, unsigned*& v, unsigned*& k2, unsigned*& v2, int n, int bits) {
+    if (n <= 0) return;
+    const int nblk = (n + RS_TILE - 1) / RS_TILE;
+    for (int shift = 0; shift < bits; shift += 8) {
+        { LaunchScope ls_(ctx, "radix sort hist", 0.0); k_rs_hist<<<nblk, RS_T, 0, ctx->stream>>>(k, n, shift, ctx->pb.hist, nblk); }
+        { LaunchScope ls_(ctx, "radix sort scan", 0.0); k_scan_excl<<<1, 1024, 0, ctx->stream>>>(ctx->pb.hist, 256 * nblk); }
+        { LaunchScope ls_(ctx, "radix sort scatter", 0.0); k_rs_scatter<<<nblk, RS_T, 0, ctx->stream>>>(k, v, k2, v2, n, shift, ctx->pb.hist, nblk); }
+        std::swap(k, k2);
+        std::swap(v, v2);
+    }
+}
+
+static int bits_for(long long maxval) {
+    int b = 1;
+    while ((1ll << b) <= maxval) ++b;
+    return b;
+}
+
+// ------------------------------------------------------------ cell list
+__device__ __forceinline__ int cell_coord(double x, double dcell, double margin) {
+    return (int)floor(x / dcell + margin / dcell);  // cluster.cpp:234-236
+}
+
+__global__ void k_cell_keys(PC pc, const double* __restrict__ p, unsigned* keys, unsigned* ids, int* status) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= pc.n) return;
+    const double x = p[i], y = p[pc.n + i], z = p[2 * pc.n + i];
+    int c[3] = {cell_coord(x, pc.dc[0], pc.margin), cell_coord(y, pc.dc[1], pc.margin),
+                cell_coord(z, pc.dc[2], pc.margin)};
+    bool bad = !(isfinite(x) && isfinite(y) && isfinite(z));
+    for (int a = 0; a < 3; ++a) {
+        if (c[a] < 0 || c[a] >= pc.nc[a]) {
+            bad = true;
+            c[a] = c[a] < 0 ? 0 : pc.nc[a] - 1;
+        }
+    }
+    if (bad) atomicOr(status, isfinite(x) && isfinite(y) && isfinite(z) ? ERR_OUT_OF_RANGE : ERR_NONFINITE);
+    keys[i] = (unsigned)(c[0] + c[1] * pc.nc[0] + c[2] * pc.nc[0] * pc.nc[1]);
+    ids[i] = (unsigned)i;
+}
+
+// off[c] = first sorted position whose key >= c, c in [0, ncells].
+__global__ void k_cell_offsets(const unsigned* __restrict__ keys, int n, int* off, int ncells) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c > ncells) return;
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if ((int)keys[mid] < c) lo = mid + 1;
+        else hi = mid;
+    }
+    off[c] = lo;
+}
+
+static void build_cells(fipi_ctx* ctx, const double* p_dev) {
+    ParticleBufs& b = ctx->pb;
+    const PC pc = make_pc(ctx);
+    const int n = b.n;
+    { LaunchScope ls_(ctx, "cell keys", 0.0); k_cell_keys<<<(n + 255) / 256, 256, 0, ctx->stream>>>(pc, p_dev, b.keys, b.ids, ctx->status); }
+    radix_sort(ctx, b.keys, b.ids, b.keys_alt, b.ids_alt, n, bits_for(b.ncells - 1));
+    { LaunchScope ls_(ctx, "cell offsets", 0.0); k_cell_offsets<<<(b.ncells + 1 + 255) / 256, 256, 0, ctx->stream>>>(b.keys, n, b.cell_off, b.ncells); }
+}
+
+// ------------------------------------------------------------ contact forces
+// Separation of exactly coincident particles: the reference draws
+// rand()%1000/1e3*2 r_p - r_p per component (cluster.cpp:328-336); here the
+// same 1e-3 lattice is drawn from a hash of the pair (lower id first).
+__device__ __forceinline__ void coincident_d(int a, int b, double r_p, double d[3]) {
+    unsigned long long h = ((unsigned long long)(unsigned)a << 32) ^ (unsigned long long)(unsigned)b;
+    for (int k = 0; k < 3; ++k) {
+        h += 0x9E3779B97F4A7C15ull;
+        unsigned long long z = h;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        d[k] = (double)(z % 1000ull) / 1e3 * 2.0 * r_p - r_p;
+    }
+}
+
+// MODE 0: forces (+ packing-energy terms); 1: count pairs (lower id side);
+// 2: write pairs at pair_off[i].
+template <typename TA, int MODE>
+__global__ void k_f_pp(PC pc, const double* __restrict__ p, const unsigned* __restrict__ ids,
+                       const int* __restrict__ off, double rmp, const double* __restrict__ f_pi,
+                       const int* __restrict__ it_mark, double* f_pp, double* tau_part, int* pair_cnt,
+                       const int* __restrict__ pair_off, int* pairs) {
+    const int lane = threadIdx.x & 31;
+    const int cell = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int ncells = pc.nc[0] * pc.nc[1] * pc.nc[2];
+    if (cell >= ncells) return;
+    const int n = pc.n;
+    const int ci = cell % pc.nc[0], cj = (cell / pc.nc[0]) % pc.nc[1], ck = cell / (pc.nc[0] * pc.nc[1]);
+    const int beg = off[cell], end = off[cell + 1];
+    const double T0 = pc.dc[0] * (pc.nc[0] - 2), T1 = pc.dc[1] * (pc.nc[1] - 2), T2 = pc.dc[2] * (pc.nc[2] - 2);
+    bool mark_ok = false;
+    if (MODE == 0 && f_pi != nullptr) {
+        const int m = *it_mark;
+        if (m >= 0) {
+            const double a = f_pi[m], b = f_pi[n + m], c = f_pi[2 * n + m];
+            mark_ok = sqrt(a * a + b * b + c * c) != 0.0;
+        }
+    }
+    for (int base = beg; base < end; base += 32) {
+        const int s = base + lane;
+        const bool active = s < end;
+        const int i = active ? (int)ids[s] : 0;
+        const double xi = p[i], yi = p[n + i], zi = p[2 * n + i];
+        bool own_ok = false;
+        if (MODE == 0 && f_pi != nullptr && active) {
+            const double a = f_pi[i], b = f_pi[n + i], c = f_pi[2 * n + i];
+            own_ok = sqrt(a * a + b * b + c * c) != 0.0;
+        }
+        TA ax = TA(0), ay = TA(0), az = TA(0);
+        double tau = 0.0;
+        int cnt = 0;
+        int wpos = (MODE == 2 && active) ? pair_off[i] : 0;
+        for (int dk = -1; dk <= 1; ++dk)
+            for (int dj = -1; dj <= 1; ++dj)
+                for (int di = -1; di <= 1; ++di) {
+                    const int co = (ci + di + pc.nc[0]) % pc.nc[0] + (cj + dj + pc.nc[1]) % pc.nc[1] * pc.nc[0] +
+                                   (ck + dk + pc.nc[2]) % pc.nc[2] * pc.nc[0] * pc.nc[1];
+                    const int qe = off[co + 1];
+                    for (int q = off[co]; q < qe; ++q) {
+                        const int j = (int)ids[q];
+                        const double xj = p[j], yj = p[n + j], zj = p[2 * n + j];
+                        if (!active || j == i) continue;
+                        const bool lo_side = i < j;  // the reference evaluates (it, id) with it < id
+                        double d[3];
+                        if (lo_side) {
+                            d[0] = xi - xj;
+                            d[1] = yi - yj;
+                            d[2] = zi - zj;
+                        } else {
+                            d[0] = xj - xi;
+                            d[1] = yj - yi;
+                            d[2] = zj - zi;
+                        }
+                        // cluster.cpp:319-326
+                        if (d[0] > T0) d[0] = d[0] - pc.L[0];
+                        else if (d[0] < -T0) d[0] = d[0] + pc.L[0];
+                        if (d[1] > T1) d[1] = d[1] - pc.L[1];
+                        else if (d[1] < -T1) d[1] = d[1] + pc.L[1];
+                        if (d[2] > T2) d[2] = d[2] - pc.L[2];
+                        else if (d[2] < -T2) d[2] = d[2] + pc.L[2];
+                        if (d[0] == 0.0 && d[1] == 0.0 && d[2] == 0.0)
+                            coincident_d(lo_side ? i : j, lo_side ? j : i, pc.r_p, d);
+                        const TA dx = (TA)d[0], dy = (TA)d[1], dz = (TA)d[2];
+                        const TA dn = sqrt(dx * dx + dy * dy + dz * dz);
+                        if (!(dn < (TA)pc.r_eq)) continue;
+                        if (MODE == 1) {
+                            if (lo_side) ++cnt;
+                            continue;
+                        }
+                        if (MODE == 2) {
+                            if (lo_side) {
+                                pairs[2 * wpos] = i;
+                                pairs[2 * wpos + 1] = j;
+                                ++wpos;
+                            }
+                            continue;
+                        }
+                        const TA sc = ((TA)pc.r_eq - dn) * (TA)rmp * (TA)pc.k_n;
+                        const TA fx = (dx / dn) * sc, fy = (dy / dn) * sc, fz = (dz / dn) * sc;
+                        if (lo_side) {
+                            ax = ax + fx;
+                            ay = ay + fy;
+                            az = az + fz;
+                            if (own_ok && mark_ok) {
+                                const double h0 = (double)fx * 0.5, h1 = (double)fy * 0.5, h2 = (double)fz * 0.5;
+                                tau += h0 * d[0] + h1 * d[1] + h2 * d[2];
+                            }
+                        } else {
+                            ax = ax - fx;
+                            ay = ay - fy;
+                            az = az - fz;
+                        }
+                    }
+                }
+        if (active) {
+            if (MODE == 0) {
+                f_pp[i] = (double)ax;
+                f_pp[n + i] = (double)ay;
+                f_pp[2 * n + i] = (double)az;
+                if (tau_part) tau_part[i] = tau;
+            } else if (MODE == 1) {
+                pair_cnt[i] = cnt;
+            }
+        }
+    }
+}
+
+// argmax of p_y with strict > from 0.0, first index wins (cluster.cpp:222-232).
+__global__ void k_it_mark(const double* __restrict__ py, int n, int* it_mark) {
+    __shared__ double bv[1024];
+    __shared__ int bi[1024];
+    double best = 0.0;
+    int idx = -1;
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+        if (py[i] > best) {
+            best = py[i];
+            idx = i;
+        }
+    bv[threadIdx.x] = best;
+    bi[threadIdx.x] = idx;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) {
+            const double ov = bv[threadIdx.x + s];
+            const int oi = bi[threadIdx.x + s];
+            if (oi >= 0 && (bi[threadIdx.x] < 0 || ov > bv[threadIdx.x] || (ov == bv[threadIdx.x] && oi < bi[threadIdx.x]))) {
+                bv[threadIdx.x] = ov;
+                bi[threadIdx.x] = oi;
+            }
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0 && bi[0] >= 0) *it_mark = bi[0];
+}
+
+__global__ void k_sum_tau(const double* __restrict__ part, int n, double* out) {
+    __shared__ double s[1024];
+    double a = 0.0;
+    const int chunk = (n + blockDim.x - 1) / blockDim.x;
+    const int b = threadIdx.x * chunk, e = min(n, b + chunk);
+    for (int i = b; i < e; ++i) a += part[i];
+    s[threadIdx.x] = a;
+    __syncthreads();
+    for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+        if (threadIdx.x < st) s[threadIdx.x] += s[threadIdx.x + st];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = s[0];
+}
+
+// ------------------------------------------------------------ per-particle stage
+// field::interpolate (field.cpp:223-248) of one real field.
+template <typename TF, typename TA>
+__device__ __forceinline__ TA interp(const TF* __restrict__ v, int i, int j, int k, int i1, int j1, int k1, TA m, TA nn,
+                                     TA o, int Nx, int Ny) {
+    const size_t sxy = (size_t)Nx * Ny;
+    TA val = (TA(1) - m) * (TA(1) - nn) * (TA(1) - o) * (TA)v[i + (size_t)j * Nx + k * sxy];
+    val += (TA(1) - m) * nn * (TA(1) - o) * (TA)v[i + (size_t)j1 * Nx + k * sxy];
+    val += m * (TA(1) - nn) * (TA(1) - o) * (TA)v[i1 + (size_t)j * Nx + k * sxy];
+    val += m * nn * (TA(1) - o) * (TA)v[i1 + (size_t)j1 * Nx + k * sxy];
+    val += (TA(1) - m) * (TA(1) - nn) * o * (TA)v[i + (size_t)j * Nx + k1 * sxy];
+    val += (TA(1) - m) * nn * o * (TA)v[i + (size_t)j1 * Nx + k1 * sxy];
+    val += m * (TA(1) - nn) * o * (TA)v[i1 + (size_t)j * Nx + k1 * sxy];
+    val += m * nn * o * (TA)v[i1 + (size_t)j1 * Nx + k1 * sxy];
+    return val;
+}
+
+__device__ __forceinline__ int wrapi(int i, int n) {
+    i %= n;
+    return i < 0 ? i + n : i;
+}
+
+// Interpolate nf fields at particle i -> out[0..nf).
+template <typename TF, typename TA>
+__device__ __forceinline__ void interp_fields(const PC& pc, double x, double y, double z, const TF* const* f, int nf,
+                                              TA* out) {
+    const double fx = floor(x / pc.dx), fy = floor(y / pc.dy), fz = floor(z / pc.dz);
+    const int i = wrapi((int)fx, pc.N[0]), j = wrapi((int)fy, pc.N[1]), k = wrapi((int)fz, pc.N[2]);
+    const TA m = (TA)(x / pc.dx - fx), nn = (TA)(y / pc.dy - fy), o = (TA)(z / pc.dz - fz);
+    const int i1 = (i + 1) % pc.N[0], j1 = (j + 1) % pc.N[1], k1 = (k + 1) % pc.N[2];
+    for (int q = 0; q < nf; ++q) out[q] = interp<TF, TA>(f[q], i, j, k, i1, j1, k1, m, nn, o, pc.N[0], pc.N[1]);
+}
+
+// element::get_f_pi (element.cpp:169-191) with f_mag = -A pi (d - r cos_theta) sigma.
+__device__ __forceinline__ void f_pi_of(const PC& pc, double phi, double gx, double gy, double gz, double r, double ct,
+                                        double* f) {
+    const double gn = sqrt(gx * gx + gy * gy + gz * gz);
+    if (fabs(phi) <= pc.tanh2 && gn != 0.0) {
+        const double d = 0.5 * log((1.0 + phi) / (1.0 - phi)) * 1.4142135623730951 * pc.epsilon;
+        double f_mag;
+        if (fabs(d) < r) f_mag = -pc.A * pc.pi * (d - r * ct) * pc.sigma;
+        else f_mag = 0.0;
+        f[0] = gx / gn * f_mag;
+        f[1] = gy / gn * f_mag;
+        f[2] = gz / gn * f_mag;
+    } else {
+        f[0] = f[1] = f[2] = 0.0;
+    }
+}
+
+// element::advect (element.cpp:250-267) and enforce_bc (element.cpp:271-280)
+// for one particle; uf = 0 and f_ext = 0 as in the reference.
+__device__ __forceinline__ void advect_one(const PC& pc, int stage, const double* fpi, const double* fpp, double r,
+                                           double* p, double* po, double* uo) {
+    double v[3];
+    for (int a = 0; a < 3; ++a) {
+        double F = fpi[a] + 0.0;
+        F = F + fpp[a];
+        v[a] = 0.0 + F / 6.0 / pc.pi / pc.mu / r;
+    }
+    if (stage == 1) {
+        for (int a = 0; a < 3; ++a) {
+            uo[a] = v[a];
+            po[a] = p[a];
+            p[a] = p[a] + v[a] * pc.dt;
+        }
+    } else {
+        const double hdt = 0.5 * pc.dt;
+        for (int a = 0; a < 3; ++a) p[a] = po[a] + (uo[a] + v[a]) * hdt;
+    }
+    for (int a = 0; a < 3; ++a) p[a] = fmod(p[a] + pc.L[a], pc.L[a]);
+}
+
+// Stage part 1: interpolate c, grad c at the stage-start positions and form
+// f_pi (cluster::interpolate_local_variables + compute_f_pi).
+template <typename TF, typename TA>
+__global__ void k_stage_fpi(PC pc, const TF* __restrict__ c, const TF* __restrict__ g0, const TF* __restrict__ g1,
+                            const TF* __restrict__ g2, const double* __restrict__ p, double* f_pi,
+                            const double* __restrict__ r, const double* __restrict__ cth) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = pc.n;
+    if (i >= n) return;
+    const TF* fl[4] = {c, g0, g1, g2};
+    TA vals[4];
+    interp_fields<TF, TA>(pc, p[i], p[n + i], p[2 * n + i], fl, 4, vals);
+    double fpi[3];
+    f_pi_of(pc, (double)vals[0], (double)vals[1], (double)vals[2], (double)vals[3], r[i], cth[i], fpi);
+    for (int a = 0; a < 3; ++a) f_pi[a * n + i] = fpi[a];
+}
+
+// Stage part 2: advect with this stage's f_pi + f_pp, then wrap.
+__global__ void k_stage_advect(PC pc, int stage, double* p, double* p_old, double* u_old,
+                               const double* __restrict__ f_pi, const double* __restrict__ f_pp,
+                               const double* __restrict__ r, int* status) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = pc.n;
+    if (i >= n) return;
+    double pp[3] = {p[i], p[n + i], p[2 * n + i]};
+    double po[3] = {p_old[i], p_old[n + i], p_old[2 * n + i]};
+    double uo[3] = {u_old[i], u_old[n + i], u_old[2 * n + i]};
+    const double fpi[3] = {f_pi[i], f_pi[n + i], f_pi[2 * n + i]};
+    const double fpp[3] = {f_pp[i], f_pp[n + i], f_pp[2 * n + i]};
+    advect_one(pc, stage, fpi, fpp, r[i], pp, po, uo);
+    for (int a = 0; a < 3; ++a) {
+        p[a * n + i] = pp[a];
+        p_old[a * n + i] = po[a];
+        u_old[a * n + i] = uo[a];
+    }
+    if (!(isfinite(pp[0]) && isfinite(pp[1]) && isfinite(pp[2]))) atomicOr(status, ERR_NONFINITE);
+}
+
+// ------------------------------------------------------------ spreading
+// Corner order of cluster.cpp:462-500: (0,0,0) (1,0,0) (1,1,0) (1,0,1) (1,1,1) (0,0,1) (0,1,0) (0,1,1).
+__constant__ int c_corner[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {1, 0, 1}, {1, 1, 1}, {0, 0, 1}, {0, 1, 0}, {0, 1, 1}};
+
+__device__ __forceinline__ void cell_and_frac(const PC& pc, double X, double Y, double Z, int* ix, double* fr) {
+    const double fx = floor(X / pc.dx), fy = floor(Y / pc.dy), fz = floor(Z / pc.dz);
+    ix[0] = wrapi((int)fx, pc.N[0]);
+    ix[1] = wrapi((int)fy, pc.N[1]);
+    ix[2] = wrapi((int)fz, pc.N[2]);
+    fr[0] = X / pc.dx - fx;
+    fr[1] = Y / pc.dy - fy;
+    fr[2] = Z / pc.dz - fz;
+}
+
+__global__ void k_spread_records(PC pc, const double* __restrict__ p, unsigned* keys, unsigned* vals) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = pc.n;
+    if (i >= n) return;
+    int ix[3];
+    double fr[3];
+    cell_and_frac(pc, p[i], p[n + i], p[2 * n + i], ix, fr);
+    for (int c = 0; c < 8; ++c) {
+        const int x = (ix[0] + c_corner[c][0]) % pc.N[0];
+        const int y = (ix[1] + c_corner[c][1]) % pc.N[1];
+        const int z = (ix[2] + c_corner[c][2]) % pc.N[2];
+        keys[8 * i + c] = (unsigned)(x + (size_t)y * pc.N[0] + (size_t)z * pc.N[0] * pc.N[1]);
+        vals[8 * i + c] = (unsigned)(8 * i + c);
+    }
+}
+
+template <typename TF>
+__global__ void k_spread_clear(const unsigned* __restrict__ nodes, int m, TF* f0, TF* f1, TF* f2) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= m) return;
+    const unsigned nd = nodes[s];
+    f0[nd] = TF(0);
+    f1[nd] = TF(0);
+    f2[nd] = TF(0);
+}
+
+// Weight products of cluster.cpp:463-500 for corner c, left to right from f.
+template <typename TA>
+__device__ __forceinline__ TA corner_value(TA f, int c, TA o, TA pp, TA q) {
+    switch (c) {
+        case 0: return f * (TA(1) - o) * (TA(1) - pp) * (TA(1) - q);
+        case 1: return f * o * (TA(1) - pp) * (TA(1) - q);
+        case 2: return f * o * pp * (TA(1) - q);
+        case 3: return f * o * (TA(1) - pp) * q;
+        case 4: return f * o * pp * q;
+        case 5: return f * (TA(1) - o) * (TA(1) - pp) * q;
+        case 6: return f * (TA(1) - o) * pp * (TA(1) - q);
+        default: return f * (TA(1) - o) * pp * q;
+    }
+}
+
+template <typename TF, typename TA>
+__global__ void k_spread_reduce(PC pc, const unsigned* __restrict__ keys, const unsigned* __restrict__ vals, int m,
+                                const double* __restrict__ p, const double* __restrict__ f_pp, TF* f0, TF* f1, TF* f2) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= m) return;
+    const unsigned node = keys[s];
+    if (s > 0 && keys[s - 1] == node) return;
+    const int n = pc.n;
+    TA acc[3] = {TA(0), TA(0), TA(0)};
+    for (int q = s; q < m && keys[q] == node; ++q) {
+        const unsigned rec = vals[q];
+        const int i = (int)(rec >> 3), c = (int)(rec & 7u);
+        int ix[3];
+        double fr[3];
+        cell_and_frac(pc, p[i], p[n + i], p[2 * n + i], ix, fr);
+        for (int a = 0; a < 3; ++a) {
+            const double f = (f_pp[a * n + i] + 0.0) / pc.dx / pc.dy / pc.dz;
+            acc[a] += corner_value<TA>((TA)f, c, (TA)fr[0], (TA)fr[1], (TA)fr[2]);
+        }
+    }
+    f0[node] = (TF)acc[0];
+    f1[node] = (TF)acc[1];
+    f2[node] = (TF)acc[2];
+}
+
+// ------------------------------------------------------------ orchestration
+// `step_grid`: the target is the step's persistent spread grid, which only
+// the nodes written by the previous spread need clearing in (the whole grid
+// after a fine-grained call reused the record buffers).
+template <typename T>
+static void spread_t(fipi_ctx* ctx, const double* p, const double* f_pp, T* const f3[3], bool step_grid) {
+    ParticleBufs& b = ctx->pb;
+    const PC pc = make_pc(ctx);
+    const int n = b.n, m = 8 * n;
+    if (step_grid) {
+        if (b.sp_prev_valid) {
+            { LaunchScope ls_(ctx, "spread clear", 0.0); k_spread_clear<T><<<(m + 255) / 256, 256, 0, ctx->stream>>>(b.sp_prev, m, f3[0], f3[1], f3[2]); }
+        } else {
+            for (int a = 0; a < 3; ++a) cudaMemsetAsync(f3[a], 0, sizeof(T) * (size_t)ctx->g.V, ctx->stream);
+        }
+    }
+    { LaunchScope ls_(ctx, "spread records", 0.0); k_spread_records<<<(n + 255) / 256, 256, 0, ctx->stream>>>(pc, p, b.sp_keys, b.sp_vals); }
+    radix_sort(ctx, b.sp_keys, b.sp_vals, b.sp_keys_alt, b.sp_vals_alt, m, bits_for(ctx->g.V - 1));
+    { LaunchScope ls_(ctx, "spread segmented reduce", 0.0); k_spread_reduce<T, T><<<(m + 255) / 256, 256, 0, ctx->stream>>>(pc, b.sp_keys, b.sp_vals, m, p, f_pp, f3[0], f3[1], f3[2]); }
+    if (step_grid) {
+        cudaMemcpyAsync(b.sp_prev, b.sp_keys, sizeof(unsigned) * m, cudaMemcpyDeviceToDevice, ctx->stream);
+        b.sp_prev_valid = 1;
+    } else {
+        b.sp_prev_valid = 0;  // the record buffers no longer describe the step grid
+    }
+}
+
+void particles_spread(fipi_ctx* ctx) {
+    if (ctx->pb.n <= 0 || !ctx->P.switch_particle) return;
+    if (ctx->prec == FIPI_MIXED) {
+        float* f3[3] = {(float*)ctx->fb.fsp[0], (float*)ctx->fb.fsp[1], (float*)ctx->fb.fsp[2]};
+        spread_t<float>(ctx, ctx->pb.p, ctx->pb.f_pp, f3, true);
+    } else {
+        double* f3[3] = {(double*)ctx->fb.fsp[0], (double*)ctx->fb.fsp[1], (double*)ctx->fb.fsp[2]};
+        spread_t<double>(ctx, ctx->pb.p, ctx->pb.f_pp, f3, true);
+    }
+}
+
+// compute_f_pp; with `tau` the packing energy of cluster.cpp:350-353 is
+// accumulated per particle and summed in a fixed order.
+template <typename TA>
+static void f_pp_launch(fipi_ctx* ctx, const double* p, double rmp, const double* f_pi, double* f_pp, bool tau) {
+    ParticleBufs& b = ctx->pb;
+    const PC pc = make_pc(ctx);
+    const int warps = b.ncells;
+    const int blocks = (warps * 32 + 255) / 256;
+    if (tau) { LaunchScope ls_(ctx, "it_mark argmax", 0.0); k_it_mark<<<1, 1024, 0, ctx->stream>>>(p + b.n, b.n, b.it_mark); }
+    { LaunchScope ls_(ctx, "contact forces (warp per cell)", 0.0); k_f_pp<TA, 0><<<blocks, 256, 0, ctx->stream>>>(pc, p, b.ids, b.cell_off, rmp, tau ? f_pi : nullptr, b.it_mark,
+                                                  f_pp, b.tau_part, nullptr, nullptr, nullptr); }
+    if (tau) { LaunchScope ls_(ctx, "packing energy sum", 0.0); k_sum_tau<<<1, 1024, 0, ctx->stream>>>(b.tau_part, b.n, b.tau); }
+}
+
+template <typename T> static void step_t(fipi_ctx* ctx, int t) {
+    ParticleBufs& b = ctx->pb;
+    const PC pc = make_pc(ctx);
+    const double rmp = ramp((double)(t + 1), 0.2 * ctx->P.t_end);  // compute_f_pp(t+1), main.cpp:299
+    const int n = b.n;
+    const int nb = (n + 255) / 256;
+    for (int stage = 1; stage <= 2; ++stage) {
+        // interpolate_local_variables, sorting, compute_f_pi, compute_f_pp(t+1),
+        // compute_f_ext (zero), advect, enforce_bc  (main.cpp:295-314)
+        { LaunchScope ls_(ctx, "stage interpolate + f_pi", 0.0); k_stage_fpi<T, T><<<nb, 256, 0, ctx->stream>>>(pc, (const T*)ctx->fb.c, (const T*)ctx->fb.g[0],
+                                                     (const T*)ctx->fb.g[1], (const T*)ctx->fb.g[2], b.p, b.f_pi,
+                                                     b.r, b.cth); }
+        build_cells(ctx, b.p);
+        f_pp_launch<T>(ctx, b.p, rmp, b.f_pi, b.f_pp, ctx->track_tau);
+        { LaunchScope ls_(ctx, "stage advect + wrap", 0.0); k_stage_advect<<<nb, 256, 0, ctx->stream>>>(pc, stage, b.p, b.p_old, b.u_old, b.f_pi, b.f_pp, b.r,
+                                                    ctx->status); }
+    }
+}
+
+void particles_step(fipi_ctx* ctx, int t) {
+    if (ctx->pb.n <= 0 || !ctx->P.switch_particle) return;
+    if (ctx->prec == FIPI_MIXED) step_t<float>(ctx, t);
+    else step_t<double>(ctx, t);
+}
+
+// ------------------------------------------------------------ allocation
+fipi_status particles_alloc(fipi_ctx* ctx) {
+    ParticleBufs& b = ctx->pb;
+    const fipi_params& P = ctx->P;
+    b.n = P.n_p;
+    fipi_cell_geometry(&P, b.ncell, b.dcell);
+    b.ncells = b.ncell[0] * b.ncell[1] * b.ncell[2];
+    const int n = b.n > 0 ? b.n : 1;
+    auto A = [&](void** ptr, size_t bytes) -> cudaError_t {
+        cudaError_t e = cudaMalloc(ptr, bytes);
+        if (e == cudaSuccess) {
+            ctx->device_bytes += bytes;
+            e = cudaMemsetAsync(*ptr, 0, bytes, ctx->stream);
+        }
+        return e;
+    };
+    FIPI_CUDA(ctx, A((void**)&b.p, sizeof(double) * 3 * n));
+    FIPI_CUDA(ctx, A((void**)&b.p_old, sizeof(double) * 3 * n));
+    FIPI_CUDA(ctx, A((void**)&b.u_old, sizeof(double) * 3 * n));
+    FIPI_CUDA(ctx, A((void**)&b.f_pp, sizeof(double) * 3 * n));
+    FIPI_CUDA(ctx, A((void**)&b.f_pi, sizeof(double) * 3 * n));
+    FIPI_CUDA(ctx, A((void**)&b.r, sizeof(double) * n));
+    FIPI_CUDA(ctx, A((void**)&b.cth, sizeof(double) * n));
+    FIPI_CUDA(ctx, A((void**)&b.keys, sizeof(unsigned) * n));
+    FIPI_CUDA(ctx, A((void**)&b.keys_alt, sizeof(unsigned) * n));
+    FIPI_CUDA(ctx, A((void**)&b.ids, sizeof(unsigned) * n));
+    FIPI_CUDA(ctx, A((void**)&b.ids_alt, sizeof(unsigned) * n));
+    FIPI_CUDA(ctx, A((void**)&b.cell_off, sizeof(int) * (b.ncells + 1)));
+    FIPI_CUDA(ctx, A((void**)&b.cell_cnt, sizeof(int) * (b.ncells + 1)));
+    FIPI_CUDA(ctx, A((void**)&b.sp_keys, sizeof(unsigned) * 8 * n));
+    FIPI_CUDA(ctx, A((void**)&b.sp_keys_alt, sizeof(unsigned) * 8 * n));
+    FIPI_CUDA(ctx, A((void**)&b.sp_vals, sizeof(unsigned) * 8 * n));
+    FIPI_CUDA(ctx, A((void**)&b.sp_vals_alt, sizeof(unsigned) * 8 * n));
+    FIPI_CUDA(ctx, A((void**)&b.sp_prev, sizeof(unsigned) * 8 * n));
+    b.hist_cap = 256 * ((8 * n + RS_TILE - 1) / RS_TILE + 1);
+    FIPI_CUDA(ctx, A((void**)&b.hist, sizeof(unsigned) * b.hist_cap));
+    FIPI_CUDA(ctx, A((void**)&b.tau_part, sizeof(double) * n));
+    FIPI_CUDA(ctx, A((void**)&b.it_mark, sizeof(int)));
+    FIPI_CUDA(ctx, cudaMemsetAsync(b.it_mark, 0xff, sizeof(int), ctx->stream));
+    FIPI_CUDA(ctx, A((void**)&b.tau, sizeof(double)));
+    b.sp_prev_valid = 0;
+    return FIPI_OK;
+}
+
+void particles_free(fipi_ctx* ctx) {
+    ParticleBufs& b = ctx->pb;
+    void* all[] = {b.p, b.p_old, b.u_old, b.f_pp, b.f_pi, b.r, b.cth, b.keys, b.keys_alt, b.ids, b.ids_alt,
+                   b.cell_off, b.cell_cnt, b.sp_keys, b.sp_keys_alt, b.sp_vals, b.sp_vals_alt, b.sp_prev,
+                   b.hist, b.tau_part, b.it_mark, b.tau};
+    for (void* p : all)
+        if (p) cudaFree(p);
+    b = ParticleBufs{};
+}
+
+// ------------------------------------------------------------ fine-grained entry points
+// Host AoS (n x 3) <-> device SoA (3 x n) staging.
+static fipi_status to_dev_soa(fipi_ctx* ctx, const double* h, double* d, int n) {
+    std::vector<double> s((size_t)3 * n);
+    for (int i = 0; i < n; ++i)
+        for (int a = 0; a < 3; ++a) s[(size_t)a * n + i] = h[3 * i + a];
+    FIPI_CUDA(ctx, h2d(ctx, d, s.data(), sizeof(double) * 3 * n));
+    return FIPI_OK;
+}
+
+static fipi_status from_dev_soa(fipi_ctx* ctx, const double* d, double* h, int n) {
+    std::vector<double> s((size_t)3 * n);
+    FIPI_CUDA(ctx, d2h(ctx, s.data(), d, sizeof(double) * 3 * n));
+    for (int i = 0; i < n; ++i)
+        for (int a = 0; a < 3; ++a) h[3 * i + a] = s[(size_t)a * n + i];
+    return FIPI_OK;
+}
+
+struct DevScratch {
+    fipi_ctx* ctx;
+    std::vector<void*> ptrs;
+    template <typename X> X* get(size_t count) {
+        void* p = nullptr;
+        if (cudaMalloc(&p, sizeof(X) * (count ? count : 1)) != cudaSuccess) return nullptr;
+        ptrs.push_back(p);
+        return (X*)p;
+    }
+    ~DevScratch() {
+        for (void* p : ptrs) cudaFree(p);
+    }
+};
+
+static fipi_status read_status(fipi_ctx* ctx) {
+    int st = 0;
+    FIPI_CUDA(ctx, d2h(ctx, &st, ctx->status, sizeof(int)));
+    FIPI_CUDA(ctx, cudaMemsetAsync(ctx->status, 0, sizeof(int), ctx->stream));
+    if (st & ERR_NONFINITE) return set_error(ctx, FIPI_ERR_NONFINITE, "non-finite particle position");
+    if (st & ERR_OUT_OF_RANGE)
+        return set_error(ctx, FIPI_ERR_OUT_OF_RANGE, "particle out of sorting range (cluster.cpp:238-257)");
+    return FIPI_OK;
+}
+
+fipi_status particles_cells_build(fipi_ctx* ctx, const double* p, int* keys, int* sorted, int* offsets) {
+    ParticleBufs& b = ctx->pb;
+    const int n = b.n;
+    DevScratch ds{ctx};
+    double* pd = ds.get<double>(3 * (size_t)n);
+    if (!pd) return set_error(ctx, FIPI_ERR_CUDA, "cudaMalloc failed");
+    fipi_status st = to_dev_soa(ctx, p, pd, n);
+    if (st != FIPI_OK) return st;
+    build_cells(ctx, pd);
+    FIPI_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    st = read_status(ctx);
+    if (st != FIPI_OK) return st;
+    // keys are needed per particle id: the sorted keys follow the sorted ids
+    std::vector<unsigned> k(n), id(n);
+    FIPI_CUDA(ctx, d2h(ctx, k.data(), b.keys, sizeof(unsigned) * n));
+    FIPI_CUDA(ctx, d2h(ctx, id.data(), b.ids, sizeof(unsigned) * n));
+    if (keys)
+        for (int s = 0; s < n; ++s) keys[id[s]] = (int)k[s];
+    if (sorted)
+        for (int s = 0; s < n; ++s) sorted[s] = (int)id[s];
+    if (offsets) FIPI_CUDA(ctx, d2h(ctx, offsets, b.cell_off, sizeof(int) * (b.ncells + 1)));
+    return FIPI_OK;
+}
+
+fipi_status particles_f_pp(fipi_ctx* ctx, const double* p, int t, const double* f_pi, double* f_pp, double* tau) {
+    ParticleBufs& b = ctx->pb;
+    const int n = b.n;
+    DevScratch ds{ctx};
+    double* pd = ds.get<double>(3 * (size_t)n);
+    double* fpid = ds.get<double>(3 * (size_t)n);
+    double* fpp = ds.get<double>(3 * (size_t)n);
+    if (!pd || !fpid || !fpp) return set_error(ctx, FIPI_ERR_CUDA, "cudaMalloc failed");
+    fipi_status st = to_dev_soa(ctx, p, pd, n);
+    if (st != FIPI_OK) return st;
+    if (f_pi) {
+        st = to_dev_soa(ctx, f_pi, fpid, n);
+        if (st != FIPI_OK) return st;
+    }
+    build_cells(ctx, pd);
+    const double rmp = ramp((double)t, 0.2 * ctx->P.t_end);
+    if (f_pi) FIPI_CUDA(ctx, cudaMemsetAsync(b.it_mark, 0xff, sizeof(int), ctx->stream));
+    if (ctx->prec == FIPI_MIXED) f_pp_launch<float>(ctx, pd, rmp, f_pi ? fpid : nullptr, fpp, f_pi != nullptr);
+    else f_pp_launch<double>(ctx, pd, rmp, f_pi ? fpid : nullptr, fpp, f_pi != nullptr);
+    FIPI_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    st = read_status(ctx);
+    if (st != FIPI_OK) return st;
+    if (f_pp) {
+        st = from_dev_soa(ctx, fpp, f_pp, n);
+        if (st != FIPI_OK) return st;
+    }
+    if (tau) {
+        if (f_pi) FIPI_CUDA(ctx, d2h(ctx, tau, b.tau, sizeof(double)));
+        else *tau = 0.0;
+    }
+    return FIPI_OK;
+}
+
+fipi_status particles_pairs(fipi_ctx* ctx, const double* p, int* pairs, int max_pairs, int* n_pairs) {
+    ParticleBufs& b = ctx->pb;
+    const int n = b.n;
+    DevScratch ds{ctx};
+    double* pd = ds.get<double>(3 * (size_t)n);
+    int* cnt = ds.get<int>(n);
+    int* offd = ds.get<int>(n);
+    if (!pd || !cnt || !offd) return set_error(ctx, FIPI_ERR_CUDA, "cudaMalloc failed");
+    fipi_status st = to_dev_soa(ctx, p, pd, n);
+    if (st != FIPI_OK) return st;
+    build_cells(ctx, pd);
+    const PC pc = make_pc(ctx);
+    const int blocks = (b.ncells * 32 + 255) / 256;
+    { LaunchScope ls_(ctx, "contact forces (warp per cell)", 0.0); k_f_pp<double, 1><<<blocks, 256, 0, ctx->stream>>>(pc, pd, b.ids, b.cell_off, 1.0, nullptr, nullptr, nullptr,
+                                                      nullptr, cnt, nullptr, nullptr); }
+    FIPI_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    st = read_status(ctx);
+    if (st != FIPI_OK) return st;
+    std::vector<int> hc(n), ho(n);
+    FIPI_CUDA(ctx, d2h(ctx, hc.data(), cnt, sizeof(int) * n));
+    long long total = 0;
+    for (int i = 0; i < n; ++i) {
+        ho[i] = (int)total;
+        total += hc[i];
+    }
+    *n_pairs = (int)total;
+    if (!pairs || total == 0) return FIPI_OK;
+    int* pr = ds.get<int>(2 * (size_t)total);
+    if (!pr) return set_error(ctx, FIPI_ERR_CUDA, "cudaMalloc failed");
+    FIPI_CUDA(ctx, h2d(ctx, offd, ho.data(), sizeof(int) * n));
+    { LaunchScope ls_(ctx, "contact forces (warp per cell)", 0.0); k_f_pp<double, 2><<<blocks, 256, 0, ctx->stream>>>(pc, pd, b.ids, b.cell_off, 1.0, nullptr, nullptr, nullptr,
+                                                      nullptr, nullptr, offd, pr); }
+    std::vector<int> hp(2 * (size_t)total);
+    FIPI_CUDA(ctx, d2h(ctx, hp.data(), pr, sizeof(int) * 2 * total));
+    std::vector<std::pair<int, int>> v((size_t)total);
+    for (long long q = 0; q < total; ++q) v[q] = {hp[2 * q], hp[2 * q + 1]};
+    std::sort(v.begin(), v.end());
+    for (long long q = 0; q < total && q < max_pairs; ++q) {
+        pairs[2 * q] = v[q].first;
+        pairs[2 * q + 1] = v[q].second;
+    }
+    return FIPI_OK;
+}
+
+template <typename T>
+__global__ void k_interp_many(PC pc, const T* __restrict__ fields, int nf, size_t V, const double* __restrict__ p,
+                              double* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= pc.n) return;
+    const double x = p[i], y = p[pc.n + i], z = p[2 * pc.n + i];
+    for (int f = 0; f < nf; ++f) {
+        const T* fl[1] = {fields + (size_t)f * V};
+        T v;
+        interp_fields<T, T>(pc, x, y, z, fl, 1, &v);
+        out[(size_t)i * nf + f] = (double)v;
+    }
+}
+
+fipi_status particles_interpolate(fipi_ctx* ctx, const double* fields, int nfields, const double* p, double* out) {
+    const int n = ctx->pb.n;
+    const size_t V = (size_t)ctx->g.V;
+    DevScratch ds{ctx};
+    double* pd = ds.get<double>(3 * (size_t)n);
+    double* od = ds.get<double>((size_t)n * nfields);
+    if (!pd || !od) return set_error(ctx, FIPI_ERR_CUDA, "cudaMalloc failed");
+    fipi_status st = to_dev_soa(ctx, p, pd, n);
+    if (st != FIPI_OK) return st;
+    const PC pc = make_pc(ctx);
+    if (ctx->prec == FIPI_MIXED) {
+        std::vector<float> hf(V * nfields);
+        for (size_t i = 0; i < V * nfields; ++i) hf[i] = (float)fields[i];
+        float* fd = ds.get<float>(V * nfields);
+        if (!fd) return set_error(ctx, FIPI_ERR_CUDA, "cudaMalloc failed");
+        FIPI_CUDA(ctx, h2d(ctx, fd, hf.data(), sizeof(float) * V * nfields));
+        { LaunchScope ls_(ctx, "interpolate", 0.0); k_interp_many<float><<<(n + 255) / 256, 256, 0, ctx->stream>>>(pc, fd, nfields, V, pd, od); }
+    } else {
+        double* fd = ds.get<double>(V * nfields);
+        if (!fd) return set_error(ctx, FIPI_ERR_CUDA, "cudaMalloc failed");
+        FIPI_CUDA(ctx, h2d(ctx, fd, fields, sizeof(double) * V * nfields));
+        { LaunchScope ls_(ctx, "interpolate", 0.0); k_interp_many<double><<<(n + 255) / 256, 256, 0, ctx->stream>>>(pc, fd, nfields, V, pd, od); }
+    }
+    FIPI_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    FIPI_CUDA(ctx, d2h(ctx, out, od, sizeof(double) * n * nfields));
+    return FIPI_OK;
+}
+
+__global__ void k_f_pi_many(PC pc, const double* __restrict__ c_loc, const double* __restrict__ dcdx,
+                            const double* __restrict__ r, const double* __restrict__ cth, double* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= pc.n) return;
+    double f[3];
+    f_pi_of(pc, c_loc[i], dcdx[3 * i], dcdx[3 * i + 1], dcdx[3 * i + 2], r ? r[i] : pc.r_p, cth ? cth[i] : 0.0, f);
+    for (int a = 0; a < 3; ++a) out[3 * i + a] = f[a];
+}
+
+fipi_status particles_f_pi(fipi_ctx* ctx, const double* c_loc, const double* dcdx, const double* r, const double* cth,
+                           double* f_pi) {
+    const int n = ctx->pb.n;
+    DevScratch ds{ctx};
+    double* cd = ds.get<double>(n);
+    double* gd = ds.get<double>(3 * (size_t)n);
+    double* rd = r ? ds.get<double>(n) : nullptr;
+    double* td = cth ? ds.get<double>(n) : nullptr;
+    double* od = ds.get<double>(3 * (size_t)n);
+    if (!cd || !gd || !od) return set_error(ctx, FIPI_ERR_CUDA, "cudaMalloc failed");
+    FIPI_CUDA(ctx, h2d(ctx, cd, c_loc, sizeof(double) * n));
+    FIPI_CUDA(ctx, h2d(ctx, gd, dcdx, sizeof(double) * 3 * n));
+    if (rd) FIPI_CUDA(ctx, h2d(ctx, rd, r, sizeof(double) * n));
+    if (td) FIPI_CUDA(ctx, h2d(ctx, td, cth, sizeof(double) * n));
+    const PC pc = make_pc(ctx);
+    { LaunchScope ls_(ctx, "f_pi", 0.0); k_f_pi_many<<<(n + 255) / 256, 256, 0, ctx->stream>>>(pc, cd, gd, rd, td, od); }
+    FIPI_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    FIPI_CUDA(ctx, d2h(ctx, f_pi, od, sizeof(double) * 3 * n));
+    return FIPI_OK;
+}
+
+__global__ void k_advect_many(PC pc, int stage, const double* __restrict__ fpi, const double* __restrict__ fpp,
+                              const double* __restrict__ r, double* p, double* po, double* uo) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= pc.n) return;
+    advect_one(pc, stage, fpi + 3 * i, fpp + 3 * i, r ? r[i] : pc.r_p, p + 3 * i, po + 3 * i, uo + 3 * i);
+}
+
+fipi_status particles_advect(fipi_ctx* ctx, int stage, const double* f_pi, const double* f_pp, const double* r,
+                             double* p, double* p_old, double* u_old) {
+    const int n = ctx->pb.n;
+    DevScratch ds{ctx};
+    const size_t b3 = sizeof(double) * 3 * n;
+    double* a = ds.get<double>(3 * (size_t)n);
+    double* bpp = ds.get<double>(3 * (size_t)n);
+    double* rd = r ? ds.get<double>(n) : nullptr;
+    double* pd = ds.get<double>(3 * (size_t)n);
+    double* pod = ds.get<double>(3 * (size_t)n);
+    double* uod = ds.get<double>(3 * (size_t)n);
+    if (!a || !bpp || !pd || !pod || !uod) return set_error(ctx, FIPI_ERR_CUDA, "cudaMalloc failed");
+    FIPI_CUDA(ctx, h2d(ctx, a, f_pi, b3));
+    FIPI_CUDA(ctx, h2d(ctx, bpp, f_pp, b3));
+    if (rd) FIPI_CUDA(ctx, h2d(ctx, rd, r, sizeof(double) * n));
+    FIPI_CUDA(ctx, h2d(ctx, pd, p, b3));
+    FIPI_CUDA(ctx, h2d(ctx, pod, p_old, b3));
+    FIPI_CUDA(ctx, h2d(ctx, uod, u_old, b3));
+    const PC pc = make_pc(ctx);
+    { LaunchScope ls_(ctx, "advect", 0.0); k_advect_many<<<(n + 255) / 256, 256, 0, ctx->stream>>>(pc, stage, a, bpp, rd, pd, pod, uod); }
+    FIPI_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    FIPI_CUDA(ctx, d2h(ctx, p, pd, b3));
+    FIPI_CUDA(ctx, d2h(ctx, p_old, pod, b3));
+    FIPI_CUDA(ctx, d2h(ctx, u_old, uod, b3));
+    return FIPI_OK;
+}
+
+fipi_status particles_spread_host(fipi_ctx* ctx, const double* p, const double* f_pp, double* out) {
+    ParticleBufs& b = ctx->pb;
+    const int n = b.n;
+    const size_t V = (size_t)ctx->g.V;
+    DevScratch ds{ctx};
+    double* pd = ds.get<double>(3 * (size_t)n);
+    double* fd = ds.get<double>(3 * (size_t)n);
+    if (!pd || !fd) return set_error(ctx, FIPI_ERR_CUDA, "cudaMalloc failed");
+    fipi_status st = to_dev_soa(ctx, p, pd, n);
+    if (st != FIPI_OK) return st;
+    st = to_dev_soa(ctx, f_pp, fd, n);
+    if (st != FIPI_OK) return st;
+    if (ctx->prec == FIPI_MIXED) {
+        float* g = ds.get<float>(3 * V);
+        if (!g) return set_error(ctx, FIPI_ERR_CUDA, "cudaMalloc failed");
+        FIPI_CUDA(ctx, cudaMemsetAsync(g, 0, sizeof(float) * 3 * V, ctx->stream));
+        float* f3[3] = {g, g + V, g + 2 * V};
+        spread_t<float>(ctx, pd, fd, f3, false);
+        std::vector<float> h(3 * V);
+        FIPI_CUDA(ctx, cudaMemcpyAsync(h.data(), g, sizeof(float) * 3 * V, cudaMemcpyDeviceToHost, ctx->stream));
+        FIPI_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        for (size_t i = 0; i < 3 * V; ++i) out[i] = h[i];
+    } else {
+        double* g = ds.get<double>(3 * V);
+        if (!g) return set_error(ctx, FIPI_ERR_CUDA, "cudaMalloc failed");
+        FIPI_CUDA(ctx, cudaMemsetAsync(g, 0, sizeof(double) * 3 * V, ctx->stream));
+        double* f3[3] = {g, g + V, g + 2 * V};
+        spread_t<double>(ctx, pd, fd, f3, false);
+        FIPI_CUDA(ctx, cudaMemcpyAsync(out, g, sizeof(double) * 3 * V, cudaMemcpyDeviceToHost, ctx->stream));
+        FIPI_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    return FIPI_OK;
+}
+
+}  // namespace fipi

@@ -1,0 +1,333 @@
+"""ctypes binding of libfipi_gb300.so (the C ABI declared in include/fipi.h).
+
+`Simulation` mirrors the reference's step interface: the loop body of
+main.cpp (`step`), the `cluster` calls (`cells_build` = sorting,
+`f_pp` = compute_f_pp, `spread` = compute_f_r, `advect` + wrap), the
+`element` calls (`f_pi` = get_f_pi, `interpolate` = get_local_c/dcdx) and
+the `field` transforms (`fft_r2c`, `fft_c2r`, `grad`).  Every call goes
+through the C ABI; there is no other implementation behind it, and a
+missing or unloadable library raises instead of falling back.
+"""
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+import numpy as np
+
+from .params import FipiParams
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+_vp = ctypes.c_void_p
+
+FIPI_FP64 = 0
+FIPI_MIXED = 1
+STATUS = {
+    0: "FIPI_OK", 1: "FIPI_ERR_BAD_PARAMS", 2: "FIPI_ERR_BAD_ARG", 3: "FIPI_ERR_CUDA",
+    4: "FIPI_ERR_OUT_OF_RANGE", 5: "FIPI_ERR_NONFINITE", 6: "FIPI_ERR_NO_DEVICE",
+    7: "FIPI_ERR_STATE", 8: "FIPI_ERR_UNSUPPORTED",
+}
+
+
+class FipiError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+# name: (restype, argtypes)
+_SIGS = {
+    "fipi_abi_version": (ctypes.c_int, []),
+    "fipi_last_error_string": (ctypes.c_char_p, []),
+    "fipi_params_reference": (ctypes.c_int, [ctypes.POINTER(FipiParams)]),
+    "fipi_cell_geometry": (ctypes.c_int, [ctypes.POINTER(FipiParams), _ip, _dp]),
+    "fipi_create": (ctypes.c_int, [ctypes.POINTER(FipiParams), ctypes.c_int, ctypes.c_int,
+                                   ctypes.POINTER(_vp)]),
+    "fipi_destroy": (ctypes.c_int, [_vp]),
+    "fipi_device_bytes": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_size_t)]),
+    "fipi_set_phase": (ctypes.c_int, [_vp, _dp]),
+    "fipi_set_velocity": (ctypes.c_int, [_vp, _dp]),
+    "fipi_set_particles": (ctypes.c_int, [_vp, _dp, _dp, _dp, _dp]),
+    "fipi_get_phase": (ctypes.c_int, [_vp, _dp]),
+    "fipi_get_velocity": (ctypes.c_int, [_vp, _dp]),
+    "fipi_get_particles": (ctypes.c_int, [_vp, _dp, _dp, _dp]),
+    "fipi_get_time": (ctypes.c_int, [_vp, _ip]),
+    "fipi_step": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "fipi_step_async": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "fipi_sync": (ctypes.c_int, [_vp]),
+    "fipi_stream": (ctypes.c_int, [_vp, ctypes.POINTER(_vp)]),
+    "fipi_mass": (ctypes.c_int, [_vp, _dp]),
+    "fipi_free_energy": (ctypes.c_int, [_vp, _dp]),
+    "fipi_packing_tau": (ctypes.c_int, [_vp, _dp]),
+    "fipi_fft_r2c": (ctypes.c_int, [_vp, _dp, _dp]),
+    "fipi_fft_c2r": (ctypes.c_int, [_vp, _dp, _dp]),
+    "fipi_grad": (ctypes.c_int, [_vp, _dp, _dp]),
+    "fipi_cells_build": (ctypes.c_int, [_vp, _dp, _ip, _ip, _ip]),
+    "fipi_f_pp": (ctypes.c_int, [_vp, _dp, ctypes.c_int, _dp, _dp, _dp]),
+    "fipi_pairs": (ctypes.c_int, [_vp, _dp, _ip, ctypes.c_int, _ip]),
+    "fipi_interpolate": (ctypes.c_int, [_vp, _dp, ctypes.c_int, _dp, _dp]),
+    "fipi_f_pi": (ctypes.c_int, [_vp, _dp, _dp, _dp, _dp, _dp]),
+    "fipi_advect": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp, _dp, _dp, _dp, _dp]),
+    "fipi_spread": (ctypes.c_int, [_vp, _dp, _dp, _dp]),
+    "fipi_seed_phase": (ctypes.c_int, [ctypes.POINTER(FipiParams), ctypes.c_uint64, ctypes.c_double,
+                                       ctypes.c_double, _dp]),
+    "fipi_seed_particles": (ctypes.c_int, [ctypes.POINTER(FipiParams), ctypes.c_uint64,
+                                           ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                           ctypes.c_double, ctypes.c_int, _dp, _dp, _dp]),
+}
+
+
+def library_path() -> Path:
+    from .build import LIB
+
+    return LIB
+
+
+def load(build_if_missing: bool = True):
+    """Load libfipi_gb300.so (building it first when absent or stale)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    from . import build as _build
+
+    if build_if_missing:
+        _build.build()
+    path = library_path()
+    if not path.exists():
+        raise FileNotFoundError(f"{path} is missing: run fipi_gb300.build.build()")
+    lib = ctypes.CDLL(str(path))
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def declared_symbols() -> list[str]:
+    return list(_SIGS)
+
+
+def _check(code: int):
+    if code != 0:
+        msg = load().fipi_last_error_string().decode(errors="replace")
+        raise FipiError(code, msg)
+
+
+def _d(a):
+    return None if a is None else a.ctypes.data_as(_dp)
+
+
+def _i(a):
+    return None if a is None else a.ctypes.data_as(_ip)
+
+
+def _f64(a, n=None):
+    if a is None:
+        return None
+    a = np.ascontiguousarray(a, dtype=np.float64).ravel()
+    if n is not None and a.size != n:
+        raise ValueError(f"expected {n} values, got {a.size}")
+    return a
+
+
+def reference_params() -> FipiParams:
+    p = FipiParams()
+    _check(load().fipi_params_reference(ctypes.byref(p)))
+    return p
+
+
+def cell_geometry(params: FipiParams):
+    nc = np.zeros(3, np.int32)
+    dc = np.zeros(3)
+    _check(load().fipi_cell_geometry(ctypes.byref(params), _i(nc), _d(dc)))
+    return nc, dc
+
+
+def seed_phase(params: FipiParams, seed: int, mean: float = 0.0, amp: float = 0.05) -> np.ndarray:
+    V = params.nx * params.ny * params.nz
+    c = np.empty(V)
+    _check(load().fipi_seed_phase(ctypes.byref(params), seed, mean, amp, _d(c)))
+    return c
+
+
+def seed_particles(params: FipiParams, seed: int, r_range=None, theta_range_deg=None,
+                   allow_overlap: bool = False):
+    n = params.n_p
+    pos = np.empty(3 * max(n, 0))
+    r = np.empty(max(n, 0))
+    ct = np.empty(max(n, 0))
+    rmin, rmax = r_range if r_range else (params.r_p, params.r_p)
+    tmin, tmax = theta_range_deg if theta_range_deg else (90.0, 90.0)
+    _check(load().fipi_seed_particles(ctypes.byref(params), seed, rmin, rmax, tmin, tmax,
+                                      1 if allow_overlap else 0, _d(pos), _d(r), _d(ct)))
+    return pos, r, ct
+
+
+class Simulation:
+    """One FIPI simulation on one GPU (a `fipi_ctx`)."""
+
+    def __init__(self, params: FipiParams, precision: str = "fp64", device: int = 0):
+        self.lib = load()
+        self.params = params
+        self.precision = precision
+        prec = {"fp64": FIPI_FP64, "mixed": FIPI_MIXED}[precision]
+        h = _vp()
+        _check(self.lib.fipi_create(ctypes.byref(params), prec, device, ctypes.byref(h)))
+        self.h = h
+        self.V = params.nx * params.ny * params.nz
+        self.n = params.n_p
+        self.SH = params.nz * (params.nx // 2 + 1) * params.ny
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            self.lib.fipi_destroy(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # ---------------------------------------------------------------- state
+    def set_phase(self, c):
+        _check(self.lib.fipi_set_phase(self.h, _d(_f64(c, self.V))))
+
+    def set_velocity(self, u):
+        _check(self.lib.fipi_set_velocity(self.h, _d(_f64(u, 3 * self.V))))
+
+    def set_particles(self, p, r=None, cos_theta=None, f_pp=None):
+        _check(self.lib.fipi_set_particles(self.h, _d(_f64(p, 3 * self.n)), _d(_f64(r, self.n)),
+                                           _d(_f64(cos_theta, self.n)), _d(_f64(f_pp, 3 * self.n))))
+
+    def get_phase(self):
+        out = np.empty(self.V)
+        _check(self.lib.fipi_get_phase(self.h, _d(out)))
+        return out
+
+    def get_velocity(self):
+        out = np.empty(3 * self.V)
+        _check(self.lib.fipi_get_velocity(self.h, _d(out)))
+        return out
+
+    def get_particles(self):
+        n = self.n
+        p, fpp, fpi = np.empty(3 * n), np.empty(3 * n), np.empty(3 * n)
+        _check(self.lib.fipi_get_particles(self.h, _d(p), _d(fpp), _d(fpi)))
+        return p, fpp, fpi
+
+    @property
+    def time(self) -> int:
+        t = ctypes.c_int()
+        _check(self.lib.fipi_get_time(self.h, ctypes.byref(t)))
+        return t.value
+
+    def step(self, n: int = 1):
+        _check(self.lib.fipi_step(self.h, n))
+
+    def step_async(self, n: int = 1):
+        _check(self.lib.fipi_step_async(self.h, n))
+
+    def sync(self):
+        _check(self.lib.fipi_sync(self.h))
+
+    def stream(self) -> int:
+        s = _vp()
+        _check(self.lib.fipi_stream(self.h, ctypes.byref(s)))
+        return s.value or 0
+
+    def device_bytes(self) -> int:
+        b = ctypes.c_size_t()
+        _check(self.lib.fipi_device_bytes(self.h, ctypes.byref(b)))
+        return b.value
+
+    def mass(self) -> float:
+        v = ctypes.c_double()
+        _check(self.lib.fipi_mass(self.h, ctypes.byref(v)))
+        return v.value
+
+    def free_energy(self) -> float:
+        v = ctypes.c_double()
+        _check(self.lib.fipi_free_energy(self.h, ctypes.byref(v)))
+        return v.value
+
+    def packing_tau(self) -> float:
+        v = ctypes.c_double()
+        _check(self.lib.fipi_packing_tau(self.h, ctypes.byref(v)))
+        return v.value
+
+    # ---------------------------------------------------------------- fine-grained
+    def fft_r2c(self, x) -> np.ndarray:
+        out = np.empty(2 * self.SH)
+        _check(self.lib.fipi_fft_r2c(self.h, _d(_f64(x, self.V)), _d(out)))
+        return out.view(np.complex128)
+
+    def fft_c2r(self, X) -> np.ndarray:
+        X = np.ascontiguousarray(X, np.complex128).ravel()
+        if X.size != self.SH:
+            raise ValueError("half spectrum size mismatch")
+        out = np.empty(self.V)
+        _check(self.lib.fipi_fft_c2r(self.h, _d(X.view(np.float64)), _d(out)))
+        return out
+
+    def grad(self, c) -> np.ndarray:
+        out = np.empty(3 * self.V)
+        _check(self.lib.fipi_grad(self.h, _d(_f64(c, self.V)), _d(out)))
+        return out
+
+    def cells_build(self, p):
+        nc, _ = cell_geometry(self.params)
+        keys = np.empty(self.n, np.int32)
+        srt = np.empty(self.n, np.int32)
+        off = np.empty(int(np.prod(nc)) + 1, np.int32)
+        _check(self.lib.fipi_cells_build(self.h, _d(_f64(p, 3 * self.n)), _i(keys), _i(srt), _i(off)))
+        return keys, srt, off
+
+    def f_pp(self, p, t, f_pi=None):
+        out = np.empty(3 * self.n)
+        tau = ctypes.c_double()
+        _check(self.lib.fipi_f_pp(self.h, _d(_f64(p, 3 * self.n)), t, _d(_f64(f_pi, 3 * self.n)),
+                                  _d(out), ctypes.byref(tau)))
+        return out, tau.value
+
+    def pairs(self, p):
+        p = _f64(p, 3 * self.n)
+        cnt = ctypes.c_int()
+        _check(self.lib.fipi_pairs(self.h, _d(p), None, 0, ctypes.byref(cnt)))
+        out = np.empty(2 * max(cnt.value, 1), np.int32)
+        _check(self.lib.fipi_pairs(self.h, _d(p), _i(out), cnt.value, ctypes.byref(cnt)))
+        return out[: 2 * cnt.value].reshape(-1, 2)
+
+    def interpolate(self, fields, p):
+        fields = _f64(fields)
+        nf = fields.size // self.V
+        out = np.empty(self.n * nf)
+        _check(self.lib.fipi_interpolate(self.h, _d(fields), nf, _d(_f64(p, 3 * self.n)), _d(out)))
+        return out.reshape(self.n, nf)
+
+    def f_pi(self, c_loc, dcdx, r=None, cos_theta=None):
+        out = np.empty(3 * self.n)
+        _check(self.lib.fipi_f_pi(self.h, _d(_f64(c_loc, self.n)), _d(_f64(dcdx, 3 * self.n)),
+                                  _d(_f64(r, self.n)), _d(_f64(cos_theta, self.n)), _d(out)))
+        return out
+
+    def advect(self, stage, f_pi, f_pp, r, p, p_old, u_old):
+        p, p_old, u_old = (_f64(a, 3 * self.n).copy() for a in (p, p_old, u_old))
+        _check(self.lib.fipi_advect(self.h, stage, _d(_f64(f_pi, 3 * self.n)), _d(_f64(f_pp, 3 * self.n)),
+                                    _d(_f64(r, self.n)), _d(p), _d(p_old), _d(u_old)))
+        return p, p_old, u_old
+
+    def spread(self, p, f_pp):
+        out = np.empty(3 * self.V)
+        _check(self.lib.fipi_spread(self.h, _d(_f64(p, 3 * self.n)), _d(_f64(f_pp, 3 * self.n)), _d(out)))
+        return out

@@ -149,6 +149,19 @@ fipi_status fipi_free_energy(fipi_ctx* ctx, double* out);
 /* Packing energy tau of the last contact-force evaluation (cluster.cpp:283-353). */
 fipi_status fipi_packing_tau(fipi_ctx* ctx, double* out);
 
+/* -------------------------------------------------------- instrumentation
+ * Not in the reference (its only timing is clock() around the whole run,
+ * main.cpp:122-123, 345-346).  Every kernel launch of the library is
+ * counted; with timing enabled each launch is bracketed by CUDA events on
+ * the context stream and accumulated per kernel class together with the
+ * kernel's algorithmic bytes per launch (arrays it must read and write). */
+fipi_status fipi_set_kernel_timing(fipi_ctx* ctx, int enable); /* also resets the stats */
+fipi_status fipi_kernel_stat_count(fipi_ctx* ctx, int* n);
+fipi_status fipi_kernel_stats(fipi_ctx* ctx, int i, char* name, int name_cap, long long* launches,
+                              double* total_ms, double* bytes_per_launch);
+/* Kernels launched by this context since creation. */
+fipi_status fipi_launch_count(const fipi_ctx* ctx, long long* n);
+
 /* ------------------------------------------ fine-grained parity entry points
  * One call per reference function, on host arrays; they use the context's
  * grid and particle count but do not touch its step state. */
@@ -199,6 +212,22 @@ fipi_status fipi_advect(fipi_ctx* ctx, int stage, const double* f_pi, const doub
  * f_pp / (dx dy dz) onto the grid, out: 3 x V.  Deterministic: per grid
  * node the contributions are summed in ascending particle id. */
 fipi_status fipi_spread(fipi_ctx* ctx, const double* p, const double* f_pp, double* out);
+
+/* ------------------------------------------------ seeded synthetic inputs
+ * Host-only helpers (no device needed).  The reference draws its initial
+ * state from unseeded rand() (field.cpp:96, cluster.cpp:153-183); these draw
+ * from a splitmix64 stream so runs are reproducible. */
+/* c[i] = mean + amp * U(-1, 1), V values. */
+fipi_status fipi_seed_phase(const fipi_params* p, uint64_t seed, double mean, double amp, double* c);
+/* n_p positions uniform in the box (n_p x 3), radii U[r_min, r_max],
+ * contact angles U[theta_min, theta_max] degrees returned as cos(theta).
+ * Without allow_overlap the spheres are placed by random sequential
+ * addition with the periodic minimum-image distance >= r_i + r_j
+ * (the reference's check_overlap, cluster.cpp:192-207, ignores periodic
+ * images).  r and cos_theta may be NULL. */
+fipi_status fipi_seed_particles(const fipi_params* p, uint64_t seed, double r_min, double r_max,
+                                double theta_min_deg, double theta_max_deg, int allow_overlap,
+                                double* pos, double* r, double* cos_theta);
 
 #ifdef __cplusplus
 }

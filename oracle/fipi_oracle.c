@@ -261,6 +261,18 @@ static void grad_spectral(oracle* o, const double* a, double* g[3]) {
     }
 }
 
+/* c.fft; grad_c = c.grad(kf); grad_c.ifft  (main.cpp:287-289) on a real c. */
+void oracle_grad(const fipi_params* P, const double* c, double* out) {
+    oracle* o = oracle_create(P);
+    if (!o) return;
+    oracle_set_phase(o, c);
+    fft(o, o->c);
+    grad_spectral(o, o->c, o->grad);
+    for (int d = 0; d < 3; ++d) ifft(o, o->grad[d]);
+    oracle_get_grad(o, out);
+    oracle_destroy(o);
+}
+
 /* f = (lambda/sqr(epsilon))*(c.power(3.0)-c)  (main.cpp:178, 250) */
 static void bulk_potential(oracle* o) {
     const double s = o->P.lambda / (o->P.epsilon * o->P.epsilon);

@@ -79,6 +79,7 @@ def port_lib():
         lib.oracle_mass.restype = ctypes.c_double
         lib.oracle_mass.argtypes = [ctypes.c_void_p]
         lib.oracle_fft3.argtypes = [P, _dp, ctypes.c_int]
+        lib.oracle_grad.argtypes = [P, _dp, _dp]
         lib.oracle_sorting.argtypes = [P, ctypes.c_int, _dp, _ip, _ip, _ip, _ip]
         lib.oracle_f_pp.argtypes = [P, ctypes.c_int, _dp, ctypes.c_int, _dp, _dp, _dp, _ip,
                                     ctypes.c_int, _ip]
@@ -178,6 +179,13 @@ def fft3(params, data_complex, sign):
     a = np.ascontiguousarray(data_complex, np.complex128).copy()
     port_lib().oracle_fft3(ctypes.byref(params), a.ctypes.data_as(_dp), sign)
     return a
+
+
+def grad(params, c):
+    V = params.nx * params.ny * params.nz
+    out = np.zeros(3 * V)
+    port_lib().oracle_grad(ctypes.byref(params), _d(np.ascontiguousarray(c, np.float64)), _d(out))
+    return out
 
 
 def sorting(params, p):
