@@ -104,6 +104,18 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def aggregate_replicas(elapsed, steps, ws, dist=None, device="cuda"):
+    """Whole-job steps/s of `ws` independent replicas: all ranks' steps over
+    the slowest rank's time (max over ranks)."""
+    if dist is not None and ws > 1:
+        import torch
+
+        t = torch.tensor([float(elapsed)], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t.item())
+    return ws * steps / elapsed, elapsed
+
+
 def seeded(w, seed):
     import fipi_gb300 as F
 
@@ -284,11 +296,7 @@ def run_gpu(args):
         elapsed = timed_steps(sim, args.steps, torch)
     launches = launch_count(sim) - l0
     barrier()
-    if dist is not None:
-        t = torch.tensor([elapsed], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed = float(t.item())
-    value = ws * args.steps / elapsed
+    value, elapsed = aggregate_replicas(elapsed, args.steps, ws, dist)
 
     # ---- per-kernel CUDA-event timing (separate region; events add overhead)
     set_timing(sim, True)

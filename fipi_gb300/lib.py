@@ -72,6 +72,11 @@ _SIGS = {
     "fipi_f_pi": (ctypes.c_int, [_vp, _dp, _dp, _dp, _dp, _dp]),
     "fipi_advect": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp, _dp, _dp, _dp, _dp]),
     "fipi_spread": (ctypes.c_int, [_vp, _dp, _dp, _dp]),
+    "fipi_set_kernel_timing": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "fipi_kernel_stat_count": (ctypes.c_int, [_vp, _ip]),
+    "fipi_kernel_stats": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_char_p, ctypes.c_int,
+                                         ctypes.POINTER(ctypes.c_longlong), _dp, _dp]),
+    "fipi_launch_count": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_longlong)]),
     "fipi_seed_phase": (ctypes.c_int, [ctypes.POINTER(FipiParams), ctypes.c_uint64, ctypes.c_double,
                                        ctypes.c_double, _dp]),
     "fipi_seed_particles": (ctypes.c_int, [ctypes.POINTER(FipiParams), ctypes.c_uint64,
