@@ -25,6 +25,8 @@
 
 #include <algorithm>
 #include <cmath>
+#include <mutex>
+#include <string>
 #include <vector>
 
 #include "ctx.hpp"
@@ -1008,3 +1010,130 @@ fipi_status particles_spread_host(fipi_ctx* ctx, const double* p, const double* 
 }
 
 }  // namespace fipi
+
+// ------------------------------------------------------------ no-allocation cell list
+// A variant of the cell-list build (cluster::sorting) for callers that may
+// not allocate device memory: code that runs inside a host framework owning
+// a fixed device-memory pool, real-time loops that forbid driver
+// allocations, or any caller that only hands over buffers it already has.
+// Its scratch (positions in SoA order, radix-sort ping-pong arrays,
+// histograms, the error word) lives in the file-scope array below, sized
+// for at most FIPI_NOALLOC_MAX_PARTICLES particles.  Every GPU that loads
+// this library holds the array until the process exits.
+namespace fipi {
+namespace {
+
+constexpr int kNoallocMaxN = FIPI_NOALLOC_MAX_PARTICLES;
+constexpr int kNoallocHistBlocks = kNoallocMaxN / RS_TILE + 1;
+constexpr size_t kNoallocPos = 0;                                                 // double[3 n]
+constexpr size_t kNoallocKA = kNoallocPos + sizeof(double) * 3 * kNoallocMaxN;    // unsigned[n]
+constexpr size_t kNoallocKB = kNoallocKA + sizeof(unsigned) * kNoallocMaxN;       // unsigned[n]
+constexpr size_t kNoallocIB = kNoallocKB + sizeof(unsigned) * kNoallocMaxN;       // unsigned[n]
+constexpr size_t kNoallocHist = kNoallocIB + sizeof(unsigned) * kNoallocMaxN;     // unsigned[256 blocks]
+constexpr size_t kNoallocStatus = kNoallocHist + sizeof(unsigned) * 256 * kNoallocHistBlocks;  // int
+constexpr size_t kNoallocBytes = kNoallocStatus + 256;
+
+static __device__ __align__(256) unsigned char g_cells_scratch[kNoallocBytes];
+
+// Device address of g_cells_scratch per device, looked up once per device.
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[256] = {};
+
+__global__ void k_aos_to_soa(const double* __restrict__ aos, double* __restrict__ soa, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    for (int a = 0; a < 3; ++a) soa[(size_t)a * n + i] = aos[3 * (size_t)i + a];
+}
+
+}  // namespace
+}  // namespace fipi
+
+extern "C" fipi_status fipi_cells_build_noalloc(const fipi_params* P, const double* d_pos, int* d_keys,
+                                                int* d_sorted, int* d_offsets, void* stream) {
+    using namespace fipi;
+    if (!P || !d_pos || !d_keys || !d_sorted || !d_offsets)
+        return set_error(nullptr, FIPI_ERR_BAD_ARG, "NULL argument");
+    const int n = P->n_p;
+    if (n <= 0) return set_error(nullptr, FIPI_ERR_BAD_ARG, "n_p must be positive");
+    if (n > kNoallocMaxN)
+        return set_error(nullptr, FIPI_ERR_UNSUPPORTED,
+                         "n_p = " + std::to_string(n) + " exceeds the " + std::to_string(kNoallocMaxN) +
+                             "-particle scratch of fipi_cells_build_noalloc");
+    int nc[3];
+    double dc[3];
+    fipi_cell_geometry(P, nc, dc);
+    if (nc[0] < 1 || nc[1] < 1 || nc[2] < 1 || !(P->r_c > 0))
+        return set_error(nullptr, FIPI_ERR_BAD_PARAMS, "empty cell grid (r_c larger than the box)");
+    const long long ncells = (long long)nc[0] * nc[1] * nc[2];
+    if (ncells > (1ll << 30)) return set_error(nullptr, FIPI_ERR_UNSUPPORTED, "too many cells");
+    cudaStream_t st = (cudaStream_t)stream;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess || dev < 0 || dev >= 256)
+        return set_error(nullptr, FIPI_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+    unsigned char* base = nullptr;
+    {
+        // set-up, once per device, with that device current: the array's name
+        // is a host-side stand-in in host code, so its device address is
+        // looked up here and passed to the kernels
+        std::lock_guard<std::mutex> lk(g_noalloc_mu);
+        if (!g_noalloc_addr[dev]) {
+            void* ptr = nullptr;
+            e = cudaGetSymbolAddress(&ptr, g_cells_scratch);
+            if (e != cudaSuccess || !ptr)
+                return set_error(nullptr, FIPI_ERR_CUDA,
+                                 std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+            g_noalloc_addr[dev] = ptr;
+        }
+        base = (unsigned char*)g_noalloc_addr[dev];
+    }
+    double* pos = (double*)(base + kNoallocPos);
+    unsigned* kA = (unsigned*)(base + kNoallocKA);
+    unsigned* kB = (unsigned*)(base + kNoallocKB);
+    unsigned* iB = (unsigned*)(base + kNoallocIB);
+    unsigned* hist = (unsigned*)(base + kNoallocHist);
+    int* status = (int*)(base + kNoallocStatus);
+    unsigned* iA = (unsigned*)d_sorted;  // ids start in the caller's output
+
+    PC pc{};
+    pc.n = n;
+    for (int a = 0; a < 3; ++a) {
+        pc.nc[a] = nc[a];
+        pc.dc[a] = dc[a];
+    }
+    pc.margin = P->margin;
+    // the error word keeps the previous call's value: clear it first
+    e = cudaMemsetAsync(status, 0, sizeof(int), st);
+    if (e != cudaSuccess) return set_error(nullptr, FIPI_ERR_CUDA, std::string("status clear: ") + cudaGetErrorString(e));
+    const int nb = (n + 255) / 256;
+    k_aos_to_soa<<<nb, 256, 0, st>>>(d_pos, pos, n);
+    k_cell_keys<<<nb, 256, 0, st>>>(pc, pos, kA, iA, status);
+    // per-particle keys in particle order, before the sort permutes them
+    e = cudaMemcpyAsync(d_keys, kA, sizeof(unsigned) * n, cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) return set_error(nullptr, FIPI_ERR_CUDA, std::string("keys copy: ") + cudaGetErrorString(e));
+    const int nblk = (n + RS_TILE - 1) / RS_TILE;
+    const int bits = bits_for(ncells - 1);
+    unsigned *k = kA, *v = iA, *k2 = kB, *v2 = iB;
+    for (int shift = 0; shift < bits; shift += 8) {
+        k_rs_hist<<<nblk, RS_T, 0, st>>>(k, n, shift, hist, nblk);
+        k_scan_excl<<<1, 1024, 0, st>>>(hist, 256 * nblk);
+        k_rs_scatter<<<nblk, RS_T, 0, st>>>(k, v, k2, v2, n, shift, hist, nblk);
+        std::swap(k, k2);
+        std::swap(v, v2);
+    }
+    if (v != iA) {
+        e = cudaMemcpyAsync(iA, v, sizeof(unsigned) * n, cudaMemcpyDeviceToDevice, st);
+        if (e != cudaSuccess) return set_error(nullptr, FIPI_ERR_CUDA, std::string("ids copy: ") + cudaGetErrorString(e));
+    }
+    k_cell_offsets<<<(int)((ncells + 1 + 255) / 256), 256, 0, st>>>(k, n, d_offsets, (int)ncells);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return set_error(nullptr, FIPI_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e));
+    int hst = 0;
+    e = cudaMemcpyAsync(&hst, status, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return set_error(nullptr, FIPI_ERR_CUDA, std::string("sync: ") + cudaGetErrorString(e));
+    if (hst & ERR_NONFINITE) return set_error(nullptr, FIPI_ERR_NONFINITE, "non-finite particle position");
+    if (hst & ERR_OUT_OF_RANGE)
+        return set_error(nullptr, FIPI_ERR_OUT_OF_RANGE, "particle out of sorting range (cluster.cpp:238-257)");
+    return FIPI_OK;
+}

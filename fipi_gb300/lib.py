@@ -72,6 +72,7 @@ _SIGS = {
     "fipi_f_pi": (ctypes.c_int, [_vp, _dp, _dp, _dp, _dp, _dp]),
     "fipi_advect": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp, _dp, _dp, _dp, _dp]),
     "fipi_spread": (ctypes.c_int, [_vp, _dp, _dp, _dp]),
+    "fipi_cells_build_noalloc": (ctypes.c_int, [ctypes.POINTER(FipiParams), _vp, _vp, _vp, _vp, _vp]),
     "fipi_set_kernel_timing": (ctypes.c_int, [_vp, ctypes.c_int]),
     "fipi_kernel_stat_count": (ctypes.c_int, [_vp, _ip]),
     "fipi_kernel_stats": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_char_p, ctypes.c_int,

@@ -213,6 +213,31 @@ fipi_status fipi_advect(fipi_ctx* ctx, int stage, const double* f_pi, const doub
  * node the contributions are summed in ascending particle id. */
 fipi_status fipi_spread(fipi_ctx* ctx, const double* p, const double* f_pp, double* out);
 
+/* ---------------------------------------------- no-allocation cell list
+ * No counterpart in the reference.  The cell-list build of
+ * fipi_cells_build (cluster::sorting) for callers that cannot call
+ * cudaMalloc: code inside a host framework that owns a fixed device pool,
+ * real-time loops that forbid driver allocations, or callers that only
+ * hand over buffers they already hold.  It needs no context and allocates
+ * nothing; its scratch is a fixed array inside the library (about 2.4 MB
+ * on every GPU that loads the library, held until the process exits),
+ * sized for at most FIPI_NOALLOC_MAX_PARTICLES particles; larger n_p is
+ * rejected with FIPI_ERR_UNSUPPORTED.
+ *   p          grid/box/cell parameters and n_p
+ *   d_pos      device, n_p x 3 doubles (particle-major)
+ *   d_keys     device, n_p ints: cell key of each particle (by id)
+ *   d_sorted   device, n_p ints: particle ids sorted by (cell, id)
+ *   d_offsets  device, n_cells + 1 ints
+ *   stream     cudaStream_t (as void*) the work is queued on; the call
+ *              synchronises it before returning the status
+ * The first call on a device looks up the scratch's device address (with
+ * that device current); make that first call before any stream capture.
+ * All calls share the one scratch array: calls whose work overlaps on the
+ * GPU (other threads, other streams) race and must be serialised. */
+#define FIPI_NOALLOC_MAX_PARTICLES 65536
+fipi_status fipi_cells_build_noalloc(const fipi_params* p, const double* d_pos, int* d_keys,
+                                     int* d_sorted, int* d_offsets, void* stream);
+
 /* ------------------------------------------------ seeded synthetic inputs
  * Host-only helpers (no device needed).  The reference draws its initial
  * state from unseeded rand() (field.cpp:96, cluster.cpp:153-183); these draw
