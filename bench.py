@@ -140,38 +140,15 @@ def timed_steps(sim, n, torch):
 
 
 def kernel_stats(sim):
-    import ctypes
-
-    lib = sim.lib
-    lib.fipi_kernel_stat_count.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
-    lib.fipi_kernel_stats.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_char_p, ctypes.c_int,
-                                      ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_double),
-                                      ctypes.POINTER(ctypes.c_double)]
-    n = ctypes.c_int()
-    lib.fipi_kernel_stat_count(sim.h, ctypes.byref(n))
-    out = []
-    for i in range(n.value):
-        name = ctypes.create_string_buffer(128)
-        la, ms, by = ctypes.c_longlong(), ctypes.c_double(), ctypes.c_double()
-        lib.fipi_kernel_stats(sim.h, i, name, 128, ctypes.byref(la), ctypes.byref(ms), ctypes.byref(by))
-        out.append({"name": name.value.decode(), "launches": la.value, "ms": ms.value, "bytes": by.value})
-    return out
+    return sim.kernel_stats()
 
 
 def launch_count(sim):
-    import ctypes
-
-    sim.lib.fipi_launch_count.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]
-    n = ctypes.c_longlong()
-    sim.lib.fipi_launch_count(sim.h, ctypes.byref(n))
-    return n.value
+    return sim.launch_count()
 
 
 def set_timing(sim, on):
-    import ctypes
-
-    sim.lib.fipi_set_kernel_timing.argtypes = [ctypes.c_void_p, ctypes.c_int]
-    sim.lib.fipi_set_kernel_timing(sim.h, 1 if on else 0)
+    sim.set_kernel_timing(on)
 
 
 def committed_traffic(kernel, workload):

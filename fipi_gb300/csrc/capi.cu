@@ -177,10 +177,15 @@ fipi_status fipi_create(const fipi_params* P, fipi_precision prec, int device, f
         return s;
     };
     if (cudaSetDevice(device) != cudaSuccess) return fail(cuda_check(ctx, cudaGetLastError(), "cudaSetDevice"));
+    cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+    if (ctx->num_sms < 1) ctx->num_sms = 1;
     cudaError_t e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) return fail(cuda_check(ctx, e, "cudaStreamCreate"));
     e = cudaMalloc(&ctx->status, sizeof(int));
     if (e != cudaSuccess) return fail(cuda_check(ctx, e, "cudaMalloc(status)"));
+    e = cudaMalloc(&ctx->d_t, sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_rmp, sizeof(double));
+    if (e != cudaSuccess) return fail(cuda_check(ctx, e, "cudaMalloc(step counter)"));
     cudaMemsetAsync(ctx->status, 0, sizeof(int), ctx->stream);
     st = fields_alloc(ctx);
     if (st != FIPI_OK) return fail(st);
@@ -198,9 +203,14 @@ fipi_status fipi_create(const fipi_params* P, fipi_precision prec, int device, f
     return FIPI_OK;
 }
 
+static void graphs_reset(fipi_ctx* ctx);
+
 fipi_status fipi_destroy(fipi_ctx* ctx) {
     if (!ctx) return FIPI_OK;
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    graphs_reset(ctx);
+    if (ctx->d_t) cudaFree(ctx->d_t);
+    if (ctx->d_rmp) cudaFree(ctx->d_rmp);
     drain_timer(ctx);
     for (cudaEvent_t e : ctx->kt.pool) cudaEventDestroy(e);
     fields_free(ctx);
@@ -224,6 +234,7 @@ static fipi_status check_status(fipi_ctx* ctx) {
     FIPI_CUDA(ctx, d2h(ctx, &st, ctx->status, sizeof(int)));
     if (st) {
         FIPI_CUDA(ctx, cudaMemsetAsync(ctx->status, 0, sizeof(int), ctx->stream));
+        if (st & ERR_TMA_TIMEOUT) return set_error(ctx, FIPI_ERR_CUDA, "a bulk-copy wait timed out in an FFT pass");
         if (st & ERR_NONFINITE) return set_error(ctx, FIPI_ERR_NONFINITE, "non-finite particle position");
         return set_error(ctx, FIPI_ERR_OUT_OF_RANGE, "particle out of sorting range (cluster.cpp:238-257)");
     }
@@ -233,9 +244,16 @@ static fipi_status check_status(fipi_ctx* ctx) {
 fipi_status fipi_set_phase(fipi_ctx* ctx, const double* c) {
     if (!ctx || !c) return set_error(ctx, FIPI_ERR_BAD_ARG, "NULL argument");
     FIPI_CUDA(ctx, cudaSetDevice(ctx->device));
+    graphs_reset(ctx);
     fipi_status st = fields_set_phase(ctx, c);
     if (st != FIPI_OK) return st;
     ctx->t = 0;
+    // device step counter and ramp(t + 1, 0.2 t_end) for t = 0
+    const int t0 = 0;
+    const double thr = 0.2 * ctx->P.t_end;
+    const double rmp = (1.0 < thr) ? 1.0 / thr : 1.0;
+    FIPI_CUDA(ctx, h2d(ctx, ctx->d_t, &t0, sizeof(int)));
+    FIPI_CUDA(ctx, h2d(ctx, ctx->d_rmp, &rmp, sizeof(double)));
     ctx->have_phase = true;
     return check_status(ctx);
 }
@@ -328,18 +346,92 @@ fipi_status fipi_get_time(const fipi_ctx* ctx, int* t) {
     return FIPI_OK;
 }
 
+static void graphs_reset(fipi_ctx* ctx) {
+    for (auto& g : ctx->graphs) {
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+        g = fipi_ctx::StepGraph{};
+    }
+}
+
+// One iteration of main.cpp:172-316, enqueued on the context stream.
+static void enqueue_step(fipi_ctx* ctx) {
+    const int t = ctx->t;
+    fields_step_ch(ctx, t);      // main.cpp:176-238
+    particles_spread(ctx);       // main.cpp:266 (compute_f_r of the previous step's state)
+    fields_step_stokes(ctx);     // main.cpp:243-278
+    particles_step(ctx);         // main.cpp:283-316
+    step_tick(ctx);
+    ctx->t = t + 1;
+}
+
+// Steps with t >= 1 are replayed from a CUDA graph of one step.  The step
+// swaps ping-pong buffers, so the buffer assignment alternates between two
+// states; each state gets its own graph, keyed by the current c_hat buffer,
+// together with the host-side assignment the step leaves behind.
+static fipi_status graph_step(fipi_ctx* ctx, bool* done) {
+    *done = false;
+    void* key = ctx->fb.chat;
+    fipi_ctx::StepGraph* g = nullptr;
+    for (auto& x : ctx->graphs)
+        if (x.exec && x.key == key) g = &x;
+    if (!g) {
+        for (auto& x : ctx->graphs)
+            if (!x.exec) g = &x;
+        if (!g) return FIPI_OK;
+        const fipi::FieldBufs fb0 = ctx->fb;
+        const fipi::ParticleBufs pb0 = ctx->pb;
+        const int t0 = ctx->t;
+        const long long l0 = ctx->kt.launches;
+        cudaGraph_t graph = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            enqueue_step(ctx);
+            e = cudaStreamEndCapture(ctx->stream, &graph);
+        }
+        cudaGraphExec_t exec = nullptr;
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        const fipi::FieldBufs fb1 = ctx->fb;
+        const fipi::ParticleBufs pb1 = ctx->pb;
+        const long long launches = ctx->kt.launches - l0;
+        ctx->fb = fb0;  // the capture did not run anything
+        ctx->pb = pb0;
+        ctx->t = t0;
+        ctx->kt.launches = l0;
+        if (e != cudaSuccess) {  // fall back to direct launches for this context
+            cudaGetLastError();
+            ctx->use_graphs = false;
+            return FIPI_OK;
+        }
+        g->exec = exec;
+        g->key = key;
+        g->fb_after = fb1;
+        g->pb_after = pb1;
+        g->launches = launches;
+    }
+    FIPI_CUDA(ctx, cudaGraphLaunch(g->exec, ctx->stream));
+    ctx->fb = g->fb_after;
+    ctx->pb = g->pb_after;
+    ctx->t += 1;
+    ctx->kt.launches += g->launches;
+    *done = true;
+    return FIPI_OK;
+}
+
 fipi_status fipi_step_async(fipi_ctx* ctx, int nsteps) {
     if (!ctx) return set_error(ctx, FIPI_ERR_BAD_ARG, "ctx is NULL");
     if (nsteps < 0) return set_error(ctx, FIPI_ERR_BAD_ARG, "nsteps < 0");
     if (!ctx->have_phase) return set_error(ctx, FIPI_ERR_STATE, "fipi_set_phase must come before fipi_step");
     FIPI_CUDA(ctx, cudaSetDevice(ctx->device));
     for (int s = 0; s < nsteps; ++s) {
-        const int t = ctx->t;
-        fields_step_ch(ctx, t);      // main.cpp:176-238
-        particles_spread(ctx);       // main.cpp:266 (compute_f_r of the previous step's state)
-        fields_step_stokes(ctx);     // main.cpp:243-278
-        particles_step(ctx, t);      // main.cpp:283-316
-        ctx->t = t + 1;
+        const bool spread_ready = ctx->pb.sp_prev_valid || ctx->pb.n == 0 || !ctx->P.switch_particle;
+        if (ctx->use_graphs && ctx->t > 0 && !ctx->kt.enabled && spread_ready) {
+            bool done = false;
+            fipi_status st = graph_step(ctx, &done);
+            if (st != FIPI_OK) return st;
+            if (done) continue;
+        }
+        enqueue_step(ctx);
     }
     FIPI_CUDA(ctx, cudaGetLastError());
     return FIPI_OK;
@@ -378,18 +470,13 @@ fipi_status fipi_free_energy(fipi_ctx* ctx, double* out) {
 fipi_status fipi_packing_tau(fipi_ctx* ctx, double* out) {
     if (!ctx || !out) return set_error(ctx, FIPI_ERR_BAD_ARG, "NULL argument");
     FIPI_CUDA(ctx, cudaSetDevice(ctx->device));
-    if (ctx->pb.n == 0) {
-        *out = 0.0;
-        return FIPI_OK;
-    }
-    FIPI_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    FIPI_CUDA(ctx, d2h(ctx, out, ctx->pb.tau, sizeof(double)));
-    return FIPI_OK;
+    return particles_packing_tau(ctx, out);
 }
 
 // ---------------------------------------------------------------- instrumentation
 fipi_status fipi_set_kernel_timing(fipi_ctx* ctx, int enable) {
     if (!ctx) return set_error(ctx, FIPI_ERR_BAD_ARG, "ctx is NULL");
+    FIPI_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     drain_timer(ctx);
     ctx->kt.stats.clear();
     ctx->kt.enabled = enable != 0;

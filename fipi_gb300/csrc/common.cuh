@@ -34,6 +34,7 @@ template <typename C> __device__ __forceinline__ C cmul_i(C a, int dir) {
 enum : int {
     ERR_OUT_OF_RANGE = 1,  // particle outside the cell grid (cluster.cpp:238-257)
     ERR_NONFINITE = 2,     // NaN/Inf seen in a particle position
+    ERR_TMA_TIMEOUT = 4,   // a bounded wait for a bulk copy gave up
 };
 
 __host__ __device__ __forceinline__ int ilog2i(int n) {

@@ -68,6 +68,10 @@ struct ParticleBufs {
     int hist_cap = 0;
     // diagnostics
     double* tau_part = nullptr;  // n, per-particle packing-energy terms
+    float4* spos = nullptr;      // n, sorted cell-relative FP32 positions + id (mixed form)
+    void* sp_fw = nullptr;       // 6 x n (TA): spread force density (3) and trilinear fractions (3)
+    unsigned long long* ymax = nullptr;  // [max p_y bits, first index] for it_mark
+    bool tau_valid = false;
     int* it_mark = nullptr;      // 1
     double* tau = nullptr;       // 1
 };
@@ -96,16 +100,29 @@ struct fipi_ctx {
     fipi_params P{};
     fipi_precision prec = FIPI_FP64;
     int device = 0;
+    int num_sms = 0;
     cudaStream_t stream = nullptr;
     fipi::Geom g{};
     fipi::FieldBufs fb;
     fipi::ParticleBufs pb;
-    double* k0 = nullptr;        // mixed form FP64 k=0 mode: [c0, c0_old, C0_old, C0_cur]
+    double* k0 = nullptr;        // mixed form FP64 k=0 mode: [c0, c0_old, C0_old, C0_cur, (float) c0/V]
     double* partials = nullptr;  // per-block FP64 partial sums
     int n_partials = 0;
     int* status = nullptr;       // device error word
     double* scratch_d = nullptr; // small FP64 device scratch (reductions)
     int t = 0;
+    int* d_t = nullptr;          // device copy of t (advanced by step_tick)
+    double* d_rmp = nullptr;     // ramp(t + 1, 0.2 t_end) for the next step
+    // CUDA graphs of one step (t >= 1) for each of the two states of the
+    // ping-pong buffers; `after` is the host-side buffer state the step leaves
+    struct StepGraph {
+        cudaGraphExec_t exec = nullptr;
+        void* key = nullptr;     // fb.chat when captured (identifies the state)
+        fipi::FieldBufs fb_after;
+        fipi::ParticleBufs pb_after;
+        long long launches = 0;
+    } graphs[2];
+    bool use_graphs = true;
     bool have_phase = false;
     bool track_tau = true;     // packing energy during the step (cluster.cpp:350-353)
     size_t device_bytes = 0;
@@ -142,8 +159,10 @@ fipi_status particles_alloc(fipi_ctx* ctx);
 void particles_free(fipi_ctx* ctx);
 // Spread f_pp at p onto the dense spread grid (enqueue).
 void particles_spread(fipi_ctx* ctx);
-// Two Heun stages (enqueue); t is the step index (ramp uses t + 1).
-void particles_step(fipi_ctx* ctx, int t);
+// Two Heun stages (enqueue); the ramp factor is read from ctx->d_rmp.
+void particles_step(fipi_ctx* ctx);
+// t += 1 on the device and the next step's ramp factor.
+void step_tick(fipi_ctx* ctx);
 // Fine-grained parity entry points (synchronous, host arrays).
 fipi_status particles_cells_build(fipi_ctx* ctx, const double* p, int* keys, int* sorted,
                                   int* offsets);
@@ -159,6 +178,8 @@ fipi_status particles_advect(fipi_ctx* ctx, int stage, const double* f_pi, const
                              const double* r, double* p, double* p_old, double* u_old);
 fipi_status particles_spread_host(fipi_ctx* ctx, const double* p, const double* f_pp,
                                   double* out);
+// Packing energy of the last contact-force evaluation.
+fipi_status particles_packing_tau(fipi_ctx* ctx, double* out);
 
 // Brackets one kernel launch: counts it and, when timing is on, records
 // events around it on the context stream (capi.cu).
@@ -186,9 +207,15 @@ inline cudaError_t d2h(fipi_ctx* ctx, void* h, const void* d, size_t n) {
     cudaError_t e = cudaMemcpyAsync(h, d, n, cudaMemcpyDeviceToHost, ctx->stream);
     return e != cudaSuccess ? e : cudaStreamSynchronize(ctx->stream);
 }
-// Raises a kernel's dynamic shared-memory limit to `bytes` when needed
-// (per kernel instantiation; `cur` remembers what was granted).
+// Raises a kernel's dynamic shared-memory limit to `bytes` when needed and,
+// on first use, asks for the largest shared-memory carveout so several
+// blocks fit per SM (per kernel instantiation; `cur` remembers the grant,
+// starting at 48 KiB).
 template <class K> inline cudaError_t ensure_smem(K kern, size_t bytes, size_t& cur) {
+    if (cur == 48 * 1024) {
+        cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+        cur = 48 * 1024 + 1;
+    }
     if (bytes <= cur) return cudaSuccess;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     if (e == cudaSuccess) cur = bytes;

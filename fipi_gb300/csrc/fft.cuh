@@ -23,6 +23,8 @@
 #pragma once
 
 #include "common.cuh"
+#include "fft2.cuh"
+#include "tma.cuh"
 
 namespace fipi {
 
@@ -42,147 +44,224 @@ template <typename T> struct Tiles {
     static constexpr int TZ = 128 / (2 * sizeof(T));
 };
 
-// In-place FFT of `rows` rows of length n (power of two, 4 <= n <= 4*blockDim)
-// held in shared memory at s[r*pitch + e].  tw[q*ts] = exp(-2 pi i q / n).
-// dir = -1 forward, +1 backward (conjugated twiddles).  All threads of the
-// block must call it.
-template <typename T>
-__device__ __forceinline__ void smem_fft(cplx<T>* s, int n, int log2n, int rows, int pitch,
-                                         const cplx<T>* __restrict__ tw, int ts, int dir) {
-    using C = cplx<T>;
-    const int tid = threadIdx.x;
-    const int q4 = n >> 2;
-    int rpg = (4 * (int)blockDim.x) / n;
-    if (rpg > rows) rpg = rows;
-    const int active = rpg * q4;
-    const int lrow = tid / q4;
-    const int i0 = tid - lrow * q4;
-    for (int r0 = 0; r0 < rows; r0 += rpg) {
-        const bool act = (tid < active) && (r0 + lrow < rows);
-        C* row = s + (size_t)(r0 + lrow) * pitch;
-        int p = 1;
-        if (log2n & 1) {  // radix-2 stage with p = 1 (no twiddles): tasks i0 and i0 + q4
-            C u0, u1, u2, u3;
-            const int half = n >> 1;
-            if (act) {
-                u0 = row[i0];
-                u1 = row[i0 + half];
-                u2 = row[i0 + q4];
-                u3 = row[i0 + q4 + half];
-            }
-            __syncthreads();
-            if (act) {
-                row[2 * i0] = cadd(u0, u1);
-                row[2 * i0 + 1] = csub(u0, u1);
-                row[2 * (i0 + q4)] = cadd(u2, u3);
-                row[2 * (i0 + q4) + 1] = csub(u2, u3);
-            }
-            __syncthreads();
-            p = 2;
-        }
-        for (; p < n; p <<= 2) {
-            C v0, v1, v2, v3;
-            const int k = i0 & (p - 1);
-            if (act) {
-                C u0 = row[i0], u1 = row[i0 + q4], u2 = row[i0 + 2 * q4], u3 = row[i0 + 3 * q4];
-                if (p > 1) {
-                    const int step = (n / (4 * p)) * k * ts;
-                    C w1 = tw[step], w2 = tw[2 * step], w3 = tw[3 * step];
-                    if (dir > 0) {
-                        w1.y = -w1.y;
-                        w2.y = -w2.y;
-                        w3.y = -w3.y;
-                    }
-                    u1 = cmul(u1, w1);
-                    u2 = cmul(u2, w2);
-                    u3 = cmul(u3, w3);
-                }
-                const C a0 = cadd(u0, u2), a1 = csub(u0, u2), a2 = cadd(u1, u3);
-                const C a3 = cmul_i(csub(u1, u3), dir);
-                v0 = cadd(a0, a2);
-                v1 = cadd(a1, a3);
-                v2 = csub(a0, a2);
-                v3 = csub(a1, a3);
-            }
-            __syncthreads();
-            if (act) {
-                const int o = (i0 - k) * 4 + k;
-                row[o] = v0;
-                row[o + p] = v1;
-                row[o + 2 * p] = v2;
-                row[o + 3 * p] = v3;
-            }
-            __syncthreads();
-        }
-    }
-}
-
 // ----------------------------------------------------------------- Y pass
 template <typename T> struct FieldPtrs {
     cplx<T>* in[8];
     cplx<T>* out[8];
 };
 
+// Rows per Y-pass block: 256 threads, Tn = fft_threads_per_row(ny) per row.
+template <typename T> __host__ __device__ inline int ypass_rows(int ny) { return kThreads / fft_threads_per_row<T>(ny); }
+
 // C2C along contiguous rows of length ny; blockIdx.y selects the field.
-template <typename T>
-__global__ void __launch_bounds__(kThreads) k_ypass(Geom g, const cplx<T>* __restrict__ twy, int dir,
-                                                   FieldPtrs<T> fp, int rows_per_block) {
+// Rows are staged in shared memory with one pad slot per 16 elements.
+template <typename T, int DIR, int N>
+__global__ void __launch_bounds__(kThreads) k_ypass(Geom g, const cplx<T>* __restrict__ twy, FieldPtrs<T> fp) {
     using C = cplx<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* s = reinterpret_cast<C*>(smem_raw);
+    constexpr int Tn = FftPlan<N, FftE<T>::value>::Tn;
+    const int rpb = kThreads / Tn;
     const long long total_rows = (long long)g.nz * g.h;
-    const long long r0 = (long long)blockIdx.x * rows_per_block;
-    int rows = rows_per_block;
-    if (r0 + rows > total_rows) rows = (int)(total_rows - r0);
-    const C* in = fp.in[blockIdx.y] + r0 * g.ny;
-    C* out = fp.out[blockIdx.y] + r0 * g.ny;
-    const int n = rows * g.ny;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) s[i] = in[i];
+    const long long r0 = (long long)blockIdx.x * rpb;
+    const int rows = (int)min((long long)rpb, total_rows - r0);
+    const C* in = fp.in[blockIdx.y] + r0 * N;
+    C* out = fp.out[blockIdx.y] + r0 * N;
+    const IdxPadded idx{padded_len(N)};
+    using IO = FftIO<T, DIR, N>;
+    const int tid = threadIdx.x;
+    const int row = tid / Tn, t = tid - row * Tn;
+    const bool act = row < rows;
+    // first stage straight from global memory, last stage straight back
+    C v[IO::E];
+    if (act) {
+#pragma unroll
+        for (int i = 0; i < IO::E; ++i) v[i] = in[(size_t)row * N + IO::in_elem(t, i)];
+    }
+    smem_fft2<T, DIR, N, true, true>(s, idx, row, t, act, twy, 1, v);
+    if (act) {
+#pragma unroll
+        for (int i = 0; i < IO::E; ++i) out[(size_t)row * N + IO::out_elem(t, i)] = v[i];
+    }
+}
+
+template <typename T> inline size_t ypass_smem(const Geom& g) {
+    return (size_t)ypass_rows<T>(g.ny) * padded_len(g.ny) * sizeof(cplx<T>);
+}
+
+// Persistent Y pass: each block streams tiles of RB consecutive rows
+// (RB * N contiguous complex values) into shared memory with one bulk TMA
+// copy per tile, double-buffered so tile k+1 is in flight while tile k is
+// transformed; the buffer a tile arrived in then serves as that tile's
+// (padded) exchange buffer.  The first stage reads the tile, the last
+// stage stores straight to global memory.  `fields` fields of rows are
+// processed in one launch.
+template <typename T, int DIR, int N>
+__global__ void __launch_bounds__(kThreads) k_ypass_tma(Geom g, const cplx<T>* __restrict__ twy, FieldPtrs<T> fp,
+                                                       int fields, int* status) {
+    using C = cplx<T>;
+    using IO = FftIO<T, DIR, N>;
+    constexpr int Tn = FftPlan<N, FftE<T>::value>::Tn;
+    constexpr int RB = kThreads / Tn;
+    constexpr int BUF = RB * ((N + (N >> 4) + 15) & ~15);  // padded rows, 128-byte multiple for FP32/FP64
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    C* buf0 = reinterpret_cast<C*>(smem_raw);
+    __shared__ __align__(8) uint64_t bar[2];
+    __shared__ int abort_flag;
+    const int tid = threadIdx.x;
+    const long long rows_f = (long long)g.nz * g.h;
+    const long long tiles_f = (rows_f + RB - 1) / RB;
+    const long long ntiles = tiles_f * fields;
+    const IdxPadded xidx{padded_len(N)};
+    if (tid == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        fence_mbar_init();
+        abort_flag = 0;
+    }
     __syncthreads();
-    smem_fft<T>(s, g.ny, g.ly, rows, g.ny, twy, 1, dir);
-    for (int i = threadIdx.x; i < n; i += blockDim.x) out[i] = s[i];
+    auto issue = [&](long long tile, int b) {
+        const int f = (int)(tile / tiles_f);
+        const long long r0 = (tile - (long long)f * tiles_f) * RB;
+        const int rows = (int)min((long long)RB, rows_f - r0);
+        const uint32_t bytes = (uint32_t)(rows * N * sizeof(C));
+        mbar_arrive_expect_tx(&bar[b], bytes);
+        bulk_g2s(buf0 + b * BUF, fp.in[f] + r0 * N, bytes, &bar[b]);
+    };
+    long long tile = blockIdx.x;
+    if (tid == 0 && tile < ntiles) issue(tile, 0);
+    uint32_t parity0 = 0, parity1 = 0;
+    int b = 0;
+    for (; tile < ntiles; tile += gridDim.x) {
+        const int f = (int)(tile / tiles_f);
+        const long long r0 = (tile - (long long)f * tiles_f) * RB;
+        const int rows = (int)min((long long)RB, rows_f - r0);
+        const uint32_t par = b ? parity1 : parity0;
+        const bool ok = mbar_wait(&bar[b], par);
+        if (b) parity1 ^= 1u;
+        else parity0 ^= 1u;
+        if (!ok) abort_flag = 1;
+        C* in = buf0 + b * BUF;
+        const int row = tid / Tn, t = tid - row * Tn;
+        const bool act = row < rows;
+        C v[IO::E];
+        if (act && ok) {
+#pragma unroll
+            for (int i = 0; i < IO::E; ++i) v[i] = in[row * N + IO::in_elem(t, i)];
+        }
+        // generic-proxy accesses of the other buffer (previous tile) are
+        // ordered before the bulk copy that will overwrite it
+        fence_proxy_async_smem();
+        __syncthreads();  // the tile is in registers; the other buffer's previous tile is finished
+        if (abort_flag) {
+            if (tid == 0) {
+                atomicOr(status, ERR_TMA_TIMEOUT);
+                mbar_wait(&bar[b], par);  // bounded: let the late copy land before the block exits
+            }
+            return;
+        }
+        const long long next = tile + gridDim.x;
+        if (tid == 0 && next < ntiles) issue(next, b ^ 1);
+        smem_fft2<T, DIR, N, true, true>(in, xidx, row, t, act, twy, 1, v);
+        if (act) {
+            C* out = fp.out[f] + (r0 + row) * N;
+#pragma unroll
+            for (int i = 0; i < IO::E; ++i) out[IO::out_elem(t, i)] = v[i];
+        }
+        b ^= 1;
+    }
+}
+
+template <typename T> inline size_t ypass_tma_smem(const Geom& g) {
+    const int tn = fft_threads_per_row<T>(g.ny);
+    const int rb = kThreads / tn;
+    const int row = (g.ny + (g.ny >> 4) + 15) & ~15;
+    return (size_t)2 * rb * row * sizeof(cplx<T>);
 }
 
 // ----------------------------------------------------------------- Z pass
-// One block = kx = blockIdx.x, ky in [blockIdx.y*TZ, +TZ), all kz, NF fields.
+// One block = kx = blockIdx.x, ky in [blockIdx.y*TZ, +TZ), all kz, NF fields
+// (TZ = zpass_cols: 128-byte runs of ky).
+// Threads: column c = tid % TZ (fastest, so global runs and shared-memory
+// accesses are contiguous), t = tid / TZ; blockDim = TZ * nz/min(16, nz).
 // Op provides
 //   void load(int kx, int ky, int kz, size_t gi, cplx<T> v[NF])
 //   void store(int kx, int ky, int kz, size_t gi, cplx<T> v[NF])
 // with gi = (kz*H + kx)*ny + ky the spectral index of the mode.
-template <typename T, int NF, class Op>
-__global__ void __launch_bounds__(kThreads) k_zpass(Geom g, const cplx<T>* __restrict__ twz, int dir, Op op) {
+// Columns per Z-pass block: 128-byte runs, fewer when nz needs > 256 threads.
+template <typename T> __host__ __device__ inline int zpass_cols(int nz) {
+    const int tn = fft_threads_per_row<T>(nz);
+    return Tiles<T>::TZ * tn <= kThreads ? Tiles<T>::TZ : kThreads / tn;
+}
+template <typename T> __host__ __device__ inline int zpass_threads(int nz) {
+    return zpass_cols<T>(nz) * fft_threads_per_row<T>(nz);
+}
+
+template <typename T, int NF, int DIR, int N, class Op>
+__global__ void __launch_bounds__(kThreads) k_zpass(Geom g, const cplx<T>* __restrict__ twz, Op op) {
     using C = cplx<T>;
-    constexpr int TZ = Tiles<T>::TZ;
+    constexpr int EM = FftE<T>::value;
+    constexpr int E = N < EM ? N : EM;
+    constexpr int Tn = N / E;
+    constexpr int TZ = Tiles<T>::TZ * Tn <= kThreads ? Tiles<T>::TZ : kThreads / Tn;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* s = reinterpret_cast<C*>(smem_raw);
     const int kx = blockIdx.x, ky0 = blockIdx.y * TZ;
-    const int pitch = g.nz + 1;
-    const int tid = threadIdx.x, nthr = blockDim.x;
-    for (int idx = tid; idx < g.nz * TZ; idx += nthr) {
-        const int kyl = idx % TZ;
-        const int z = idx / TZ;
-        const size_t gi = ((size_t)z * g.h + kx) * g.ny + ky0 + kyl;
-        C v[NF];
-        op.load(kx, ky0 + kyl, z, gi, v);
+    const int c = threadIdx.x % TZ, t = threadIdx.x / TZ;
+    const int ky = ky0 + c;
+    const size_t zstride = (size_t)g.h * g.ny;
+    const size_t base = (size_t)kx * g.ny + ky;
+    const IdxColumns idx{TZ};
+    constexpr size_t fstride = (size_t)N * TZ;
+    if constexpr (NF == 1) {
+        // the loaded modes are exactly the first stage's inputs
+        using IO = FftIO<T, DIR, N>;
+        C v[IO::E];
 #pragma unroll
-        for (int f = 0; f < NF; ++f) s[(f * TZ + kyl) * pitch + z] = v[f];
+        for (int i = 0; i < IO::E; ++i) {
+            const int z = IO::in_elem(t, i);
+            C w[1];
+            op.load(kx, ky, z, base + z * zstride, w);
+            v[i] = w[0];
+        }
+        smem_fft2<T, DIR, N, true, false>(s, idx, c, t, true, twz, 1, v);
+    } else {
+        // loads in chunks of CH modes per thread: CH * NF independent loads in flight
+        constexpr int CH = 8 / NF >= 2 ? 8 / NF : 2;
+#pragma unroll
+        for (int i0 = 0; i0 < E; i0 += CH) {
+            C v[CH][NF];
+#pragma unroll
+            for (int u = 0; u < CH; ++u)
+                if (i0 + u < E) {
+                    const int z = t + Tn * (i0 + u);
+                    op.load(kx, ky, z, base + z * zstride, v[u]);
+                }
+#pragma unroll
+            for (int u = 0; u < CH; ++u)
+                if (i0 + u < E) {
+                    const int z = t + Tn * (i0 + u);
+#pragma unroll
+                    for (int f = 0; f < NF; ++f) s[f * fstride + idx(c, z)] = v[u][f];
+                }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int f = 0; f < NF; ++f) smem_fft2<T, DIR, N>(s + f * fstride, idx, c, t, true, twz, 1);
     }
-    __syncthreads();
-    smem_fft<T>(s, g.nz, g.lz, NF * TZ, pitch, twz, 1, dir);
-    for (int idx = tid; idx < g.nz * TZ; idx += nthr) {
-        const int kyl = idx % TZ;
-        const int z = idx / TZ;
-        const size_t gi = ((size_t)z * g.h + kx) * g.ny + ky0 + kyl;
+#pragma unroll 4
+    for (int i = 0; i < E; ++i) {
+        const int z = t + Tn * i;
         C v[NF];
 #pragma unroll
-        for (int f = 0; f < NF; ++f) v[f] = s[(f * TZ + kyl) * pitch + z];
-        op.store(kx, ky0 + kyl, z, gi, v);
+        for (int f = 0; f < NF; ++f) v[f] = s[f * fstride + idx(c, z)];
+        op.store(kx, ky, z, base + z * zstride, v);
     }
 }
 
 template <typename T, int NF>
 inline size_t zpass_smem(const Geom& g) {
-    return (size_t)NF * Tiles<T>::TZ * (g.nz + 1) * sizeof(cplx<T>);
+    return (size_t)NF * zpass_cols<T>(g.nz) * g.nz * sizeof(cplx<T>);
 }
 
 }  // namespace fipi

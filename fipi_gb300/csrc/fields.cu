@@ -89,6 +89,12 @@ __device__ __forceinline__ double block_sum(double v) {
     return s;  // valid in thread 0
 }
 
+// Row pitch of the X pass: padded M plus the X_M slot, kept odd.
+__host__ __device__ inline int xpass_pitch(int M) {
+    const int p = padded_len(M) + 1;
+    return (p & 1) ? p : p + 1;
+}
+
 // ------------------------------------------------------------ X-pass ops
 // R2C of c and of f = (lambda/eps^2)(c^3 - c) from the real c (set-up).
 template <typename T> struct OpInitCF {
@@ -144,7 +150,7 @@ template <typename T, bool MIXED> struct OpConv {
     int nx, ny;
     __device__ const C* in(int f) const { return uS[f]; }
     __device__ C* out(int) const { return o0; }
-    __device__ void point(int z, int y, int n, C* v, double& acc) const {
+    template <class A> __device__ void point(int z, int y, int n, C* v, A& acc) const {
         const size_t row = ((size_t)z * ny + y) * nx;
         T s0 = T(0), s1 = T(0);
 #pragma unroll
@@ -154,7 +160,7 @@ template <typename T, bool MIXED> struct OpConv {
             s1 += v[d].y * gg.y;
         }
         v[0] = mkc<C>(s0, s1);
-        if (MIXED) acc += (double)s0 + (double)s1;
+        if (MIXED) acc += s0 + s1;  // per-thread FP32 partial; FP64 from the block sum on
     }
 };
 
@@ -164,18 +170,17 @@ template <typename T, bool MIXED> struct OpCF {
     const C* cS;
     T* c;
     C* o0;
-    const double* k0;  // mixed: k0[0] = c_hat(0) in FP64
-    double invV;
+    const float* cbar;  // mixed: mean of c (the FP64 k = 0 mode / V) rounded to FP32
     T lam_eps;
     int nx, ny;
     __device__ const C* in(int) const { return cS; }
     __device__ C* out(int) const { return o0; }
-    __device__ void point(int z, int y, int n, C* v, double&) const {
+    template <class A> __device__ void point(int z, int y, int n, C* v, A&) const {
         C cc = v[0];
         if (MIXED) {
-            const T cbar = T(k0[0] * invV);
-            cc.x += cbar;
-            cc.y += cbar;
+            const T cb = (T)*cbar;
+            cc.x += cb;
+            cc.y += cb;
         }
         reinterpret_cast<C*>(c + ((size_t)z * ny + y) * nx)[n] = cc;
         v[0] = mkc<C>((cc.x * cc.x * cc.x - cc.x) * lam_eps, (cc.y * cc.y * cc.y - cc.y) * lam_eps);
@@ -195,7 +200,7 @@ template <typename T> struct OpForce {
     int nx, ny;
     __device__ const C* in(int f) const { return S[f]; }
     __device__ C* out(int f) const { return const_cast<C*>(S[f]); }
-    __device__ void point(int z, int y, int n, C* v, double&) const {
+    template <class A> __device__ void point(int z, int y, int n, C* v, A&) const {
         const size_t row = ((size_t)z * ny + y) * nx;
         const C mu = v[0];
         const C cc = reinterpret_cast<const C*>(c + row)[n];
@@ -225,97 +230,120 @@ template <class Op> struct NoAcc {
     Op op;
     __device__ const auto* in(int f) const { return op.in(f); }
     __device__ auto* out(int f) const { return op.out(f); }
-    template <class C> __device__ void point(int z, int y, int n, C* v, double&) const { op.point(z, y, n, v); }
+    template <class C, class A> __device__ void point(int z, int y, int n, C* v, A&) const { op.point(z, y, n, v); }
 };
 
-// X pass with an FP64 per-block reduction of point()'s accumulator.
-template <typename T, int NIN, int NOUT, bool REDUCE, class Op>
-__global__ void __launch_bounds__(kThreads) k_xpass_acc(Geom g, const cplx<T>* __restrict__ twx, Op op,
+// X pass: one block = TY consecutive rows y0..y0+TY-1 of plane z, NIN
+// spectral inputs (transposed runs of TY along y, C2R) and NOUT spectral
+// outputs (R2C, transposed store); point() does the fused real-space work
+// and may accumulate an FP64 per-block sum.  Rows of M = nx/2 complex pairs
+// live in shared memory with one pad slot per 16 (pitch odd, so the
+// transposed column accesses are conflict-free); X_M sits at index M.
+template <typename T, int NIN, int NOUT, bool REDUCE, int M, class Op>
+__global__ void __launch_bounds__(kThreads, 3) k_xpass_acc(Geom g, const cplx<T>* __restrict__ twx, Op op,
                                                       double* partials) {
     using C = cplx<T>;
     constexpr int TY = Tiles<T>::TY;
     constexpr int NF = NIN > NOUT ? NIN : NOUT;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* s = reinterpret_cast<C*>(smem_raw);
-    const int M = g.m, H = g.h, pitch = M + 1;
+    constexpr int H = M + 1;
+    const IdxPadded idx{xpass_pitch(M)};
     const int z = blockIdx.y, y0 = blockIdx.x * TY;
     const int tid = threadIdx.x, nthr = blockDim.x;
-    const int halfM = M / 2;
+    constexpr int halfM = M / 2;
+    constexpr int Tn = FftPlan<M, FftE<T>::value>::Tn;
+    constexpr int rpr = kThreads / Tn;  // row FFTs per round
     if constexpr (NIN > 0) {
-        for (int idx = tid; idx < NIN * H * TY; idx += nthr) {
-            const int ty = idx % TY;
-            const int rest = idx / TY;
-            const int kx = rest % H;
-            const int f = rest / H;
-            s[(f * TY + ty) * pitch + kx] = op.in(f)[((size_t)z * H + kx) * g.ny + y0 + ty];
-        }
-        __syncthreads();
-        for (int idx = tid; idx < NIN * TY * (halfM + 1); idx += nthr) {
-            const int k = idx % (halfM + 1);
-            C* r = s + (idx / (halfM + 1)) * pitch;
-            if (k == 0) {
-                const T a = r[0].x, c = r[M].x;
-                r[0] = mkc<C>(a + c, a - c);
-            } else {
-                const int km = M - k;
-                const C Xk = r[k], Xm = r[km];
-                const C Wk = twx[k], Wm = twx[km];
-                const C A = cadd(Xk, cconj(Xm)), B = csub(Xk, cconj(Xm));
-                const C A2 = cadd(Xm, cconj(Xk)), B2 = csub(Xm, cconj(Xk));
-                const C Zk = cadd(A, cmul_i(cmul(B, cconj(Wk)), +1));
-                const C Zm = cadd(A2, cmul_i(cmul(B2, cconj(Wm)), +1));
-                r[k] = Zk;
-                if (km != k) r[km] = Zm;
+        const int n = NIN * H * TY;
+        for (int b = tid; b < n; b += 8 * kThreads) {
+            C tmp[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int i = b + u * kThreads;
+                if (i < n) {
+                    const int ty = i % TY, rest = i / TY, kx = rest % H, f = rest / H;
+                    tmp[u] = op.in(f)[((size_t)z * H + kx) * g.ny + y0 + ty];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int i = b + u * kThreads;
+                if (i < n) {
+                    const int ty = i % TY, rest = i / TY, kx = rest % H, f = rest / H;
+                    s[idx(f * TY + ty, kx)] = tmp[u];
+                }
             }
         }
         __syncthreads();
-        smem_fft<T>(s, M, g.lm, NIN * TY, pitch, twx, 2, +1);
+        // C2R split pre-processing (only the real parts of X_0 and X_M enter).
+        for (int i = tid; i < NIN * TY * (halfM + 1); i += nthr) {
+            const int k = i % (halfM + 1);
+            const int row = i / (halfM + 1);
+            if (k == 0) {
+                const T a = s[idx(row, 0)].x, c = s[idx(row, M)].x;
+                s[idx(row, 0)] = mkc<C>(a + c, a - c);
+            } else {
+                const int km = M - k;
+                const C Xk = s[idx(row, k)], Xm = s[idx(row, km)];
+                const C Wk = twx[k], Wm = twx[km];
+                const C A = cadd(Xk, cconj(Xm)), B = csub(Xk, cconj(Xm));
+                const C A2 = cadd(Xm, cconj(Xk)), B2 = csub(Xm, cconj(Xk));
+                s[idx(row, k)] = cadd(A, cmul_i(cmul(B, cconj(Wk)), +1));
+                if (km != k) s[idx(row, km)] = cadd(A2, cmul_i(cmul(B2, cconj(Wm)), +1));
+            }
+        }
+        __syncthreads();
+        for (int r0 = 0; r0 < NIN * TY; r0 += rpr) {
+            const int row = r0 + tid / Tn;
+            smem_fft2<T, +1, M>(s, idx, row, tid % Tn, row < NIN * TY, twx, 2);
+        }
     }
     const T invV = T(1) / T(g.V);
-    double acc = 0.0;
-    for (int idx = tid; idx < TY * M; idx += nthr) {
-        const int n = idx % M;
-        const int ty = idx / M;
+    T acc = T(0);  // per-thread partial sum in the arithmetic type (FP64 only per block)
+    for (int i = tid; i < TY * M; i += nthr) {
+        const int n = i % M;
+        const int ty = i / M;
         C v[NF];
 #pragma unroll
-        for (int f = 0; f < NIN; ++f) v[f] = cscale(s[(f * TY + ty) * pitch + n], invV);
+        for (int f = 0; f < NIN; ++f) v[f] = cscale(s[idx(f * TY + ty, n)], invV);
         op.point(z, y0 + ty, n, v, acc);
 #pragma unroll
-        for (int f = 0; f < NOUT; ++f) s[(f * TY + ty) * pitch + n] = v[f];
+        for (int f = 0; f < NOUT; ++f) s[idx(f * TY + ty, n)] = v[f];
     }
     if constexpr (REDUCE) {
-        const double bs = block_sum(acc);
+        const double bs = block_sum((double)acc);
         if (tid == 0) partials[(size_t)blockIdx.y * gridDim.x + blockIdx.x] = bs;
     }
     __syncthreads();
     if constexpr (NOUT > 0) {
-        smem_fft<T>(s, M, g.lm, NOUT * TY, pitch, twx, 2, -1);
-        for (int idx = tid; idx < NOUT * TY * (halfM + 1); idx += nthr) {
-            const int k = idx % (halfM + 1);
-            C* r = s + (idx / (halfM + 1)) * pitch;
+        for (int r0 = 0; r0 < NOUT * TY; r0 += rpr) {
+            const int row = r0 + tid / Tn;
+            smem_fft2<T, -1, M>(s, idx, row, tid % Tn, row < NOUT * TY, twx, 2);
+        }
+        // R2C split post-processing; X_M lands at index M.
+        for (int i = tid; i < NOUT * TY * (halfM + 1); i += nthr) {
+            const int k = i % (halfM + 1);
+            const int row = i / (halfM + 1);
             if (k == 0) {
-                const C Z0 = r[0];
-                r[0] = mkc<C>(Z0.x + Z0.y, T(0));
-                r[M] = mkc<C>(Z0.x - Z0.y, T(0));
+                const C Z0 = s[idx(row, 0)];
+                s[idx(row, 0)] = mkc<C>(Z0.x + Z0.y, T(0));
+                s[idx(row, M)] = mkc<C>(Z0.x - Z0.y, T(0));
             } else {
                 const int km = M - k;
-                const C Zk = r[k], Zm = r[km];
+                const C Zk = s[idx(row, k)], Zm = s[idx(row, km)];
                 const C Wk = twx[k], Wm = twx[km];
                 const C E1 = cadd(Zk, cconj(Zm)), D1 = csub(Zk, cconj(Zm));
                 const C E2 = cadd(Zm, cconj(Zk)), D2 = csub(Zm, cconj(Zk));
-                const C Xk = cscale(csub(E1, cmul_i(cmul(Wk, D1), +1)), T(0.5));
-                const C Xm = cscale(csub(E2, cmul_i(cmul(Wm, D2), +1)), T(0.5));
-                r[k] = Xk;
-                if (km != k) r[km] = Xm;
+                s[idx(row, k)] = cscale(csub(E1, cmul_i(cmul(Wk, D1), +1)), T(0.5));
+                if (km != k) s[idx(row, km)] = cscale(csub(E2, cmul_i(cmul(Wm, D2), +1)), T(0.5));
             }
         }
         __syncthreads();
-        for (int idx = tid; idx < NOUT * H * TY; idx += nthr) {
-            const int ty = idx % TY;
-            const int rest = idx / TY;
-            const int kx = rest % H;
-            const int f = rest / H;
-            op.out(f)[((size_t)z * H + kx) * g.ny + y0 + ty] = s[(f * TY + ty) * pitch + kx];
+        const int n = NOUT * H * TY;
+        for (int i = tid; i < n; i += nthr) {
+            const int ty = i % TY, rest = i / TY, kx = rest % H, f = rest / H;
+            op.out(f)[((size_t)z * H + kx) * g.ny + y0 + ty] = s[idx(f * TY + ty, kx)];
         }
     }
 }
@@ -487,7 +515,7 @@ template <typename T, int NF> struct ZOpStore {
 // FP64 k = 0 update of the mixed form: c_hat(0) follows the same IMEX /
 // SBDF2 recurrence with k = 0 (the f terms vanish), C(0) from the FP64
 // per-block sums of conv.  k0 = [c0, c0_old, C0_old, C0_cur].
-__global__ void k_k0_update(double* k0, const double* partials, int np, int first, double dt) {
+__global__ void k_k0_update(double* k0, const double* partials, int np, int first, double dt, double invV) {
     double s = 0.0;
     for (int i = threadIdx.x; i < np; i += blockDim.x) s += partials[i];
     s = block_sum(s);
@@ -506,6 +534,7 @@ __global__ void k_k0_update(double* k0, const double* partials, int np, int firs
         k0[0] = nw;
         k0[2] = s;
         k0[3] = s;
+        *reinterpret_cast<float*>(k0 + 4) = (float)(nw * invV);  // mean of c for the FP32 fields
     }
 }
 
@@ -558,12 +587,15 @@ void launch_x(fipi_ctx* ctx, const char* name, int nreal, const Op& op, double* 
     LaunchScope ls(ctx, name,
                    (double)(NIN + NOUT) * g.SH * sizeof(cplx<T>) + (double)nreal * g.V * sizeof(T));
     constexpr int NF = NIN > NOUT ? NIN : NOUT;
-    const size_t smem = (size_t)NF * Tiles<T>::TY * (g.m + 1) * sizeof(cplx<T>);
-    auto kern = k_xpass_acc<T, NIN, NOUT, REDUCE, Op>;
-    static size_t granted = 48 * 1024;
-    ensure_smem(kern, smem, granted);
+    const size_t smem = (size_t)NF * Tiles<T>::TY * xpass_pitch(g.m) * sizeof(cplx<T>);
     dim3 grid(g.ny / Tiles<T>::TY, g.nz);
-    kern<<<grid, kThreads, smem, ctx->stream>>>(g, (const cplx<T>*)ctx->fb.twx, op, partials);
+    dispatch_pow2(g.m, [&](auto MC) {
+        constexpr int M = decltype(MC)::value;
+        auto kern = k_xpass_acc<T, NIN, NOUT, REDUCE, M, Op>;
+        static size_t granted = 48 * 1024;
+        ensure_smem(kern, smem, granted);
+        kern<<<grid, kThreads, smem, ctx->stream>>>(g, (const cplx<T>*)ctx->fb.twx, op, partials);
+    });
 }
 
 template <typename T> void launch_y(fipi_ctx* ctx, int nf, void* const* in, void* const* out, int dir) {
@@ -576,26 +608,41 @@ template <typename T> void launch_y(fipi_ctx* ctx, int nf, void* const* in, void
         fp.in[f] = (cplx<T>*)in[f];
         fp.out[f] = (cplx<T>*)out[f];
     }
-    int rows = (4 * kThreads) / g.ny;
-    if (rows < 1) rows = 1;
-    const long long total = (long long)g.nz * g.h;
-    dim3 grid((unsigned)((total + rows - 1) / rows), nf);
-    const size_t smem = (size_t)rows * g.ny * sizeof(cplx<T>);
-    static size_t granted = 48 * 1024;
-    ensure_smem(k_ypass<T>, smem, granted);
-    k_ypass<T><<<grid, kThreads, smem, ctx->stream>>>(g, (const cplx<T>*)ctx->fb.twy, dir, fp, rows);
+    // persistent, TMA double-buffered: a grid of resident blocks walks all tiles
+    const size_t smem = ypass_tma_smem<T>(g);
+    dispatch_pow2(g.ny, [&](auto NC) {
+        constexpr int N = decltype(NC)::value;
+        auto kern = (dir < 0) ? k_ypass_tma<T, -1, N> : k_ypass_tma<T, +1, N>;
+        static size_t granted[2] = {48 * 1024, 48 * 1024};
+        static int blocks_per_sm[2] = {0, 0};
+        const int di = dir < 0 ? 0 : 1;
+        ensure_smem(kern, smem, granted[di]);
+        if (!blocks_per_sm[di]) {
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm[di], kern, kThreads, smem);
+            if (blocks_per_sm[di] < 1) blocks_per_sm[di] = 1;
+        }
+        const int rb = ypass_rows<T>(g.ny);
+        const long long tiles = ((long long)g.nz * g.h + rb - 1) / rb * nf;
+        long long grid = (long long)ctx->num_sms * blocks_per_sm[di];
+        if (grid > tiles) grid = tiles;
+        kern<<<(unsigned)grid, kThreads, smem, ctx->stream>>>(g, (const cplx<T>*)ctx->fb.twy, fp, nf, ctx->status);
+    });
 }
 
 // nspec: spectral arrays the pass and its fused operation read or write.
-template <typename T, int NF, class Op> void launch_z(fipi_ctx* ctx, const char* name, int nspec, const Op& op, int dir) {
+template <typename T, int NF, int DIR, class Op> void launch_z(fipi_ctx* ctx, const char* name, int nspec, const Op& op) {
     const Geom& g = ctx->g;
     LaunchScope ls(ctx, name, (double)nspec * g.SH * sizeof(cplx<T>));
-    const size_t smem = (size_t)NF * Tiles<T>::TZ * (g.nz + 1) * sizeof(cplx<T>);
-    auto kern = k_zpass<T, NF, Op>;
-    static size_t granted = 48 * 1024;
-    ensure_smem(kern, smem, granted);
-    dim3 grid(g.h, g.ny / Tiles<T>::TZ);
-    kern<<<grid, kThreads, smem, ctx->stream>>>(g, (const cplx<T>*)ctx->fb.twz, dir, op);
+    const size_t smem = zpass_smem<T, NF>(g);
+    dim3 grid(g.h, g.ny / zpass_cols<T>(g.nz));
+    const int threads = zpass_threads<T>(g.nz);
+    dispatch_pow2(g.nz, [&](auto NC) {
+        constexpr int N = decltype(NC)::value;
+        auto kern = k_zpass<T, NF, DIR, N, Op>;
+        static size_t granted = 48 * 1024;
+        ensure_smem(kern, smem, granted);
+        kern<<<grid, threads, smem, ctx->stream>>>(g, (const cplx<T>*)ctx->fb.twz, op);
+    });
 }
 
 // grad c (real, 3 fields) from c_hat.
@@ -604,7 +651,7 @@ template <typename T> void grad_from_chat(fipi_ctx* ctx, const cplx<T>* chat, T*
     const Geom& g = ctx->g;
     ZOpGrad<T> zg{chat, {F<T>::S(ctx, 1), F<T>::S(ctx, 2), F<T>::S(ctx, 3)}, F<T>::ktabs(ctx), g.m,
                   g.ny / 2, g.nz / 2};
-    launch_z<T, 3>(ctx, "Z inverse grad", 4, zg, +1);
+    launch_z<T, 3, +1>(ctx, "Z inverse grad", 4, zg);
     void* sp[3] = {ctx->fb.S[1], ctx->fb.S[2], ctx->fb.S[3]};
     launch_y<T>(ctx, 3, sp, sp, +1);
     OpC2RStore<T, 3> op{{F<T>::S(ctx, 1), F<T>::S(ctx, 2), F<T>::S(ctx, 3)}, {g3[0], g3[1], g3[2]}, g.nx, g.ny};
@@ -690,8 +737,8 @@ fipi_status fields_alloc(fipi_ctx* ctx) {
     ctx->n_partials = (g.ny / 8) * g.nz;  // upper bound of X-pass blocks (TY >= 8)
     if (ctx->n_partials < 1024) ctx->n_partials = 1024;
     FIPI_CUDA(ctx, cudaMalloc(&ctx->partials, sizeof(double) * ctx->n_partials));
-    FIPI_CUDA(ctx, cudaMalloc(&ctx->k0, sizeof(double) * 4));
-    FIPI_CUDA(ctx, cudaMemsetAsync(ctx->k0, 0, sizeof(double) * 4, ctx->stream));
+    FIPI_CUDA(ctx, cudaMalloc(&ctx->k0, sizeof(double) * 6));
+    FIPI_CUDA(ctx, cudaMemsetAsync(ctx->k0, 0, sizeof(double) * 6, ctx->stream));
     ctx->device_bytes += sizeof(double) * (ctx->n_partials + 4);
     return FIPI_OK;
 }
@@ -762,7 +809,7 @@ template <typename T> static fipi_status set_phase_t(fipi_ctx* ctx, const double
     void* sp[2] = {ctx->fb.S[0], ctx->fb.S[1]};
     launch_y<T>(ctx, 2, sp, sp, -1);
     ZOpStore<T, 2> zs{{F<T>::S(ctx, 0), F<T>::S(ctx, 1)}, {F<T>::sp(ctx->fb.chat), F<T>::sp(ctx->fb.fhat)}, mixed ? 1 : 0};
-    launch_z<T, 2>(ctx, "Z forward store", 4, zs, -1);
+    launch_z<T, 2, -1>(ctx, "Z forward store", 4, zs);
     T* g3[3] = {(T*)ctx->fb.g[0], (T*)ctx->fb.g[1], (T*)ctx->fb.g[2]};
     grad_from_chat<T>(ctx, F<T>::sp(ctx->fb.chat), g3);
     FIPI_CUDA(ctx, cudaGetLastError());
@@ -785,7 +832,7 @@ template <typename T> static fipi_status set_velocity_t(fipi_ctx* ctx, const dou
         void* sp[1] = {ctx->fb.S[0]};
         launch_y<T>(ctx, 1, sp, sp, -1);
         ZOpStore<T, 1> zs{{F<T>::S(ctx, 0)}, {F<T>::sp(ctx->fb.uhat[d])}, 0};
-        launch_z<T, 1>(ctx, "Z forward store", 2, zs, -1);
+        launch_z<T, 1, -1>(ctx, "Z forward store", 2, zs);
     }
     FIPI_CUDA(ctx, cudaGetLastError());
     return FIPI_OK;
@@ -804,7 +851,7 @@ template <typename T> static fipi_status get_velocity_t(fipi_ctx* ctx, double* u
     const Geom& g = ctx->g;
     ZOpStore<T, 3> zs{{F<T>::sp(ctx->fb.uhat[0]), F<T>::sp(ctx->fb.uhat[1]), F<T>::sp(ctx->fb.uhat[2])},
                       {F<T>::S(ctx, 0), F<T>::S(ctx, 1), F<T>::S(ctx, 2)}, 0};
-    launch_z<T, 3>(ctx, "Z inverse copy", 6, zs, +1);
+    launch_z<T, 3, +1>(ctx, "Z inverse copy", 6, zs);
     void* sp[3] = {ctx->fb.S[0], ctx->fb.S[1], ctx->fb.S[2]};
     launch_y<T>(ctx, 3, sp, sp, +1);
     T* ur = (T*)ctx->fb.ureal;
@@ -827,7 +874,7 @@ template <typename T, bool MIXED> static void step_ch_t(fipi_ctx* ctx, int t) {
     // A: u_hat -> u (Z, Y inverse; X inverse fused with conv and its R2C)
     ZOpStore<T, 3> zu{{F<T>::sp(b.uhat[0]), F<T>::sp(b.uhat[1]), F<T>::sp(b.uhat[2])},
                       {F<T>::S(ctx, 0), F<T>::S(ctx, 1), F<T>::S(ctx, 2)}, 0};
-    launch_z<T, 3>(ctx, "Z inverse copy", 6, zu, +1);
+    launch_z<T, 3, +1>(ctx, "Z inverse copy", 6, zu);
     void* s3[3] = {b.S[0], b.S[1], b.S[2]};
     launch_y<T>(ctx, 3, s3, s3, +1);
     OpConv<T, MIXED> oc{{F<T>::S(ctx, 0), F<T>::S(ctx, 1), F<T>::S(ctx, 2)},
@@ -839,23 +886,25 @@ template <typename T, bool MIXED> static void step_ch_t(fipi_ctx* ctx, int t) {
     if (MIXED) {
         const int nblk = (g.ny / Tiles<T>::TY) * g.nz;
         LaunchScope ls(ctx, "k0 update", 0.0);
-        k_k0_update<<<1, 256, 0, ctx->stream>>>(ctx->k0, ctx->partials, nblk, t == 0, ctx->P.dt);
+        k_k0_update<<<1, 256, 0, ctx->stream>>>(ctx->k0, ctx->partials, nblk, t == 0, ctx->P.dt,
+                                                 1.0 / (double)g.V);
     }
     ZOpCH<T, MIXED> zc{F<T>::S(ctx, 3), F<T>::sp(b.chat), F<T>::sp(b.chat_old), F<T>::sp(b.fhat),
                        F<T>::sp(b.fhat_old), F<T>::sp(b.Chat_old), F<T>::ktabs(ctx), k, t == 0 ? 1 : 0};
-    launch_z<T, 1>(ctx, t == 0 ? "Z forward + IMEX update" : "Z forward + SBDF2 update", t == 0 ? 5 : 8, zc, -1);
+    launch_z<T, 1, -1>(ctx, t == 0 ? "Z forward + IMEX update" : "Z forward + SBDF2 update", t == 0 ? 5 : 8, zc);
     std::swap(b.chat, b.chat_old);  // chat = c^{n+1}, chat_old = c^n
     // B: c^{n+1} = C2R(c_hat), f fused, f_hat = R2C(f)
     ZOpStore<T, 1> zc2{{F<T>::sp(b.chat)}, {F<T>::S(ctx, 0)}, 0};
-    launch_z<T, 1>(ctx, "Z inverse copy", 2, zc2, +1);
+    launch_z<T, 1, +1>(ctx, "Z inverse copy", 2, zc2);
     void* s0[1] = {b.S[0]};
     launch_y<T>(ctx, 1, s0, s0, +1);
-    OpCF<T, MIXED> ocf{F<T>::S(ctx, 0), (T*)b.c, F<T>::S(ctx, 1), ctx->k0, 1.0 / (double)g.V, k.lam_eps, g.nx, g.ny};
+    OpCF<T, MIXED> ocf{F<T>::S(ctx, 0), (T*)b.c, F<T>::S(ctx, 1), reinterpret_cast<const float*>(ctx->k0 + 4),
+                       k.lam_eps, g.nx, g.ny};
     launch_x<T, 1, 1, false>(ctx, "X inverse c, f, forward", 1, ocf);
     void* s1b[1] = {b.S[1]};
     launch_y<T>(ctx, 1, s1b, s1b, -1);
     ZOpStore<T, 1> zf{{F<T>::S(ctx, 1)}, {F<T>::sp(b.fhat_old)}, 0};
-    launch_z<T, 1>(ctx, "Z forward store", 2, zf, -1);
+    launch_z<T, 1, -1>(ctx, "Z forward store", 2, zf);
     std::swap(b.fhat, b.fhat_old);  // fhat = f^{n+1}, fhat_old = f^n
     (void)sizeof(C);
 }
@@ -871,9 +920,9 @@ template <typename T> static void step_stokes_t(fipi_ctx* ctx) {
     const StepConsts<T> k = make_consts<T>(ctx);
     const KTabs<T> kt = F<T>::ktabs(ctx);
     ZOpMu<T> zm{F<T>::sp(b.chat), F<T>::sp(b.fhat), F<T>::S(ctx, 0), kt, k.lam};
-    launch_z<T, 1>(ctx, "Z inverse mu", 3, zm, +1);
+    launch_z<T, 1, +1>(ctx, "Z inverse mu", 3, zm);
     ZOpGrad<T> zg{F<T>::sp(b.chat), {F<T>::S(ctx, 1), F<T>::S(ctx, 2), F<T>::S(ctx, 3)}, kt, g.m, g.ny / 2, g.nz / 2};
-    launch_z<T, 3>(ctx, "Z inverse grad", 4, zg, +1);
+    launch_z<T, 3, +1>(ctx, "Z inverse grad", 4, zg);
     void* s4[4] = {b.S[0], b.S[1], b.S[2], b.S[3]};
     launch_y<T>(ctx, 4, s4, s4, +1);
     OpForce<T> of{{F<T>::S(ctx, 0), F<T>::S(ctx, 1), F<T>::S(ctx, 2), F<T>::S(ctx, 3)},
@@ -887,7 +936,7 @@ template <typename T> static void step_stokes_t(fipi_ctx* ctx) {
     launch_y<T>(ctx, 3, s3, s3, -1);
     ZOpProj<T> zp{{F<T>::S(ctx, 0), F<T>::S(ctx, 1), F<T>::S(ctx, 2)},
                   {F<T>::sp(b.uhat[0]), F<T>::sp(b.uhat[1]), F<T>::sp(b.uhat[2])}, kt, k.mu, g.m, g.ny / 2, g.nz / 2};
-    launch_z<T, 3>(ctx, "Z forward + projection", 6, zp, -1);
+    launch_z<T, 3, -1>(ctx, "Z forward + projection", 6, zp);
 }
 
 void fields_step_stokes(fipi_ctx* ctx) {
@@ -947,7 +996,7 @@ template <typename T> static fipi_status r2c_t(fipi_ctx* ctx, const double* in, 
     void* sp[1] = {ctx->fb.S[0]};
     launch_y<T>(ctx, 1, sp, sp, -1);
     ZOpStore<T, 1> zs{{F<T>::S(ctx, 0)}, {F<T>::S(ctx, 1)}, 0};
-    launch_z<T, 1>(ctx, "Z forward store", 2, zs, -1);
+    launch_z<T, 1, -1>(ctx, "Z forward store", 2, zs);
     FIPI_CUDA(ctx, cudaGetLastError());
     return download<T>(ctx, (const T*)F<T>::S(ctx, 1), out, (size_t)g.SH * 2);
     (void)sizeof(C);
@@ -962,7 +1011,7 @@ template <typename T> static fipi_status c2r_t(fipi_ctx* ctx, const double* in, 
     fipi_status st = upload<T>(ctx, in, (T*)F<T>::S(ctx, 0), (size_t)g.SH * 2);
     if (st != FIPI_OK) return st;
     ZOpStore<T, 1> zs{{F<T>::S(ctx, 0)}, {F<T>::S(ctx, 1)}, 0};
-    launch_z<T, 1>(ctx, "Z inverse copy", 2, zs, +1);
+    launch_z<T, 1, +1>(ctx, "Z inverse copy", 2, zs);
     void* sp[1] = {ctx->fb.S[1]};
     launch_y<T>(ctx, 1, sp, sp, +1);
     T* dst = (T*)ctx->fb.ureal;
@@ -986,7 +1035,7 @@ template <typename T> static fipi_status grad_t(fipi_ctx* ctx, const double* c, 
     void* sp[1] = {ctx->fb.S[0]};
     launch_y<T>(ctx, 1, sp, sp, -1);
     ZOpStore<T, 1> zs{{F<T>::S(ctx, 0)}, {F<T>::S(ctx, 0)}, 0};
-    launch_z<T, 1>(ctx, "Z forward store", 2, zs, -1);
+    launch_z<T, 1, -1>(ctx, "Z forward store", 2, zs);
     T* g3[3] = {tmp, tmp + g.V, tmp + 2 * g.V};
     grad_from_chat<T>(ctx, F<T>::S(ctx, 0), g3);
     FIPI_CUDA(ctx, cudaGetLastError());

@@ -253,7 +253,7 @@ __device__ __forceinline__ void coincident_d(int a, int b, double r_p, double d[
 // 2: write pairs at pair_off[i].
 template <typename TA, int MODE>
 __global__ void k_f_pp(PC pc, const double* __restrict__ p, const unsigned* __restrict__ ids,
-                       const int* __restrict__ off, double rmp, const double* __restrict__ f_pi,
+                       const int* __restrict__ off, const double* __restrict__ rmp_p, const double* __restrict__ f_pi,
                        const int* __restrict__ it_mark, double* f_pp, double* tau_part, int* pair_cnt,
                        const int* __restrict__ pair_off, int* pairs) {
     const int lane = threadIdx.x & 31;
@@ -263,6 +263,7 @@ __global__ void k_f_pp(PC pc, const double* __restrict__ p, const unsigned* __re
     const int n = pc.n;
     const int ci = cell % pc.nc[0], cj = (cell / pc.nc[0]) % pc.nc[1], ck = cell / (pc.nc[0] * pc.nc[1]);
     const int beg = off[cell], end = off[cell + 1];
+    const double rmp = rmp_p ? *rmp_p : 1.0;
     const double T0 = pc.dc[0] * (pc.nc[0] - 2), T1 = pc.dc[1] * (pc.nc[1] - 2), T2 = pc.dc[2] * (pc.nc[2] - 2);
     bool mark_ok = false;
     if (MODE == 0 && f_pi != nullptr) {
@@ -361,34 +362,164 @@ __global__ void k_f_pp(PC pc, const double* __restrict__ p, const unsigned* __re
     }
 }
 
-// argmax of p_y with strict > from 0.0, first index wins (cluster.cpp:222-232).
-__global__ void k_it_mark(const double* __restrict__ py, int n, int* it_mark) {
-    __shared__ double bv[1024];
-    __shared__ int bi[1024];
-    double best = 0.0;
-    int idx = -1;
-    for (int i = threadIdx.x; i < n; i += blockDim.x)
-        if (py[i] > best) {
-            best = py[i];
-            idx = i;
-        }
-    bv[threadIdx.x] = best;
-    bi[threadIdx.x] = idx;
-    __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-        if (threadIdx.x < s) {
-            const double ov = bv[threadIdx.x + s];
-            const int oi = bi[threadIdx.x + s];
-            if (oi >= 0 && (bi[threadIdx.x] < 0 || ov > bv[threadIdx.x] || (ov == bv[threadIdx.x] && oi < bi[threadIdx.x]))) {
-                bv[threadIdx.x] = ov;
-                bi[threadIdx.x] = oi;
+// Mixed-form contact forces when every axis has at least 4 cells.  Then
+// the reference's minimum-image rule (shift d by L when |d| exceeds
+// d_cell (n_cell - 2), cluster.cpp:319-326) shifts exactly the pairs whose
+// neighbour cell was reached through the periodic wrap, so d can be formed
+// from cell-relative FP32 coordinates plus the neighbour cell's offset
+// (di, dj, dk) d_cell, with no per-pair test.  A warp owns a home cell;
+// candidates are read 32 at a time (coalesced float4: x, y, z relative to
+// their cell, id) and broadcast by shuffles.  The force on the home
+// particle from a pair is (d/|d|) s with d = p_i - p_j for either id
+// order (exactly the reference's sign rule), summed in the reference's
+// cell order.
+__global__ void k_sorted_pos(PC pc, const double* __restrict__ p, const unsigned* __restrict__ keys,
+                             const unsigned* __restrict__ ids, float4* __restrict__ spos) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= pc.n) return;
+    const unsigned key = keys[s];
+    const int i = (int)ids[s];
+    const int cx = key % pc.nc[0], cy = (key / pc.nc[0]) % pc.nc[1], cz = key / (pc.nc[0] * pc.nc[1]);
+    const int n = pc.n;
+    float4 v;
+    v.x = (float)(p[i] - cx * pc.dc[0]);
+    v.y = (float)(p[n + i] - cy * pc.dc[1]);
+    v.z = (float)(p[2 * n + i] - cz * pc.dc[2]);
+    v.w = __int_as_float(i);
+    spos[s] = v;
+}
+
+// One block per home cell, one warp per (dk, dj) neighbour row of three
+// cells (9 warps); the nine partial forces of each home particle are then
+// added in the reference's (k, j) cell order, so the result is
+// deterministic.  Lanes own the home cell's particles, 32 at a time.
+constexpr int kFppRows = 9;
+
+__global__ void __launch_bounds__(32 * kFppRows) k_f_pp_fast(PC pc, const float4* __restrict__ spos,
+                                                             const int* __restrict__ off,
+                                                             const double* __restrict__ rmp_p,
+                                                             const double* __restrict__ f_pi,
+                                                             const int* __restrict__ it_mark, double* f_pp,
+                                                             double* tau_part) {
+    __shared__ float4 stage[kFppRows][32];
+    __shared__ float part[kFppRows][4][32];  // fx, fy, fz, tau per row warp and lane
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int cell = blockIdx.x;
+    float4* buf = stage[w];
+    const int n = pc.n;
+    const int ci = cell % pc.nc[0], cj = (cell / pc.nc[0]) % pc.nc[1], ck = cell / (pc.nc[0] * pc.nc[1]);
+    const int dk = w / 3 - 1, dj = w % 3 - 1;
+    const int beg = off[cell], end = off[cell + 1];
+    const float req = (float)pc.r_eq, req2 = req * req, kn = (float)pc.k_n;
+    const float rmp = (float)*rmp_p;
+    const float dcx = (float)pc.dc[0], dcy = (float)pc.dc[1], dcz = (float)pc.dc[2];
+    bool mark_ok = false;
+    if (f_pi != nullptr) {
+        const int m = *it_mark;
+        if (m >= 0) mark_ok = f_pi[m] != 0.0 || f_pi[n + m] != 0.0 || f_pi[2 * n + m] != 0.0;
+    }
+    const int rowbase = (cj + dj + pc.nc[1]) % pc.nc[1] * pc.nc[0] + (ck + dk + pc.nc[2]) % pc.nc[2] * pc.nc[0] * pc.nc[1];
+    for (int base = beg; base < end; base += 32) {
+        const int s = base + lane;
+        const bool active = s < end;
+        const float4 h = active ? spos[s] : make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
+        const int i = __float_as_int(h.w);
+        bool own_ok = false;
+        if (f_pi != nullptr && active) own_ok = f_pi[i] != 0.0 || f_pi[n + i] != 0.0 || f_pi[2 * n + i] != 0.0;
+        float ax = 0.f, ay = 0.f, az = 0.f, tau = 0.f;
+        for (int di = -1; di <= 1; ++di) {
+            const int co = (ci + di + pc.nc[0]) % pc.nc[0] + rowbase;
+            // home particle relative to the neighbour cell's origin (home frame)
+            const float hx = h.x - di * dcx, hy = h.y - dj * dcy, hz = h.z - dk * dcz;
+            const int qb = off[co], qe = off[co + 1];
+            for (int q0 = qb; q0 < qe; q0 += 32) {
+                __syncwarp();
+                if (q0 + lane < qe) buf[lane] = spos[q0 + lane];
+                __syncwarp();
+                const int cnt = min(32, qe - q0);
+                if (!active) continue;
+                for (int q = 0; q < cnt; ++q) {
+                    const float4 cd = buf[q];
+                    const int j = __float_as_int(cd.w);
+                    float dx = hx - cd.x, dy = hy - cd.y, dz = hz - cd.z;
+                    float d2 = dx * dx + dy * dy + dz * dz;
+                    if (!(d2 < req2) || j == i) continue;
+                    if (d2 == 0.f) {  // coincident in FP32: the hashed separation of the FP64 path
+                        double d[3];
+                        coincident_d(min(i, j), max(i, j), pc.r_p, d);
+                        const float sg = i < j ? 1.f : -1.f;
+                        dx = sg * (float)d[0];
+                        dy = sg * (float)d[1];
+                        dz = sg * (float)d[2];
+                        d2 = dx * dx + dy * dy + dz * dz;
+                        if (!(d2 < req2)) continue;
+                    }
+                    // (r_eq - |d|) ramp k_n d/|d|  =  (r_eq/|d| - 1) ramp k_n d
+                    const float sc = (req * rsqrtf(d2) - 1.f) * rmp * kn;
+                    const float fx = dx * sc, fy = dy * sc, fz = dz * sc;
+                    ax += fx;
+                    ay += fy;
+                    az += fz;
+                    if (own_ok && mark_ok && i < j) tau += (fx * 0.5f) * dx + (fy * 0.5f) * dy + (fz * 0.5f) * dz;
+                }
             }
+        }
+        part[w][0][lane] = ax;
+        part[w][1][lane] = ay;
+        part[w][2][lane] = az;
+        part[w][3][lane] = tau;
+        __syncthreads();
+        if (w == 0 && active) {
+            float sx = 0.f, sy = 0.f, sz = 0.f, st = 0.f;
+#pragma unroll
+            for (int r = 0; r < kFppRows; ++r) {
+                sx += part[r][0][lane];
+                sy += part[r][1][lane];
+                sz += part[r][2][lane];
+                st += part[r][3][lane];
+            }
+            f_pp[i] = (double)sx;
+            f_pp[n + i] = (double)sy;
+            f_pp[2 * n + i] = (double)sz;
+            if (tau_part) tau_part[i] = (double)st;
         }
         __syncthreads();
     }
-    if (threadIdx.x == 0 && bi[0] >= 0) *it_mark = bi[0];
 }
 
+// it_mark of cluster::sorting (cluster.cpp:222-232): the first index of
+// the largest p_y, kept from the previous call when no p_y > 0.  For
+// non-negative doubles the bit pattern orders like the value, so the
+// maximum is an integer atomicMax and the first index an atomicMin.
+// mk[0] = max bits, mk[1] = first index (as unsigned long long).
+__global__ void k_ymax(const double* __restrict__ py, int n, unsigned long long* mk) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long b = 0;
+    if (i < n) {
+        const double y = py[i];
+        b = (y > 0.0) ? (unsigned long long)__double_as_longlong(y) : 0ull;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long x = __shfl_down_sync(0xffffffffu, b, o);
+        b = x > b ? x : b;
+    }
+    if ((threadIdx.x & 31) == 0 && b) atomicMax(&mk[0], b);
+}
+
+__global__ void k_ymax_index(const double* __restrict__ py, int n, unsigned long long* mk, int* it_mark) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned long long best = mk[0];
+    if (i < n && best != 0ull && (unsigned long long)__double_as_longlong(py[i]) == best)
+        atomicMin(&mk[1], (unsigned long long)i);
+}
+
+__global__ void k_ymax_resolve(unsigned long long* mk, int* it_mark) {
+    if (mk[0] != 0ull) *it_mark = (int)mk[1];
+    mk[0] = 0ull;
+    mk[1] = ~0ull;
+}
+
+// Sum of the per-particle packing-energy terms in a fixed order.
 __global__ void k_sum_tau(const double* __restrict__ part, int n, double* out) {
     __shared__ double s[1024];
     double a = 0.0;
@@ -529,7 +660,12 @@ __device__ __forceinline__ void cell_and_frac(const PC& pc, double X, double Y, 
     fr[2] = Z / pc.dz - fz;
 }
 
-__global__ void k_spread_records(PC pc, const double* __restrict__ p, unsigned* keys, unsigned* vals) {
+// Per particle: the 8 corner records (node, particle*8 + corner), the force
+// density f = (f_pp + f_ext)/dx/dy/dz and the fractions (o, p, q) of
+// cluster.cpp:452-460, computed once here instead of once per record.
+template <typename TA>
+__global__ void k_spread_records(PC pc, const double* __restrict__ p, const double* __restrict__ f_pp,
+                                 unsigned* keys, unsigned* vals, TA* __restrict__ fw) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = pc.n;
     if (i >= n) return;
@@ -542,6 +678,10 @@ __global__ void k_spread_records(PC pc, const double* __restrict__ p, unsigned* 
         const int z = (ix[2] + c_corner[c][2]) % pc.N[2];
         keys[8 * i + c] = (unsigned)(x + (size_t)y * pc.N[0] + (size_t)z * pc.N[0] * pc.N[1]);
         vals[8 * i + c] = (unsigned)(8 * i + c);
+    }
+    for (int a = 0; a < 3; ++a) {
+        fw[a * n + i] = (TA)((f_pp[a * n + i] + 0.0) / pc.dx / pc.dy / pc.dz);
+        fw[(3 + a) * n + i] = (TA)fr[a];
     }
 }
 
@@ -572,7 +712,7 @@ __device__ __forceinline__ TA corner_value(TA f, int c, TA o, TA pp, TA q) {
 
 template <typename TF, typename TA>
 __global__ void k_spread_reduce(PC pc, const unsigned* __restrict__ keys, const unsigned* __restrict__ vals, int m,
-                                const double* __restrict__ p, const double* __restrict__ f_pp, TF* f0, TF* f1, TF* f2) {
+                                const TA* __restrict__ fw, TF* f0, TF* f1, TF* f2) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= m) return;
     const unsigned node = keys[s];
@@ -582,13 +722,9 @@ __global__ void k_spread_reduce(PC pc, const unsigned* __restrict__ keys, const 
     for (int q = s; q < m && keys[q] == node; ++q) {
         const unsigned rec = vals[q];
         const int i = (int)(rec >> 3), c = (int)(rec & 7u);
-        int ix[3];
-        double fr[3];
-        cell_and_frac(pc, p[i], p[n + i], p[2 * n + i], ix, fr);
-        for (int a = 0; a < 3; ++a) {
-            const double f = (f_pp[a * n + i] + 0.0) / pc.dx / pc.dy / pc.dz;
-            acc[a] += corner_value<TA>((TA)f, c, (TA)fr[0], (TA)fr[1], (TA)fr[2]);
-        }
+        const TA o = fw[3 * n + i], pp = fw[4 * n + i], qq = fw[5 * n + i];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) acc[a] += corner_value<TA>(fw[a * n + i], c, o, pp, qq);
     }
     f0[node] = (TF)acc[0];
     f1[node] = (TF)acc[1];
@@ -611,14 +747,12 @@ static void spread_t(fipi_ctx* ctx, const double* p, const double* f_pp, T* cons
             for (int a = 0; a < 3; ++a) cudaMemsetAsync(f3[a], 0, sizeof(T) * (size_t)ctx->g.V, ctx->stream);
         }
     }
-    { LaunchScope ls_(ctx, "spread records", 0.0); k_spread_records<<<(n + 255) / 256, 256, 0, ctx->stream>>>(pc, p, b.sp_keys, b.sp_vals); }
+    { LaunchScope ls_(ctx, "spread records", 0.0); k_spread_records<T><<<(n + 255) / 256, 256, 0, ctx->stream>>>(pc, p, f_pp, b.sp_keys, b.sp_vals, (T*)b.sp_fw); }
     radix_sort(ctx, b.sp_keys, b.sp_vals, b.sp_keys_alt, b.sp_vals_alt, m, bits_for(ctx->g.V - 1));
-    { LaunchScope ls_(ctx, "spread segmented reduce", 0.0); k_spread_reduce<T, T><<<(m + 255) / 256, 256, 0, ctx->stream>>>(pc, b.sp_keys, b.sp_vals, m, p, f_pp, f3[0], f3[1], f3[2]); }
+    { LaunchScope ls_(ctx, "spread segmented reduce", 0.0); k_spread_reduce<T, T><<<(m + 255) / 256, 256, 0, ctx->stream>>>(pc, b.sp_keys, b.sp_vals, m, (const T*)b.sp_fw, f3[0], f3[1], f3[2]); }
     if (step_grid) {
         cudaMemcpyAsync(b.sp_prev, b.sp_keys, sizeof(unsigned) * m, cudaMemcpyDeviceToDevice, ctx->stream);
         b.sp_prev_valid = 1;
-    } else {
-        b.sp_prev_valid = 0;  // the record buffers no longer describe the step grid
     }
 }
 
@@ -634,42 +768,86 @@ void particles_spread(fipi_ctx* ctx) {
 }
 
 // compute_f_pp; with `tau` the packing energy of cluster.cpp:350-353 is
-// accumulated per particle and summed in a fixed order.
+// accumulated per particle and summed in a fixed order.  TA = float with
+// at least 4 cells per axis takes the FP32 cell-relative path.
+// it_mark for the packing energy: the first index of the largest p_y.
+static void it_mark_launch(fipi_ctx* ctx, const double* p) {
+    ParticleBufs& b = ctx->pb;
+    const int nb = (b.n + 255) / 256;
+    { LaunchScope ls_(ctx, "it_mark argmax", 0.0); k_ymax<<<nb, 256, 0, ctx->stream>>>(p + b.n, b.n, b.ymax); }
+    { LaunchScope ls_(ctx, "it_mark argmax", 0.0); k_ymax_index<<<nb, 256, 0, ctx->stream>>>(p + b.n, b.n, b.ymax, b.it_mark); }
+    { LaunchScope ls_(ctx, "it_mark argmax", 0.0); k_ymax_resolve<<<1, 1, 0, ctx->stream>>>(b.ymax, b.it_mark); }
+}
+
+// compute_f_pp; with `tau` the packing energy of cluster.cpp:350-353 is
+// accumulated per particle (tau_part) and summed when it is asked for.
+// TA = float with at least 4 cells per axis takes the FP32 cell-relative path.
 template <typename TA>
-static void f_pp_launch(fipi_ctx* ctx, const double* p, double rmp, const double* f_pi, double* f_pp, bool tau) {
+static void f_pp_launch(fipi_ctx* ctx, const double* p, const double* rmp, const double* f_pi, double* f_pp, bool tau) {
     ParticleBufs& b = ctx->pb;
     const PC pc = make_pc(ctx);
     const int warps = b.ncells;
     const int blocks = (warps * 32 + 255) / 256;
-    if (tau) { LaunchScope ls_(ctx, "it_mark argmax", 0.0); k_it_mark<<<1, 1024, 0, ctx->stream>>>(p + b.n, b.n, b.it_mark); }
-    { LaunchScope ls_(ctx, "contact forces (warp per cell)", 0.0); k_f_pp<TA, 0><<<blocks, 256, 0, ctx->stream>>>(pc, p, b.ids, b.cell_off, rmp, tau ? f_pi : nullptr, b.it_mark,
+    if (tau) it_mark_launch(ctx, p);
+    const bool fast = sizeof(TA) == sizeof(float) && b.ncell[0] >= 4 && b.ncell[1] >= 4 && b.ncell[2] >= 4;
+    if (fast) {
+        { LaunchScope ls_(ctx, "sorted FP32 positions", 0.0); k_sorted_pos<<<(b.n + 255) / 256, 256, 0, ctx->stream>>>(pc, p, b.keys, b.ids, b.spos); }
+        { LaunchScope ls_(ctx, "contact forces (warp per cell)", 0.0); k_f_pp_fast<<<b.ncells, 32 * kFppRows, 0, ctx->stream>>>(pc, b.spos, b.cell_off, rmp, tau ? f_pi : nullptr, b.it_mark, f_pp, b.tau_part); }
+    } else {
+        { LaunchScope ls_(ctx, "contact forces (warp per cell)", 0.0); k_f_pp<TA, 0><<<blocks, 256, 0, ctx->stream>>>(pc, p, b.ids, b.cell_off, rmp, tau ? f_pi : nullptr, b.it_mark,
                                                   f_pp, b.tau_part, nullptr, nullptr, nullptr); }
-    if (tau) { LaunchScope ls_(ctx, "packing energy sum", 0.0); k_sum_tau<<<1, 1024, 0, ctx->stream>>>(b.tau_part, b.n, b.tau); }
+    }
+    b.tau_valid = tau;
 }
 
-template <typename T> static void step_t(fipi_ctx* ctx, int t) {
+// The packing energy of the last contact-force evaluation (fixed-order sum).
+fipi_status particles_packing_tau(fipi_ctx* ctx, double* out) {
+    ParticleBufs& b = ctx->pb;
+    if (!b.tau_valid || b.n == 0) {
+        *out = 0.0;
+        return FIPI_OK;
+    }
+    { LaunchScope ls_(ctx, "packing energy sum", 0.0); k_sum_tau<<<1, 1024, 0, ctx->stream>>>(b.tau_part, b.n, b.tau); }
+    FIPI_CUDA(ctx, d2h(ctx, out, b.tau, sizeof(double)));
+    return FIPI_OK;
+}
+
+template <typename T> static void step_t(fipi_ctx* ctx) {
     ParticleBufs& b = ctx->pb;
     const PC pc = make_pc(ctx);
-    const double rmp = ramp((double)(t + 1), 0.2 * ctx->P.t_end);  // compute_f_pp(t+1), main.cpp:299
     const int n = b.n;
     const int nb = (n + 255) / 256;
     for (int stage = 1; stage <= 2; ++stage) {
         // interpolate_local_variables, sorting, compute_f_pi, compute_f_pp(t+1),
-        // compute_f_ext (zero), advect, enforce_bc  (main.cpp:295-314)
+        // compute_f_ext (zero), advect, enforce_bc  (main.cpp:295-314); the
+        // ramp(t+1, 0.2 t_end) factor is kept on the device (step_tick)
         { LaunchScope ls_(ctx, "stage interpolate + f_pi", 0.0); k_stage_fpi<T, T><<<nb, 256, 0, ctx->stream>>>(pc, (const T*)ctx->fb.c, (const T*)ctx->fb.g[0],
                                                      (const T*)ctx->fb.g[1], (const T*)ctx->fb.g[2], b.p, b.f_pi,
                                                      b.r, b.cth); }
         build_cells(ctx, b.p);
-        f_pp_launch<T>(ctx, b.p, rmp, b.f_pi, b.f_pp, ctx->track_tau);
+        f_pp_launch<T>(ctx, b.p, ctx->d_rmp, b.f_pi, b.f_pp, ctx->track_tau);
         { LaunchScope ls_(ctx, "stage advect + wrap", 0.0); k_stage_advect<<<nb, 256, 0, ctx->stream>>>(pc, stage, b.p, b.p_old, b.u_old, b.f_pi, b.f_pp, b.r,
                                                     ctx->status); }
     }
 }
 
-void particles_step(fipi_ctx* ctx, int t) {
+void particles_step(fipi_ctx* ctx) {
     if (ctx->pb.n <= 0 || !ctx->P.switch_particle) return;
-    if (ctx->prec == FIPI_MIXED) step_t<float>(ctx, t);
-    else step_t<double>(ctx, t);
+    if (ctx->prec == FIPI_MIXED) step_t<float>(ctx);
+    else step_t<double>(ctx);
+}
+
+// End of a step: t += 1 and the next step's ramp(t + 1, 0.2 t_end)
+// (compute_f_pp(t+1), main.cpp:299; primitive.cpp:205-212).
+__global__ void k_step_tick(int* d_t, double* d_rmp, double thr) {
+    const int t = ++(*d_t);
+    const double x = (double)(t + 1);
+    *d_rmp = (x < 0) ? 0.0 : (x < thr ? x / thr : 1.0);
+}
+
+void step_tick(fipi_ctx* ctx) {
+    LaunchScope ls_(ctx, "step tick", 0.0);
+    k_step_tick<<<1, 1, 0, ctx->stream>>>(ctx->d_t, ctx->d_rmp, 0.2 * ctx->P.t_end);
 }
 
 // ------------------------------------------------------------ allocation
@@ -709,6 +887,13 @@ fipi_status particles_alloc(fipi_ctx* ctx) {
     b.hist_cap = 256 * ((8 * n + RS_TILE - 1) / RS_TILE + 1);
     FIPI_CUDA(ctx, A((void**)&b.hist, sizeof(unsigned) * b.hist_cap));
     FIPI_CUDA(ctx, A((void**)&b.tau_part, sizeof(double) * n));
+    FIPI_CUDA(ctx, A((void**)&b.spos, sizeof(float4) * n));
+    FIPI_CUDA(ctx, A((void**)&b.sp_fw, sizeof(double) * 6 * n));
+    FIPI_CUDA(ctx, A((void**)&b.ymax, sizeof(unsigned long long) * 2));
+    {
+        const unsigned long long init[2] = {0ull, ~0ull};
+        FIPI_CUDA(ctx, h2d(ctx, b.ymax, init, sizeof(init)));
+    }
     FIPI_CUDA(ctx, A((void**)&b.it_mark, sizeof(int)));
     FIPI_CUDA(ctx, cudaMemsetAsync(b.it_mark, 0xff, sizeof(int), ctx->stream));
     FIPI_CUDA(ctx, A((void**)&b.tau, sizeof(double)));
@@ -720,7 +905,7 @@ void particles_free(fipi_ctx* ctx) {
     ParticleBufs& b = ctx->pb;
     void* all[] = {b.p, b.p_old, b.u_old, b.f_pp, b.f_pi, b.r, b.cth, b.keys, b.keys_alt, b.ids, b.ids_alt,
                    b.cell_off, b.cell_cnt, b.sp_keys, b.sp_keys_alt, b.sp_vals, b.sp_vals_alt, b.sp_prev,
-                   b.hist, b.tau_part, b.it_mark, b.tau};
+                   b.hist, b.tau_part, b.it_mark, b.tau, b.spos, b.sp_fw, b.ymax};
     for (void* p : all)
         if (p) cudaFree(p);
     b = ParticleBufs{};
@@ -808,9 +993,12 @@ fipi_status particles_f_pp(fipi_ctx* ctx, const double* p, int t, const double* 
     }
     build_cells(ctx, pd);
     const double rmp = ramp((double)t, 0.2 * ctx->P.t_end);
+    double* rmpd = ds.get<double>(1);
+    if (!rmpd) return set_error(ctx, FIPI_ERR_CUDA, "cudaMalloc failed");
+    FIPI_CUDA(ctx, h2d(ctx, rmpd, &rmp, sizeof(double)));
     if (f_pi) FIPI_CUDA(ctx, cudaMemsetAsync(b.it_mark, 0xff, sizeof(int), ctx->stream));
-    if (ctx->prec == FIPI_MIXED) f_pp_launch<float>(ctx, pd, rmp, f_pi ? fpid : nullptr, fpp, f_pi != nullptr);
-    else f_pp_launch<double>(ctx, pd, rmp, f_pi ? fpid : nullptr, fpp, f_pi != nullptr);
+    if (ctx->prec == FIPI_MIXED) f_pp_launch<float>(ctx, pd, rmpd, f_pi ? fpid : nullptr, fpp, f_pi != nullptr);
+    else f_pp_launch<double>(ctx, pd, rmpd, f_pi ? fpid : nullptr, fpp, f_pi != nullptr);
     FIPI_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     st = read_status(ctx);
     if (st != FIPI_OK) return st;
@@ -819,8 +1007,12 @@ fipi_status particles_f_pp(fipi_ctx* ctx, const double* p, int t, const double* 
         if (st != FIPI_OK) return st;
     }
     if (tau) {
-        if (f_pi) FIPI_CUDA(ctx, d2h(ctx, tau, b.tau, sizeof(double)));
-        else *tau = 0.0;
+        if (f_pi) {
+            st = particles_packing_tau(ctx, tau);
+            if (st != FIPI_OK) return st;
+        } else {
+            *tau = 0.0;
+        }
     }
     return FIPI_OK;
 }
@@ -838,7 +1030,7 @@ fipi_status particles_pairs(fipi_ctx* ctx, const double* p, int* pairs, int max_
     build_cells(ctx, pd);
     const PC pc = make_pc(ctx);
     const int blocks = (b.ncells * 32 + 255) / 256;
-    { LaunchScope ls_(ctx, "contact forces (warp per cell)", 0.0); k_f_pp<double, 1><<<blocks, 256, 0, ctx->stream>>>(pc, pd, b.ids, b.cell_off, 1.0, nullptr, nullptr, nullptr,
+    { LaunchScope ls_(ctx, "contact forces (warp per cell)", 0.0); k_f_pp<double, 1><<<blocks, 256, 0, ctx->stream>>>(pc, pd, b.ids, b.cell_off, nullptr, nullptr, nullptr, nullptr,
                                                       nullptr, cnt, nullptr, nullptr); }
     FIPI_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     st = read_status(ctx);
@@ -855,7 +1047,7 @@ fipi_status particles_pairs(fipi_ctx* ctx, const double* p, int* pairs, int max_
     int* pr = ds.get<int>(2 * (size_t)total);
     if (!pr) return set_error(ctx, FIPI_ERR_CUDA, "cudaMalloc failed");
     FIPI_CUDA(ctx, h2d(ctx, offd, ho.data(), sizeof(int) * n));
-    { LaunchScope ls_(ctx, "contact forces (warp per cell)", 0.0); k_f_pp<double, 2><<<blocks, 256, 0, ctx->stream>>>(pc, pd, b.ids, b.cell_off, 1.0, nullptr, nullptr, nullptr,
+    { LaunchScope ls_(ctx, "contact forces (warp per cell)", 0.0); k_f_pp<double, 2><<<blocks, 256, 0, ctx->stream>>>(pc, pd, b.ids, b.cell_off, nullptr, nullptr, nullptr, nullptr,
                                                       nullptr, nullptr, offd, pr); }
     std::vector<int> hp(2 * (size_t)total);
     FIPI_CUDA(ctx, d2h(ctx, hp.data(), pr, sizeof(int) * 2 * total));

@@ -272,6 +272,28 @@ class Simulation:
         _check(self.lib.fipi_packing_tau(self.h, ctypes.byref(v)))
         return v.value
 
+    # ---------------------------------------------------------------- instrumentation
+    def set_kernel_timing(self, on: bool):
+        """Per-kernel CUDA-event timing (steps then launch directly, not from graphs)."""
+        _check(self.lib.fipi_set_kernel_timing(self.h, 1 if on else 0))
+
+    def kernel_stats(self) -> list[dict]:
+        n = ctypes.c_int()
+        _check(self.lib.fipi_kernel_stat_count(self.h, ctypes.byref(n)))
+        out = []
+        for i in range(n.value):
+            name = ctypes.create_string_buffer(128)
+            la, ms, by = ctypes.c_longlong(), ctypes.c_double(), ctypes.c_double()
+            _check(self.lib.fipi_kernel_stats(self.h, i, name, 128, ctypes.byref(la), ctypes.byref(ms),
+                                              ctypes.byref(by)))
+            out.append({"name": name.value.decode(), "launches": la.value, "ms": ms.value, "bytes": by.value})
+        return out
+
+    def launch_count(self) -> int:
+        n = ctypes.c_longlong()
+        _check(self.lib.fipi_launch_count(self.h, ctypes.byref(n)))
+        return n.value
+
     # ---------------------------------------------------------------- fine-grained
     def fft_r2c(self, x) -> np.ndarray:
         out = np.empty(2 * self.SH)

@@ -197,6 +197,29 @@ def test_deterministic(fipi):
     assert np.array_equal(res[0][1], res[1][1])
 
 
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_graph_replay_matches_direct_launches(fipi, prec):
+    """Steps t >= 1 replay CUDA graphs; with kernel timing on they launch
+    directly.  Both must give the same bits."""
+    w = fipi.workload("t32")
+    P, c, p, r, ct = seeded_state(w, 25)
+    res = []
+    for timing in (False, True):
+        with fipi.Simulation(P, prec) as s:
+            s.set_phase(c)
+            s.set_particles(p)
+            s.set_kernel_timing(timing)
+            for _ in range(3):  # odd count: both buffer states and the step-by-step path
+                s.step(1)
+            s.step(2)
+            res.append((s.get_phase(), s.get_velocity(), s.get_particles()[0], s.packing_tau()))
+            if timing:
+                assert any(k["launches"] > 0 for k in s.kernel_stats())
+    for x, y in zip(res[0][:3], res[1][:3]):
+        assert np.array_equal(x, y)
+    assert res[0][3] == res[1][3]
+
+
 def test_out_of_range_particle_reports_error(fipi):
     w = fipi.workload("t32")
     P, c, p, r, ct = seeded_state(w, 24)
