@@ -211,10 +211,13 @@ inline cudaError_t d2h(fipi_ctx* ctx, void* h, const void* d, size_t n) {
 // on first use, asks for the largest shared-memory carveout so several
 // blocks fit per SM (per kernel instantiation; `cur` remembers the grant,
 // starting at 48 KiB).
+// The dynamic shared memory a kernel may take without the attribute is
+// 48 KB minus its static shared memory, so the attribute is set on first use
+// whatever the size (`cur` starts at the 48 KB sentinel).
 template <class K> inline cudaError_t ensure_smem(K kern, size_t bytes, size_t& cur) {
     if (cur == 48 * 1024) {
         cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-        cur = 48 * 1024 + 1;
+        cur = 0;
     }
     if (bytes <= cur) return cudaSuccess;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);

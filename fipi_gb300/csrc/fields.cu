@@ -18,82 +18,9 @@
 #include <vector>
 
 #include "ctx.hpp"
+#include "passes.cuh"
 
 namespace fipi {
-
-// ------------------------------------------------------------ constants
-template <typename T> struct StepConsts {
-    T lam_eps;    // lambda/sqr(epsilon)              main.cpp:178
-    T lam;        // lambda
-    T dt;
-    T s1, s2;     // t = 0: dt*M, dt*M*lambda          main.cpp:203-210
-    T s4, s2m;    // t > 0: 4 dt M, 2 dt M             main.cpp:215-216
-    T s4c, s2c;   // 4 dt, 2 dt                        main.cpp:220-221
-    T s3;         // 2 dt M lambda                     main.cpp:224
-    T mu;
-    T rho1, rho2, gravity;
-    int ny2, nz2, m;  // Nyquist indices
-};
-
-template <typename T> StepConsts<T> make_consts(const fipi_ctx* ctx) {
-    const fipi_params& P = ctx->P;
-    StepConsts<T> k;
-    const double dt = P.dt, M = P.mobility, lam = P.lambda;
-    k.lam_eps = T(P.lambda / (P.epsilon * P.epsilon));
-    k.lam = T(lam);
-    k.dt = T(dt);
-    k.s1 = T(dt * M);
-    k.s2 = T(dt * M * lam);
-    k.s4 = T(4.0 * dt * M);
-    k.s2m = T(2.0 * dt * M);
-    k.s4c = T(4.0 * dt);
-    k.s2c = T(2.0 * dt);
-    k.s3 = T(2.0 * dt * M * lam);
-    k.mu = T(P.mu);
-    k.rho1 = T(P.rho1);
-    k.rho2 = T(P.rho2);
-    k.gravity = T(P.gravity);
-    k.ny2 = P.ny / 2;
-    k.nz2 = P.nz / 2;
-    k.m = P.nx / 2;
-    return k;
-}
-
-template <typename T> struct KTabs {
-    const T* kx;
-    const T* ky;
-    const T* kz;
-    __device__ __forceinline__ T k2(int ix, int iy, int iz) const {
-        const T a = kx[ix], b = ky[iy], c = kz[iz];
-        T s = a * a;
-        s += b * b;
-        s += c * c;
-        return s;
-    }
-};
-
-// ------------------------------------------------------------ block reduce
-__device__ __forceinline__ double block_sum(double v) {
-    __shared__ double red[32];
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    __syncthreads();
-    if (lane == 0) red[w] = v;
-    __syncthreads();
-    double s = 0.0;
-    if (w == 0) {
-        const int nw = (blockDim.x + 31) >> 5;
-        s = lane < nw ? red[lane] : 0.0;
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-    }
-    return s;  // valid in thread 0
-}
-
-// Row pitch of the X pass: padded M plus the X_M slot, kept odd.
-__host__ __device__ inline int xpass_pitch(int M) {
-    const int p = padded_len(M) + 1;
-    return (p & 1) ? p : p + 1;
-}
 
 // ------------------------------------------------------------ X-pass ops
 // R2C of c and of f = (lambda/eps^2)(c^3 - c) from the real c (set-up).
@@ -225,129 +152,6 @@ template <typename T> struct OpForce {
     }
 };
 
-// Adapter giving point() an accumulator when the op does not take one.
-template <class Op> struct NoAcc {
-    Op op;
-    __device__ const auto* in(int f) const { return op.in(f); }
-    __device__ auto* out(int f) const { return op.out(f); }
-    template <class C, class A> __device__ void point(int z, int y, int n, C* v, A&) const { op.point(z, y, n, v); }
-};
-
-// X pass: one block = TY consecutive rows y0..y0+TY-1 of plane z, NIN
-// spectral inputs (transposed runs of TY along y, C2R) and NOUT spectral
-// outputs (R2C, transposed store); point() does the fused real-space work
-// and may accumulate an FP64 per-block sum.  Rows of M = nx/2 complex pairs
-// live in shared memory with one pad slot per 16 (pitch odd, so the
-// transposed column accesses are conflict-free); X_M sits at index M.
-template <typename T, int NIN, int NOUT, bool REDUCE, int M, class Op>
-__global__ void __launch_bounds__(kThreads, 3) k_xpass_acc(Geom g, const cplx<T>* __restrict__ twx, Op op,
-                                                      double* partials) {
-    using C = cplx<T>;
-    constexpr int TY = Tiles<T>::TY;
-    constexpr int NF = NIN > NOUT ? NIN : NOUT;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    C* s = reinterpret_cast<C*>(smem_raw);
-    constexpr int H = M + 1;
-    const IdxPadded idx{xpass_pitch(M)};
-    const int z = blockIdx.y, y0 = blockIdx.x * TY;
-    const int tid = threadIdx.x, nthr = blockDim.x;
-    constexpr int halfM = M / 2;
-    constexpr int Tn = FftPlan<M, FftE<T>::value>::Tn;
-    constexpr int rpr = kThreads / Tn;  // row FFTs per round
-    if constexpr (NIN > 0) {
-        const int n = NIN * H * TY;
-        for (int b = tid; b < n; b += 8 * kThreads) {
-            C tmp[8];
-#pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                const int i = b + u * kThreads;
-                if (i < n) {
-                    const int ty = i % TY, rest = i / TY, kx = rest % H, f = rest / H;
-                    tmp[u] = op.in(f)[((size_t)z * H + kx) * g.ny + y0 + ty];
-                }
-            }
-#pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                const int i = b + u * kThreads;
-                if (i < n) {
-                    const int ty = i % TY, rest = i / TY, kx = rest % H, f = rest / H;
-                    s[idx(f * TY + ty, kx)] = tmp[u];
-                }
-            }
-        }
-        __syncthreads();
-        // C2R split pre-processing (only the real parts of X_0 and X_M enter).
-        for (int i = tid; i < NIN * TY * (halfM + 1); i += nthr) {
-            const int k = i % (halfM + 1);
-            const int row = i / (halfM + 1);
-            if (k == 0) {
-                const T a = s[idx(row, 0)].x, c = s[idx(row, M)].x;
-                s[idx(row, 0)] = mkc<C>(a + c, a - c);
-            } else {
-                const int km = M - k;
-                const C Xk = s[idx(row, k)], Xm = s[idx(row, km)];
-                const C Wk = twx[k], Wm = twx[km];
-                const C A = cadd(Xk, cconj(Xm)), B = csub(Xk, cconj(Xm));
-                const C A2 = cadd(Xm, cconj(Xk)), B2 = csub(Xm, cconj(Xk));
-                s[idx(row, k)] = cadd(A, cmul_i(cmul(B, cconj(Wk)), +1));
-                if (km != k) s[idx(row, km)] = cadd(A2, cmul_i(cmul(B2, cconj(Wm)), +1));
-            }
-        }
-        __syncthreads();
-        for (int r0 = 0; r0 < NIN * TY; r0 += rpr) {
-            const int row = r0 + tid / Tn;
-            smem_fft2<T, +1, M>(s, idx, row, tid % Tn, row < NIN * TY, twx, 2);
-        }
-    }
-    const T invV = T(1) / T(g.V);
-    T acc = T(0);  // per-thread partial sum in the arithmetic type (FP64 only per block)
-    for (int i = tid; i < TY * M; i += nthr) {
-        const int n = i % M;
-        const int ty = i / M;
-        C v[NF];
-#pragma unroll
-        for (int f = 0; f < NIN; ++f) v[f] = cscale(s[idx(f * TY + ty, n)], invV);
-        op.point(z, y0 + ty, n, v, acc);
-#pragma unroll
-        for (int f = 0; f < NOUT; ++f) s[idx(f * TY + ty, n)] = v[f];
-    }
-    if constexpr (REDUCE) {
-        const double bs = block_sum((double)acc);
-        if (tid == 0) partials[(size_t)blockIdx.y * gridDim.x + blockIdx.x] = bs;
-    }
-    __syncthreads();
-    if constexpr (NOUT > 0) {
-        for (int r0 = 0; r0 < NOUT * TY; r0 += rpr) {
-            const int row = r0 + tid / Tn;
-            smem_fft2<T, -1, M>(s, idx, row, tid % Tn, row < NOUT * TY, twx, 2);
-        }
-        // R2C split post-processing; X_M lands at index M.
-        for (int i = tid; i < NOUT * TY * (halfM + 1); i += nthr) {
-            const int k = i % (halfM + 1);
-            const int row = i / (halfM + 1);
-            if (k == 0) {
-                const C Z0 = s[idx(row, 0)];
-                s[idx(row, 0)] = mkc<C>(Z0.x + Z0.y, T(0));
-                s[idx(row, M)] = mkc<C>(Z0.x - Z0.y, T(0));
-            } else {
-                const int km = M - k;
-                const C Zk = s[idx(row, k)], Zm = s[idx(row, km)];
-                const C Wk = twx[k], Wm = twx[km];
-                const C E1 = cadd(Zk, cconj(Zm)), D1 = csub(Zk, cconj(Zm));
-                const C E2 = cadd(Zm, cconj(Zk)), D2 = csub(Zm, cconj(Zk));
-                s[idx(row, k)] = cscale(csub(E1, cmul_i(cmul(Wk, D1), +1)), T(0.5));
-                if (km != k) s[idx(row, km)] = cscale(csub(E2, cmul_i(cmul(Wm, D2), +1)), T(0.5));
-            }
-        }
-        __syncthreads();
-        const int n = NOUT * H * TY;
-        for (int i = tid; i < n; i += nthr) {
-            const int ty = i % TY, rest = i / TY, kx = rest % H, f = rest / H;
-            op.out(f)[((size_t)z * H + kx) * g.ny + y0 + ty] = s[idx(f * TY + ty, kx)];
-        }
-    }
-}
-
 // ------------------------------------------------------------ Z-pass ops
 // Z forward with the Cahn-Hilliard update (main.cpp:192-235) fused.
 // The conv spectrum C^n is the transformed input; c_hat^{n+1} is written
@@ -438,79 +242,6 @@ template <typename T> struct ZOpGrad {
     }
 };
 
-// Z forward with the Leray projection (main.cpp:274-275) fused:
-// u_hat = (F - k (k.F)/k^2) / (mu k^2), 0 at k = 0.  At modes with a Nyquist
-// index the reference's C2C inverse keeps only the real part of a
-// non-Hermitian spectrum; that equals the inverse of the average of the
-// projections with k and with the Nyquist components of k negated, which is
-// what is stored here (a Hermitian half spectrum).
-template <typename T> struct ZOpProj {
-    using C = cplx<T>;
-    const C* in[3];
-    C* out[3];
-    KTabs<T> kt;
-    T mu;
-    int m, ny2, nz2;
-    __device__ void load(int, int, int, size_t gi, C* v) const {
-        v[0] = in[0][gi];
-        v[1] = in[1][gi];
-        v[2] = in[2][gi];
-    }
-    __device__ static void project(const T* kv, T k2, T mk2, const C* F, C* u) {
-        T dre = T(0), dim = T(0);
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            dre += kv[d] * F[d].x;
-            dim += kv[d] * F[d].y;
-        }
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            const T qre = (kv[d] * dre) / k2, qim = (kv[d] * dim) / k2;
-            u[d] = mkc<C>((F[d].x - qre) / mk2, (F[d].y - qim) / mk2);
-        }
-    }
-    __device__ void store(int ix, int iy, int iz, size_t gi, const C* F) const {
-        const T kv[3] = {kt.kx[ix], kt.ky[iy], kt.kz[iz]};
-        const T k2 = kt.k2(ix, iy, iz);
-        C u[3];
-        if (k2 == T(0)) {
-            u[0] = u[1] = u[2] = mkc<C>(T(0), T(0));
-        } else {
-            const T mk2 = k2 * mu;
-            project(kv, k2, mk2, F, u);
-            const bool nx_ = ix == m, ny_ = iy == ny2, nz_ = iz == nz2;
-            if (nx_ || ny_ || nz_) {
-                const T ks[3] = {nx_ ? -kv[0] : kv[0], ny_ ? -kv[1] : kv[1], nz_ ? -kv[2] : kv[2]};
-                C u2[3];
-                project(ks, k2, mk2, F, u2);
-#pragma unroll
-                for (int d = 0; d < 3; ++d)
-                    u[d] = mkc<C>(T(0.5) * (u[d].x + u2[d].x), T(0.5) * (u[d].y + u2[d].y));
-            }
-        }
-        out[0][gi] = u[0];
-        out[1][gi] = u[1];
-        out[2][gi] = u[2];
-    }
-};
-
-// Z forward plain store; in the mixed form the k = 0 entry of c_hat is held
-// in FP64 and zeroed in the FP32 array.
-template <typename T, int NF> struct ZOpStore {
-    using C = cplx<T>;
-    const C* in[NF];
-    C* out[NF];
-    int zero_k0_mask;
-    __device__ void load(int, int, int, size_t gi, C* v) const {
-#pragma unroll
-        for (int f = 0; f < NF; ++f) v[f] = in[f][gi];
-    }
-    __device__ void store(int, int, int, size_t gi, const C* v) const {
-#pragma unroll
-        for (int f = 0; f < NF; ++f)
-            out[f][gi] = (gi == 0 && ((zero_k0_mask >> f) & 1)) ? mkc<C>(T(0), T(0)) : v[f];
-    }
-};
 
 // FP64 k = 0 update of the mixed form: c_hat(0) follows the same IMEX /
 // SBDF2 recurrence with k = 0 (the f terms vanish), C(0) from the FP64
@@ -538,11 +269,6 @@ __global__ void k_k0_update(double* k0, const double* partials, int np, int firs
     }
 }
 
-template <typename Tin, typename Tout>
-__global__ void k_convert(const Tin* __restrict__ a, Tout* __restrict__ b, size_t n) {
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-        b[i] = (Tout)a[i];
-}
 
 // FP64 per-block sums for mass and free energy (main.cpp:329, field.cpp:507-516).
 template <typename T>
@@ -568,82 +294,6 @@ __global__ void k_diag(const T* __restrict__ c, const T* __restrict__ g0, const 
     if (threadIdx.x == 0) partials[blockIdx.x] = s;
 }
 
-// ------------------------------------------------------------ launch glue
-template <typename T> struct F {
-    using C = cplx<T>;
-    static C* S(fipi_ctx* ctx, int i) { return (C*)ctx->fb.S[i]; }
-    static C* sp(void* p) { return (C*)p; }
-    static T* re(void* p) { return (T*)p; }
-    static const C* tw(void* p) { return (const C*)p; }
-    static KTabs<T> ktabs(fipi_ctx* ctx) {
-        return KTabs<T>{(const T*)ctx->fb.kx, (const T*)ctx->fb.ky, (const T*)ctx->fb.kz};
-    }
-};
-
-// nreal: real (V-sized) arrays the fused point operation reads or writes.
-template <typename T, int NIN, int NOUT, bool REDUCE, class Op>
-void launch_x(fipi_ctx* ctx, const char* name, int nreal, const Op& op, double* partials = nullptr) {
-    const Geom& g = ctx->g;
-    LaunchScope ls(ctx, name,
-                   (double)(NIN + NOUT) * g.SH * sizeof(cplx<T>) + (double)nreal * g.V * sizeof(T));
-    constexpr int NF = NIN > NOUT ? NIN : NOUT;
-    const size_t smem = (size_t)NF * Tiles<T>::TY * xpass_pitch(g.m) * sizeof(cplx<T>);
-    dim3 grid(g.ny / Tiles<T>::TY, g.nz);
-    dispatch_pow2(g.m, [&](auto MC) {
-        constexpr int M = decltype(MC)::value;
-        auto kern = k_xpass_acc<T, NIN, NOUT, REDUCE, M, Op>;
-        static size_t granted = 48 * 1024;
-        ensure_smem(kern, smem, granted);
-        kern<<<grid, kThreads, smem, ctx->stream>>>(g, (const cplx<T>*)ctx->fb.twx, op, partials);
-    });
-}
-
-template <typename T> void launch_y(fipi_ctx* ctx, int nf, void* const* in, void* const* out, int dir) {
-    const Geom& g = ctx->g;
-    static const char* names[9] = {"Y pass x0", "Y pass x1", "Y pass x2", "Y pass x3", "Y pass x4",
-                                   "Y pass x5", "Y pass x6", "Y pass x7", "Y pass x8"};
-    LaunchScope ls(ctx, names[nf], 2.0 * nf * g.SH * sizeof(cplx<T>));
-    FieldPtrs<T> fp{};
-    for (int f = 0; f < nf; ++f) {
-        fp.in[f] = (cplx<T>*)in[f];
-        fp.out[f] = (cplx<T>*)out[f];
-    }
-    // persistent, TMA double-buffered: a grid of resident blocks walks all tiles
-    const size_t smem = ypass_tma_smem<T>(g);
-    dispatch_pow2(g.ny, [&](auto NC) {
-        constexpr int N = decltype(NC)::value;
-        auto kern = (dir < 0) ? k_ypass_tma<T, -1, N> : k_ypass_tma<T, +1, N>;
-        static size_t granted[2] = {48 * 1024, 48 * 1024};
-        static int blocks_per_sm[2] = {0, 0};
-        const int di = dir < 0 ? 0 : 1;
-        ensure_smem(kern, smem, granted[di]);
-        if (!blocks_per_sm[di]) {
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm[di], kern, kThreads, smem);
-            if (blocks_per_sm[di] < 1) blocks_per_sm[di] = 1;
-        }
-        const int rb = ypass_rows<T>(g.ny);
-        const long long tiles = ((long long)g.nz * g.h + rb - 1) / rb * nf;
-        long long grid = (long long)ctx->num_sms * blocks_per_sm[di];
-        if (grid > tiles) grid = tiles;
-        kern<<<(unsigned)grid, kThreads, smem, ctx->stream>>>(g, (const cplx<T>*)ctx->fb.twy, fp, nf, ctx->status);
-    });
-}
-
-// nspec: spectral arrays the pass and its fused operation read or write.
-template <typename T, int NF, int DIR, class Op> void launch_z(fipi_ctx* ctx, const char* name, int nspec, const Op& op) {
-    const Geom& g = ctx->g;
-    LaunchScope ls(ctx, name, (double)nspec * g.SH * sizeof(cplx<T>));
-    const size_t smem = zpass_smem<T, NF>(g);
-    dim3 grid(g.h, g.ny / zpass_cols<T>(g.nz));
-    const int threads = zpass_threads<T>(g.nz);
-    dispatch_pow2(g.nz, [&](auto NC) {
-        constexpr int N = decltype(NC)::value;
-        auto kern = k_zpass<T, NF, DIR, N, Op>;
-        static size_t granted = 48 * 1024;
-        ensure_smem(kern, smem, granted);
-        kern<<<grid, threads, smem, ctx->stream>>>(g, (const cplx<T>*)ctx->fb.twz, op);
-    });
-}
 
 // grad c (real, 3 fields) from c_hat.
 template <typename T> void grad_from_chat(fipi_ctx* ctx, const cplx<T>* chat, T* const g3[3]) {
@@ -755,35 +405,6 @@ void fields_free(fipi_ctx* ctx) {
     ctx->k0 = nullptr;
 }
 
-// ------------------------------------------------------------ state I/O
-// Copies host doubles into a T device array through a staging buffer.
-template <typename T> static fipi_status upload(fipi_ctx* ctx, const double* h, T* d, size_t n) {
-    if (sizeof(T) == sizeof(double)) {
-        FIPI_CUDA(ctx, cudaMemcpyAsync(d, h, n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-        return FIPI_OK;
-    }
-    double* stage = nullptr;
-    FIPI_CUDA(ctx, cudaMallocAsync((void**)&stage, n * sizeof(double), ctx->stream));
-    FIPI_CUDA(ctx, cudaMemcpyAsync(stage, h, n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-    { LaunchScope ls(ctx, "convert", 0.0); k_convert<double, T><<<1024, 256, 0, ctx->stream>>>(stage, d, n); }
-    FIPI_CUDA(ctx, cudaFreeAsync(stage, ctx->stream));
-    return FIPI_OK;
-}
-
-template <typename T> static fipi_status download(fipi_ctx* ctx, const T* d, double* h, size_t n) {
-    if (sizeof(T) == sizeof(double)) {
-        FIPI_CUDA(ctx, cudaMemcpyAsync(h, d, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-        FIPI_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-        return FIPI_OK;
-    }
-    double* stage = nullptr;
-    FIPI_CUDA(ctx, cudaMallocAsync((void**)&stage, n * sizeof(double), ctx->stream));
-    { LaunchScope ls(ctx, "convert", 0.0); k_convert<T, double><<<1024, 256, 0, ctx->stream>>>(d, stage, n); }
-    FIPI_CUDA(ctx, cudaMemcpyAsync(h, stage, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-    FIPI_CUDA(ctx, cudaFreeAsync(stage, ctx->stream));
-    FIPI_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    return FIPI_OK;
-}
 
 // t = 0 state: c, c_hat, f_hat, grad c (everything main.cpp:178-189 needs).
 template <typename T> static fipi_status set_phase_t(fipi_ctx* ctx, const double* c_host) {
