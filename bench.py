@@ -139,6 +139,53 @@ def timed_steps(sim, n, torch):
     return e0.elapsed_time(e1) / 1e3
 
 
+def adjoint_ratio(F, P, c, p, r, ct, device, torch, steps, traj_steps):
+    """FP64 adjoint cost against the FP64 forward step on the same state.
+
+    adjoint_step: one fipi_adjoint_step (checkpoint load, the step recomputed
+    with its intermediates kept, the reverse pass), host wall time of the
+    synchronous call; forward: CUDA-event time of one plain FP64 step.
+    trajectory: fipi_trajectory_forward + fipi_trajectory_backward over
+    `traj_steps` steps (sqrt(N) checkpoints) against as many plain steps."""
+    import numpy as np
+
+    s = F.Simulation(P, "fp64", device=device)
+    s.set_phase(c)
+    s.set_particles(p, r, ct)
+    s.step(2)  # into the SBDF2 regime
+    fwd = timed_steps(s, steps, torch) / steps
+    s.checkpoint_reserve(2)
+    s.checkpoint_save(0)
+    s.step(1)
+    s.checkpoint_save(1)
+    dc = np.random.default_rng(0).standard_normal(s.V)
+    times = []
+    for _ in range(steps + 1):
+        s.checkpoint_load(1)
+        s.adjoint_seed(dc)
+        t0 = time.perf_counter()
+        s.adjoint_step(0)
+        times.append(time.perf_counter() - t0)
+    adj = statistics.median(times[1:])
+    s.checkpoint_load(0)
+    s.sync()
+    t0 = time.perf_counter()
+    s.trajectory_forward(traj_steps)
+    s.sync()
+    tf = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    s.trajectory_backward(dc)
+    tb = time.perf_counter() - t0
+    s.close()
+    stride = int(np.ceil(np.sqrt(traj_steps)))
+    return {"form": "fp64", "forward_ms": fwd * 1e3, "adjoint_step_ms": adj * 1e3,
+            "adjoint_step_over_forward": adj / fwd,
+            "trajectory": {"steps": traj_steps, "stride": stride,
+                           "slots": -(-traj_steps // stride) + stride,
+                           "forward_s": tf, "backward_s": tb,
+                           "gradient_over_forward": (tf + tb) / (traj_steps * fwd)}}
+
+
 def kernel_stats(sim):
     return sim.kernel_stats()
 
@@ -333,7 +380,11 @@ def run_gpu(args):
 
     # ---- roofline of the dominant kernel
     hbm, src = peaks()
-    dom = max(ks, key=lambda k: k["ms"]) if ks else None
+    # the dominant grid kernel: particle kernels carry no algorithmic bytes
+    # (latency-bound, reported as particle updates/s) and never dominate here
+    grid = [k for k in ks if k["bytes"] > 0]
+    dom = max(grid, key=lambda k: k["ms"]) if grid else None
+    top = max(ks, key=lambda k: k["ms"]) if ks else None
     roof = None
     if dom and dom["ms"] > 0:
         per_launch_s = dom["ms"] / dom["launches"] / 1e3
@@ -342,7 +393,13 @@ def run_gpu(args):
                 "traffic": committed_traffic(dom["name"], w.name), "kernel": dom["name"],
                 "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs)" if src == "measured" else src,
                 "alg_bytes_per_launch": dom["bytes"], "us_per_launch": per_launch_s * 1e6,
-                "share_of_step": dom["ms"] / sum(k["ms"] for k in ks)}
+                "share_of_step": dom["ms"] / sum(k["ms"] for k in ks),
+                "top_kernel_overall": top["name"] if top else None}
+
+    # ---- adjoint / forward (FP64 form)
+    adj = None
+    if args.adj_steps > 0:
+        adj = adjoint_ratio(F, P, c, p, r, ct, local, torch, args.adj_steps, args.traj_steps)
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
@@ -360,7 +417,8 @@ def run_gpu(args):
             "particle_updates_per_s": value * w.n_p,
             "fp64": {"steps_per_s": fp64_rate * ws, "mixed_over_fp64": value / (fp64_rate * ws)},
             "error_mixed_vs_fp64": err,
-            "adjoint_over_forward": None,
+            "adjoint_over_forward": adj["adjoint_step_over_forward"] if adj else None,
+            "adjoint": adj,
             "e2e": {"value": e2e_val, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,
             "roofline": roof,
@@ -387,6 +445,8 @@ def main():
     ap.add_argument("--err-steps", type=int, default=1000)
     ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--kernel-steps", type=int, default=20)
+    ap.add_argument("--adj-steps", type=int, default=5, help="adjoint steps timed (0 = skip)")
+    ap.add_argument("--traj-steps", type=int, default=16, help="steps of the checkpointed gradient")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", type=int, default=0, help="only run N steps (for ncu)")
     ap.add_argument("--form", default="mixed", choices=["mixed", "fp64"])

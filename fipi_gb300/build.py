@@ -22,6 +22,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 UNITS = {
     "capi.cu": [],
     "fields.cu": [],
+    "adjoint.cu": [],
     "particles.cu": ["-fmad=false"],
 }
 

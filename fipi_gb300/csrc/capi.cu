@@ -40,14 +40,14 @@ static cudaEvent_t take_event(fipi_ctx* ctx) {
     return e;
 }
 
-LaunchScope::LaunchScope(fipi_ctx* c, const char* name, double bytes) : ctx(c) {
+LaunchScope::LaunchScope(fipi_ctx* c, const char* name, double b) : ctx(c), bytes(b) {
     ctx->kt.launches++;
     if (!ctx->kt.enabled) return;
     auto& st = ctx->kt.stats;
     for (size_t i = 0; i < st.size(); ++i)
         if (st[i].name == name) idx = (int)i;
     if (idx < 0) {
-        st.push_back(KernelStat{name, 0, 0.0, bytes});
+        st.push_back(KernelStat{name, 0, 0.0, 0.0, 0.0});
         idx = (int)st.size() - 1;
     }
     e0 = take_event(ctx);
@@ -58,7 +58,7 @@ LaunchScope::LaunchScope(fipi_ctx* c, const char* name, double bytes) : ctx(c) {
 LaunchScope::~LaunchScope() {
     if (idx < 0) return;
     cudaEventRecord(e1, ctx->stream);
-    ctx->kt.pending.push_back({idx, {e0, e1}});
+    ctx->kt.pending.push_back({idx, bytes, {e0, e1}});
 }
 
 // Folds finished event pairs into the per-kernel totals.
@@ -66,12 +66,14 @@ static void drain_timer(fipi_ctx* ctx) {
     cudaStreamSynchronize(ctx->stream);
     for (auto& p : ctx->kt.pending) {
         float ms = 0.f;
-        cudaEventElapsedTime(&ms, p.second.first, p.second.second);
-        KernelStat& s = ctx->kt.stats[p.first];
+        cudaEventElapsedTime(&ms, p.ev.first, p.ev.second);
+        KernelStat& s = ctx->kt.stats[p.idx];
         s.launches++;
         s.ms += ms;
-        ctx->kt.pool.push_back(p.second.first);
-        ctx->kt.pool.push_back(p.second.second);
+        s.bytes_sum += p.bytes;
+        s.bytes = s.bytes_sum / (double)s.launches;
+        ctx->kt.pool.push_back(p.ev.first);
+        ctx->kt.pool.push_back(p.ev.second);
     }
     ctx->kt.pending.clear();
 }
@@ -203,7 +205,6 @@ fipi_status fipi_create(const fipi_params* P, fipi_precision prec, int device, f
     return FIPI_OK;
 }
 
-static void graphs_reset(fipi_ctx* ctx);
 
 fipi_status fipi_destroy(fipi_ctx* ctx) {
     if (!ctx) return FIPI_OK;
@@ -213,6 +214,7 @@ fipi_status fipi_destroy(fipi_ctx* ctx) {
     if (ctx->d_rmp) cudaFree(ctx->d_rmp);
     drain_timer(ctx);
     for (cudaEvent_t e : ctx->kt.pool) cudaEventDestroy(e);
+    adjoint_free(ctx);
     fields_free(ctx);
     particles_free(ctx);
     if (ctx->status) cudaFree(ctx->status);
@@ -227,7 +229,9 @@ fipi_status fipi_device_bytes(const fipi_ctx* ctx, size_t* out) {
     return FIPI_OK;
 }
 
-static fipi_status check_status(fipi_ctx* ctx) {
+}  // extern "C"
+
+fipi_status fipi::check_status(fipi_ctx* ctx) {
     FIPI_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     FIPI_CUDA(ctx, cudaGetLastError());
     int st = 0;
@@ -240,6 +244,8 @@ static fipi_status check_status(fipi_ctx* ctx) {
     }
     return FIPI_OK;
 }
+
+extern "C" {
 
 fipi_status fipi_set_phase(fipi_ctx* ctx, const double* c) {
     if (!ctx || !c) return set_error(ctx, FIPI_ERR_BAD_ARG, "NULL argument");
@@ -266,7 +272,9 @@ fipi_status fipi_set_velocity(fipi_ctx* ctx, const double* u) {
     return check_status(ctx);
 }
 
-static fipi_status upload_soa(fipi_ctx* ctx, const double* h, double* d, int n) {
+}  // extern "C"
+
+fipi_status fipi::upload_soa(fipi_ctx* ctx, const double* h, double* d, int n) {
     std::vector<double> s((size_t)3 * n);
     for (int i = 0; i < n; ++i)
         for (int a = 0; a < 3; ++a) s[(size_t)a * n + i] = h[3 * i + a];
@@ -275,7 +283,7 @@ static fipi_status upload_soa(fipi_ctx* ctx, const double* h, double* d, int n) 
     return FIPI_OK;
 }
 
-static fipi_status download_soa(fipi_ctx* ctx, const double* d, double* h, int n) {
+fipi_status fipi::download_soa(fipi_ctx* ctx, const double* d, double* h, int n) {
     std::vector<double> s((size_t)3 * n);
     FIPI_CUDA(ctx, cudaMemcpyAsync(s.data(), d, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
     FIPI_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -283,6 +291,8 @@ static fipi_status download_soa(fipi_ctx* ctx, const double* d, double* h, int n
         for (int a = 0; a < 3; ++a) h[3 * i + a] = s[(size_t)a * n + i];
     return FIPI_OK;
 }
+
+extern "C" {
 
 fipi_status fipi_set_particles(fipi_ctx* ctx, const double* p, const double* r, const double* cos_theta,
                                const double* f_pp) {
@@ -346,15 +356,18 @@ fipi_status fipi_get_time(const fipi_ctx* ctx, int* t) {
     return FIPI_OK;
 }
 
-static void graphs_reset(fipi_ctx* ctx) {
+}  // extern "C"
+
+void fipi::graphs_reset(fipi_ctx* ctx) {
     for (auto& g : ctx->graphs) {
         if (g.exec) cudaGraphExecDestroy(g.exec);
         g = fipi_ctx::StepGraph{};
     }
 }
 
+
 // One iteration of main.cpp:172-316, enqueued on the context stream.
-static void enqueue_step(fipi_ctx* ctx) {
+void fipi::enqueue_step(fipi_ctx* ctx) {
     const int t = ctx->t;
     fields_step_ch(ctx, t);      // main.cpp:176-238
     particles_spread(ctx);       // main.cpp:266 (compute_f_r of the previous step's state)
@@ -363,6 +376,8 @@ static void enqueue_step(fipi_ctx* ctx) {
     step_tick(ctx);
     ctx->t = t + 1;
 }
+
+extern "C" {
 
 // Steps with t >= 1 are replayed from a CUDA graph of one step.  The step
 // swaps ping-pong buffers, so the buffer assignment alternates between two

@@ -76,6 +76,60 @@ struct ParticleBufs {
     double* tau = nullptr;       // 1
 };
 
+// Device-resident checkpoints of the step state (one allocation, `slots`
+// payloads of `bytes` each).
+struct CheckpointStore {
+    int slots = 0;
+    size_t bytes = 0;
+    unsigned char* base = nullptr;
+    std::vector<int> t;  // step index held by each slot, -1 = empty
+    // the last fipi_trajectory_forward: first step, steps, stride, segments
+    struct Traj {
+        int t0 = -1, n = 0, s = 0, K = 0;
+    } traj;
+};
+
+// Reverse-mode state of the FP64 step.  Cotangents of spectral state are
+// kept as half spectra of the real-field cotangent (la = R2C(lambda)), so
+// every Fourier multiplier of the step is its own adjoint.
+struct AdjBufs {
+    bool ready = false;
+    int t = -1;  // step index of the state the cotangent refers to
+    // spectral (cplx<double>, SH each)
+    void* la_c = nullptr;   // c of the state (c_hat, f_hat, grad c folded in)
+    void* la_co = nullptr;  // SBDF2 histories c_hat_old, f_hat_old, C_hat_old
+    void* la_fo = nullptr;
+    void* la_Co = nullptr;
+    void* AS[5] = {};       // transform scratch
+    // real fields (double)
+    double* la_u = nullptr;  // 3V
+    double* lamF = nullptr;  // 3V cotangent of the force density F of the Stokes solve
+    double* part = nullptr;  // 4V particle cotangents on c^{n+1}, grad c^{n+1}
+    double* tc0 = nullptr;   // V   tape: c^n
+    double* tg0 = nullptr;   // 3V  tape: grad c^n
+    double* tu = nullptr;    // 3V  tape: u^n
+    double* tmu = nullptr;   // V   tape: mu^{n+1}
+    // particles (SoA, 3n unless noted)
+    double* la_p = nullptr;
+    double* la_fpp = nullptr;
+    double* tp0 = nullptr;     // positions at the step start
+    double* tfpp0 = nullptr;   // f_pp at the step start (spread in the step)
+    double* p1 = nullptr;      // stage-1 positions
+    double* fpi1 = nullptr;
+    double* fpp1 = nullptr;
+    double* loc = nullptr;     // 8n: c, grad c interpolated at p^n (4n) and p1 (4n)
+    double* lamF1 = nullptr;   // cotangent of the stage-1 contact forces
+    double* lamF2 = nullptr;   // cotangent of the stage-2 contact forces
+    double* lam_p1 = nullptr;  // cotangent of p1
+    double* lamloc = nullptr;  // 8n cotangents of `loc`
+    unsigned* rk = nullptr;    // 16n spreading records (node, record) + ping-pong
+    unsigned* rv = nullptr;
+    unsigned* rk2 = nullptr;
+    unsigned* rv2 = nullptr;
+    double* rw = nullptr;      // 14n: fractions (3) and cotangents (4) of 2n interpolations
+    double* rmp = nullptr;     // 1: ramp factor of the reversed step
+};
+
 }  // namespace fipi
 
 namespace fipi {
@@ -85,13 +139,19 @@ struct KernelStat {
     std::string name;
     long long launches = 0;
     double ms = 0.0;
-    double bytes = 0.0;  // algorithmic bytes of one launch
+    double bytes = 0.0;      // algorithmic bytes per launch (mean over the timed launches)
+    double bytes_sum = 0.0;  // algorithmic bytes of all timed launches
+};
+struct PendingLaunch {
+    int idx;
+    double bytes;
+    std::pair<cudaEvent_t, cudaEvent_t> ev;
 };
 struct KTimer {
     bool enabled = false;
     long long launches = 0;
     std::vector<KernelStat> stats;
-    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
+    std::vector<PendingLaunch> pending;
     std::vector<cudaEvent_t> pool;
 };
 }  // namespace fipi
@@ -128,6 +188,12 @@ struct fipi_ctx {
     size_t device_bytes = 0;
     std::string last_error;
     fipi::KTimer kt;
+    fipi::CheckpointStore ck;
+    fipi::AdjBufs ad;
+    // forward-step tape (non-NULL only while the adjoint recomputes a step):
+    // u^n from the conv pass, mu^{n+1} from the force pass
+    void* tape_u[3] = {};
+    void* tape_mu = nullptr;
 };
 
 namespace fipi {
@@ -181,10 +247,25 @@ fipi_status particles_spread_host(fipi_ctx* ctx, const double* p, const double* 
 // Packing energy of the last contact-force evaluation.
 fipi_status particles_packing_tau(fipi_ctx* ctx, double* out);
 
+// Reverse mode (adjoint.cu / particles.cu).
+void enqueue_step(fipi_ctx* ctx);  // one forward step, direct launches
+// Sets the device step index and the ramp factor of step t (particles.cu).
+void set_tick(fipi_ctx* ctx, int t);
+// Particle stages of the step reversed (after the taped forward step):
+// la_p, la_fpp of the end state -> la_p of the start state (stage part) and
+// the particle cotangents `part` on c^{n+1}, grad c^{n+1}.
+fipi_status particles_adjoint(fipi_ctx* ctx);
+// Adjoint of the spreading of f_pp^n at p^n, given lamF: la_fpp = I(p) lamF / dV,
+// la_p += (f_pp / dV) grad_p I(p) lamF.
+void particles_adjoint_spread(fipi_ctx* ctx);
+fipi_status particles_adjoint_alloc(fipi_ctx* ctx);
+void particles_adjoint_free(fipi_ctx* ctx);
+
 // Brackets one kernel launch: counts it and, when timing is on, records
 // events around it on the context stream (capi.cu).
 struct LaunchScope {
     fipi_ctx* ctx;
+    double bytes;
     int idx = -1;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     LaunchScope(fipi_ctx* c, const char* name, double bytes);
@@ -194,6 +275,14 @@ struct LaunchScope {
 // capi.cu helpers
 fipi_status set_error(fipi_ctx* ctx, fipi_status st, const std::string& msg);
 fipi_status cuda_check(fipi_ctx* ctx, cudaError_t e, const char* what);
+// Synchronises the stream and turns the device error word into a status.
+fipi_status check_status(fipi_ctx* ctx);
+// Host n x 3 (particle-major) <-> device 3 x n (SoA), synchronous.
+fipi_status upload_soa(fipi_ctx* ctx, const double* h, double* d, int n);
+fipi_status download_soa(fipi_ctx* ctx, const double* d, double* h, int n);
+void graphs_reset(fipi_ctx* ctx);
+// adjoint.cu: frees checkpoint slots and adjoint buffers.
+void adjoint_free(fipi_ctx* ctx);
 
 }  // namespace fipi
 
@@ -209,11 +298,10 @@ inline cudaError_t d2h(fipi_ctx* ctx, void* h, const void* d, size_t n) {
 }
 // Raises a kernel's dynamic shared-memory limit to `bytes` when needed and,
 // on first use, asks for the largest shared-memory carveout so several
-// blocks fit per SM (per kernel instantiation; `cur` remembers the grant,
-// starting at 48 KiB).
-// The dynamic shared memory a kernel may take without the attribute is
-// 48 KB minus its static shared memory, so the attribute is set on first use
-// whatever the size (`cur` starts at the 48 KB sentinel).
+// blocks fit per SM (per kernel instantiation; `cur` remembers the grant and
+// starts at a 48 KiB sentinel).  Without the attribute a kernel may only take
+// 48 KiB minus its static shared memory, so the attribute is set on first
+// use whatever the size.
 template <class K> inline cudaError_t ensure_smem(K kern, size_t bytes, size_t& cur) {
     if (cur == 48 * 1024) {
         cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);

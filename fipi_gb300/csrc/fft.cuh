@@ -104,7 +104,7 @@ __global__ void __launch_bounds__(kThreads) k_ypass_tma(Geom g, const cplx<T>* _
     constexpr int Tn = FftPlan<N, FftE<T>::value>::Tn;
     constexpr int RB = kThreads / Tn;
     constexpr int BUF = RB * ((N + (N >> 4) + 15) & ~15);  // padded rows, 128-byte multiple for FP32/FP64
-    extern __shared__ __align__(128) unsigned char smem_raw[];
+    extern __shared__ __align__(16) unsigned char smem_raw[];
     C* buf0 = reinterpret_cast<C*>(smem_raw);
     __shared__ __align__(8) uint64_t bar[2];
     __shared__ int abort_flag;

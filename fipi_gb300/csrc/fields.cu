@@ -53,19 +53,6 @@ template <typename T> struct OpR2C {
     }
 };
 
-// C2R of NIN fields into real arrays dst[f] (+ optional constant offset).
-template <typename T, int NIN> struct OpC2RStore {
-    using C = cplx<T>;
-    const C* src[NIN];
-    T* dst[NIN];
-    int nx, ny;
-    __device__ const C* in(int f) const { return src[f]; }
-    __device__ C* out(int) const { return nullptr; }
-    __device__ void point(int z, int y, int n, C* v) const {
-#pragma unroll
-        for (int f = 0; f < NIN; ++f) reinterpret_cast<C*>(dst[f] + ((size_t)z * ny + y) * nx)[n] = v[f];
-    }
-};
 
 // Step A: u (3 inverse) . grad c -> conv (1 forward).  main.cpp:188-189
 template <typename T, bool MIXED> struct OpConv {
@@ -74,12 +61,17 @@ template <typename T, bool MIXED> struct OpConv {
     const T* g[3];
     C* o0;
     double* partials;
+    T* tape_u[3];  // non-NULL: u is also stored (adjoint recompute)
     int nx, ny;
     __device__ const C* in(int f) const { return uS[f]; }
     __device__ C* out(int) const { return o0; }
     template <class A> __device__ void point(int z, int y, int n, C* v, A& acc) const {
         const size_t row = ((size_t)z * ny + y) * nx;
         T s0 = T(0), s1 = T(0);
+        if (tape_u[0]) {
+#pragma unroll
+            for (int d = 0; d < 3; ++d) reinterpret_cast<C*>(tape_u[d] + row)[n] = v[d];
+        }
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             const C gg = reinterpret_cast<const C*>(g[d] + row)[n];
@@ -124,12 +116,14 @@ template <typename T> struct OpForce {
     const T* fsp[3];
     int spread;
     T rho1, rho2, gravity;
+    T* tape_mu;  // non-NULL: mu is also stored (adjoint recompute)
     int nx, ny;
     __device__ const C* in(int f) const { return S[f]; }
     __device__ C* out(int f) const { return const_cast<C*>(S[f]); }
     template <class A> __device__ void point(int z, int y, int n, C* v, A&) const {
         const size_t row = ((size_t)z * ny + y) * nx;
         const C mu = v[0];
+        if (tape_mu) reinterpret_cast<C*>(tape_mu + row)[n] = mu;
         const C cc = reinterpret_cast<const C*>(c + row)[n];
         // buoyancy ((1+c)/2 rho1 + (1-c)/2 rho2) g, g = (0, 0, gravity)
         const T b0 = ((cc.x + T(1)) / T(2)) * rho1 + ((cc.x * T(-1) + T(1)) / T(2)) * rho2;
@@ -500,7 +494,7 @@ template <typename T, bool MIXED> static void step_ch_t(fipi_ctx* ctx, int t) {
     launch_y<T>(ctx, 3, s3, s3, +1);
     OpConv<T, MIXED> oc{{F<T>::S(ctx, 0), F<T>::S(ctx, 1), F<T>::S(ctx, 2)},
                         {(const T*)b.g[0], (const T*)b.g[1], (const T*)b.g[2]}, F<T>::S(ctx, 3), ctx->partials,
-                        g.nx, g.ny};
+                        {(T*)ctx->tape_u[0], (T*)ctx->tape_u[1], (T*)ctx->tape_u[2]}, g.nx, g.ny};
     launch_x<T, 3, 1, MIXED>(ctx, "X inverse u, conv, forward", 3, oc, ctx->partials);
     void* s1[1] = {b.S[3]};
     launch_y<T>(ctx, 1, s1, s1, -1);
@@ -551,7 +545,7 @@ template <typename T> static void step_stokes_t(fipi_ctx* ctx) {
                   (const T*)b.c,
                   {(const T*)b.fsp[0], (const T*)b.fsp[1], (const T*)b.fsp[2]},
                   (ctx->P.switch_particle && ctx->P.n_p > 0) ? 1 : 0,
-                  k.rho1, k.rho2, k.gravity, g.nx, g.ny};
+                  k.rho1, k.rho2, k.gravity, (T*)ctx->tape_mu, g.nx, g.ny};
     launch_x<T, 4, 3, false>(ctx, "X inverse mu,grad, force, forward", (of.spread ? 7 : 4), of);
     void* s3[3] = {b.S[0], b.S[1], b.S[2]};
     launch_y<T>(ctx, 3, s3, s3, -1);

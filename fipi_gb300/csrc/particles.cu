@@ -884,7 +884,7 @@ fipi_status particles_alloc(fipi_ctx* ctx) {
     FIPI_CUDA(ctx, A((void**)&b.sp_vals, sizeof(unsigned) * 8 * n));
     FIPI_CUDA(ctx, A((void**)&b.sp_vals_alt, sizeof(unsigned) * 8 * n));
     FIPI_CUDA(ctx, A((void**)&b.sp_prev, sizeof(unsigned) * 8 * n));
-    b.hist_cap = 256 * ((8 * n + RS_TILE - 1) / RS_TILE + 1);
+    b.hist_cap = 256 * ((16 * n + RS_TILE - 1) / RS_TILE + 1);  // up to 16 records per particle (adjoint)
     FIPI_CUDA(ctx, A((void**)&b.hist, sizeof(unsigned) * b.hist_cap));
     FIPI_CUDA(ctx, A((void**)&b.tau_part, sizeof(double) * n));
     FIPI_CUDA(ctx, A((void**)&b.spos, sizeof(float4) * n));
@@ -1199,6 +1199,351 @@ fipi_status particles_spread_host(fipi_ctx* ctx, const double* p, const double* 
         FIPI_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     }
     return FIPI_OK;
+}
+
+// ------------------------------------------------------------ step index
+__global__ void k_set_tick(int* d_t, double* d_rmp, int t, double thr) {
+    *d_t = t;
+    const double x = (double)(t + 1);
+    *d_rmp = (x < 0) ? 0.0 : (x < thr ? x / thr : 1.0);
+}
+
+void set_tick(fipi_ctx* ctx, int t) {
+    LaunchScope ls_(ctx, "step tick", 0.0);
+    k_set_tick<<<1, 1, 0, ctx->stream>>>(ctx->d_t, ctx->d_rmp, t, 0.2 * ctx->P.t_end);
+}
+
+// ------------------------------------------------------------ adjoint
+// Reverse mode of the two Heun stages (element.cpp:250-280,
+// cluster.cpp:268-369, element.cpp:169-191, field.cpp:223-248) and of the
+// spreading (cluster.cpp:438-504), FP64.  Branches (interpolation cell,
+// |phi| <= tanh 2, |d| < r, |d| < r_eq) are those of the forward step.
+
+// Trilinear value and position gradient of v at (x, y, z) (field.cpp:223-248).
+__device__ __forceinline__ void interp_grad(const PC& pc, double x, double y, double z, const double* __restrict__ v,
+                                            double g[3]) {
+    const double fx = floor(x / pc.dx), fy = floor(y / pc.dy), fz = floor(z / pc.dz);
+    const int i = wrapi((int)fx, pc.N[0]), j = wrapi((int)fy, pc.N[1]), k = wrapi((int)fz, pc.N[2]);
+    const double m = x / pc.dx - fx, nn = y / pc.dy - fy, o = z / pc.dz - fz;
+    const int i1 = (i + 1) % pc.N[0], j1 = (j + 1) % pc.N[1], k1 = (k + 1) % pc.N[2];
+    const size_t sy = (size_t)pc.N[0], sz = (size_t)pc.N[0] * pc.N[1];
+    const double v000 = v[i + j * sy + k * sz], v100 = v[i1 + j * sy + k * sz];
+    const double v010 = v[i + j1 * sy + k * sz], v110 = v[i1 + j1 * sy + k * sz];
+    const double v001 = v[i + j * sy + k1 * sz], v101 = v[i1 + j * sy + k1 * sz];
+    const double v011 = v[i + j1 * sy + k1 * sz], v111 = v[i1 + j1 * sy + k1 * sz];
+    const double dm = (1 - nn) * (1 - o) * (v100 - v000) + nn * (1 - o) * (v110 - v010) +
+                      (1 - nn) * o * (v101 - v001) + nn * o * (v111 - v011);
+    const double dn = (1 - m) * (1 - o) * (v010 - v000) + m * (1 - o) * (v110 - v100) +
+                      (1 - m) * o * (v011 - v001) + m * o * (v111 - v101);
+    const double dd = (1 - m) * (1 - nn) * (v001 - v000) + m * (1 - nn) * (v101 - v100) +
+                      (1 - m) * nn * (v011 - v010) + m * nn * (v111 - v110);
+    g[0] = dm / pc.dx;
+    g[1] = dn / pc.dy;
+    g[2] = dd / pc.dz;
+}
+
+// Adjoint of f_pi_of: lf = cotangent of f_pi -> cotangents of phi and grad c.
+__device__ __forceinline__ void f_pi_adj(const PC& pc, double phi, double gx, double gy, double gz, double r, double ct,
+                                         const double lf[3], double* lphi, double lg[3]) {
+    const double gn = sqrt(gx * gx + gy * gy + gz * gz);
+    *lphi = 0.0;
+    lg[0] = lg[1] = lg[2] = 0.0;
+    if (!(fabs(phi) <= pc.tanh2 && gn != 0.0)) return;
+    const double s2e = 1.4142135623730951 * pc.epsilon;
+    const double d = 0.5 * log((1.0 + phi) / (1.0 - phi)) * s2e;
+    double f_mag = 0.0, dmag = 0.0;
+    if (fabs(d) < r) {
+        f_mag = -pc.A * pc.pi * (d - r * ct) * pc.sigma;
+        dmag = -pc.A * pc.pi * pc.sigma * s2e / (1.0 - phi * phi);  // d(d)/d(phi) = sqrt2 eps / (1 - phi^2)
+    }
+    const double nh[3] = {gx / gn, gy / gn, gz / gn};
+    const double s = nh[0] * lf[0] + nh[1] * lf[1] + nh[2] * lf[2];
+    *lphi = s * dmag;
+    for (int a = 0; a < 3; ++a) lg[a] = f_mag / gn * (lf[a] - nh[a] * s);
+}
+
+// Forward recompute of one stage's interpolation (c, grad c) and f_pi.
+__global__ void k_adj_interp(PC pc, const double* __restrict__ p, const double* __restrict__ c,
+                             const double* __restrict__ g0, const double* __restrict__ g1,
+                             const double* __restrict__ g2, const double* __restrict__ r,
+                             const double* __restrict__ cth, double* loc, double* fpi) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = pc.n;
+    if (i >= n) return;
+    const double* fl[4] = {c, g0, g1, g2};
+    double vals[4];
+    interp_fields<double, double>(pc, p[i], p[n + i], p[2 * n + i], fl, 4, vals);
+    for (int q = 0; q < 4; ++q) loc[q * n + i] = vals[q];
+    if (fpi) {
+        double f[3];
+        f_pi_of(pc, vals[0], vals[1], vals[2], vals[3], r[i], cth[i], f);
+        for (int a = 0; a < 3; ++a) fpi[a * n + i] = f[a];
+    }
+}
+
+// Stage-1 advection recomputed: p1 = wrap(p + dt (f_pi + f_pp)/(6 pi mu r)).
+__global__ void k_adj_advect1(PC pc, const double* __restrict__ p0, const double* __restrict__ fpi,
+                              const double* __restrict__ fpp, const double* __restrict__ r, double* p1) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = pc.n;
+    if (i >= n) return;
+    double pp[3] = {p0[i], p0[n + i], p0[2 * n + i]}, po[3], uo[3];
+    const double a[3] = {fpi[i], fpi[n + i], fpi[2 * n + i]};
+    const double b[3] = {fpp[i], fpp[n + i], fpp[2 * n + i]};
+    advect_one(pc, 1, a, b, r[i], pp, po, uo);
+    for (int q = 0; q < 3; ++q) p1[q * n + i] = pp[q];
+}
+
+// Adjoint of one stage at positions p: given the cotangent lv of this
+// stage's velocity, writes the cotangent of its contact forces (lamF =
+// kappa lv + extra), of the interpolated values (lamloc, 4n) and of p
+// through the interpolation (lam_p = base + ...), kappa = 1/(6 pi mu r).
+//   stage 2: lv = dt/2 lp_end,              extra = lfpp_end, base = 0
+//   stage 1: lv = dt/2 lp_end + dt lam_p1,  extra = 0,        base = lp_end + lam_p1
+__global__ void k_adj_stage(PC pc, int stage, const double* __restrict__ p, const double* __restrict__ c,
+                            const double* __restrict__ g0, const double* __restrict__ g1,
+                            const double* __restrict__ g2, const double* __restrict__ loc,
+                            const double* __restrict__ r, const double* __restrict__ cth,
+                            const double* lp_end, const double* __restrict__ lfpp_end,
+                            const double* __restrict__ lam_p1_in, double* lamF, double* lamloc, double* lam_p) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = pc.n;
+    if (i >= n) return;
+    const double kappa = 1.0 / 6.0 / pc.pi / pc.mu / r[i];
+    double lv[3], lf[3];
+    for (int a = 0; a < 3; ++a) {
+        lv[a] = 0.5 * pc.dt * lp_end[a * n + i];
+        if (stage == 1) lv[a] += pc.dt * lam_p1_in[a * n + i];
+        lf[a] = kappa * lv[a];
+        lamF[a * n + i] = lf[a] + (stage == 2 ? lfpp_end[a * n + i] : 0.0);
+    }
+    double lphi, lg[3];
+    f_pi_adj(pc, loc[i], loc[n + i], loc[2 * n + i], loc[3 * n + i], r[i], cth[i], lf, &lphi, lg);
+    lamloc[i] = lphi;
+    for (int a = 0; a < 3; ++a) lamloc[(1 + a) * n + i] = lg[a];
+    const double x = p[i], y = p[n + i], z = p[2 * n + i];
+    double acc[3], gr[3];
+    interp_grad(pc, x, y, z, c, gr);
+    for (int a = 0; a < 3; ++a) acc[a] = lphi * gr[a];
+    const double* gf[3] = {g0, g1, g2};
+    for (int d = 0; d < 3; ++d) {
+        interp_grad(pc, x, y, z, gf[d], gr);
+        for (int a = 0; a < 3; ++a) acc[a] += lg[d] * gr[a];
+    }
+    for (int a = 0; a < 3; ++a) {
+        double base = 0.0;
+        if (stage == 1) base = lp_end[a * n + i] + lam_p1_in[a * n + i];
+        lam_p[a * n + i] = base + acc[a];
+    }
+}
+
+// Adjoint of compute_f_pp with respect to positions: for every pair of the
+// forward evaluation (same cells, minimum-image rule of cluster.cpp:319-326
+// and |d| < r_eq test), lam_p[i] += J(d) (lamF[i] - lamF[j]) with
+// J = ramp k_n ((r_eq/|d| - 1) I - r_eq d d^T / |d|^3), which is even in d.
+// Warp per home cell, lane per home particle as in k_f_pp; coincident pairs
+// (random separation in the reference) contribute nothing.
+__global__ void k_f_pp_adj(PC pc, const double* __restrict__ p, const unsigned* __restrict__ ids,
+                           const int* __restrict__ off, const double* __restrict__ rmp_p,
+                           const double* __restrict__ lamF, double* lam_p) {
+    const int lane = threadIdx.x & 31;
+    const int cell = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int ncells = pc.nc[0] * pc.nc[1] * pc.nc[2];
+    if (cell >= ncells) return;
+    const int n = pc.n;
+    const int ci = cell % pc.nc[0], cj = (cell / pc.nc[0]) % pc.nc[1], ck = cell / (pc.nc[0] * pc.nc[1]);
+    const int beg = off[cell], end = off[cell + 1];
+    const double T0 = pc.dc[0] * (pc.nc[0] - 2), T1 = pc.dc[1] * (pc.nc[1] - 2), T2 = pc.dc[2] * (pc.nc[2] - 2);
+    const double sc = (*rmp_p) * pc.k_n;
+    for (int base = beg; base < end; base += 32) {
+        const int s = base + lane;
+        const bool active = s < end;
+        const int i = active ? (int)ids[s] : 0;
+        const double xi = p[i], yi = p[n + i], zi = p[2 * n + i];
+        const double li[3] = {lamF[i], lamF[n + i], lamF[2 * n + i]};
+        double acc[3] = {0.0, 0.0, 0.0};
+        for (int dk = -1; dk <= 1; ++dk)
+            for (int dj = -1; dj <= 1; ++dj)
+                for (int di = -1; di <= 1; ++di) {
+                    const int co = (ci + di + pc.nc[0]) % pc.nc[0] + (cj + dj + pc.nc[1]) % pc.nc[1] * pc.nc[0] +
+                                   (ck + dk + pc.nc[2]) % pc.nc[2] * pc.nc[0] * pc.nc[1];
+                    const int qe = off[co + 1];
+                    for (int q = off[co]; q < qe; ++q) {
+                        const int j = (int)ids[q];
+                        if (!active || j == i) continue;
+                        double d[3];
+                        if (i < j) {
+                            d[0] = xi - p[j];
+                            d[1] = yi - p[n + j];
+                            d[2] = zi - p[2 * n + j];
+                        } else {
+                            d[0] = p[j] - xi;
+                            d[1] = p[n + j] - yi;
+                            d[2] = p[2 * n + j] - zi;
+                        }
+                        if (d[0] > T0) d[0] = d[0] - pc.L[0];
+                        else if (d[0] < -T0) d[0] = d[0] + pc.L[0];
+                        if (d[1] > T1) d[1] = d[1] - pc.L[1];
+                        else if (d[1] < -T1) d[1] = d[1] + pc.L[1];
+                        if (d[2] > T2) d[2] = d[2] - pc.L[2];
+                        else if (d[2] < -T2) d[2] = d[2] + pc.L[2];
+                        const double dn = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+                        if (!(dn < pc.r_eq) || dn == 0.0) continue;
+                        const double dl[3] = {li[0] - lamF[j], li[1] - lamF[n + j], li[2] - lamF[2 * n + j]};
+                        const double a = pc.r_eq / dn - 1.0;
+                        const double b = pc.r_eq / (dn * dn * dn) * (d[0] * dl[0] + d[1] * dl[1] + d[2] * dl[2]);
+                        for (int e = 0; e < 3; ++e) acc[e] += sc * (a * dl[e] - b * d[e]);
+                    }
+                }
+        if (active)
+            for (int e = 0; e < 3; ++e) lam_p[e * n + i] += acc[e];
+    }
+}
+
+// Spreading records of the interpolation adjoint: 8 corners of each of the
+// 2n interpolations (entity e = stage * n + i), node keys, fractions and
+// the 4 cotangents per entity.
+__global__ void k_adj_records(PC pc, const double* __restrict__ p0, const double* __restrict__ p1,
+                              const double* __restrict__ lamloc, unsigned* keys, unsigned* vals, double* rw) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = pc.n;
+    if (e >= 2 * n) return;
+    const int st = e / n, i = e - st * n;
+    const double* p = st == 0 ? p0 : p1;
+    int ix[3];
+    double fr[3];
+    cell_and_frac(pc, p[i], p[n + i], p[2 * n + i], ix, fr);
+    for (int c = 0; c < 8; ++c) {
+        const int x = (ix[0] + c_corner[c][0]) % pc.N[0];
+        const int y = (ix[1] + c_corner[c][1]) % pc.N[1];
+        const int z = (ix[2] + c_corner[c][2]) % pc.N[2];
+        keys[8 * e + c] = (unsigned)(x + (size_t)y * pc.N[0] + (size_t)z * pc.N[0] * pc.N[1]);
+        vals[8 * e + c] = (unsigned)(8 * e + c);
+    }
+    const int m = 2 * n;
+    for (int a = 0; a < 3; ++a) rw[a * m + e] = fr[a];
+    for (int q = 0; q < 4; ++q) rw[(3 + q) * m + e] = lamloc[(st * 4 + q) * n + i];
+}
+
+// Sorted segmented reduction of the records: part[q][node] = sum of w_c lam_q
+// in ascending record order (deterministic, no atomics).
+__global__ void k_adj_reduce(const unsigned* __restrict__ keys, const unsigned* __restrict__ vals, int m, int ne,
+                             const double* __restrict__ rw, double* part, size_t V) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= m) return;
+    const unsigned node = keys[s];
+    if (s > 0 && keys[s - 1] == node) return;
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int q = s; q < m && keys[q] == node; ++q) {
+        const unsigned rec = vals[q];
+        const int e = (int)(rec >> 3), c = (int)(rec & 7u);
+        const double o = rw[e], pp = rw[ne + e], qq = rw[2 * ne + e];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) acc[k] += corner_value<double>(rw[(3 + k) * ne + e], c, o, pp, qq);
+    }
+    for (int k = 0; k < 4; ++k) part[k * V + node] = acc[k];
+}
+
+// Adjoint of the spreading of f_pp^n at p^n given lamF (3 real fields).
+__global__ void k_adj_spread(PC pc, const double* __restrict__ p, const double* __restrict__ fpp,
+                             const double* __restrict__ lamF, size_t V, double* la_fpp, double* la_p) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = pc.n;
+    if (i >= n) return;
+    const double x = p[i], y = p[n + i], z = p[2 * n + i];
+    const double inv = 1.0 / pc.dx / pc.dy / pc.dz;
+    double acc[3] = {0.0, 0.0, 0.0};
+    for (int d = 0; d < 3; ++d) {
+        const double* f = lamF + d * V;
+        const double* fl[1] = {f};
+        double val;
+        interp_fields<double, double>(pc, x, y, z, fl, 1, &val);
+        la_fpp[d * n + i] = val * inv;
+        double gr[3];
+        interp_grad(pc, x, y, z, f, gr);
+        const double w = fpp[d * n + i] * inv;
+        for (int a = 0; a < 3; ++a) acc[a] += w * gr[a];
+    }
+    for (int a = 0; a < 3; ++a) la_p[a * n + i] += acc[a];
+}
+
+fipi_status particles_adjoint_alloc(fipi_ctx* ctx) {
+    AdjBufs& a = ctx->ad;
+    const int n = ctx->pb.n > 0 ? ctx->pb.n : 1;
+    auto A = [&](void** ptr, size_t bytes) -> cudaError_t {
+        cudaError_t e = cudaMalloc(ptr, bytes);
+        if (e == cudaSuccess) {
+            ctx->device_bytes += bytes;
+            e = cudaMemsetAsync(*ptr, 0, bytes, ctx->stream);
+        }
+        return e;
+    };
+    const size_t b3 = sizeof(double) * 3 * n;
+    double** v3[] = {&a.la_p, &a.la_fpp, &a.tp0, &a.tfpp0, &a.p1, &a.fpi1, &a.fpp1, &a.lamF1, &a.lamF2, &a.lam_p1};
+    for (double** q : v3) FIPI_CUDA(ctx, A((void**)q, b3));
+    FIPI_CUDA(ctx, A((void**)&a.loc, sizeof(double) * 8 * n));
+    FIPI_CUDA(ctx, A((void**)&a.lamloc, sizeof(double) * 8 * n));
+    unsigned** r16[] = {&a.rk, &a.rv, &a.rk2, &a.rv2};
+    for (unsigned** q : r16) FIPI_CUDA(ctx, A((void**)q, sizeof(unsigned) * 16 * n));
+    FIPI_CUDA(ctx, A((void**)&a.rw, sizeof(double) * 14 * n));
+    FIPI_CUDA(ctx, A((void**)&a.rmp, sizeof(double)));
+    return FIPI_OK;
+}
+
+void particles_adjoint_free(fipi_ctx* ctx) {
+    AdjBufs& a = ctx->ad;
+    void* all[] = {a.la_p, a.la_fpp, a.tp0, a.tfpp0, a.p1, a.fpi1, a.fpp1, a.lamF1, a.lamF2, a.lam_p1,
+                   a.loc, a.lamloc, a.rk, a.rv, a.rk2, a.rv2, a.rw, a.rmp};
+    for (void* p : all)
+        if (p) cudaFree(p);
+    a.la_p = a.la_fpp = a.tp0 = a.tfpp0 = a.p1 = a.fpi1 = a.fpp1 = a.lamF1 = a.lamF2 = a.lam_p1 = nullptr;
+    a.loc = a.lamloc = a.rw = a.rmp = nullptr;
+    a.rk = a.rv = a.rk2 = a.rv2 = nullptr;
+}
+
+// Runs after the taped forward step: ctx->fb.c, fb.g hold c^{n+1}, grad c^{n+1};
+// a.tp0 holds p^n, a.rmp the ramp(t + 1, 0.2 t_end) factor of the reversed step.
+fipi_status particles_adjoint(fipi_ctx* ctx) {
+    ParticleBufs& b = ctx->pb;
+    AdjBufs& a = ctx->ad;
+    const PC pc = make_pc(ctx);
+    const int n = b.n;
+    const int nb = (n + 255) / 256;
+    const double* c = (const double*)ctx->fb.c;
+    const double* g0 = (const double*)ctx->fb.g[0];
+    const double* g1 = (const double*)ctx->fb.g[1];
+    const double* g2 = (const double*)ctx->fb.g[2];
+    const int cells_blocks = (b.ncells * 32 + 255) / 256;
+    // stage 1 recomputed at p^n: interpolation, f_pi, contact forces, p1
+    { LaunchScope ls_(ctx, "adjoint: interpolate + f_pi", 0.0); k_adj_interp<<<nb, 256, 0, ctx->stream>>>(pc, a.tp0, c, g0, g1, g2, b.r, b.cth, a.loc, a.fpi1); }
+    build_cells(ctx, a.tp0);
+    { LaunchScope ls_(ctx, "adjoint: contact forces", 0.0); k_f_pp<double, 0><<<cells_blocks, 256, 0, ctx->stream>>>(pc, a.tp0, b.ids, b.cell_off, a.rmp, nullptr, b.it_mark, a.fpp1, nullptr, nullptr, nullptr, nullptr); }
+    { LaunchScope ls_(ctx, "adjoint: advect", 0.0); k_adj_advect1<<<nb, 256, 0, ctx->stream>>>(pc, a.tp0, a.fpi1, a.fpp1, b.r, a.p1); }
+    { LaunchScope ls_(ctx, "adjoint: interpolate", 0.0); k_adj_interp<<<nb, 256, 0, ctx->stream>>>(pc, a.p1, c, g0, g1, g2, b.r, b.cth, a.loc + 4 * n, nullptr); }
+    // stage 2 reversed at p1
+    { LaunchScope ls_(ctx, "adjoint: stage", 0.0); k_adj_stage<<<nb, 256, 0, ctx->stream>>>(pc, 2, a.p1, c, g0, g1, g2, a.loc + 4 * n, b.r, b.cth, a.la_p, a.la_fpp, nullptr, a.lamF2, a.lamloc + 4 * n, a.lam_p1); }
+    build_cells(ctx, a.p1);
+    { LaunchScope ls_(ctx, "adjoint: contact forces", 0.0); k_f_pp_adj<<<cells_blocks, 256, 0, ctx->stream>>>(pc, a.p1, b.ids, b.cell_off, a.rmp, a.lamF2, a.lam_p1); }
+    // stage 1 reversed at p^n (la_p becomes the start-state cotangent)
+    { LaunchScope ls_(ctx, "adjoint: stage", 0.0); k_adj_stage<<<nb, 256, 0, ctx->stream>>>(pc, 1, a.tp0, c, g0, g1, g2, a.loc, b.r, b.cth, a.la_p, nullptr, a.lam_p1, a.lamF1, a.lamloc, a.la_p); }
+    build_cells(ctx, a.tp0);
+    { LaunchScope ls_(ctx, "adjoint: contact forces", 0.0); k_f_pp_adj<<<cells_blocks, 256, 0, ctx->stream>>>(pc, a.tp0, b.ids, b.cell_off, a.rmp, a.lamF1, a.la_p); }
+    // interpolation adjoint onto the grid: part = [c, g0, g1, g2] cotangents
+    const int m = 16 * n;
+    { LaunchScope ls_(ctx, "adjoint: records", 0.0); k_adj_records<<<(2 * n + 255) / 256, 256, 0, ctx->stream>>>(pc, a.tp0, a.p1, a.lamloc, a.rk, a.rv, a.rw); }
+    radix_sort(ctx, a.rk, a.rv, a.rk2, a.rv2, m, bits_for(ctx->g.V - 1));
+    FIPI_CUDA(ctx, cudaMemsetAsync(a.part, 0, sizeof(double) * 4 * (size_t)ctx->g.V, ctx->stream));
+    { LaunchScope ls_(ctx, "adjoint: records reduce", 0.0); k_adj_reduce<<<(m + 255) / 256, 256, 0, ctx->stream>>>(a.rk, a.rv, m, 2 * n, a.rw, a.part, (size_t)ctx->g.V); }
+    FIPI_CUDA(ctx, cudaGetLastError());
+    return FIPI_OK;
+}
+
+void particles_adjoint_spread(fipi_ctx* ctx) {
+    AdjBufs& a = ctx->ad;
+    const PC pc = make_pc(ctx);
+    const int n = ctx->pb.n;
+    LaunchScope ls_(ctx, "adjoint: spread", 0.0);
+    k_adj_spread<<<(n + 255) / 256, 256, 0, ctx->stream>>>(pc, a.tp0, a.tfpp0, a.lamF, (size_t)ctx->g.V, a.la_fpp, a.la_p);
 }
 
 }  // namespace fipi

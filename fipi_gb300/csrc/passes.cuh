@@ -86,6 +86,20 @@ __host__ __device__ inline int xpass_pitch(int M) {
     return (p & 1) ? p : p + 1;
 }
 
+// C2R of NIN fields into real arrays dst[f].
+template <typename T, int NIN> struct OpC2RStore {
+    using C = cplx<T>;
+    const C* src[NIN];
+    T* dst[NIN];
+    int nx, ny;
+    __device__ const C* in(int f) const { return src[f]; }
+    __device__ C* out(int) const { return nullptr; }
+    __device__ void point(int z, int y, int n, C* v) const {
+#pragma unroll
+        for (int f = 0; f < NIN; ++f) reinterpret_cast<C*>(dst[f] + ((size_t)z * ny + y) * nx)[n] = v[f];
+    }
+};
+
 // Adapter giving point() an accumulator when the op does not take one.
 template <class Op> struct NoAcc {
     Op op;

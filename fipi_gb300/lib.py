@@ -78,6 +78,18 @@ _SIGS = {
     "fipi_kernel_stats": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_char_p, ctypes.c_int,
                                          ctypes.POINTER(ctypes.c_longlong), _dp, _dp]),
     "fipi_launch_count": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_longlong)]),
+    "fipi_checkpoint_reserve": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "fipi_checkpoint_bytes": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_size_t)]),
+    "fipi_checkpoint_save": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "fipi_checkpoint_load": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "fipi_checkpoint_export": (ctypes.c_int, [_vp, ctypes.c_int, _vp, ctypes.c_size_t]),
+    "fipi_checkpoint_import": (ctypes.c_int, [_vp, ctypes.c_int, _vp, ctypes.c_size_t]),
+    "fipi_adjoint_seed": (ctypes.c_int, [_vp, _dp, _dp, _dp, _dp]),
+    "fipi_adjoint_step": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "fipi_adjoint_get": (ctypes.c_int, [_vp, _dp, _dp, _dp, _dp]),
+    "fipi_adjoint_get_history": (ctypes.c_int, [_vp, _dp, _dp, _dp]),
+    "fipi_trajectory_forward": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int]),
+    "fipi_trajectory_backward": (ctypes.c_int, [_vp, _dp, _dp, _dp, _dp]),
     "fipi_seed_phase": (ctypes.c_int, [ctypes.POINTER(FipiParams), ctypes.c_uint64, ctypes.c_double,
                                        ctypes.c_double, _dp]),
     "fipi_seed_particles": (ctypes.c_int, [ctypes.POINTER(FipiParams), ctypes.c_uint64,
@@ -293,6 +305,61 @@ class Simulation:
         n = ctypes.c_longlong()
         _check(self.lib.fipi_launch_count(self.h, ctypes.byref(n)))
         return n.value
+
+    # ---------------------------------------------------------------- checkpoints
+    def checkpoint_reserve(self, slots: int):
+        _check(self.lib.fipi_checkpoint_reserve(self.h, slots))
+
+    def checkpoint_bytes(self) -> int:
+        b = ctypes.c_size_t()
+        _check(self.lib.fipi_checkpoint_bytes(self.h, ctypes.byref(b)))
+        return b.value
+
+    def checkpoint_save(self, slot: int):
+        _check(self.lib.fipi_checkpoint_save(self.h, slot))
+
+    def checkpoint_load(self, slot: int):
+        _check(self.lib.fipi_checkpoint_load(self.h, slot))
+
+    def checkpoint_export(self, slot: int) -> bytes:
+        """Header (64 bytes) + payload of one slot."""
+        buf = ctypes.create_string_buffer(64 + self.checkpoint_bytes())
+        _check(self.lib.fipi_checkpoint_export(self.h, slot, ctypes.cast(buf, _vp), len(buf)))
+        return buf.raw
+
+    def checkpoint_import(self, slot: int, blob: bytes):
+        buf = ctypes.create_string_buffer(bytes(blob), len(blob))
+        _check(self.lib.fipi_checkpoint_import(self.h, slot, ctypes.cast(buf, _vp), len(blob)))
+
+    # ---------------------------------------------------------------- adjoint (FP64)
+    def adjoint_seed(self, dc=None, du=None, dp=None, df_pp=None):
+        """Cotangent of the current state (None = zero)."""
+        _check(self.lib.fipi_adjoint_seed(self.h, _d(_f64(dc, self.V)), _d(_f64(du, 3 * self.V)),
+                                          _d(_f64(dp, 3 * self.n)), _d(_f64(df_pp, 3 * self.n))))
+
+    def adjoint_step(self, slot: int):
+        _check(self.lib.fipi_adjoint_step(self.h, slot))
+
+    def adjoint_get(self):
+        """(dc, du, dp, df_pp) of the state the cotangent refers to."""
+        dc, du = np.empty(self.V), np.empty(3 * self.V)
+        dp, df = np.empty(3 * self.n), np.empty(3 * self.n)
+        _check(self.lib.fipi_adjoint_get(self.h, _d(dc), _d(du), _d(dp) if self.n else None,
+                                         _d(df) if self.n else None))
+        return dc, du, dp, df
+
+    def adjoint_get_history(self):
+        """Real-field cotangents of the SBDF2 histories (c_old, f_old, conv_old)."""
+        a, b, c = np.empty(self.V), np.empty(self.V), np.empty(self.V)
+        _check(self.lib.fipi_adjoint_get_history(self.h, _d(a), _d(b), _d(c)))
+        return a, b, c
+
+    def trajectory_forward(self, nsteps: int, stride: int = 0):
+        _check(self.lib.fipi_trajectory_forward(self.h, nsteps, stride))
+
+    def trajectory_backward(self, dc=None, du=None, dp=None, df_pp=None):
+        _check(self.lib.fipi_trajectory_backward(self.h, _d(_f64(dc, self.V)), _d(_f64(du, 3 * self.V)),
+                                                 _d(_f64(dp, 3 * self.n)), _d(_f64(df_pp, 3 * self.n))))
 
     # ---------------------------------------------------------------- fine-grained
     def fft_r2c(self, x) -> np.ndarray:

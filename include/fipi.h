@@ -238,6 +238,64 @@ fipi_status fipi_spread(fipi_ctx* ctx, const double* p, const double* f_pp, doub
 fipi_status fipi_cells_build_noalloc(const fipi_params* p, const double* d_pos, int* d_keys,
                                      int* d_sorted, int* d_offsets, void* stream);
 
+/* ------------------------------------------------------------ checkpoints
+ * No counterpart in the reference (it has no checkpoint or restart).  A
+ * checkpoint is a device-resident copy of everything one step reads from
+ * the previous one: c, grad c, the spectra c_hat, f_hat and the SBDF2
+ * histories c_hat_old, f_hat_old, C_hat_old, u_hat, particle positions,
+ * radii, cos(theta) and f_pp (spread at the next step, cluster.cpp:452),
+ * the step index t (the contact ramp depends on it) and, in the mixed form,
+ * the FP64 k = 0 record.  Slots live in HBM so the sqrt(N) schedule of the
+ * adjoint costs device copies only.  Resuming from a slot is bit-exact. */
+/* Allocates `slots` checkpoint slots (frees the previous ones). */
+fipi_status fipi_checkpoint_reserve(fipi_ctx* ctx, int slots);
+/* Bytes of one slot's payload; the exported blob is this plus a 64-byte header. */
+fipi_status fipi_checkpoint_bytes(const fipi_ctx* ctx, size_t* bytes);
+fipi_status fipi_checkpoint_save(fipi_ctx* ctx, int slot);
+fipi_status fipi_checkpoint_load(fipi_ctx* ctx, int slot);
+/* Host copies of a slot: a header (magic "FIPICKP1", precision, grid, n_p,
+ * t, payload size) followed by the payload.  Import checks the header
+ * against the context. */
+fipi_status fipi_checkpoint_export(fipi_ctx* ctx, int slot, void* blob, size_t blob_bytes);
+fipi_status fipi_checkpoint_import(fipi_ctx* ctx, int slot, const void* blob, size_t blob_bytes);
+
+/* ---------------------------------------------------------------- adjoint
+ * No counterpart in the reference.  Reverse-mode derivative of the FP64
+ * step (FIPI_FP64 contexts; FIPI_ERR_UNSUPPORTED otherwise).  The
+ * cotangent lives in the context and refers to one state: its c (as a real
+ * field; c_hat, f_hat and grad c of that state are functions of c), the
+ * real-field equivalents of the three SBDF2 histories, u, the positions and
+ * f_pp.  Branches of the step (floor of the interpolation cell, the
+ * |phi| <= tanh 2 and |d| < r tests of element.cpp:175-182, the pair test
+ * |d| < r_eq of cluster.cpp:327) are held fixed: the derivative is the one
+ * of the branch the forward step took. */
+/* Sets the cotangent of the context's current state (any pointer NULL =
+ * zero): dc V reals, du 3 x V, dp and df_pp n_p x 3. */
+fipi_status fipi_adjoint_seed(fipi_ctx* ctx, const double* dc, const double* du, const double* dp,
+                              const double* df_pp);
+/* Reverses one step.  `slot` holds the state at the start of the step
+ * whose end state the cotangent refers to (its t must be one less); the
+ * step is recomputed from it with its intermediates kept, then the
+ * cotangent is carried back to that state.  The context's state is left
+ * at the end of the recomputed step. */
+fipi_status fipi_adjoint_step(fipi_ctx* ctx, int slot);
+/* The cotangent (any pointer may be NULL): dc V, du 3 x V, dp, df_pp n_p x 3. */
+fipi_status fipi_adjoint_get(fipi_ctx* ctx, double* dc, double* du, double* dp, double* df_pp);
+/* Cotangents of the SBDF2 histories as real fields (V each, NULL = skip). */
+fipi_status fipi_adjoint_get_history(fipi_ctx* ctx, double* dc_old, double* df_old, double* dconv_old);
+/* Whole-trajectory gradient with sqrt(N) checkpointing.
+ * fipi_trajectory_forward advances nsteps from the current state, saving a
+ * checkpoint every `stride` steps (stride <= 0: ceil(sqrt(nsteps))) into
+ * slots it reserves (ceil(nsteps/stride) + stride of them).
+ * fipi_trajectory_backward seeds the cotangent of the final state and
+ * reverses every step: each segment is recomputed once from its
+ * checkpoint, its states kept in slots, then reversed step by step.  The
+ * gradient with respect to the trajectory's first state is then read with
+ * fipi_adjoint_get. */
+fipi_status fipi_trajectory_forward(fipi_ctx* ctx, int nsteps, int stride);
+fipi_status fipi_trajectory_backward(fipi_ctx* ctx, const double* dc, const double* du, const double* dp,
+                                     const double* df_pp);
+
 /* ------------------------------------------------ seeded synthetic inputs
  * Host-only helpers (no device needed).  The reference draws its initial
  * state from unseeded rand() (field.cpp:96, cluster.cpp:153-183); these draw
