@@ -201,11 +201,15 @@ def set_timing(sim, on):
 def committed_traffic(kernel, workload):
     """DRAM bytes per launch from the committed ncu summary, if it covers this kernel."""
     try:
-        d = json.loads((REPO / "profiles" / "dram_traffic.json").read_text())
-        e = d.get(workload, {}).get(kernel)
-        return None if e is None else float(e)
-    except Exception:
-        return None
+        for line in (REPO / "profiles" / "dram_traffic.txt").read_text().splitlines():
+            if line.startswith("#") or not line.strip():
+                continue
+            w, k, v = line.split("\t")
+            if w == workload and k == kernel:
+                return float(v)
+    except (OSError, ValueError):
+        pass
+    return None
 
 
 def cpu_baseline(w, seed, steps=1):
