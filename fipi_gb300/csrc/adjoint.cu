@@ -397,6 +397,7 @@ fipi_status ck_load(fipi_ctx* ctx, int slot) {
         FIPI_CUDA(ctx, cudaMemcpyAsync(c.ctxbuf, c.slot, c.bytes, cudaMemcpyDeviceToDevice, ctx->stream));
     ctx->t = ctx->ck.t[slot];
     set_tick(ctx, ctx->t);
+    fields_refresh_upre(ctx);
     ctx->pb.tau_valid = false;
     ctx->have_phase = true;
     return FIPI_OK;

@@ -32,6 +32,7 @@ struct FieldBufs {
     void* fhat_old = nullptr;
     void* Chat_old = nullptr;
     void* uhat[3] = {};
+    void* upre[3] = {};  // Z inverse of u_hat (the first pass of u = C2R(u_hat)), kept by the step
     void* S[4] = {};  // scratch
 };
 
@@ -62,6 +63,7 @@ struct ParticleBufs {
     unsigned* sp_vals = nullptr;      // 8n record id = particle*8 + corner
     unsigned* sp_vals_alt = nullptr;  // 8n
     unsigned* sp_prev = nullptr;      // 8n nodes written by the previous spread
+    unsigned long long* sp_acc = nullptr;  // mixed form: 3 x V fixed-point spread accumulators
     int sp_prev_valid = 0;
     // radix sort scratch
     unsigned* hist = nullptr;  // 256 * max_blocks
@@ -209,6 +211,7 @@ fipi_status fields_get_velocity(fipi_ctx* ctx, double* u_host);
 // The three grid sub-steps of one iteration (enqueue only).
 void fields_step_ch(fipi_ctx* ctx, int t);        // conv, CH update, c, f
 void fields_step_stokes(fipi_ctx* ctx);           // mu, grad c, force, projection
+void fields_refresh_upre(fipi_ctx* ctx);          // after u_hat changed outside the step
 fipi_status fields_mass(fipi_ctx* ctx, double* out);
 fipi_status fields_free_energy(fipi_ctx* ctx, double* out);
 // Fine-grained transforms on host arrays.

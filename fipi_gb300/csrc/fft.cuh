@@ -181,7 +181,8 @@ template <typename T> inline size_t ypass_tma_smem(const Geom& g) {
 
 // ----------------------------------------------------------------- Z pass
 // One block = kx = blockIdx.x, ky in [blockIdx.y*TZ, +TZ), all kz, NF fields
-// (TZ = zpass_cols: 128-byte runs of ky).
+// (TZ = zpass_cols: 128-byte runs of ky).  kx fastest in the grid measured
+// faster than ky-tile fastest on GB300.
 // Threads: column c = tid % TZ (fastest, so global runs and shared-memory
 // accesses are contiguous), t = tid / TZ; blockDim = TZ * nz/min(16, nz).
 // Op provides
@@ -256,6 +257,80 @@ __global__ void __launch_bounds__(kThreads) k_zpass(Geom g, const cplx<T>* __res
 #pragma unroll
         for (int f = 0; f < NF; ++f) v[f] = s[f * fstride + idx(c, z)];
         op.store(kx, ky, z, base + z * zstride, v);
+    }
+}
+
+// Z pass with a round trip: the NF loaded fields are transformed along z
+// in direction DIR; op.mid() maps each mode's NF values to NB values
+// (writing whatever state it owns) that are transformed back in the other
+// direction and handed to op.store2().  It replaces a forward Z pass and the
+// inverse Z pass that read its output again (one write and one read of
+// every intermediate spectrum less).  COLS ky columns per block (a run of
+// COLS complex values per kz).
+template <typename T, int N, int COLS> struct ZRtShape {
+    static constexpr int E = N < FftE<T>::value ? N : FftE<T>::value;
+    static constexpr int Tn = N / E;
+    static constexpr int TZ = COLS * Tn <= kThreads ? COLS : kThreads / Tn;
+};
+
+template <typename T, int NF, int NB, int DIR, int N, int COLS, class Op>
+__global__ void __launch_bounds__(kThreads) k_zpass_rt(Geom g, const cplx<T>* __restrict__ twz, Op op) {
+    using C = cplx<T>;
+    using SH = ZRtShape<T, N, COLS>;
+    constexpr int E = SH::E, Tn = SH::Tn, TZ = SH::TZ;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C* s = reinterpret_cast<C*>(smem_raw);
+    const int kx = blockIdx.x, ky0 = blockIdx.y * TZ;
+    const int c = threadIdx.x % TZ, t = threadIdx.x / TZ;
+    const int ky = ky0 + c;
+    const size_t zstride = (size_t)g.h * g.ny;
+    const size_t base = (size_t)kx * g.ny + ky;
+    const IdxColumns idx{TZ};
+    constexpr size_t fstride = (size_t)N * TZ;
+    {
+        constexpr int CH = 8 / NF >= 2 ? 8 / NF : 2;
+#pragma unroll
+        for (int i0 = 0; i0 < E; i0 += CH) {
+            C v[CH][NF];
+#pragma unroll
+            for (int u = 0; u < CH; ++u)
+                if (i0 + u < E) {
+                    const int z = t + Tn * (i0 + u);
+                    op.load(kx, ky, z, base + z * zstride, v[u]);
+                }
+#pragma unroll
+            for (int u = 0; u < CH; ++u)
+                if (i0 + u < E) {
+                    const int z = t + Tn * (i0 + u);
+#pragma unroll
+                    for (int f = 0; f < NF; ++f) s[f * fstride + idx(c, z)] = v[u][f];
+                }
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int f = 0; f < NF; ++f) smem_fft2<T, DIR, N>(s + f * fstride, idx, c, t, true, twz, 1);
+    // each thread's outputs of the last stage are the modes z = t + Tn i
+#pragma unroll 2
+    for (int i = 0; i < E; ++i) {
+        const int z = t + Tn * i;
+        C vi[NF], vo[NB];
+#pragma unroll
+        for (int f = 0; f < NF; ++f) vi[f] = s[f * fstride + idx(c, z)];
+        op.mid(kx, ky, z, base + z * zstride, vi, vo);
+#pragma unroll
+        for (int b = 0; b < NB; ++b) s[b * fstride + idx(c, z)] = vo[b];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int b = 0; b < NB; ++b) smem_fft2<T, -DIR, N>(s + b * fstride, idx, c, t, true, twz, 1);
+#pragma unroll 4
+    for (int i = 0; i < E; ++i) {
+        const int z = t + Tn * i;
+        C v[NB];
+#pragma unroll
+        for (int b = 0; b < NB; ++b) v[b] = s[b * fstride + idx(c, z)];
+        op.store2(kx, ky, z, base + z * zstride, v);
     }
 }
 

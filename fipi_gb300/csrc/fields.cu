@@ -162,8 +162,9 @@ template <typename T, bool MIXED> struct ZOpCH {
     StepConsts<T> k;
     int first;  // t == 0
     __device__ void load(int, int, int, size_t gi, C* v) const { v[0] = conv[gi]; }
-    __device__ void store(int ix, int iy, int iz, size_t gi, const C* v) const {
-        const C Cn = v[0];
+    __device__ void store(int ix, int iy, int iz, size_t gi, const C* v) const { update(ix, iy, iz, gi, v[0]); }
+    // Writes c_hat^{n+1} and C^n at gi and returns c_hat^{n+1}.
+    __device__ C update(int ix, int iy, int iz, size_t gi, const C Cn) const {
         const C c = chat[gi];
         const C f = fhat[gi];
         const T k2 = kt.k2(ix, iy, iz);
@@ -196,6 +197,77 @@ template <typename T, bool MIXED> struct ZOpCH {
         if (MIXED && gi == 0) out = mkc<C>(T(0), T(0));  // k = 0 lives in FP64 scalars
         chat_old[gi] = out;
         Chat_old[gi] = Cn;
+        return out;
+    }
+};
+
+// Round trip A -> B (k_zpass_rt, NF = NB = 1): the CH update of ZOpCH in
+// the forward Z pass, then the inverse Z transform of c_hat^{n+1} (the
+// first pass of c^{n+1} = C2R(c_hat^{n+1})) into `out`.
+template <typename T, bool MIXED> struct ZOpCHRt {
+    using C = cplx<T>;
+    ZOpCH<T, MIXED> ch;
+    C* out;
+    __device__ void load(int, int, int, size_t gi, C* v) const { v[0] = ch.conv[gi]; }
+    __device__ void mid(int ix, int iy, int iz, size_t gi, const C* vi, C* vo) const {
+        vo[0] = ch.update(ix, iy, iz, gi, vi[0]);
+    }
+    __device__ void store2(int, int, int, size_t gi, const C* v) const { out[gi] = v[0]; }
+};
+
+// Round trip B -> C (NF = 1, NB = 4): the forward Z transform of f gives
+// f_hat^{n+1} (stored); mu_hat = lambda k^2 c_hat + f_hat (main.cpp:254) and
+// i k_d c_hat with the Nyquist index of d zeroed (field.cpp:288-328) are
+// transformed back along z into out[0..3] (the inverses of mu and grad c).
+template <typename T> struct ZOpFRt {
+    using C = cplx<T>;
+    const C* fin;
+    C* fhat_out;
+    const C* chat;
+    C* out[4];
+    KTabs<T> kt;
+    T lam;
+    int m, ny2, nz2;
+    __device__ void load(int, int, int, size_t gi, C* v) const { v[0] = fin[gi]; }
+    __device__ void mid(int ix, int iy, int iz, size_t gi, const C* vi, C* vo) const {
+        const C f = vi[0];
+        fhat_out[gi] = f;
+        const C c = chat[gi];
+        const T a = kt.k2(ix, iy, iz) * lam;
+        vo[0] = mkc<C>(a * c.x + f.x, a * c.y + f.y);
+        const T kx = kt.kx[ix], ky = kt.ky[iy], kz = kt.kz[iz];
+        vo[1] = (ix == m) ? mkc<C>(T(0), T(0)) : mkc<C>(-kx * c.y, kx * c.x);
+        vo[2] = (iy == ny2) ? mkc<C>(T(0), T(0)) : mkc<C>(-ky * c.y, ky * c.x);
+        vo[3] = (iz == nz2) ? mkc<C>(T(0), T(0)) : mkc<C>(-kz * c.y, kz * c.x);
+    }
+    __device__ void store2(int, int, int, size_t gi, const C* v) const {
+#pragma unroll
+        for (int b = 0; b < 4; ++b) out[b][gi] = v[b];
+    }
+};
+
+// Round trip C -> next A (NF = NB = 3): the Leray projection of ZOpProj in
+// the forward Z pass (u_hat stored), then the inverse Z transform of u_hat
+// into upre, which the next step's conv pass starts from.
+template <typename T> struct ZOpProjRt {
+    using C = cplx<T>;
+    ZOpProj<T> pj;
+    C* upre[3];
+    __device__ void load(int, int, int, size_t gi, C* v) const {
+        v[0] = pj.in[0][gi];
+        v[1] = pj.in[1][gi];
+        v[2] = pj.in[2][gi];
+    }
+    __device__ void mid(int ix, int iy, int iz, size_t gi, const C* vi, C* vo) const {
+        pj.compute(ix, iy, iz, vi, vo);
+        pj.out[0][gi] = vo[0];
+        pj.out[1][gi] = vo[1];
+        pj.out[2][gi] = vo[2];
+    }
+    __device__ void store2(int, int, int, size_t gi, const C* v) const {
+        upre[0][gi] = v[0];
+        upre[1][gi] = v[1];
+        upre[2][gi] = v[2];
     }
 };
 
@@ -327,6 +399,8 @@ template <typename T> static fipi_status alloc_fields_t(fipi_ctx* ctx) {
         FIPI_CUDA(ctx, cudaMemsetAsync(b.fsp[d], 0, sizeof(T) * V, ctx->stream));
         FIPI_CUDA(ctx, A(&b.uhat[d], sizeof(C) * SH));
         FIPI_CUDA(ctx, cudaMemsetAsync(b.uhat[d], 0, sizeof(C) * SH, ctx->stream));
+        FIPI_CUDA(ctx, A(&b.upre[d], sizeof(C) * SH));
+        FIPI_CUDA(ctx, cudaMemsetAsync(b.upre[d], 0, sizeof(C) * SH, ctx->stream));
     }
     FIPI_CUDA(ctx, A(&b.ureal, sizeof(T) * V * 3));
     void** specs[] = {&b.chat, &b.chat_old, &b.fhat, &b.fhat_old, &b.Chat_old, &b.S[0], &b.S[1], &b.S[2], &b.S[3]};
@@ -391,7 +465,8 @@ void fields_free(fipi_ctx* ctx) {
     FieldBufs& b = ctx->fb;
     void* all[] = {b.twx, b.twy, b.twz, b.kx, b.ky, b.kz, b.c, b.ureal, b.chat, b.chat_old, b.fhat,
                    b.fhat_old, b.Chat_old, b.S[0], b.S[1], b.S[2], b.S[3], b.g[0], b.g[1], b.g[2],
-                   b.fsp[0], b.fsp[1], b.fsp[2], b.uhat[0], b.uhat[1], b.uhat[2], ctx->partials, ctx->k0};
+                   b.fsp[0], b.fsp[1], b.fsp[2], b.uhat[0], b.uhat[1], b.uhat[2], b.upre[0], b.upre[1],
+                   b.upre[2], ctx->partials, ctx->k0};
     for (void* p : all)
         if (p) cudaFree(p);
     b = FieldBufs{};
@@ -435,6 +510,14 @@ fipi_status fields_set_phase(fipi_ctx* ctx, const double* c_host) {
     return ctx->prec == FIPI_MIXED ? set_phase_t<float>(ctx, c_host) : set_phase_t<double>(ctx, c_host);
 }
 
+// upre = Z inverse of u_hat (after u_hat changed outside the step).
+template <typename T> static void refresh_upre_t(fipi_ctx* ctx) {
+    FieldBufs& b = ctx->fb;
+    ZOpStore<T, 3> zs{{F<T>::sp(b.uhat[0]), F<T>::sp(b.uhat[1]), F<T>::sp(b.uhat[2])},
+                      {F<T>::sp(b.upre[0]), F<T>::sp(b.upre[1]), F<T>::sp(b.upre[2])}, 0};
+    launch_z<T, 3, +1>(ctx, "Z inverse copy", 6, zs);
+}
+
 // u_hat = R2C(u): the step only needs the spectrum of the velocity.
 template <typename T> static fipi_status set_velocity_t(fipi_ctx* ctx, const double* u_host) {
     const Geom& g = ctx->g;
@@ -449,6 +532,7 @@ template <typename T> static fipi_status set_velocity_t(fipi_ctx* ctx, const dou
         ZOpStore<T, 1> zs{{F<T>::S(ctx, 0)}, {F<T>::sp(ctx->fb.uhat[d])}, 0};
         launch_z<T, 1, -1>(ctx, "Z forward store", 2, zs);
     }
+    refresh_upre_t<T>(ctx);
     FIPI_CUDA(ctx, cudaGetLastError());
     return FIPI_OK;
 }
@@ -482,16 +566,17 @@ fipi_status fields_get_velocity(fipi_ctx* ctx, double* u_host) {
 
 // ------------------------------------------------------------ the step
 template <typename T, bool MIXED> static void step_ch_t(fipi_ctx* ctx, int t) {
-    using C = cplx<T>;
     const Geom& g = ctx->g;
     FieldBufs& b = ctx->fb;
     const StepConsts<T> k = make_consts<T>(ctx);
-    // A: u_hat -> u (Z, Y inverse; X inverse fused with conv and its R2C)
-    ZOpStore<T, 3> zu{{F<T>::sp(b.uhat[0]), F<T>::sp(b.uhat[1]), F<T>::sp(b.uhat[2])},
-                      {F<T>::S(ctx, 0), F<T>::S(ctx, 1), F<T>::S(ctx, 2)}, 0};
-    launch_z<T, 3, +1>(ctx, "Z inverse copy", 6, zu);
+    const KTabs<T> kt = F<T>::ktabs(ctx);
+    constexpr int TZ = Tiles<T>::TZ;
+    // A: u^n (its Z inverse kept in upre by the previous step) -> Y inverse;
+    //    X inverse with conv = u . grad c and the R2C of conv; Y forward;
+    //    Z forward + CH update + Z inverse of c_hat^{n+1}
+    void* up[3] = {b.upre[0], b.upre[1], b.upre[2]};
     void* s3[3] = {b.S[0], b.S[1], b.S[2]};
-    launch_y<T>(ctx, 3, s3, s3, +1);
+    launch_y<T>(ctx, 3, up, s3, +1);
     OpConv<T, MIXED> oc{{F<T>::S(ctx, 0), F<T>::S(ctx, 1), F<T>::S(ctx, 2)},
                         {(const T*)b.g[0], (const T*)b.g[1], (const T*)b.g[2]}, F<T>::S(ctx, 3), ctx->partials,
                         {(T*)ctx->tape_u[0], (T*)ctx->tape_u[1], (T*)ctx->tape_u[2]}, g.nx, g.ny};
@@ -505,12 +590,13 @@ template <typename T, bool MIXED> static void step_ch_t(fipi_ctx* ctx, int t) {
                                                  1.0 / (double)g.V);
     }
     ZOpCH<T, MIXED> zc{F<T>::S(ctx, 3), F<T>::sp(b.chat), F<T>::sp(b.chat_old), F<T>::sp(b.fhat),
-                       F<T>::sp(b.fhat_old), F<T>::sp(b.Chat_old), F<T>::ktabs(ctx), k, t == 0 ? 1 : 0};
-    launch_z<T, 1, -1>(ctx, t == 0 ? "Z forward + IMEX update" : "Z forward + SBDF2 update", t == 0 ? 5 : 8, zc);
+                       F<T>::sp(b.fhat_old), F<T>::sp(b.Chat_old), kt, k, t == 0 ? 1 : 0};
+    ZOpCHRt<T, MIXED> zcr{zc, F<T>::S(ctx, 0)};
+    launch_zrt<T, 1, 1, -1, TZ>(ctx, t == 0 ? "Z forward + IMEX update + inverse" : "Z forward + SBDF2 update + inverse",
+                                t == 0 ? 6 : 9, zcr);
     std::swap(b.chat, b.chat_old);  // chat = c^{n+1}, chat_old = c^n
-    // B: c^{n+1} = C2R(c_hat), f fused, f_hat = R2C(f)
-    ZOpStore<T, 1> zc2{{F<T>::sp(b.chat)}, {F<T>::S(ctx, 0)}, 0};
-    launch_z<T, 1, +1>(ctx, "Z inverse copy", 2, zc2);
+    // B: Y inverse; X inverse c^{n+1} (stored) with f = (lambda/eps^2)(c^3 - c) and its
+    //    R2C; Y forward; Z forward f (f_hat^{n+1} stored) + Z inverse of mu_hat, i k c_hat
     void* s0[1] = {b.S[0]};
     launch_y<T>(ctx, 1, s0, s0, +1);
     OpCF<T, MIXED> ocf{F<T>::S(ctx, 0), (T*)b.c, F<T>::S(ctx, 1), reinterpret_cast<const float*>(ctx->k0 + 4),
@@ -518,10 +604,11 @@ template <typename T, bool MIXED> static void step_ch_t(fipi_ctx* ctx, int t) {
     launch_x<T, 1, 1, false>(ctx, "X inverse c, f, forward", 1, ocf);
     void* s1b[1] = {b.S[1]};
     launch_y<T>(ctx, 1, s1b, s1b, -1);
-    ZOpStore<T, 1> zf{{F<T>::S(ctx, 1)}, {F<T>::sp(b.fhat_old)}, 0};
-    launch_z<T, 1, -1>(ctx, "Z forward store", 2, zf);
+    ZOpFRt<T> zf{F<T>::S(ctx, 1), F<T>::sp(b.fhat_old), F<T>::sp(b.chat),
+                 {F<T>::S(ctx, 0), F<T>::S(ctx, 1), F<T>::S(ctx, 2), F<T>::S(ctx, 3)}, kt, k.lam, g.m, g.ny / 2,
+                 g.nz / 2};
+    launch_zrt<T, 1, 4, -1, TZ / 2>(ctx, "Z forward f + inverse mu, grad", 7, zf);
     std::swap(b.fhat, b.fhat_old);  // fhat = f^{n+1}, fhat_old = f^n
-    (void)sizeof(C);
 }
 
 void fields_step_ch(fipi_ctx* ctx, int t) {
@@ -529,15 +616,14 @@ void fields_step_ch(fipi_ctx* ctx, int t) {
     else step_ch_t<double, false>(ctx, t);
 }
 
+// C: Y inverse of mu, grad c; X inverse with grad c stored and
+//    F = mu grad c + spread + buoyancy, R2C of F; Y forward; Z forward +
+//    projection (u_hat stored) + Z inverse of u_hat for the next step.
 template <typename T> static void step_stokes_t(fipi_ctx* ctx) {
     const Geom& g = ctx->g;
     FieldBufs& b = ctx->fb;
     const StepConsts<T> k = make_consts<T>(ctx);
     const KTabs<T> kt = F<T>::ktabs(ctx);
-    ZOpMu<T> zm{F<T>::sp(b.chat), F<T>::sp(b.fhat), F<T>::S(ctx, 0), kt, k.lam};
-    launch_z<T, 1, +1>(ctx, "Z inverse mu", 3, zm);
-    ZOpGrad<T> zg{F<T>::sp(b.chat), {F<T>::S(ctx, 1), F<T>::S(ctx, 2), F<T>::S(ctx, 3)}, kt, g.m, g.ny / 2, g.nz / 2};
-    launch_z<T, 3, +1>(ctx, "Z inverse grad", 4, zg);
     void* s4[4] = {b.S[0], b.S[1], b.S[2], b.S[3]};
     launch_y<T>(ctx, 4, s4, s4, +1);
     OpForce<T> of{{F<T>::S(ctx, 0), F<T>::S(ctx, 1), F<T>::S(ctx, 2), F<T>::S(ctx, 3)},
@@ -551,7 +637,13 @@ template <typename T> static void step_stokes_t(fipi_ctx* ctx) {
     launch_y<T>(ctx, 3, s3, s3, -1);
     ZOpProj<T> zp{{F<T>::S(ctx, 0), F<T>::S(ctx, 1), F<T>::S(ctx, 2)},
                   {F<T>::sp(b.uhat[0]), F<T>::sp(b.uhat[1]), F<T>::sp(b.uhat[2])}, kt, k.mu, g.m, g.ny / 2, g.nz / 2};
-    launch_z<T, 3, -1>(ctx, "Z forward + projection", 6, zp);
+    ZOpProjRt<T> zpr{zp, {F<T>::sp(b.upre[0]), F<T>::sp(b.upre[1]), F<T>::sp(b.upre[2])}};
+    launch_zrt<T, 3, 3, -1, Tiles<T>::TZ>(ctx, "Z forward + projection + inverse", 9, zpr);
+}
+
+void fields_refresh_upre(fipi_ctx* ctx) {
+    if (ctx->prec == FIPI_MIXED) refresh_upre_t<float>(ctx);
+    else refresh_upre_t<double>(ctx);
 }
 
 void fields_step_stokes(fipi_ctx* ctx) {

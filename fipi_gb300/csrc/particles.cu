@@ -193,10 +193,9 @@ __device__ __forceinline__ int cell_coord(double x, double dcell, double margin)
     return (int)floor(x / dcell + margin / dcell);  // cluster.cpp:234-236
 }
 
-__global__ void k_cell_keys(PC pc, const double* __restrict__ p, unsigned* keys, unsigned* ids, int* status) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= pc.n) return;
-    const double x = p[i], y = p[pc.n + i], z = p[2 * pc.n + i];
+// Cell key of one position (cluster.cpp:234-257); out-of-range or
+// non-finite positions are clamped and reported through the error word.
+__device__ __forceinline__ unsigned cell_key(const PC& pc, double x, double y, double z, int* status) {
     int c[3] = {cell_coord(x, pc.dc[0], pc.margin), cell_coord(y, pc.dc[1], pc.margin),
                 cell_coord(z, pc.dc[2], pc.margin)};
     bool bad = !(isfinite(x) && isfinite(y) && isfinite(z));
@@ -207,7 +206,13 @@ __global__ void k_cell_keys(PC pc, const double* __restrict__ p, unsigned* keys,
         }
     }
     if (bad) atomicOr(status, isfinite(x) && isfinite(y) && isfinite(z) ? ERR_OUT_OF_RANGE : ERR_NONFINITE);
-    keys[i] = (unsigned)(c[0] + c[1] * pc.nc[0] + c[2] * pc.nc[0] * pc.nc[1]);
+    return (unsigned)(c[0] + c[1] * pc.nc[0] + c[2] * pc.nc[0] * pc.nc[1]);
+}
+
+__global__ void k_cell_keys(PC pc, const double* __restrict__ p, unsigned* keys, unsigned* ids, int* status) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= pc.n) return;
+    keys[i] = cell_key(pc, p[i], p[pc.n + i], p[2 * pc.n + i], status);
     ids[i] = (unsigned)i;
 }
 
@@ -224,12 +229,122 @@ __global__ void k_cell_offsets(const unsigned* __restrict__ keys, int n, int* of
     off[c] = lo;
 }
 
+// The whole cell list in one block of 1024 threads (keys, stable LSD radix
+// sort of (key, id) in 8-bit digits, offsets): one launch instead of eight
+// for the particle counts of one GPU's workloads.  Stability as in
+// k_rs_scatter: ranks within a warp by __match_any_sync, warps in order
+// through per-warp digit counts, chunks in order through the running
+// digit cursors.  Output identical to the multi-block path.
+constexpr int kCB_T = 1024;
+constexpr int kCellsOneBlockMax = 65536;
+
+__global__ void __launch_bounds__(kCB_T) k_cells_one_block(PC pc, const double* __restrict__ p, unsigned* k0,
+                                                           unsigned* v0, unsigned* k1, unsigned* v1, int* off,
+                                                           int ncells, int bits, int* status) {
+    __shared__ unsigned cur[256];
+    __shared__ unsigned wcnt[kCB_T / 32][256];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int n = pc.n;
+    for (int i = tid; i < n; i += kCB_T) {
+        k0[i] = cell_key(pc, p[i], p[n + i], p[2 * n + i], status);
+        v0[i] = (unsigned)i;
+    }
+    __syncthreads();
+    unsigned *kin = k0, *vin = v0, *kout = k1, *vout = v1;
+    const unsigned lt = (1u << lane) - 1u;
+    for (int shift = 0; shift < bits; shift += 8) {
+        if (tid < 256) cur[tid] = 0;
+        __syncthreads();
+        for (int i = tid; i < n; i += kCB_T) atomicAdd(&cur[(kin[i] >> shift) & 255u], 1u);
+        __syncthreads();
+        if (warp == 0) {  // exclusive scan of the 256 digit counts, 8 per lane
+            unsigned v[8], sum = 0;
+            for (int j = 0; j < 8; ++j) {
+                v[j] = cur[lane * 8 + j];
+                sum += v[j];
+            }
+            unsigned incl = sum;
+            for (int o = 1; o < 32; o <<= 1) {
+                const unsigned t = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += t;
+            }
+            unsigned run = incl - sum;
+            for (int j = 0; j < 8; ++j) {
+                cur[lane * 8 + j] = run;
+                run += v[j];
+            }
+        }
+        __syncthreads();
+        for (int c0 = 0; c0 < n; c0 += kCB_T) {
+            const int s = c0 + tid;
+            const bool valid = s < n;
+            unsigned key = 0, val = 0, d = 256;
+            if (valid) {
+                key = kin[s];
+                val = vin[s];
+                d = (key >> shift) & 255u;
+            }
+            for (int j = tid; j < (kCB_T / 32) * 256; j += kCB_T) (&wcnt[0][0])[j] = 0;
+            __syncthreads();
+            const unsigned peers = __match_any_sync(0xffffffffu, d);
+            const unsigned rank = __popc(peers & lt);
+            if (valid && rank == 0) wcnt[warp][d] = __popc(peers);
+            __syncthreads();
+            if (tid < 256) {
+                unsigned run = cur[tid];
+                for (int w = 0; w < kCB_T / 32; ++w) {
+                    const unsigned c = wcnt[w][tid];
+                    wcnt[w][tid] = run;
+                    run += c;
+                }
+                cur[tid] = run;
+            }
+            __syncthreads();
+            if (valid) {
+                const unsigned pos = wcnt[warp][d] + rank;
+                kout[pos] = key;
+                vout[pos] = val;
+            }
+            __syncthreads();
+        }
+        unsigned* t = kin;
+        kin = kout;
+        kout = t;
+        t = vin;
+        vin = vout;
+        vout = t;
+    }
+    // offsets: first sorted position whose key >= c
+    for (int c = tid; c <= ncells; c += kCB_T) {
+        int lo = 0, hi = n;
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if ((int)kin[mid] < c) lo = mid + 1;
+            else hi = mid;
+        }
+        off[c] = lo;
+    }
+}
+
 static void build_cells(fipi_ctx* ctx, const double* p_dev) {
     ParticleBufs& b = ctx->pb;
     const PC pc = make_pc(ctx);
     const int n = b.n;
+    const int bits = bits_for(b.ncells - 1);
+    if (n <= kCellsOneBlockMax) {
+        {
+            LaunchScope ls_(ctx, "cell list (one block)", 0.0);
+            k_cells_one_block<<<1, kCB_T, 0, ctx->stream>>>(pc, p_dev, b.keys, b.ids, b.keys_alt, b.ids_alt,
+                                                             b.cell_off, b.ncells, bits, ctx->status);
+        }
+        if (((bits + 7) / 8) & 1) {  // an odd number of digit passes leaves the result in the alternates
+            std::swap(b.keys, b.keys_alt);
+            std::swap(b.ids, b.ids_alt);
+        }
+        return;
+    }
     { LaunchScope ls_(ctx, "cell keys", 0.0); k_cell_keys<<<(n + 255) / 256, 256, 0, ctx->stream>>>(pc, p_dev, b.keys, b.ids, ctx->status); }
-    radix_sort(ctx, b.keys, b.ids, b.keys_alt, b.ids_alt, n, bits_for(b.ncells - 1));
+    radix_sort(ctx, b.keys, b.ids, b.keys_alt, b.ids_alt, n, bits);
     { LaunchScope ls_(ctx, "cell offsets", 0.0); k_cell_offsets<<<(b.ncells + 1 + 255) / 256, 256, 0, ctx->stream>>>(b.keys, n, b.cell_off, b.ncells); }
 }
 
@@ -756,11 +871,86 @@ static void spread_t(fipi_ctx* ctx, const double* p, const double* f_pp, T* cons
     }
 }
 
+// Mixed-form spreading of the step: the 8 FP32 corner contributions of each
+// particle (the weight products of cluster.cpp:463-500) are added as 64-bit
+// fixed-point integers (units of 2^-32) with atomics.  Integer addition is
+// associative, so the sums do not depend on the order of the atomics (the
+// result is deterministic) and no sort is needed; the touched nodes are
+// then converted to FP32.  The FP64 form keeps the sorted reduction in
+// ascending particle id, bit-identical to the reference.
+constexpr double kFxScale = 4294967296.0;  // 2^32
+
+__global__ void k_spread_fx_clear(const unsigned* __restrict__ nodes, int m, size_t V, unsigned long long* acc,
+                                  float* f0, float* f1, float* f2) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= m) return;
+    const unsigned nd = nodes[s];
+    acc[nd] = 0ull;
+    acc[V + nd] = 0ull;
+    acc[2 * V + nd] = 0ull;
+    f0[nd] = 0.f;
+    f1[nd] = 0.f;
+    f2[nd] = 0.f;
+}
+
+__global__ void k_spread_fx(PC pc, const double* __restrict__ p, const double* __restrict__ f_pp, size_t V,
+                            unsigned long long* acc, unsigned* nodes) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = pc.n;
+    if (i >= n) return;
+    int ix[3];
+    double fr[3];
+    cell_and_frac(pc, p[i], p[n + i], p[2 * n + i], ix, fr);
+    float f[3];
+    for (int a = 0; a < 3; ++a) f[a] = (float)((f_pp[a * n + i] + 0.0) / pc.dx / pc.dy / pc.dz);
+    const float o = (float)fr[0], pp = (float)fr[1], q = (float)fr[2];
+    for (int c = 0; c < 8; ++c) {
+        const int x = (ix[0] + c_corner[c][0]) % pc.N[0];
+        const int y = (ix[1] + c_corner[c][1]) % pc.N[1];
+        const int z = (ix[2] + c_corner[c][2]) % pc.N[2];
+        const unsigned node = (unsigned)(x + (size_t)y * pc.N[0] + (size_t)z * pc.N[0] * pc.N[1]);
+        nodes[8 * i + c] = node;
+        for (int a = 0; a < 3; ++a) {
+            const float v = corner_value<float>(f[a], c, o, pp, q);
+            atomicAdd(acc + a * V + node, (unsigned long long)llrint((double)v * kFxScale));
+        }
+    }
+}
+
+__global__ void k_spread_fx_store(const unsigned* __restrict__ nodes, int m, size_t V,
+                                  const unsigned long long* __restrict__ acc, float* f0, float* f1, float* f2) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= m) return;
+    const unsigned nd = nodes[s];
+    f0[nd] = (float)((double)(long long)acc[nd] / kFxScale);
+    f1[nd] = (float)((double)(long long)acc[V + nd] / kFxScale);
+    f2[nd] = (float)((double)(long long)acc[2 * V + nd] / kFxScale);
+}
+
+static void spread_fx(fipi_ctx* ctx) {
+    ParticleBufs& b = ctx->pb;
+    const PC pc = make_pc(ctx);
+    const int n = b.n, m = 8 * n;
+    const size_t V = (size_t)ctx->g.V;
+    float* f0 = (float*)ctx->fb.fsp[0];
+    float* f1 = (float*)ctx->fb.fsp[1];
+    float* f2 = (float*)ctx->fb.fsp[2];
+    if (b.sp_prev_valid) {
+        LaunchScope ls_(ctx, "spread clear", 0.0);
+        k_spread_fx_clear<<<(m + 255) / 256, 256, 0, ctx->stream>>>(b.sp_prev, m, V, b.sp_acc, f0, f1, f2);
+    } else {
+        cudaMemsetAsync(b.sp_acc, 0, sizeof(unsigned long long) * 3 * V, ctx->stream);
+        for (int a = 0; a < 3; ++a) cudaMemsetAsync(ctx->fb.fsp[a], 0, sizeof(float) * V, ctx->stream);
+    }
+    { LaunchScope ls_(ctx, "spread fixed-point atomics", 0.0); k_spread_fx<<<(n + 255) / 256, 256, 0, ctx->stream>>>(pc, b.p, b.f_pp, V, b.sp_acc, b.sp_prev); }
+    { LaunchScope ls_(ctx, "spread store", 0.0); k_spread_fx_store<<<(m + 255) / 256, 256, 0, ctx->stream>>>(b.sp_prev, m, V, b.sp_acc, f0, f1, f2); }
+    b.sp_prev_valid = 1;
+}
+
 void particles_spread(fipi_ctx* ctx) {
     if (ctx->pb.n <= 0 || !ctx->P.switch_particle) return;
     if (ctx->prec == FIPI_MIXED) {
-        float* f3[3] = {(float*)ctx->fb.fsp[0], (float*)ctx->fb.fsp[1], (float*)ctx->fb.fsp[2]};
-        spread_t<float>(ctx, ctx->pb.p, ctx->pb.f_pp, f3, true);
+        spread_fx(ctx);
     } else {
         double* f3[3] = {(double*)ctx->fb.fsp[0], (double*)ctx->fb.fsp[1], (double*)ctx->fb.fsp[2]};
         spread_t<double>(ctx, ctx->pb.p, ctx->pb.f_pp, f3, true);
@@ -884,6 +1074,8 @@ fipi_status particles_alloc(fipi_ctx* ctx) {
     FIPI_CUDA(ctx, A((void**)&b.sp_vals, sizeof(unsigned) * 8 * n));
     FIPI_CUDA(ctx, A((void**)&b.sp_vals_alt, sizeof(unsigned) * 8 * n));
     FIPI_CUDA(ctx, A((void**)&b.sp_prev, sizeof(unsigned) * 8 * n));
+    if (ctx->prec == FIPI_MIXED && b.n > 0)
+        FIPI_CUDA(ctx, A((void**)&b.sp_acc, sizeof(unsigned long long) * 3 * (size_t)P.nx * P.ny * P.nz));
     b.hist_cap = 256 * ((16 * n + RS_TILE - 1) / RS_TILE + 1);  // up to 16 records per particle (adjoint)
     FIPI_CUDA(ctx, A((void**)&b.hist, sizeof(unsigned) * b.hist_cap));
     FIPI_CUDA(ctx, A((void**)&b.tau_part, sizeof(double) * n));
@@ -905,7 +1097,7 @@ void particles_free(fipi_ctx* ctx) {
     ParticleBufs& b = ctx->pb;
     void* all[] = {b.p, b.p_old, b.u_old, b.f_pp, b.f_pi, b.r, b.cth, b.keys, b.keys_alt, b.ids, b.ids_alt,
                    b.cell_off, b.cell_cnt, b.sp_keys, b.sp_keys_alt, b.sp_vals, b.sp_vals_alt, b.sp_prev,
-                   b.hist, b.tau_part, b.it_mark, b.tau, b.spos, b.sp_fw, b.ymax};
+                   b.hist, b.tau_part, b.it_mark, b.tau, b.spos, b.sp_fw, b.ymax, b.sp_acc};
     for (void* p : all)
         if (p) cudaFree(p);
     b = ParticleBufs{};

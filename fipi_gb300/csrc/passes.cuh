@@ -115,7 +115,8 @@ template <class Op> struct NoAcc {
 // live in shared memory with one pad slot per 16 (pitch odd, so the
 // transposed column accesses are conflict-free); X_M sits at index M.
 template <typename T, int NIN, int NOUT, bool REDUCE, int M, class Op>
-__global__ void __launch_bounds__(kThreads, 3) k_xpass_acc(Geom g, const cplx<T>* __restrict__ twx, Op op,
+__global__ void __launch_bounds__(kThreads, (NIN > NOUT ? NIN : NOUT) <= 3 ? 4 : 3)
+    k_xpass_acc(Geom g, const cplx<T>* __restrict__ twx, Op op,
                                                       double* partials) {
     using C = cplx<T>;
     constexpr int TY = Tiles<T>::TY;
@@ -255,9 +256,15 @@ template <typename T> struct ZOpProj {
         }
     }
     __device__ void store(int ix, int iy, int iz, size_t gi, const C* F) const {
+        C u[3];
+        compute(ix, iy, iz, F, u);
+        out[0][gi] = u[0];
+        out[1][gi] = u[1];
+        out[2][gi] = u[2];
+    }
+    __device__ void compute(int ix, int iy, int iz, const C* F, C* u) const {
         const T kv[3] = {kt.kx[ix], kt.ky[iy], kt.kz[iz]};
         const T k2 = kt.k2(ix, iy, iz);
-        C u[3];
         if (k2 == T(0)) {
             u[0] = u[1] = u[2] = mkc<C>(T(0), T(0));
         } else {
@@ -273,9 +280,6 @@ template <typename T> struct ZOpProj {
                     u[d] = mkc<C>(T(0.5) * (u[d].x + u2[d].x), T(0.5) * (u[d].y + u2[d].y));
             }
         }
-        out[0][gi] = u[0];
-        out[1][gi] = u[1];
-        out[2][gi] = u[2];
     }
 };
 
@@ -377,6 +381,24 @@ template <typename T, int NF, int DIR, class Op> void launch_z(fipi_ctx* ctx, co
         static size_t granted = 48 * 1024;
         ensure_smem(kern, smem, granted);
         kern<<<grid, threads, smem, ctx->stream>>>(g, (const cplx<T>*)ctx->fb.twz, op);
+    });
+}
+
+// Round-trip Z pass (k_zpass_rt): NF fields in, NB fields out.
+template <typename T, int NF, int NB, int DIR, int COLS, class Op>
+void launch_zrt(fipi_ctx* ctx, const char* name, int nspec, const Op& op) {
+    const Geom& g = ctx->g;
+    LaunchScope ls(ctx, name, (double)nspec * g.SH * sizeof(cplx<T>));
+    dispatch_pow2(g.nz, [&](auto NC) {
+        constexpr int N = decltype(NC)::value;
+        using SHP = ZRtShape<T, N, COLS>;
+        constexpr int NS = NF > NB ? NF : NB;
+        const size_t smem = (size_t)NS * SHP::TZ * N * sizeof(cplx<T>);
+        dim3 grid(g.h, g.ny / SHP::TZ);
+        auto kern = k_zpass_rt<T, NF, NB, DIR, N, COLS, Op>;
+        static size_t granted = 48 * 1024;
+        ensure_smem(kern, smem, granted);
+        kern<<<grid, SHP::TZ * SHP::Tn, smem, ctx->stream>>>(g, (const cplx<T>*)ctx->fb.twz, op);
     });
 }
 

@@ -84,6 +84,24 @@ def test_cells_bit_exact(fipi, oracle_mod, name):
     assert np.array_equal(off, o2)
 
 
+@pytest.mark.parametrize("n_p", [1000, 70000])
+def test_cells_bit_exact_one_block_and_multi_block(fipi, oracle_mod, n_p):
+    """Up to 65,536 particles the cell list is built by one block, above by
+    the multi-block radix sort; both must equal the reference's sorting."""
+    w = fipi.workload("cfg1_64")
+    P = w.params()
+    P.n_p = n_p
+    rng = np.random.default_rng(n_p)
+    p = (rng.random((n_p, 3)) * np.array([P.lx, P.ly, P.lz])).ravel()
+    with fipi.Simulation(P, "fp64") as s:
+        keys, srt, off = s.cells_build(p)
+    st, k2, s2, o2, _ = oracle_mod.sorting(P, p)
+    assert st == 0
+    assert np.array_equal(keys, k2)
+    assert np.array_equal(srt, s2)
+    assert np.array_equal(off, o2)
+
+
 @pytest.mark.parametrize("name", ["t16", "t32", "t32_aniso", "t32_2pi", "cfg1_64"])
 def test_pairs_and_f_pp(fipi, oracle_mod, name):
     w = fipi.workload(name)
