@@ -287,6 +287,7 @@ __global__ void __launch_bounds__(kThreads) k_zpass_rt(Geom g, const cplx<T>* __
     const size_t base = (size_t)kx * g.ny + ky;
     const IdxColumns idx{TZ};
     constexpr size_t fstride = (size_t)N * TZ;
+    op.prologue();
     {
         constexpr int CH = 8 / NF >= 2 ? 8 / NF : 2;
 #pragma unroll

@@ -201,13 +201,50 @@ template <typename T, bool MIXED> struct ZOpCH {
     }
 };
 
+// FP64 k = 0 update of the mixed form: c_hat(0) follows the same IMEX /
+// SBDF2 recurrence with k = 0 (the f terms vanish), C(0) from the FP64
+// per-block sums of conv.  k0 = [c0, c0_old, C0_old, C0_cur].
+// All threads of one block call it.
+__device__ __forceinline__ void k0_update_block(double* k0, const double* partials, int np, int first, double dt,
+                                                double invV) {
+    double s = 0.0;
+    for (int i = threadIdx.x; i < np; i += blockDim.x) s += partials[i];
+    s = block_sum(s);
+    if (threadIdx.x == 0) {
+        const double c0 = k0[0], c0o = k0[1], C0o = k0[2];
+        double nw;
+        if (first) {
+            nw = c0 - s * dt;
+        } else {
+            double re = c0 * 4.0 - c0o;
+            re -= s * (4.0 * dt);
+            re += C0o * (2.0 * dt);
+            nw = re / 3.0;
+        }
+        k0[1] = c0;
+        k0[0] = nw;
+        k0[2] = s;
+        k0[3] = s;
+        *reinterpret_cast<float*>(k0 + 4) = (float)(nw * invV);  // mean of c for the FP32 fields
+    }
+}
+
 // Round trip A -> B (k_zpass_rt, NF = NB = 1): the CH update of ZOpCH in
 // the forward Z pass, then the inverse Z transform of c_hat^{n+1} (the
 // first pass of c^{n+1} = C2R(c_hat^{n+1})) into `out`.
+// In the mixed form the first block also advances the FP64 k = 0 record
+// from the conv pass's block sums (nothing else in this pass reads it).
 template <typename T, bool MIXED> struct ZOpCHRt {
     using C = cplx<T>;
     ZOpCH<T, MIXED> ch;
     C* out;
+    double* k0;
+    const double* partials;
+    int np;
+    double dt, invV;
+    __device__ void prologue() const {
+        if (MIXED && blockIdx.x == 0 && blockIdx.y == 0) k0_update_block(k0, partials, np, ch.first, dt, invV);
+    }
     __device__ void load(int, int, int, size_t gi, C* v) const { v[0] = ch.conv[gi]; }
     __device__ void mid(int ix, int iy, int iz, size_t gi, const C* vi, C* vo) const {
         vo[0] = ch.update(ix, iy, iz, gi, vi[0]);
@@ -228,6 +265,7 @@ template <typename T> struct ZOpFRt {
     KTabs<T> kt;
     T lam;
     int m, ny2, nz2;
+    __device__ void prologue() const {}
     __device__ void load(int, int, int, size_t gi, C* v) const { v[0] = fin[gi]; }
     __device__ void mid(int ix, int iy, int iz, size_t gi, const C* vi, C* vo) const {
         const C f = vi[0];
@@ -253,6 +291,7 @@ template <typename T> struct ZOpProjRt {
     using C = cplx<T>;
     ZOpProj<T> pj;
     C* upre[3];
+    __device__ void prologue() const {}
     __device__ void load(int, int, int, size_t gi, C* v) const {
         v[0] = pj.in[0][gi];
         v[1] = pj.in[1][gi];
@@ -309,31 +348,6 @@ template <typename T> struct ZOpGrad {
 };
 
 
-// FP64 k = 0 update of the mixed form: c_hat(0) follows the same IMEX /
-// SBDF2 recurrence with k = 0 (the f terms vanish), C(0) from the FP64
-// per-block sums of conv.  k0 = [c0, c0_old, C0_old, C0_cur].
-__global__ void k_k0_update(double* k0, const double* partials, int np, int first, double dt, double invV) {
-    double s = 0.0;
-    for (int i = threadIdx.x; i < np; i += blockDim.x) s += partials[i];
-    s = block_sum(s);
-    if (threadIdx.x == 0) {
-        const double c0 = k0[0], c0o = k0[1], C0o = k0[2];
-        double nw;
-        if (first) {
-            nw = c0 - s * dt;
-        } else {
-            double re = c0 * 4.0 - c0o;
-            re -= s * (4.0 * dt);
-            re += C0o * (2.0 * dt);
-            nw = re / 3.0;
-        }
-        k0[1] = c0;
-        k0[0] = nw;
-        k0[2] = s;
-        k0[3] = s;
-        *reinterpret_cast<float*>(k0 + 4) = (float)(nw * invV);  // mean of c for the FP32 fields
-    }
-}
 
 
 // FP64 per-block sums for mass and free energy (main.cpp:329, field.cpp:507-516).
@@ -583,15 +597,10 @@ template <typename T, bool MIXED> static void step_ch_t(fipi_ctx* ctx, int t) {
     launch_x<T, 3, 1, MIXED>(ctx, "X inverse u, conv, forward", 3, oc, ctx->partials);
     void* s1[1] = {b.S[3]};
     launch_y<T>(ctx, 1, s1, s1, -1);
-    if (MIXED) {
-        const int nblk = (g.ny / Tiles<T>::TY) * g.nz;
-        LaunchScope ls(ctx, "k0 update", 0.0);
-        k_k0_update<<<1, 256, 0, ctx->stream>>>(ctx->k0, ctx->partials, nblk, t == 0, ctx->P.dt,
-                                                 1.0 / (double)g.V);
-    }
     ZOpCH<T, MIXED> zc{F<T>::S(ctx, 3), F<T>::sp(b.chat), F<T>::sp(b.chat_old), F<T>::sp(b.fhat),
                        F<T>::sp(b.fhat_old), F<T>::sp(b.Chat_old), kt, k, t == 0 ? 1 : 0};
-    ZOpCHRt<T, MIXED> zcr{zc, F<T>::S(ctx, 0)};
+    ZOpCHRt<T, MIXED> zcr{zc, F<T>::S(ctx, 0), ctx->k0, ctx->partials, (g.ny / Tiles<T>::TY) * g.nz,
+                          ctx->P.dt, 1.0 / (double)g.V};
     launch_zrt<T, 1, 1, -1, TZ>(ctx, t == 0 ? "Z forward + IMEX update + inverse" : "Z forward + SBDF2 update + inverse",
                                 t == 0 ? 6 : 9, zcr);
     std::swap(b.chat, b.chat_old);  // chat = c^{n+1}, chat_old = c^n

@@ -229,123 +229,110 @@ __global__ void k_cell_offsets(const unsigned* __restrict__ keys, int n, int* of
     off[c] = lo;
 }
 
-// The whole cell list in one block of 1024 threads (keys, stable LSD radix
-// sort of (key, id) in 8-bit digits, offsets): one launch instead of eight
-// for the particle counts of one GPU's workloads.  Stability as in
-// k_rs_scatter: ranks within a warp by __match_any_sync, warps in order
-// through per-warp digit counts, chunks in order through the running
-// digit cursors.  Output identical to the multi-block path.
-constexpr int kCB_T = 1024;
-constexpr int kCellsOneBlockMax = 65536;
-
-__global__ void __launch_bounds__(kCB_T) k_cells_one_block(PC pc, const double* __restrict__ p, unsigned* k0,
-                                                           unsigned* v0, unsigned* k1, unsigned* v1, int* off,
-                                                           int ncells, int bits, int* status) {
-    __shared__ unsigned cur[256];
-    __shared__ unsigned wcnt[kCB_T / 32][256];
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+// Cell list in four small kernels: keys and per-cell counts (the arrival
+// slot from atomicAdd is arbitrary), an exclusive scan of the counts (the
+// offsets), placement at offset + slot, then one warp per cell ranks its
+// ids so each cell lists its particles in ascending id — the order of the
+// stable sort of cluster::sorting (cluster.cpp:210-263).  The result does
+// not depend on the order of the atomics.  With `ymax` the same kernels
+// find it_mark of cluster.cpp:222-232 (the first id with the largest
+// p_y > 0; unchanged when there is none).
+__global__ void k_cells_count(PC pc, const double* __restrict__ p, unsigned* keys, unsigned* slot, int* cnt,
+                              unsigned long long* ymax, int* status) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = pc.n;
-    for (int i = tid; i < n; i += kCB_T) {
-        k0[i] = cell_key(pc, p[i], p[n + i], p[2 * n + i], status);
-        v0[i] = (unsigned)i;
+    unsigned long long yb = 0;
+    if (i < n) {
+        const double y = p[n + i];
+        const unsigned key = cell_key(pc, p[i], y, p[2 * n + i], status);
+        keys[i] = key;
+        slot[i] = (unsigned)atomicAdd(&cnt[key], 1);
+        yb = (y > 0.0) ? (unsigned long long)__double_as_longlong(y) : 0ull;
     }
-    __syncthreads();
-    unsigned *kin = k0, *vin = v0, *kout = k1, *vout = v1;
-    const unsigned lt = (1u << lane) - 1u;
-    for (int shift = 0; shift < bits; shift += 8) {
-        if (tid < 256) cur[tid] = 0;
-        __syncthreads();
-        for (int i = tid; i < n; i += kCB_T) atomicAdd(&cur[(kin[i] >> shift) & 255u], 1u);
-        __syncthreads();
-        if (warp == 0) {  // exclusive scan of the 256 digit counts, 8 per lane
-            unsigned v[8], sum = 0;
-            for (int j = 0; j < 8; ++j) {
-                v[j] = cur[lane * 8 + j];
-                sum += v[j];
-            }
-            unsigned incl = sum;
-            for (int o = 1; o < 32; o <<= 1) {
-                const unsigned t = __shfl_up_sync(0xffffffffu, incl, o);
-                if (lane >= o) incl += t;
-            }
-            unsigned run = incl - sum;
-            for (int j = 0; j < 8; ++j) {
-                cur[lane * 8 + j] = run;
-                run += v[j];
-            }
+    if (ymax) {
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long x = __shfl_down_sync(0xffffffffu, yb, o);
+            yb = x > yb ? x : yb;
         }
-        __syncthreads();
-        for (int c0 = 0; c0 < n; c0 += kCB_T) {
-            const int s = c0 + tid;
-            const bool valid = s < n;
-            unsigned key = 0, val = 0, d = 256;
-            if (valid) {
-                key = kin[s];
-                val = vin[s];
-                d = (key >> shift) & 255u;
-            }
-            for (int j = tid; j < (kCB_T / 32) * 256; j += kCB_T) (&wcnt[0][0])[j] = 0;
-            __syncthreads();
-            const unsigned peers = __match_any_sync(0xffffffffu, d);
-            const unsigned rank = __popc(peers & lt);
-            if (valid && rank == 0) wcnt[warp][d] = __popc(peers);
-            __syncthreads();
-            if (tid < 256) {
-                unsigned run = cur[tid];
-                for (int w = 0; w < kCB_T / 32; ++w) {
-                    const unsigned c = wcnt[w][tid];
-                    wcnt[w][tid] = run;
-                    run += c;
-                }
-                cur[tid] = run;
-            }
-            __syncthreads();
-            if (valid) {
-                const unsigned pos = wcnt[warp][d] + rank;
-                kout[pos] = key;
-                vout[pos] = val;
-            }
-            __syncthreads();
-        }
-        unsigned* t = kin;
-        kin = kout;
-        kout = t;
-        t = vin;
-        vin = vout;
-        vout = t;
-    }
-    // offsets: first sorted position whose key >= c
-    for (int c = tid; c <= ncells; c += kCB_T) {
-        int lo = 0, hi = n;
-        while (lo < hi) {
-            const int mid = (lo + hi) >> 1;
-            if ((int)kin[mid] < c) lo = mid + 1;
-            else hi = mid;
-        }
-        off[c] = lo;
+        if ((threadIdx.x & 31) == 0 && yb) atomicMax(&ymax[0], yb);
     }
 }
 
-static void build_cells(fipi_ctx* ctx, const double* p_dev) {
+// Exclusive scan of ncells counts into off[0..ncells] (one block).
+__global__ void k_cells_scan(const int* __restrict__ cnt, int ncells, int* off) {
+    __shared__ int part[1024];
+    const int t = threadIdx.x;
+    const int chunk = (ncells + 1023) / 1024;
+    const int b = t * chunk, e = min(ncells, b + chunk);
+    int s = 0;
+    for (int i = b; i < e; ++i) s += cnt[i];
+    part[t] = s;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+        const int v = (t >= o) ? part[t - o] : 0;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    int run = part[t] - s;
+    for (int i = b; i < e; ++i) {
+        off[i] = run;
+        run += cnt[i];
+    }
+    if (t == 1023) off[ncells] = part[1023];
+}
+
+__global__ void k_cells_place(PC pc, const double* __restrict__ p, const unsigned* __restrict__ keys,
+                              const unsigned* __restrict__ slot, const int* __restrict__ off, unsigned* tmp,
+                              unsigned long long* ymax) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = pc.n;
+    if (i >= n) return;
+    tmp[off[keys[i]] + slot[i]] = (unsigned)i;
+    if (ymax) {
+        const unsigned long long best = ymax[0];
+        if (best != 0ull && (unsigned long long)__double_as_longlong(p[n + i]) == best)
+            atomicMin(&ymax[1], (unsigned long long)i);
+    }
+}
+
+// One warp per cell: rank of each id among the cell's ids.
+__global__ void k_cells_order(const int* __restrict__ off, int ncells, const unsigned* __restrict__ tmp,
+                              unsigned* ids, unsigned* skeys, unsigned long long* ymax, int* it_mark) {
+    const int cell = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (ymax && blockIdx.x == 0 && threadIdx.x == 0) {
+        if (ymax[0] != 0ull) *it_mark = (int)ymax[1];
+        ymax[0] = 0ull;
+        ymax[1] = ~0ull;
+    }
+    if (cell >= ncells) return;
+    const int beg = off[cell], end = off[cell + 1];
+    for (int e = beg + lane; e < end; e += 32) {
+        const unsigned id = tmp[e];
+        int r = 0;
+        for (int j = beg; j < end; ++j) r += tmp[j] < id;
+        ids[beg + r] = id;
+        skeys[beg + r] = (unsigned)cell;
+    }
+}
+
+// Returns true when it also computed it_mark (asked for by `want_it_mark`).
+static bool build_cells(fipi_ctx* ctx, const double* p_dev, bool want_it_mark = false) {
     ParticleBufs& b = ctx->pb;
     const PC pc = make_pc(ctx);
     const int n = b.n;
-    const int bits = bits_for(b.ncells - 1);
-    if (n <= kCellsOneBlockMax) {
-        {
-            LaunchScope ls_(ctx, "cell list (one block)", 0.0);
-            k_cells_one_block<<<1, kCB_T, 0, ctx->stream>>>(pc, p_dev, b.keys, b.ids, b.keys_alt, b.ids_alt,
-                                                             b.cell_off, b.ncells, bits, ctx->status);
-        }
-        if (((bits + 7) / 8) & 1) {  // an odd number of digit passes leaves the result in the alternates
-            std::swap(b.keys, b.keys_alt);
-            std::swap(b.ids, b.ids_alt);
-        }
-        return;
-    }
-    { LaunchScope ls_(ctx, "cell keys", 0.0); k_cell_keys<<<(n + 255) / 256, 256, 0, ctx->stream>>>(pc, p_dev, b.keys, b.ids, ctx->status); }
-    radix_sort(ctx, b.keys, b.ids, b.keys_alt, b.ids_alt, n, bits);
-    { LaunchScope ls_(ctx, "cell offsets", 0.0); k_cell_offsets<<<(b.ncells + 1 + 255) / 256, 256, 0, ctx->stream>>>(b.keys, n, b.cell_off, b.ncells); }
+    if (n <= 0) return false;
+    const int nb = (n + 255) / 256;
+    unsigned long long* ym = want_it_mark ? b.ymax : nullptr;
+    // keys_alt holds the per-particle keys (by id), ids_alt the arrival slots, then the placed ids
+    cudaMemsetAsync(b.cell_cnt, 0, sizeof(int) * (b.ncells + 1), ctx->stream);
+    { LaunchScope ls_(ctx, "cell keys + counts", 0.0); k_cells_count<<<nb, 256, 0, ctx->stream>>>(pc, p_dev, b.keys_alt, b.ids_alt, b.cell_cnt, ym, ctx->status); }
+    { LaunchScope ls_(ctx, "cell offsets", 0.0); k_cells_scan<<<1, 1024, 0, ctx->stream>>>(b.cell_cnt, b.ncells, b.cell_off); }
+    { LaunchScope ls_(ctx, "cell placement", 0.0); k_cells_place<<<nb, 256, 0, ctx->stream>>>(pc, p_dev, b.keys_alt, b.ids_alt, b.cell_off, b.keys, ym); }
+    { LaunchScope ls_(ctx, "cell order", 0.0); k_cells_order<<<(b.ncells * 32 + 255) / 256, 256, 0, ctx->stream>>>(b.cell_off, b.ncells, b.keys, b.ids, b.keys_alt, ym, b.it_mark); }
+    std::swap(b.keys, b.keys_alt);  // sorted keys now in keys
+    return want_it_mark;
 }
 
 // ------------------------------------------------------------ contact forces
@@ -973,12 +960,13 @@ static void it_mark_launch(fipi_ctx* ctx, const double* p) {
 // accumulated per particle (tau_part) and summed when it is asked for.
 // TA = float with at least 4 cells per axis takes the FP32 cell-relative path.
 template <typename TA>
-static void f_pp_launch(fipi_ctx* ctx, const double* p, const double* rmp, const double* f_pi, double* f_pp, bool tau) {
+static void f_pp_launch(fipi_ctx* ctx, const double* p, const double* rmp, const double* f_pi, double* f_pp, bool tau,
+                        bool have_it_mark = false) {
     ParticleBufs& b = ctx->pb;
     const PC pc = make_pc(ctx);
     const int warps = b.ncells;
     const int blocks = (warps * 32 + 255) / 256;
-    if (tau) it_mark_launch(ctx, p);
+    if (tau && !have_it_mark) it_mark_launch(ctx, p);
     const bool fast = sizeof(TA) == sizeof(float) && b.ncell[0] >= 4 && b.ncell[1] >= 4 && b.ncell[2] >= 4;
     if (fast) {
         { LaunchScope ls_(ctx, "sorted FP32 positions", 0.0); k_sorted_pos<<<(b.n + 255) / 256, 256, 0, ctx->stream>>>(pc, p, b.keys, b.ids, b.spos); }
@@ -1014,8 +1002,8 @@ template <typename T> static void step_t(fipi_ctx* ctx) {
         { LaunchScope ls_(ctx, "stage interpolate + f_pi", 0.0); k_stage_fpi<T, T><<<nb, 256, 0, ctx->stream>>>(pc, (const T*)ctx->fb.c, (const T*)ctx->fb.g[0],
                                                      (const T*)ctx->fb.g[1], (const T*)ctx->fb.g[2], b.p, b.f_pi,
                                                      b.r, b.cth); }
-        build_cells(ctx, b.p);
-        f_pp_launch<T>(ctx, b.p, ctx->d_rmp, b.f_pi, b.f_pp, ctx->track_tau);
+        const bool im = build_cells(ctx, b.p, ctx->track_tau);
+        f_pp_launch<T>(ctx, b.p, ctx->d_rmp, b.f_pi, b.f_pp, ctx->track_tau, im);
         { LaunchScope ls_(ctx, "stage advect + wrap", 0.0); k_stage_advect<<<nb, 256, 0, ctx->stream>>>(pc, stage, b.p, b.p_old, b.u_old, b.f_pi, b.f_pp, b.r,
                                                     ctx->status); }
     }
