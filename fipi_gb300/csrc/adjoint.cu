@@ -156,6 +156,7 @@ template <typename T> struct ZOpAdjC {
     KTabs<T> kt;
     StepConsts<T> k;
     int first;
+    __device__ const C* src(int f) const { return S[f]; }
     __device__ void load(int, int, int, size_t gi, C* v) const {
 #pragma unroll
         for (int f = 0; f < 5; ++f) v[f] = S[f][gi];
@@ -205,6 +206,7 @@ template <typename T> struct ZOpAdjAcc {
     C* la_c;
     KTabs<T> kt;
     int m, ny2, nz2;
+    __device__ const C* src(int f) const { return S[f]; }
     __device__ void load(int, int, int, size_t gi, C* v) const {
 #pragma unroll
         for (int f = 0; f < 4; ++f) v[f] = S[f][gi];

@@ -22,6 +22,8 @@
 // post-processing; C2R is the mirror image.  Unnormalised, like FFTW.
 #pragma once
 
+#include <type_traits>
+
 #include "common.cuh"
 #include "fft2.cuh"
 #include "tma.cuh"
@@ -44,10 +46,23 @@ template <typename T> struct Tiles {
     static constexpr int TZ = 128 / (2 * sizeof(T));
 };
 
+// A Z-pass operation whose load() only copies NF spectral arrays declares
+// src(f) (the array of field f); its tiles are then fetched with cp.async.
+template <class O, class = void> struct HasSrc : std::false_type {};
+template <class O> struct HasSrc<O, std::void_t<decltype(std::declval<const O&>().src(0))>> : std::true_type {};
+
 // ----------------------------------------------------------------- Y pass
 template <typename T> struct FieldPtrs {
     cplx<T>* in[8];
     cplx<T>* out[8];
+    // in[f] / out[f] for a run-time f without copying the parameter to local memory
+    __device__ __forceinline__ cplx<T>* pick(cplx<T>* const (&a)[8], int f) const {
+        cplx<T>* p = a[0];
+#pragma unroll
+        for (int k = 1; k < 8; ++k)
+            if (f == k) p = a[k];
+        return p;
+    }
 };
 
 // Rows per Y-pass block: 256 threads, Tn = fft_threads_per_row(ny) per row.
@@ -91,22 +106,25 @@ template <typename T> inline size_t ypass_smem(const Geom& g) {
 
 // Persistent Y pass: each block streams tiles of RB consecutive rows
 // (RB * N contiguous complex values) into shared memory with one bulk TMA
-// copy per tile, double-buffered so tile k+1 is in flight while tile k is
-// transformed; the buffer a tile arrived in then serves as that tile's
-// (padded) exchange buffer.  The first stage reads the tile, the last
-// stage stores straight to global memory.  `fields` fields of rows are
-// processed in one launch.
+// copy per tile through a ring of kYStages buffers, so kYStages - 1 tiles
+// are in flight while one is transformed; the buffer a tile arrived in then
+// serves as that tile's (padded) exchange buffer.  The first stage reads the
+// tile, the last stage stores straight to global memory.  `fields` fields of
+// rows are processed in one launch.
+constexpr int kYStages = 2;  // 3 measured no faster on GB300 (more registers)
+
 template <typename T, int DIR, int N>
 __global__ void __launch_bounds__(kThreads) k_ypass_tma(Geom g, const cplx<T>* __restrict__ twy, FieldPtrs<T> fp,
                                                        int fields, int* status) {
     using C = cplx<T>;
     using IO = FftIO<T, DIR, N>;
+    constexpr int S = kYStages;
     constexpr int Tn = FftPlan<N, FftE<T>::value>::Tn;
     constexpr int RB = kThreads / Tn;
     constexpr int BUF = RB * ((N + (N >> 4) + 15) & ~15);  // padded rows, 128-byte multiple for FP32/FP64
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* buf0 = reinterpret_cast<C*>(smem_raw);
-    __shared__ __align__(8) uint64_t bar[2];
+    __shared__ __align__(8) uint64_t bar[S];
     __shared__ int abort_flag;
     const int tid = threadIdx.x;
     const long long rows_f = (long long)g.nz * g.h;
@@ -114,33 +132,39 @@ __global__ void __launch_bounds__(kThreads) k_ypass_tma(Geom g, const cplx<T>* _
     const long long ntiles = tiles_f * fields;
     const IdxPadded xidx{padded_len(N)};
     if (tid == 0) {
-        mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
+        for (int k = 0; k < S; ++k) mbar_init(&bar[k], 1);
         fence_mbar_init();
         abort_flag = 0;
     }
     __syncthreads();
+    uint32_t inflight = 0;  // stages with a copy issued and not yet waited for (thread 0)
     auto issue = [&](long long tile, int b) {
         const int f = (int)(tile / tiles_f);
         const long long r0 = (tile - (long long)f * tiles_f) * RB;
         const int rows = (int)min((long long)RB, rows_f - r0);
         const uint32_t bytes = (uint32_t)(rows * N * sizeof(C));
         mbar_arrive_expect_tx(&bar[b], bytes);
-        bulk_g2s(buf0 + b * BUF, fp.in[f] + r0 * N, bytes, &bar[b]);
+        bulk_g2s(buf0 + b * BUF, fp.pick(fp.in, f) + r0 * N, bytes, &bar[b]);
+        inflight |= 1u << b;
     };
-    long long tile = blockIdx.x;
-    if (tid == 0 && tile < ntiles) issue(tile, 0);
-    uint32_t parity0 = 0, parity1 = 0;
+    if (tid == 0)
+        for (int k = 0; k < S - 1; ++k) {
+            const long long tl = blockIdx.x + (long long)k * gridDim.x;
+            if (tl < ntiles) issue(tl, k);
+        }
+    uint32_t parity = 0;  // bit k: parity of the next phase of stage k
     int b = 0;
-    for (; tile < ntiles; tile += gridDim.x) {
+    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int f = (int)(tile / tiles_f);
         const long long r0 = (tile - (long long)f * tiles_f) * RB;
         const int rows = (int)min((long long)RB, rows_f - r0);
-        const uint32_t par = b ? parity1 : parity0;
-        const bool ok = mbar_wait(&bar[b], par);
-        if (b) parity1 ^= 1u;
-        else parity0 ^= 1u;
-        if (!ok) abort_flag = 1;
+        const bool ok = mbar_wait(&bar[b], (parity >> b) & 1u);
+        if (ok) {
+            parity ^= 1u << b;
+            inflight &= ~(1u << b);
+        } else {
+            abort_flag = 1;
+        }
         C* in = buf0 + b * BUF;
         const int row = tid / Tn, t = tid - row * Tn;
         const bool act = row < rows;
@@ -149,26 +173,27 @@ __global__ void __launch_bounds__(kThreads) k_ypass_tma(Geom g, const cplx<T>* _
 #pragma unroll
             for (int i = 0; i < IO::E; ++i) v[i] = in[row * N + IO::in_elem(t, i)];
         }
-        // generic-proxy accesses of the other buffer (previous tile) are
-        // ordered before the bulk copy that will overwrite it
+        // generic-proxy accesses of the previous tile's buffer are ordered
+        // before the bulk copy that will overwrite it
         fence_proxy_async_smem();
-        __syncthreads();  // the tile is in registers; the other buffer's previous tile is finished
+        __syncthreads();  // this tile is in registers; the previous tile is finished
         if (abort_flag) {
             if (tid == 0) {
                 atomicOr(status, ERR_TMA_TIMEOUT);
-                mbar_wait(&bar[b], par);  // bounded: let the late copy land before the block exits
+                for (int k = 0; k < S; ++k)  // bounded: let late copies land before the block exits
+                    if ((inflight >> k) & 1u) mbar_wait(&bar[k], (parity >> k) & 1u);
             }
             return;
         }
-        const long long next = tile + gridDim.x;
-        if (tid == 0 && next < ntiles) issue(next, b ^ 1);
+        const long long next = tile + (long long)(S - 1) * gridDim.x;
+        if (tid == 0 && next < ntiles) issue(next, (b + S - 1) % S);
         smem_fft2<T, DIR, N, true, true>(in, xidx, row, t, act, twy, 1, v);
         if (act) {
-            C* out = fp.out[f] + (r0 + row) * N;
+            C* out = fp.pick(fp.out, f) + (r0 + row) * N;
 #pragma unroll
             for (int i = 0; i < IO::E; ++i) out[IO::out_elem(t, i)] = v[i];
         }
-        b ^= 1;
+        b = (b + 1) % S;
     }
 }
 
@@ -176,7 +201,7 @@ template <typename T> inline size_t ypass_tma_smem(const Geom& g) {
     const int tn = fft_threads_per_row<T>(g.ny);
     const int rb = kThreads / tn;
     const int row = (g.ny + (g.ny >> 4) + 15) & ~15;
-    return (size_t)2 * rb * row * sizeof(cplx<T>);
+    return (size_t)kYStages * rb * row * sizeof(cplx<T>);
 }
 
 // ----------------------------------------------------------------- Z pass
@@ -226,6 +251,20 @@ __global__ void __launch_bounds__(kThreads) k_zpass(Geom g, const cplx<T>* __res
             v[i] = w[0];
         }
         smem_fft2<T, DIR, N, true, false>(s, idx, c, t, true, twz, 1, v);
+    } else if constexpr (HasSrc<Op>::value) {
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+            const C* src = op.src(f);
+#pragma unroll
+            for (int i = 0; i < E; ++i) {
+                const int z = t + Tn * i;
+                cp_async<sizeof(C)>(&s[f * fstride + idx(c, z)], src + base + z * zstride);
+            }
+        }
+        cp_async_wait_all();
+        __syncthreads();
+#pragma unroll
+        for (int f = 0; f < NF; ++f) smem_fft2<T, DIR, N>(s + f * fstride, idx, c, t, true, twz, 1);
     } else {
         // loads in chunks of CH modes per thread: CH * NF independent loads in flight
         constexpr int CH = 8 / NF >= 2 ? 8 / NF : 2;
@@ -269,14 +308,94 @@ __global__ void __launch_bounds__(kThreads) k_zpass(Geom g, const cplx<T>* __res
 // COLS complex values per kz).
 template <typename T, int N, int COLS> struct ZRtShape {
     static constexpr int E = N < FftE<T>::value ? N : FftE<T>::value;
+    static constexpr int Tn = N / E;                                      // threads per column FFT
+    static constexpr int RC = COLS * Tn <= kThreads ? COLS : kThreads / Tn;  // columns per FFT round
+    static constexpr int THREADS = RC * Tn;
+    static constexpr int P = COLS + 1;  // shared-memory pitch of one kz row (odd: fewer bank conflicts)
+};
+
+// The tile is COLS columns (a 128-byte run of ky per kz for FP32 and FP64)
+// of all kz; the column FFTs run in rounds of RC columns, while loads, the
+// mid operation and stores walk the tile with ky fastest (full runs per
+// warp).  Tiles whose load() only copies arrays (src()) arrive by cp.async.
+template <typename T, int NF, int NB, int DIR, int N, int COLS, class Op>
+__global__ void __launch_bounds__(kThreads) k_zpass_rt(Geom g, const cplx<T>* __restrict__ twz, Op op) {
+    using C = cplx<T>;
+    using SH = ZRtShape<T, N, COLS>;
+    constexpr int RC = SH::RC, P = SH::P, NT = SH::THREADS;
+    constexpr int ELEMS = COLS * N;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C* s = reinterpret_cast<C*>(smem_raw);
+    const int kx = blockIdx.x, ky0 = blockIdx.y * COLS;
+    const int tid = threadIdx.x;
+    const size_t zstride = (size_t)g.h * g.ny;
+    const size_t base = (size_t)kx * g.ny + ky0;
+    const IdxColumns idx{P};
+    constexpr size_t fstride = (size_t)N * P;
+    op.prologue();
+    if constexpr (HasSrc<Op>::value) {
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+            const C* src = op.src(f);
+            for (int e = tid; e < ELEMS; e += NT) {
+                const int c = e % COLS, z = e / COLS;
+                cp_async<sizeof(C)>(&s[f * fstride + z * P + c], src + base + c + z * zstride);
+            }
+        }
+        cp_async_wait_all();
+    } else {
+        for (int e = tid; e < ELEMS; e += NT) {
+            const int c = e % COLS, z = e / COLS;
+            C v[NF];
+            op.load(kx, ky0 + c, z, base + c + z * zstride, v);
+#pragma unroll
+            for (int f = 0; f < NF; ++f) s[f * fstride + z * P + c] = v[f];
+        }
+    }
+    __syncthreads();
+    const int cl = tid % RC, t = tid / RC;
+#pragma unroll
+    for (int f = 0; f < NF; ++f)
+        for (int r = 0; r < COLS; r += RC) smem_fft2<T, DIR, N>(s + f * fstride + r, idx, cl, t, true, twz, 1);
+    __syncthreads();
+    for (int e = tid; e < ELEMS; e += NT) {
+        const int c = e % COLS, z = e / COLS;
+        C vi[NF], vo[NB];
+#pragma unroll
+        for (int f = 0; f < NF; ++f) vi[f] = s[f * fstride + z * P + c];
+        op.mid(kx, ky0 + c, z, base + c + z * zstride, vi, vo);
+#pragma unroll
+        for (int b = 0; b < NB; ++b) s[b * fstride + z * P + c] = vo[b];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int b = 0; b < NB; ++b)
+        for (int r = 0; r < COLS; r += RC) smem_fft2<T, -DIR, N>(s + b * fstride + r, idx, cl, t, true, twz, 1);
+    __syncthreads();
+    for (int e = tid; e < ELEMS; e += NT) {
+        const int c = e % COLS, z = e / COLS;
+        C v[NB];
+#pragma unroll
+        for (int b = 0; b < NB; ++b) v[b] = s[b * fstride + z * P + c];
+        op.store2(kx, ky0 + c, z, base + c + z * zstride, v);
+    }
+}
+
+// Round trip with the column-per-thread-group mapping of k_zpass: the tile
+// is ZRtShapeT::TZ columns (one FFT round), loaded through registers, and
+// each thread's mid and store work is on the modes its last FFT stage
+// produced.  Measured faster than k_zpass_rt for three or more fields
+// (smaller tiles, more blocks per SM); k_zpass_rt is faster for one.
+template <typename T, int N, int COLS> struct ZRtShapeT {
+    static constexpr int E = N < FftE<T>::value ? N : FftE<T>::value;
     static constexpr int Tn = N / E;
     static constexpr int TZ = COLS * Tn <= kThreads ? COLS : kThreads / Tn;
 };
 
 template <typename T, int NF, int NB, int DIR, int N, int COLS, class Op>
-__global__ void __launch_bounds__(kThreads) k_zpass_rt(Geom g, const cplx<T>* __restrict__ twz, Op op) {
+__global__ void __launch_bounds__(kThreads) k_zpass_rt_t(Geom g, const cplx<T>* __restrict__ twz, Op op) {
     using C = cplx<T>;
-    using SH = ZRtShape<T, N, COLS>;
+    using SH = ZRtShapeT<T, N, COLS>;
     constexpr int E = SH::E, Tn = SH::Tn, TZ = SH::TZ;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* s = reinterpret_cast<C*>(smem_raw);

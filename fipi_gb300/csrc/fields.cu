@@ -66,15 +66,18 @@ template <typename T, bool MIXED> struct OpConv {
     __device__ const C* in(int f) const { return uS[f]; }
     __device__ C* out(int) const { return o0; }
     template <class A> __device__ void point(int z, int y, int n, C* v, A& acc) const {
-        const size_t row = ((size_t)z * ny + y) * nx;
+        point(z, y, n, v, acc, XGlobalRow<T, 3>{{g[0], g[1], g[2]}, ((size_t)z * ny + y) * nx});
+    }
+    template <class A, class R> __device__ void point(int z, int y, int n, C* v, A& acc, const R& r) const {
         T s0 = T(0), s1 = T(0);
         if (tape_u[0]) {
+            const size_t row = ((size_t)z * ny + y) * nx;
 #pragma unroll
             for (int d = 0; d < 3; ++d) reinterpret_cast<C*>(tape_u[d] + row)[n] = v[d];
         }
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-            const C gg = reinterpret_cast<const C*>(g[d] + row)[n];
+            const C gg = r.get(d, n);
             s0 += v[d].x * gg.x;
             s1 += v[d].y * gg.y;
         }
@@ -120,11 +123,14 @@ template <typename T> struct OpForce {
     int nx, ny;
     __device__ const C* in(int f) const { return S[f]; }
     __device__ C* out(int f) const { return const_cast<C*>(S[f]); }
-    template <class A> __device__ void point(int z, int y, int n, C* v, A&) const {
+    template <class A> __device__ void point(int z, int y, int n, C* v, A& acc) const {
+        point(z, y, n, v, acc, XGlobalRow<T, 4>{{c, fsp[0], fsp[1], fsp[2]}, ((size_t)z * ny + y) * nx});
+    }
+    template <class A, class R> __device__ void point(int z, int y, int n, C* v, A&, const R& r) const {
         const size_t row = ((size_t)z * ny + y) * nx;
         const C mu = v[0];
         if (tape_mu) reinterpret_cast<C*>(tape_mu + row)[n] = mu;
-        const C cc = reinterpret_cast<const C*>(c + row)[n];
+        const C cc = r.get(0, n);
         // buoyancy ((1+c)/2 rho1 + (1-c)/2 rho2) g, g = (0, 0, gravity)
         const T b0 = ((cc.x + T(1)) / T(2)) * rho1 + ((cc.x * T(-1) + T(1)) / T(2)) * rho2;
         const T b1 = ((cc.y + T(1)) / T(2)) * rho1 + ((cc.y * T(-1) + T(1)) / T(2)) * rho2;
@@ -134,7 +140,7 @@ template <typename T> struct OpForce {
             reinterpret_cast<C*>(g[d] + row)[n] = gd;
             T f0 = mu.x * gd.x, f1 = mu.y * gd.y;
             if (spread) {
-                const C sp = reinterpret_cast<const C*>(fsp[d] + row)[n];
+                const C sp = r.get(1 + d, n);
                 f0 += sp.x;
                 f1 += sp.y;
             }
@@ -162,11 +168,27 @@ template <typename T, bool MIXED> struct ZOpCH {
     StepConsts<T> k;
     int first;  // t == 0
     __device__ void load(int, int, int, size_t gi, C* v) const { v[0] = conv[gi]; }
-    __device__ void store(int ix, int iy, int iz, size_t gi, const C* v) const { update(ix, iy, iz, gi, v[0]); }
+    __device__ void store(int ix, int iy, int iz, size_t gi, const C* v) const {
+        Pre p;
+        pre(gi, p);
+        update(ix, iy, iz, gi, v[0], p);
+    }
+    struct Pre {
+        C c, f, co, fo, Co;
+    };
+    __device__ void pre(size_t gi, Pre& p) const {
+        p.c = chat[gi];
+        p.f = fhat[gi];
+        if (!first) {
+            p.co = chat_old[gi];
+            p.fo = fhat_old[gi];
+            p.Co = Chat_old[gi];
+        }
+    }
     // Writes c_hat^{n+1} and C^n at gi and returns c_hat^{n+1}.
-    __device__ C update(int ix, int iy, int iz, size_t gi, const C Cn) const {
-        const C c = chat[gi];
-        const C f = fhat[gi];
+    __device__ C update(int ix, int iy, int iz, size_t gi, const C Cn, const Pre& p) const {
+        const C c = p.c;
+        const C f = p.f;
         const T k2 = kt.k2(ix, iy, iz);
         const T k4 = k2 * k2;
         C out;
@@ -178,9 +200,9 @@ template <typename T, bool MIXED> struct ZOpCH {
             const T den = k4 * k.s2 + T(1);
             out = mkc<C>(re / den, im / den);
         } else {
-            const C co = chat_old[gi];
-            const C fo = fhat_old[gi];
-            const C Co = Chat_old[gi];
+            const C co = p.co;
+            const C fo = p.fo;
+            const C Co = p.Co;
             T re = c.x * T(4) - co.x, im = c.y * T(4) - co.y;
             const T a4 = k2 * k.s4, a2 = k2 * k.s2m;
             re -= a4 * f.x;
@@ -246,8 +268,16 @@ template <typename T, bool MIXED> struct ZOpCHRt {
         if (MIXED && blockIdx.x == 0 && blockIdx.y == 0) k0_update_block(k0, partials, np, ch.first, dt, invV);
     }
     __device__ void load(int, int, int, size_t gi, C* v) const { v[0] = ch.conv[gi]; }
+    __device__ const C* src(int) const { return ch.conv; }
+    using PreT = typename ZOpCH<T, MIXED>::Pre;
+    __device__ void pre(int, int, int, size_t gi, PreT& p) const { ch.pre(gi, p); }
+    __device__ void mid(int ix, int iy, int iz, size_t gi, const C* vi, C* vo, const PreT& p) const {
+        vo[0] = ch.update(ix, iy, iz, gi, vi[0], p);
+    }
     __device__ void mid(int ix, int iy, int iz, size_t gi, const C* vi, C* vo) const {
-        vo[0] = ch.update(ix, iy, iz, gi, vi[0]);
+        PreT p;
+        ch.pre(gi, p);
+        mid(ix, iy, iz, gi, vi, vo, p);
     }
     __device__ void store2(int, int, int, size_t gi, const C* v) const { out[gi] = v[0]; }
 };
@@ -267,10 +297,20 @@ template <typename T> struct ZOpFRt {
     int m, ny2, nz2;
     __device__ void prologue() const {}
     __device__ void load(int, int, int, size_t gi, C* v) const { v[0] = fin[gi]; }
+    __device__ const C* src(int) const { return fin; }
+    struct PreT {
+        C c;
+    };
+    __device__ void pre(int, int, int, size_t gi, PreT& p) const { p.c = chat[gi]; }
     __device__ void mid(int ix, int iy, int iz, size_t gi, const C* vi, C* vo) const {
+        PreT p;
+        pre(ix, iy, iz, gi, p);
+        mid(ix, iy, iz, gi, vi, vo, p);
+    }
+    __device__ void mid(int ix, int iy, int iz, size_t gi, const C* vi, C* vo, const PreT& p) const {
         const C f = vi[0];
         fhat_out[gi] = f;
-        const C c = chat[gi];
+        const C c = p.c;
         const T a = kt.k2(ix, iy, iz) * lam;
         vo[0] = mkc<C>(a * c.x + f.x, a * c.y + f.y);
         const T kx = kt.kx[ix], ky = kt.ky[iy], kz = kt.kz[iz];
@@ -291,6 +331,7 @@ template <typename T> struct ZOpProjRt {
     using C = cplx<T>;
     ZOpProj<T> pj;
     C* upre[3];
+    __device__ const C* src(int f) const { return pj.in[f]; }
     __device__ void prologue() const {}
     __device__ void load(int, int, int, size_t gi, C* v) const {
         v[0] = pj.in[0][gi];
@@ -601,7 +642,7 @@ template <typename T, bool MIXED> static void step_ch_t(fipi_ctx* ctx, int t) {
                        F<T>::sp(b.fhat_old), F<T>::sp(b.Chat_old), kt, k, t == 0 ? 1 : 0};
     ZOpCHRt<T, MIXED> zcr{zc, F<T>::S(ctx, 0), ctx->k0, ctx->partials, (g.ny / Tiles<T>::TY) * g.nz,
                           ctx->P.dt, 1.0 / (double)g.V};
-    launch_zrt<T, 1, 1, -1, TZ>(ctx, t == 0 ? "Z forward + IMEX update + inverse" : "Z forward + SBDF2 update + inverse",
+    launch_zrt<T, 1, 1, -1, 16 / (sizeof(T) / 4), true>(ctx, t == 0 ? "Z forward + IMEX update + inverse" : "Z forward + SBDF2 update + inverse",
                                 t == 0 ? 6 : 9, zcr);
     std::swap(b.chat, b.chat_old);  // chat = c^{n+1}, chat_old = c^n
     // B: Y inverse; X inverse c^{n+1} (stored) with f = (lambda/eps^2)(c^3 - c) and its
@@ -616,7 +657,7 @@ template <typename T, bool MIXED> static void step_ch_t(fipi_ctx* ctx, int t) {
     ZOpFRt<T> zf{F<T>::S(ctx, 1), F<T>::sp(b.fhat_old), F<T>::sp(b.chat),
                  {F<T>::S(ctx, 0), F<T>::S(ctx, 1), F<T>::S(ctx, 2), F<T>::S(ctx, 3)}, kt, k.lam, g.m, g.ny / 2,
                  g.nz / 2};
-    launch_zrt<T, 1, 4, -1, TZ / 2>(ctx, "Z forward f + inverse mu, grad", 7, zf);
+    launch_zrt<T, 1, 4, -1, 8 / (sizeof(T) / 4), false>(ctx, "Z forward f + inverse mu, grad", 7, zf);
     std::swap(b.fhat, b.fhat_old);  // fhat = f^{n+1}, fhat_old = f^n
 }
 
@@ -647,7 +688,7 @@ template <typename T> static void step_stokes_t(fipi_ctx* ctx) {
     ZOpProj<T> zp{{F<T>::S(ctx, 0), F<T>::S(ctx, 1), F<T>::S(ctx, 2)},
                   {F<T>::sp(b.uhat[0]), F<T>::sp(b.uhat[1]), F<T>::sp(b.uhat[2])}, kt, k.mu, g.m, g.ny / 2, g.nz / 2};
     ZOpProjRt<T> zpr{zp, {F<T>::sp(b.upre[0]), F<T>::sp(b.upre[1]), F<T>::sp(b.upre[2])}};
-    launch_zrt<T, 3, 3, -1, Tiles<T>::TZ>(ctx, "Z forward + projection + inverse", 9, zpr);
+    launch_zrt<T, 3, 3, -1, 16 / (sizeof(T) / 4), false>(ctx, "Z forward + projection + inverse", 9, zpr);
 }
 
 void fields_refresh_upre(fipi_ctx* ctx) {

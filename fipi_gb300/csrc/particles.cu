@@ -33,6 +33,11 @@
 
 namespace fipi {
 
+// Threads per block of the per-particle kernels of the step: 20,000
+// particles in 64-thread blocks reach every SM (256-thread blocks would
+// leave half of the 152 SMs idle).
+constexpr int kPT = 64;
+
 struct PC {
     int n;
     int nc[3];
@@ -323,13 +328,13 @@ static bool build_cells(fipi_ctx* ctx, const double* p_dev, bool want_it_mark = 
     const PC pc = make_pc(ctx);
     const int n = b.n;
     if (n <= 0) return false;
-    const int nb = (n + 255) / 256;
+    const int nb = (n + kPT - 1) / kPT;
     unsigned long long* ym = want_it_mark ? b.ymax : nullptr;
     // keys_alt holds the per-particle keys (by id), ids_alt the arrival slots, then the placed ids
     cudaMemsetAsync(b.cell_cnt, 0, sizeof(int) * (b.ncells + 1), ctx->stream);
-    { LaunchScope ls_(ctx, "cell keys + counts", 0.0); k_cells_count<<<nb, 256, 0, ctx->stream>>>(pc, p_dev, b.keys_alt, b.ids_alt, b.cell_cnt, ym, ctx->status); }
+    { LaunchScope ls_(ctx, "cell keys + counts", 0.0); k_cells_count<<<nb, kPT, 0, ctx->stream>>>(pc, p_dev, b.keys_alt, b.ids_alt, b.cell_cnt, ym, ctx->status); }
     { LaunchScope ls_(ctx, "cell offsets", 0.0); k_cells_scan<<<1, 1024, 0, ctx->stream>>>(b.cell_cnt, b.ncells, b.cell_off); }
-    { LaunchScope ls_(ctx, "cell placement", 0.0); k_cells_place<<<nb, 256, 0, ctx->stream>>>(pc, p_dev, b.keys_alt, b.ids_alt, b.cell_off, b.keys, ym); }
+    { LaunchScope ls_(ctx, "cell placement", 0.0); k_cells_place<<<nb, kPT, 0, ctx->stream>>>(pc, p_dev, b.keys_alt, b.ids_alt, b.cell_off, b.keys, ym); }
     { LaunchScope ls_(ctx, "cell order", 0.0); k_cells_order<<<(b.ncells * 32 + 255) / 256, 256, 0, ctx->stream>>>(b.cell_off, b.ncells, b.keys, b.ids, b.keys_alt, ym, b.it_mark); }
     std::swap(b.keys, b.keys_alt);  // sorted keys now in keys
     return want_it_mark;
@@ -929,7 +934,7 @@ static void spread_fx(fipi_ctx* ctx) {
         cudaMemsetAsync(b.sp_acc, 0, sizeof(unsigned long long) * 3 * V, ctx->stream);
         for (int a = 0; a < 3; ++a) cudaMemsetAsync(ctx->fb.fsp[a], 0, sizeof(float) * V, ctx->stream);
     }
-    { LaunchScope ls_(ctx, "spread fixed-point atomics", 0.0); k_spread_fx<<<(n + 255) / 256, 256, 0, ctx->stream>>>(pc, b.p, b.f_pp, V, b.sp_acc, b.sp_prev); }
+    { LaunchScope ls_(ctx, "spread fixed-point atomics", 0.0); k_spread_fx<<<(n + kPT - 1) / kPT, kPT, 0, ctx->stream>>>(pc, b.p, b.f_pp, V, b.sp_acc, b.sp_prev); }
     { LaunchScope ls_(ctx, "spread store", 0.0); k_spread_fx_store<<<(m + 255) / 256, 256, 0, ctx->stream>>>(b.sp_prev, m, V, b.sp_acc, f0, f1, f2); }
     b.sp_prev_valid = 1;
 }
@@ -969,7 +974,7 @@ static void f_pp_launch(fipi_ctx* ctx, const double* p, const double* rmp, const
     if (tau && !have_it_mark) it_mark_launch(ctx, p);
     const bool fast = sizeof(TA) == sizeof(float) && b.ncell[0] >= 4 && b.ncell[1] >= 4 && b.ncell[2] >= 4;
     if (fast) {
-        { LaunchScope ls_(ctx, "sorted FP32 positions", 0.0); k_sorted_pos<<<(b.n + 255) / 256, 256, 0, ctx->stream>>>(pc, p, b.keys, b.ids, b.spos); }
+        { LaunchScope ls_(ctx, "sorted FP32 positions", 0.0); k_sorted_pos<<<(b.n + kPT - 1) / kPT, kPT, 0, ctx->stream>>>(pc, p, b.keys, b.ids, b.spos); }
         { LaunchScope ls_(ctx, "contact forces (warp per cell)", 0.0); k_f_pp_fast<<<b.ncells, 32 * kFppRows, 0, ctx->stream>>>(pc, b.spos, b.cell_off, rmp, tau ? f_pi : nullptr, b.it_mark, f_pp, b.tau_part); }
     } else {
         { LaunchScope ls_(ctx, "contact forces (warp per cell)", 0.0); k_f_pp<TA, 0><<<blocks, 256, 0, ctx->stream>>>(pc, p, b.ids, b.cell_off, rmp, tau ? f_pi : nullptr, b.it_mark,
@@ -994,17 +999,17 @@ template <typename T> static void step_t(fipi_ctx* ctx) {
     ParticleBufs& b = ctx->pb;
     const PC pc = make_pc(ctx);
     const int n = b.n;
-    const int nb = (n + 255) / 256;
+    const int nb = (n + kPT - 1) / kPT;
     for (int stage = 1; stage <= 2; ++stage) {
         // interpolate_local_variables, sorting, compute_f_pi, compute_f_pp(t+1),
         // compute_f_ext (zero), advect, enforce_bc  (main.cpp:295-314); the
         // ramp(t+1, 0.2 t_end) factor is kept on the device (step_tick)
-        { LaunchScope ls_(ctx, "stage interpolate + f_pi", 0.0); k_stage_fpi<T, T><<<nb, 256, 0, ctx->stream>>>(pc, (const T*)ctx->fb.c, (const T*)ctx->fb.g[0],
+        { LaunchScope ls_(ctx, "stage interpolate + f_pi", 0.0); k_stage_fpi<T, T><<<nb, kPT, 0, ctx->stream>>>(pc, (const T*)ctx->fb.c, (const T*)ctx->fb.g[0],
                                                      (const T*)ctx->fb.g[1], (const T*)ctx->fb.g[2], b.p, b.f_pi,
                                                      b.r, b.cth); }
         const bool im = build_cells(ctx, b.p, ctx->track_tau);
         f_pp_launch<T>(ctx, b.p, ctx->d_rmp, b.f_pi, b.f_pp, ctx->track_tau, im);
-        { LaunchScope ls_(ctx, "stage advect + wrap", 0.0); k_stage_advect<<<nb, 256, 0, ctx->stream>>>(pc, stage, b.p, b.p_old, b.u_old, b.f_pi, b.f_pp, b.r,
+        { LaunchScope ls_(ctx, "stage advect + wrap", 0.0); k_stage_advect<<<nb, kPT, 0, ctx->stream>>>(pc, stage, b.p, b.p_old, b.u_old, b.f_pi, b.f_pp, b.r,
                                                     ctx->status); }
     }
 }

@@ -100,12 +100,39 @@ template <typename T, int NIN> struct OpC2RStore {
     }
 };
 
+// op.in(f) / op.out(f) for a run-time f through a chain of compile-time
+// indices: indexing a kernel parameter's pointer array with a run-time
+// value would copy the whole parameter to local memory.
+template <int NF, class Op> __device__ __forceinline__ auto in_sel(const Op& op, int f) {
+    auto p = op.in(0);
+#pragma unroll
+    for (int k = 1; k < NF; ++k)
+        if (f == k) p = op.in(k);
+    return p;
+}
+template <int NF, class Op> __device__ __forceinline__ auto out_sel(const Op& op, int f) {
+    auto p = op.out(0);
+#pragma unroll
+    for (int k = 1; k < NF; ++k)
+        if (f == k) p = op.out(k);
+    return p;
+}
+
 // Adapter giving point() an accumulator when the op does not take one.
 template <class Op> struct NoAcc {
     Op op;
     __device__ const auto* in(int f) const { return op.in(f); }
     __device__ auto* out(int f) const { return op.out(f); }
     template <class C, class A> __device__ void point(int z, int y, int n, C* v, A&) const { op.point(z, y, n, v); }
+};
+
+// The same access to the real inputs read straight from global memory.
+template <typename T, int NRF> struct XGlobalRow {
+    const T* p[NRF];
+    size_t row;  // element offset of the row
+    __device__ __forceinline__ cplx<T> get(int f, int n) const {
+        return reinterpret_cast<const cplx<T>*>(p[f] + row)[n];
+    }
 };
 
 // X pass: one block = TY consecutive rows y0..y0+TY-1 of plane z, NIN
@@ -115,7 +142,8 @@ template <class Op> struct NoAcc {
 // live in shared memory with one pad slot per 16 (pitch odd, so the
 // transposed column accesses are conflict-free); X_M sits at index M.
 template <typename T, int NIN, int NOUT, bool REDUCE, int M, class Op>
-__global__ void __launch_bounds__(kThreads, (NIN > NOUT ? NIN : NOUT) <= 3 ? 4 : 3)
+__global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? ((NIN > NOUT ? NIN : NOUT) <= 3 ? 4 : 3)
+                                                            : ((NIN > NOUT ? NIN : NOUT) <= 3 ? 3 : 2))
     k_xpass_acc(Geom g, const cplx<T>* __restrict__ twx, Op op,
                                                       double* partials) {
     using C = cplx<T>;
@@ -131,26 +159,13 @@ __global__ void __launch_bounds__(kThreads, (NIN > NOUT ? NIN : NOUT) <= 3 ? 4 :
     constexpr int Tn = FftPlan<M, FftE<T>::value>::Tn;
     constexpr int rpr = kThreads / Tn;  // row FFTs per round
     if constexpr (NIN > 0) {
+        // every element of the tile is requested before any is waited for
         const int n = NIN * H * TY;
-        for (int b = tid; b < n; b += 8 * kThreads) {
-            C tmp[8];
-#pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                const int i = b + u * kThreads;
-                if (i < n) {
-                    const int ty = i % TY, rest = i / TY, kx = rest % H, f = rest / H;
-                    tmp[u] = op.in(f)[((size_t)z * H + kx) * g.ny + y0 + ty];
-                }
-            }
-#pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                const int i = b + u * kThreads;
-                if (i < n) {
-                    const int ty = i % TY, rest = i / TY, kx = rest % H, f = rest / H;
-                    s[idx(f * TY + ty, kx)] = tmp[u];
-                }
-            }
+        for (int i = tid; i < n; i += kThreads) {
+            const int ty = i % TY, rest = i / TY, kx = rest % H, f = rest / H;
+            cp_async<sizeof(C)>(&s[idx(f * TY + ty, kx)], in_sel<NIN>(op, f) + ((size_t)z * H + kx) * g.ny + y0 + ty);
         }
+        cp_async_wait_all();
         __syncthreads();
         // C2R split pre-processing (only the real parts of X_0 and X_M enter).
         for (int i = tid; i < NIN * TY * (halfM + 1); i += nthr) {
@@ -219,7 +234,7 @@ __global__ void __launch_bounds__(kThreads, (NIN > NOUT ? NIN : NOUT) <= 3 ? 4 :
         const int n = NOUT * H * TY;
         for (int i = tid; i < n; i += nthr) {
             const int ty = i % TY, rest = i / TY, kx = rest % H, f = rest / H;
-            op.out(f)[((size_t)z * H + kx) * g.ny + y0 + ty] = s[idx(f * TY + ty, kx)];
+            out_sel<NOUT>(op, f)[((size_t)z * H + kx) * g.ny + y0 + ty] = s[idx(f * TY + ty, kx)];
         }
     }
 }
@@ -234,6 +249,7 @@ template <typename T> struct ZOpProj {
     using C = cplx<T>;
     const C* in[3];
     C* out[3];
+    __device__ const C* src(int f) const { return in[f]; }
     KTabs<T> kt;
     T mu;
     int m, ny2, nz2;
@@ -290,6 +306,7 @@ template <typename T, int NF> struct ZOpStore {
     const C* in[NF];
     C* out[NF];
     int zero_k0_mask;
+    __device__ const C* src(int f) const { return in[f]; }
     __device__ void load(int, int, int, size_t gi, C* v) const {
 #pragma unroll
         for (int f = 0; f < NF; ++f) v[f] = in[f][gi];
@@ -384,21 +401,37 @@ template <typename T, int NF, int DIR, class Op> void launch_z(fipi_ctx* ctx, co
     });
 }
 
-// Round-trip Z pass (k_zpass_rt): NF fields in, NB fields out.
-template <typename T, int NF, int NB, int DIR, int COLS, class Op>
+// Round-trip Z pass: NF fields in, NB fields out; WIDE: k_zpass_rt with
+// tiles of COLS ky columns (COLS <= 16 for FP32, whose grids have
+// ny >= 16, and <= 8 for FP64, ny >= 8), else k_zpass_rt_t.
+template <typename T, int NF, int NB, int DIR, int COLS, bool WIDE, class Op>
 void launch_zrt(fipi_ctx* ctx, const char* name, int nspec, const Op& op) {
     const Geom& g = ctx->g;
     LaunchScope ls(ctx, name, (double)nspec * g.SH * sizeof(cplx<T>));
+    if constexpr (!WIDE) {
+        dispatch_pow2(g.nz, [&](auto NC) {
+            constexpr int N = decltype(NC)::value;
+            using SHP = ZRtShapeT<T, N, COLS>;
+            constexpr int NS = NF > NB ? NF : NB;
+            const size_t smem = (size_t)NS * SHP::TZ * N * sizeof(cplx<T>);
+            dim3 grid(g.h, g.ny / SHP::TZ);
+            auto kern = k_zpass_rt_t<T, NF, NB, DIR, N, COLS, Op>;
+            static size_t granted = 48 * 1024;
+            ensure_smem(kern, smem, granted);
+            kern<<<grid, SHP::TZ * SHP::Tn, smem, ctx->stream>>>(g, (const cplx<T>*)ctx->fb.twz, op);
+        });
+        return;
+    } else
     dispatch_pow2(g.nz, [&](auto NC) {
         constexpr int N = decltype(NC)::value;
         using SHP = ZRtShape<T, N, COLS>;
         constexpr int NS = NF > NB ? NF : NB;
-        const size_t smem = (size_t)NS * SHP::TZ * N * sizeof(cplx<T>);
-        dim3 grid(g.h, g.ny / SHP::TZ);
+        const size_t smem = (size_t)NS * SHP::P * N * sizeof(cplx<T>);
+        dim3 grid(g.h, g.ny / COLS);
         auto kern = k_zpass_rt<T, NF, NB, DIR, N, COLS, Op>;
         static size_t granted = 48 * 1024;
         ensure_smem(kern, smem, granted);
-        kern<<<grid, SHP::TZ * SHP::Tn, smem, ctx->stream>>>(g, (const cplx<T>*)ctx->fb.twz, op);
+        kern<<<grid, SHP::THREADS, smem, ctx->stream>>>(g, (const cplx<T>*)ctx->fb.twz, op);
     });
 }
 

@@ -1,5 +1,6 @@
-// Bulk asynchronous copies (TMA, cp.async.bulk) into shared memory with
-// mbarrier completion, for sm_90+ / sm_103a, written as inline PTX.
+// Asynchronous copies into shared memory for sm_103a, as inline PTX: bulk
+// copies (TMA, cp.async.bulk) completing on an mbarrier, and per-thread
+// cp.async.
 //
 // Every wait is bounded: after kSpinLimit polls the caller gets `false`
 // and must report an error instead of waiting on.
@@ -63,5 +64,18 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
+
+// Per-thread asynchronous global -> shared copies (LDGSTS): many loads in
+// flight per thread without holding registers; completion by
+// cp.async.wait_all, then a block barrier.
+template <int BYTES> __device__ __forceinline__ void cp_async(void* dst, const void* src) {
+    static_assert(BYTES == 4 || BYTES == 8 || BYTES == 16, "cp.async moves 4, 8 or 16 bytes");
+    if constexpr (BYTES == 16)
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(smem_addr(dst)), "l"(src), "n"(BYTES)
+                     : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 }  // namespace fipi
