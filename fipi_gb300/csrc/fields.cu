@@ -20,6 +20,12 @@
 #include "ctx.hpp"
 #include "passes.cuh"
 
+#ifndef FIPI_EXP_S_CONV
+#define FIPI_EXP_S_CONV 2
+#define FIPI_EXP_S_CF 3
+#define FIPI_EXP_S_FORCE 1
+#endif
+
 namespace fipi {
 
 // ------------------------------------------------------------ X-pass ops
@@ -635,7 +641,7 @@ template <typename T, bool MIXED> static void step_ch_t(fipi_ctx* ctx, int t) {
     OpConv<T, MIXED> oc{{F<T>::S(ctx, 0), F<T>::S(ctx, 1), F<T>::S(ctx, 2)},
                         {(const T*)b.g[0], (const T*)b.g[1], (const T*)b.g[2]}, F<T>::S(ctx, 3), ctx->partials,
                         {(T*)ctx->tape_u[0], (T*)ctx->tape_u[1], (T*)ctx->tape_u[2]}, g.nx, g.ny};
-    launch_x<T, 3, 1, MIXED>(ctx, "X inverse u, conv, forward", 3, oc, ctx->partials);
+    launch_x<T, 3, 1, MIXED, OpConv<T, MIXED>, FIPI_EXP_S_CONV>(ctx, "X inverse u, conv, forward", 3, oc, ctx->partials);
     void* s1[1] = {b.S[3]};
     launch_y<T>(ctx, 1, s1, s1, -1);
     ZOpCH<T, MIXED> zc{F<T>::S(ctx, 3), F<T>::sp(b.chat), F<T>::sp(b.chat_old), F<T>::sp(b.fhat),
@@ -651,7 +657,7 @@ template <typename T, bool MIXED> static void step_ch_t(fipi_ctx* ctx, int t) {
     launch_y<T>(ctx, 1, s0, s0, +1);
     OpCF<T, MIXED> ocf{F<T>::S(ctx, 0), (T*)b.c, F<T>::S(ctx, 1), reinterpret_cast<const float*>(ctx->k0 + 4),
                        k.lam_eps, g.nx, g.ny};
-    launch_x<T, 1, 1, false>(ctx, "X inverse c, f, forward", 1, ocf);
+    launch_x<T, 1, 1, false, OpCF<T, MIXED>, FIPI_EXP_S_CF>(ctx, "X inverse c, f, forward", 1, ocf);
     void* s1b[1] = {b.S[1]};
     launch_y<T>(ctx, 1, s1b, s1b, -1);
     ZOpFRt<T> zf{F<T>::S(ctx, 1), F<T>::sp(b.fhat_old), F<T>::sp(b.chat),
@@ -682,7 +688,7 @@ template <typename T> static void step_stokes_t(fipi_ctx* ctx) {
                   {(const T*)b.fsp[0], (const T*)b.fsp[1], (const T*)b.fsp[2]},
                   (ctx->P.switch_particle && ctx->P.n_p > 0) ? 1 : 0,
                   k.rho1, k.rho2, k.gravity, (T*)ctx->tape_mu, g.nx, g.ny};
-    launch_x<T, 4, 3, false>(ctx, "X inverse mu,grad, force, forward", (of.spread ? 7 : 4), of);
+    launch_x<T, 4, 3, false, OpForce<T>, FIPI_EXP_S_FORCE>(ctx, "X inverse mu,grad, force, forward", (of.spread ? 7 : 4), of);
     void* s3[3] = {b.S[0], b.S[1], b.S[2]};
     launch_y<T>(ctx, 3, s3, s3, -1);
     ZOpProj<T> zp{{F<T>::S(ctx, 0), F<T>::S(ctx, 1), F<T>::S(ctx, 2)},
