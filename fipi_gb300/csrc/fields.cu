@@ -20,11 +20,6 @@
 #include "ctx.hpp"
 #include "passes.cuh"
 
-#ifndef FIPI_EXP_S_CONV
-#define FIPI_EXP_S_CONV 2
-#define FIPI_EXP_S_CF 3
-#define FIPI_EXP_S_FORCE 1
-#endif
 
 namespace fipi {
 
@@ -136,10 +131,14 @@ template <typename T> struct OpForce {
         const size_t row = ((size_t)z * ny + y) * nx;
         const C mu = v[0];
         if (tape_mu) reinterpret_cast<C*>(tape_mu + row)[n] = mu;
-        const C cc = r.get(0, n);
-        // buoyancy ((1+c)/2 rho1 + (1-c)/2 rho2) g, g = (0, 0, gravity)
-        const T b0 = ((cc.x + T(1)) / T(2)) * rho1 + ((cc.x * T(-1) + T(1)) / T(2)) * rho2;
-        const T b1 = ((cc.y + T(1)) / T(2)) * rho1 + ((cc.y * T(-1) + T(1)) / T(2)) * rho2;
+        // buoyancy ((1+c)/2 rho1 + (1-c)/2 rho2) g, g = (0, 0, gravity); with
+        // gravity = 0 it adds exactly zero and c is not read
+        T b0 = T(0), b1 = T(0);
+        if (gravity != T(0)) {
+            const C cc = r.get(0, n);
+            b0 = ((cc.x + T(1)) / T(2)) * rho1 + ((cc.x * T(-1) + T(1)) / T(2)) * rho2;
+            b1 = ((cc.y + T(1)) / T(2)) * rho1 + ((cc.y * T(-1) + T(1)) / T(2)) * rho2;
+        }
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             const C gd = v[1 + d];
@@ -150,9 +149,10 @@ template <typename T> struct OpForce {
                 f0 += sp.x;
                 f1 += sp.y;
             }
-            const T gz = (d == 2) ? gravity : T(0);
-            f0 += b0 * gz;
-            f1 += b1 * gz;
+            if (d == 2 && gravity != T(0)) {
+                f0 += b0 * gravity;
+                f1 += b1 * gravity;
+            }
             v[d] = mkc<C>(f0, f1);
         }
     }
@@ -631,7 +631,6 @@ template <typename T, bool MIXED> static void step_ch_t(fipi_ctx* ctx, int t) {
     FieldBufs& b = ctx->fb;
     const StepConsts<T> k = make_consts<T>(ctx);
     const KTabs<T> kt = F<T>::ktabs(ctx);
-    constexpr int TZ = Tiles<T>::TZ;
     // A: u^n (its Z inverse kept in upre by the previous step) -> Y inverse;
     //    X inverse with conv = u . grad c and the R2C of conv; Y forward;
     //    Z forward + CH update + Z inverse of c_hat^{n+1}
@@ -641,7 +640,7 @@ template <typename T, bool MIXED> static void step_ch_t(fipi_ctx* ctx, int t) {
     OpConv<T, MIXED> oc{{F<T>::S(ctx, 0), F<T>::S(ctx, 1), F<T>::S(ctx, 2)},
                         {(const T*)b.g[0], (const T*)b.g[1], (const T*)b.g[2]}, F<T>::S(ctx, 3), ctx->partials,
                         {(T*)ctx->tape_u[0], (T*)ctx->tape_u[1], (T*)ctx->tape_u[2]}, g.nx, g.ny};
-    launch_x<T, 3, 1, MIXED, OpConv<T, MIXED>, FIPI_EXP_S_CONV>(ctx, "X inverse u, conv, forward", 3, oc, ctx->partials);
+    launch_x<T, 3, 1, MIXED>(ctx, "X inverse u, conv, forward", 3, oc, ctx->partials);
     void* s1[1] = {b.S[3]};
     launch_y<T>(ctx, 1, s1, s1, -1);
     ZOpCH<T, MIXED> zc{F<T>::S(ctx, 3), F<T>::sp(b.chat), F<T>::sp(b.chat_old), F<T>::sp(b.fhat),
@@ -657,7 +656,7 @@ template <typename T, bool MIXED> static void step_ch_t(fipi_ctx* ctx, int t) {
     launch_y<T>(ctx, 1, s0, s0, +1);
     OpCF<T, MIXED> ocf{F<T>::S(ctx, 0), (T*)b.c, F<T>::S(ctx, 1), reinterpret_cast<const float*>(ctx->k0 + 4),
                        k.lam_eps, g.nx, g.ny};
-    launch_x<T, 1, 1, false, OpCF<T, MIXED>, FIPI_EXP_S_CF>(ctx, "X inverse c, f, forward", 1, ocf);
+    launch_x<T, 1, 1, false>(ctx, "X inverse c, f, forward", 1, ocf);
     void* s1b[1] = {b.S[1]};
     launch_y<T>(ctx, 1, s1b, s1b, -1);
     ZOpFRt<T> zf{F<T>::S(ctx, 1), F<T>::sp(b.fhat_old), F<T>::sp(b.chat),
@@ -688,7 +687,9 @@ template <typename T> static void step_stokes_t(fipi_ctx* ctx) {
                   {(const T*)b.fsp[0], (const T*)b.fsp[1], (const T*)b.fsp[2]},
                   (ctx->P.switch_particle && ctx->P.n_p > 0) ? 1 : 0,
                   k.rho1, k.rho2, k.gravity, (T*)ctx->tape_mu, g.nx, g.ny};
-    launch_x<T, 4, 3, false, OpForce<T>, FIPI_EXP_S_FORCE>(ctx, "X inverse mu,grad, force, forward", (of.spread ? 7 : 4), of);
+    // real arrays: grad c written; the spread grid and c (buoyancy) read when they matter
+    const int nreal = 3 + (of.spread ? 3 : 0) + (ctx->P.gravity != 0.0 ? 1 : 0);
+    launch_x<T, 4, 3, false>(ctx, "X inverse mu,grad, force, forward", nreal, of);
     void* s3[3] = {b.S[0], b.S[1], b.S[2]};
     launch_y<T>(ctx, 3, s3, s3, -1);
     ZOpProj<T> zp{{F<T>::S(ctx, 0), F<T>::S(ctx, 1), F<T>::S(ctx, 2)},

@@ -301,9 +301,12 @@ __global__ void k_cells_place(PC pc, const double* __restrict__ p, const unsigne
     }
 }
 
-// One warp per cell: rank of each id among the cell's ids.
-__global__ void k_cells_order(const int* __restrict__ off, int ncells, const unsigned* __restrict__ tmp,
-                              unsigned* ids, unsigned* skeys, unsigned long long* ymax, int* it_mark) {
+// One warp per cell: rank of each id among the cell's ids.  With spos the
+// sorted cell-relative FP32 positions of the mixed-form contact forces are
+// written as well (what k_sorted_pos computes).
+__global__ void k_cells_order(PC pc, const double* __restrict__ p, const int* __restrict__ off, int ncells,
+                              const unsigned* __restrict__ tmp, unsigned* ids, unsigned* skeys,
+                              unsigned long long* ymax, int* it_mark, float4* spos) {
     const int cell = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (ymax && blockIdx.x == 0 && threadIdx.x == 0) {
@@ -313,17 +316,28 @@ __global__ void k_cells_order(const int* __restrict__ off, int ncells, const uns
     }
     if (cell >= ncells) return;
     const int beg = off[cell], end = off[cell + 1];
+    const int cx = cell % pc.nc[0], cy = (cell / pc.nc[0]) % pc.nc[1], cz = cell / (pc.nc[0] * pc.nc[1]);
+    const int n = pc.n;
     for (int e = beg + lane; e < end; e += 32) {
         const unsigned id = tmp[e];
         int r = 0;
         for (int j = beg; j < end; ++j) r += tmp[j] < id;
         ids[beg + r] = id;
         skeys[beg + r] = (unsigned)cell;
+        if (spos) {
+            float4 v;
+            v.x = (float)(p[id] - cx * pc.dc[0]);
+            v.y = (float)(p[n + id] - cy * pc.dc[1]);
+            v.z = (float)(p[2 * n + id] - cz * pc.dc[2]);
+            v.w = __int_as_float((int)id);
+            spos[beg + r] = v;
+        }
     }
 }
 
 // Returns true when it also computed it_mark (asked for by `want_it_mark`).
-static bool build_cells(fipi_ctx* ctx, const double* p_dev, bool want_it_mark = false) {
+// With spos the sorted FP32 positions of the mixed-form contact forces too.
+static bool build_cells(fipi_ctx* ctx, const double* p_dev, bool want_it_mark = false, float4* spos = nullptr) {
     ParticleBufs& b = ctx->pb;
     const PC pc = make_pc(ctx);
     const int n = b.n;
@@ -335,7 +349,7 @@ static bool build_cells(fipi_ctx* ctx, const double* p_dev, bool want_it_mark = 
     { LaunchScope ls_(ctx, "cell keys + counts", 0.0); k_cells_count<<<nb, kPT, 0, ctx->stream>>>(pc, p_dev, b.keys_alt, b.ids_alt, b.cell_cnt, ym, ctx->status); }
     { LaunchScope ls_(ctx, "cell offsets", 0.0); k_cells_scan<<<1, 1024, 0, ctx->stream>>>(b.cell_cnt, b.ncells, b.cell_off); }
     { LaunchScope ls_(ctx, "cell placement", 0.0); k_cells_place<<<nb, kPT, 0, ctx->stream>>>(pc, p_dev, b.keys_alt, b.ids_alt, b.cell_off, b.keys, ym); }
-    { LaunchScope ls_(ctx, "cell order", 0.0); k_cells_order<<<(b.ncells * 32 + 255) / 256, 256, 0, ctx->stream>>>(b.cell_off, b.ncells, b.keys, b.ids, b.keys_alt, ym, b.it_mark); }
+    { LaunchScope ls_(ctx, "cell order", 0.0); k_cells_order<<<(b.ncells * 32 + 255) / 256, 256, 0, ctx->stream>>>(pc, p_dev, b.cell_off, b.ncells, b.keys, b.ids, b.keys_alt, ym, b.it_mark, spos); }
     std::swap(b.keys, b.keys_alt);  // sorted keys now in keys
     return want_it_mark;
 }
@@ -732,6 +746,40 @@ __global__ void k_stage_fpi(PC pc, const TF* __restrict__ c, const TF* __restric
     for (int a = 0; a < 3; ++a) f_pi[a * n + i] = fpi[a];
 }
 
+// Stage 1's advection and wrap followed, for the same particle, by stage 2's
+// interpolation of c, grad c and f_pi at the new position (k_stage_advect
+// with stage = 1, then k_stage_fpi).
+template <typename TF, typename TA>
+__global__ void k_stage_advect1_fpi2(PC pc, double* p, double* p_old, double* u_old, double* f_pi,
+                                     const double* __restrict__ f_pp, const double* __restrict__ r,
+                                     const double* __restrict__ cth, const TF* __restrict__ c,
+                                     const TF* __restrict__ g0, const TF* __restrict__ g1,
+                                     const TF* __restrict__ g2, int* status) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = pc.n;
+    if (i >= n) return;
+    double pp[3] = {p[i], p[n + i], p[2 * n + i]};
+    double po[3], uo[3];
+    const double fpi[3] = {f_pi[i], f_pi[n + i], f_pi[2 * n + i]};
+    const double fpp[3] = {f_pp[i], f_pp[n + i], f_pp[2 * n + i]};
+    advect_one(pc, 1, fpi, fpp, r[i], pp, po, uo);
+    for (int a = 0; a < 3; ++a) {
+        p[a * n + i] = pp[a];
+        p_old[a * n + i] = po[a];
+        u_old[a * n + i] = uo[a];
+    }
+    if (!(isfinite(pp[0]) && isfinite(pp[1]) && isfinite(pp[2]))) {
+        atomicOr(status, ERR_NONFINITE);
+        return;
+    }
+    const TF* fl[4] = {c, g0, g1, g2};
+    TA vals[4];
+    interp_fields<TF, TA>(pc, pp[0], pp[1], pp[2], fl, 4, vals);
+    double f2[3];
+    f_pi_of(pc, (double)vals[0], (double)vals[1], (double)vals[2], (double)vals[3], r[i], cth[i], f2);
+    for (int a = 0; a < 3; ++a) f_pi[a * n + i] = f2[a];
+}
+
 // Stage part 2: advect with this stage's f_pi + f_pp, then wrap.
 __global__ void k_stage_advect(PC pc, int stage, double* p, double* p_old, double* u_old,
                                const double* __restrict__ f_pi, const double* __restrict__ f_pp,
@@ -964,17 +1012,22 @@ static void it_mark_launch(fipi_ctx* ctx, const double* p) {
 // compute_f_pp; with `tau` the packing energy of cluster.cpp:350-353 is
 // accumulated per particle (tau_part) and summed when it is asked for.
 // TA = float with at least 4 cells per axis takes the FP32 cell-relative path.
+static bool f_pp_fast_path(const fipi_ctx* ctx, bool fp32) {
+    const ParticleBufs& b = ctx->pb;
+    return fp32 && b.ncell[0] >= 4 && b.ncell[1] >= 4 && b.ncell[2] >= 4;
+}
+
 template <typename TA>
 static void f_pp_launch(fipi_ctx* ctx, const double* p, const double* rmp, const double* f_pi, double* f_pp, bool tau,
-                        bool have_it_mark = false) {
+                        bool have_it_mark = false, bool have_spos = false) {
     ParticleBufs& b = ctx->pb;
     const PC pc = make_pc(ctx);
     const int warps = b.ncells;
     const int blocks = (warps * 32 + 255) / 256;
     if (tau && !have_it_mark) it_mark_launch(ctx, p);
-    const bool fast = sizeof(TA) == sizeof(float) && b.ncell[0] >= 4 && b.ncell[1] >= 4 && b.ncell[2] >= 4;
+    const bool fast = f_pp_fast_path(ctx, sizeof(TA) == sizeof(float));
     if (fast) {
-        { LaunchScope ls_(ctx, "sorted FP32 positions", 0.0); k_sorted_pos<<<(b.n + kPT - 1) / kPT, kPT, 0, ctx->stream>>>(pc, p, b.keys, b.ids, b.spos); }
+        if (!have_spos) { LaunchScope ls_(ctx, "sorted FP32 positions", 0.0); k_sorted_pos<<<(b.n + kPT - 1) / kPT, kPT, 0, ctx->stream>>>(pc, p, b.keys, b.ids, b.spos); }
         { LaunchScope ls_(ctx, "contact forces (warp per cell)", 0.0); k_f_pp_fast<<<b.ncells, 32 * kFppRows, 0, ctx->stream>>>(pc, b.spos, b.cell_off, rmp, tau ? f_pi : nullptr, b.it_mark, f_pp, b.tau_part); }
     } else {
         { LaunchScope ls_(ctx, "contact forces (warp per cell)", 0.0); k_f_pp<TA, 0><<<blocks, 256, 0, ctx->stream>>>(pc, p, b.ids, b.cell_off, rmp, tau ? f_pi : nullptr, b.it_mark,
@@ -1000,17 +1053,28 @@ template <typename T> static void step_t(fipi_ctx* ctx) {
     const PC pc = make_pc(ctx);
     const int n = b.n;
     const int nb = (n + kPT - 1) / kPT;
+    const T* c = (const T*)ctx->fb.c;
+    const T* g0 = (const T*)ctx->fb.g[0];
+    const T* g1 = (const T*)ctx->fb.g[1];
+    const T* g2 = (const T*)ctx->fb.g[2];
+    float4* spos = f_pp_fast_path(ctx, sizeof(T) == sizeof(float)) ? b.spos : nullptr;
+    // per stage: interpolate_local_variables, sorting, compute_f_pi,
+    // compute_f_pp(t+1), compute_f_ext (zero), advect, enforce_bc
+    // (main.cpp:295-314); the ramp(t+1, 0.2 t_end) factor is kept on the
+    // device (step_tick).  Stage 1's advection and stage 2's interpolation
+    // run in one kernel.
+    { LaunchScope ls_(ctx, "stage interpolate + f_pi", 0.0); k_stage_fpi<T, T><<<nb, kPT, 0, ctx->stream>>>(pc, c, g0, g1, g2, b.p, b.f_pi, b.r, b.cth); }
     for (int stage = 1; stage <= 2; ++stage) {
-        // interpolate_local_variables, sorting, compute_f_pi, compute_f_pp(t+1),
-        // compute_f_ext (zero), advect, enforce_bc  (main.cpp:295-314); the
-        // ramp(t+1, 0.2 t_end) factor is kept on the device (step_tick)
-        { LaunchScope ls_(ctx, "stage interpolate + f_pi", 0.0); k_stage_fpi<T, T><<<nb, kPT, 0, ctx->stream>>>(pc, (const T*)ctx->fb.c, (const T*)ctx->fb.g[0],
-                                                     (const T*)ctx->fb.g[1], (const T*)ctx->fb.g[2], b.p, b.f_pi,
-                                                     b.r, b.cth); }
-        const bool im = build_cells(ctx, b.p, ctx->track_tau);
-        f_pp_launch<T>(ctx, b.p, ctx->d_rmp, b.f_pi, b.f_pp, ctx->track_tau, im);
-        { LaunchScope ls_(ctx, "stage advect + wrap", 0.0); k_stage_advect<<<nb, kPT, 0, ctx->stream>>>(pc, stage, b.p, b.p_old, b.u_old, b.f_pi, b.f_pp, b.r,
-                                                    ctx->status); }
+        const bool im = build_cells(ctx, b.p, ctx->track_tau, spos);
+        f_pp_launch<T>(ctx, b.p, ctx->d_rmp, b.f_pi, b.f_pp, ctx->track_tau, im, spos != nullptr);
+        if (stage == 1) {
+            LaunchScope ls_(ctx, "stage advect + interpolate + f_pi", 0.0);
+            k_stage_advect1_fpi2<T, T><<<nb, kPT, 0, ctx->stream>>>(pc, b.p, b.p_old, b.u_old, b.f_pi, b.f_pp, b.r,
+                                                                     b.cth, c, g0, g1, g2, ctx->status);
+        } else {
+            LaunchScope ls_(ctx, "stage advect + wrap", 0.0);
+            k_stage_advect<<<nb, kPT, 0, ctx->stream>>>(pc, 2, b.p, b.p_old, b.u_old, b.f_pi, b.f_pp, b.r, ctx->status);
+        }
     }
 }
 

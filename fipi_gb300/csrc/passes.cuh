@@ -135,22 +135,21 @@ template <typename T, int NRF> struct XGlobalRow {
     }
 };
 
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N> __device__ __forceinline__ void cp_async_wait_group() {
-    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
-}
-
 // X pass: one block = TY consecutive rows y0..y0+TY-1 of plane z, NIN
 // spectral inputs (transposed runs of TY along y, C2R) and NOUT spectral
 // outputs (R2C, transposed store); point() does the fused real-space work
 // and may accumulate an FP64 per-block sum.  Rows of M = nx/2 complex pairs
 // live in shared memory with one pad slot per 16 (pitch odd, so the
 // transposed column accesses are conflict-free); X_M sits at index M.
-template <typename T, int NIN, int NOUT, bool REDUCE, int M, class Op>
-__global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? ((NIN > NOUT ? NIN : NOUT) <= 3 ? 4 : 3)
-                                                            : ((NIN > NOUT ? NIN : NOUT) <= 3 ? 3 : 2))
-    k_xpass_acc(Geom g, const cplx<T>* __restrict__ twx, Op op,
-                                                      double* partials) {
+// Blocks per SM the register budget is set for: FP32 4 (3 with four
+// fields), FP64 3 (2).  512-thread blocks measured slower.
+template <typename T, int NF, int NT> struct XMinBlocks {
+    static constexpr int value = sizeof(T) == 4 ? (NF <= 3 ? 4 : 3) : (NF <= 3 ? 3 : 2);
+};
+
+template <typename T, int NIN, int NOUT, bool REDUCE, int M, class Op, int NT = kThreads>
+__global__ void __launch_bounds__(NT, XMinBlocks<T, (NIN > NOUT ? NIN : NOUT), NT>::value)
+    k_xpass_acc(Geom g, const cplx<T>* __restrict__ twx, Op op, double* partials) {
     using C = cplx<T>;
     constexpr int TY = Tiles<T>::TY;
     constexpr int NF = NIN > NOUT ? NIN : NOUT;
@@ -162,11 +161,11 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? ((NIN > NOUT ? NIN 
     const int tid = threadIdx.x, nthr = blockDim.x;
     constexpr int halfM = M / 2;
     constexpr int Tn = FftPlan<M, FftE<T>::value>::Tn;
-    constexpr int rpr = kThreads / Tn;  // row FFTs per round
+    constexpr int rpr = NT / Tn;  // row FFTs per round
     if constexpr (NIN > 0) {
         // every element of the tile is requested before any is waited for
         const int n = NIN * H * TY;
-        for (int i = tid; i < n; i += kThreads) {
+        for (int i = tid; i < n; i += NT) {
             const int ty = i % TY, rest = i / TY, kx = rest % H, f = rest / H;
             cp_async<sizeof(C)>(&s[idx(f * TY + ty, kx)], in_sel<NIN>(op, f) + ((size_t)z * H + kx) * g.ny + y0 + ty);
         }
@@ -242,126 +241,6 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? ((NIN > NOUT ? NIN 
             out_sel<NOUT>(op, f)[((size_t)z * H + kx) * g.ny + y0 + ty] = s[idx(f * TY + ty, kx)];
         }
     }
-}
-
-// Persistent X pass with an S-stage cp.async pipeline: each block walks
-// tiles (z, y-tile) with the loads of the next S - 1 tiles in flight while
-// it transforms the current one; a tile's stage buffer is also its FFT
-// buffer.  The per-tile work is that of k_xpass_acc.  Commit groups are
-// issued one per tile (empty past the end) so cp.async.wait_group S - 1
-// always means "this tile has landed".
-template <typename T, int NIN, int NOUT, bool REDUCE, int M, int S, class Op>
-__global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? ((NIN > NOUT ? NIN : NOUT) <= 3 ? 4 : 3)
-                                                            : ((NIN > NOUT ? NIN : NOUT) <= 3 ? 3 : 2))
-    k_xpass_pipe(Geom g, const cplx<T>* __restrict__ twx, Op op, double* partials) {
-    static_assert(NIN > 0, "the pipeline streams spectral inputs");
-    using C = cplx<T>;
-    constexpr int TY = Tiles<T>::TY;
-    constexpr int NF = NIN > NOUT ? NIN : NOUT;
-    constexpr int H = M + 1;
-    constexpr int halfM = M / 2;
-    constexpr int Tn = FftPlan<M, FftE<T>::value>::Tn;
-    constexpr int rpr = kThreads / Tn;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    C* s0 = reinterpret_cast<C*>(smem_raw);
-    const IdxPadded idx{xpass_pitch(M)};
-    const size_t BUF = (size_t)NF * TY * xpass_pitch(M);
-    const int tid = threadIdx.x, nthr = blockDim.x;
-    const int tiles_y = g.ny / TY;
-    const long long ntiles = (long long)tiles_y * g.nz;
-    auto load_tile = [&](long long tile, C* s) {
-        const int z = (int)(tile / tiles_y), y0 = (int)(tile % tiles_y) * TY;
-        for (int i = tid; i < NIN * H * TY; i += nthr) {
-            const int ty = i % TY, rest = i / TY, kx = rest % H, f = rest / H;
-            cp_async<sizeof(C)>(&s[idx(f * TY + ty, kx)], in_sel<NIN>(op, f) + ((size_t)z * H + kx) * g.ny + y0 + ty);
-        }
-    };
-    for (int j = 0; j < S - 1; ++j) {
-        const long long tl = blockIdx.x + (long long)j * gridDim.x;
-        if (tl < ntiles) load_tile(tl, s0 + j * BUF);
-        cp_async_commit();
-    }
-    int st = 0;
-    const T invV = T(1) / T(g.V);
-    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        __syncthreads();  // the previous tile (its buffer is refilled next) is finished
-        {
-            const long long tl = tile + (long long)(S - 1) * gridDim.x;
-            if (tl < ntiles) load_tile(tl, s0 + ((st + S - 1) % S) * BUF);
-            cp_async_commit();
-        }
-        cp_async_wait_group<S - 1>();
-        __syncthreads();
-        C* s = s0 + st * BUF;
-        const int z = (int)(tile / tiles_y), y0 = (int)(tile % tiles_y) * TY;
-        for (int i = tid; i < NIN * TY * (halfM + 1); i += nthr) {
-            const int k = i % (halfM + 1);
-            const int row = i / (halfM + 1);
-            if (k == 0) {
-                const T a = s[idx(row, 0)].x, c = s[idx(row, M)].x;
-                s[idx(row, 0)] = mkc<C>(a + c, a - c);
-            } else {
-                const int km = M - k;
-                const C Xk = s[idx(row, k)], Xm = s[idx(row, km)];
-                const C Wk = twx[k], Wm = twx[km];
-                const C A = cadd(Xk, cconj(Xm)), B = csub(Xk, cconj(Xm));
-                const C A2 = cadd(Xm, cconj(Xk)), B2 = csub(Xm, cconj(Xk));
-                s[idx(row, k)] = cadd(A, cmul_i(cmul(B, cconj(Wk)), +1));
-                if (km != k) s[idx(row, km)] = cadd(A2, cmul_i(cmul(B2, cconj(Wm)), +1));
-            }
-        }
-        __syncthreads();
-        for (int r0 = 0; r0 < NIN * TY; r0 += rpr) {
-            const int row = r0 + tid / Tn;
-            smem_fft2<T, +1, M>(s, idx, row, tid % Tn, row < NIN * TY, twx, 2);
-        }
-        T acc = T(0);
-        for (int i = tid; i < TY * M; i += nthr) {
-            const int n = i % M;
-            const int ty = i / M;
-            C v[NF];
-#pragma unroll
-            for (int f = 0; f < NIN; ++f) v[f] = cscale(s[idx(f * TY + ty, n)], invV);
-            op.point(z, y0 + ty, n, v, acc);
-#pragma unroll
-            for (int f = 0; f < NOUT; ++f) s[idx(f * TY + ty, n)] = v[f];
-        }
-        if constexpr (REDUCE) {
-            const double bs = block_sum((double)acc);
-            if (tid == 0) partials[tile] = bs;
-        }
-        __syncthreads();
-        if constexpr (NOUT > 0) {
-            for (int r0 = 0; r0 < NOUT * TY; r0 += rpr) {
-                const int row = r0 + tid / Tn;
-                smem_fft2<T, -1, M>(s, idx, row, tid % Tn, row < NOUT * TY, twx, 2);
-            }
-            for (int i = tid; i < NOUT * TY * (halfM + 1); i += nthr) {
-                const int k = i % (halfM + 1);
-                const int row = i / (halfM + 1);
-                if (k == 0) {
-                    const C Z0 = s[idx(row, 0)];
-                    s[idx(row, 0)] = mkc<C>(Z0.x + Z0.y, T(0));
-                    s[idx(row, M)] = mkc<C>(Z0.x - Z0.y, T(0));
-                } else {
-                    const int km = M - k;
-                    const C Zk = s[idx(row, k)], Zm = s[idx(row, km)];
-                    const C Wk = twx[k], Wm = twx[km];
-                    const C E1 = cadd(Zk, cconj(Zm)), D1 = csub(Zk, cconj(Zm));
-                    const C E2 = cadd(Zm, cconj(Zk)), D2 = csub(Zm, cconj(Zk));
-                    s[idx(row, k)] = cscale(csub(E1, cmul_i(cmul(Wk, D1), +1)), T(0.5));
-                    if (km != k) s[idx(row, km)] = cscale(csub(E2, cmul_i(cmul(Wm, D2), +1)), T(0.5));
-                }
-            }
-            __syncthreads();
-            for (int i = tid; i < NOUT * H * TY; i += nthr) {
-                const int ty = i % TY, rest = i / TY, kx = rest % H, f = rest / H;
-                out_sel<NOUT>(op, f)[((size_t)z * H + kx) * g.ny + y0 + ty] = s[idx(f * TY + ty, kx)];
-            }
-        }
-        st = (st + 1) % S;
-    }
-    cp_async_wait_all();
 }
 
 // Z forward with the Leray projection (main.cpp:274-275) fused:
@@ -462,38 +341,21 @@ template <typename T> struct F {
 };
 
 // nreal: real (V-sized) arrays the fused point operation reads or writes.
-// S = 1: one block per tile (k_xpass_acc); S >= 2: persistent blocks with
-// an S-stage pipeline (k_xpass_pipe).
-template <typename T, int NIN, int NOUT, bool REDUCE, class Op, int S = 1>
+// One block per tile of Tiles<T>::TY rows; NT threads per block.
+template <typename T, int NIN, int NOUT, bool REDUCE, class Op, int NT = kThreads>
 void launch_x(fipi_ctx* ctx, const char* name, int nreal, const Op& op, double* partials = nullptr) {
     const Geom& g = ctx->g;
     LaunchScope ls(ctx, name,
                    (double)(NIN + NOUT) * g.SH * sizeof(cplx<T>) + (double)nreal * g.V * sizeof(T));
     constexpr int NF = NIN > NOUT ? NIN : NOUT;
-    const size_t buf = (size_t)NF * Tiles<T>::TY * xpass_pitch(g.m) * sizeof(cplx<T>);
+    const size_t smem = (size_t)NF * Tiles<T>::TY * xpass_pitch(g.m) * sizeof(cplx<T>);
+    dim3 grid(g.ny / Tiles<T>::TY, g.nz);
     dispatch_pow2(g.m, [&](auto MC) {
         constexpr int M = decltype(MC)::value;
-        if constexpr (S == 1 || NIN == 0) {
-            dim3 grid(g.ny / Tiles<T>::TY, g.nz);
-            auto kern = k_xpass_acc<T, NIN, NOUT, REDUCE, M, Op>;
-            static size_t granted = 48 * 1024;
-            ensure_smem(kern, buf, granted);
-            kern<<<grid, kThreads, buf, ctx->stream>>>(g, (const cplx<T>*)ctx->fb.twx, op, partials);
-        } else {
-            auto kern = k_xpass_pipe<T, NIN, NOUT, REDUCE, M, S, Op>;
-            const size_t smem = S * buf;
-            static size_t granted = 48 * 1024;
-            static int per_sm = 0;
-            ensure_smem(kern, smem, granted);
-            if (!per_sm) {
-                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem);
-                if (per_sm < 1) per_sm = 1;
-            }
-            const long long tiles = (long long)(g.ny / Tiles<T>::TY) * g.nz;
-            long long grid = (long long)ctx->num_sms * per_sm;
-            if (grid > tiles) grid = tiles;
-            kern<<<(unsigned)grid, kThreads, smem, ctx->stream>>>(g, (const cplx<T>*)ctx->fb.twx, op, partials);
-        }
+        auto kern = k_xpass_acc<T, NIN, NOUT, REDUCE, M, Op, NT>;
+        static size_t granted = 48 * 1024;
+        ensure_smem(kern, smem, granted);
+        kern<<<grid, NT, smem, ctx->stream>>>(g, (const cplx<T>*)ctx->fb.twx, op, partials);
     });
 }
 

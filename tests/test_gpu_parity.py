@@ -251,3 +251,33 @@ def test_out_of_range_particle_reports_error(fipi):
         assert e.value.code == 4
         with pytest.raises(fipi.FipiError):
             s.cells_build(p)
+
+
+def test_full_size_512_forms_agree(fipi):
+    """The 512³, 200,000-sphere workload (polydisperse radii, contact angles)
+    at full size, where the oracle cannot follow: both forms run, stay
+    finite, agree with each other to mixed-precision accuracy, keep the same
+    mass history, and the FP64 form is deterministic."""
+    w = fipi.workload("cfg3_512")
+    P, c, p, r, ct = seeded_state(w, 3)
+    res = {}
+    for prec in ("fp64", "mixed"):
+        with fipi.Simulation(P, prec) as s:
+            s.set_phase(c)
+            s.set_particles(p, r, ct)
+            m0 = s.mass()
+            s.step(2)
+            res[prec] = (s.get_phase(), s.get_particles()[0], s.mass(), m0)
+    a, b = res["mixed"], res["fp64"]
+    assert np.isfinite(a[0]).all() and np.isfinite(b[0]).all()
+    assert rel_l2(a[0], b[0]) < 1e-5
+    L = np.array([P.lx, P.ly, P.lz])
+    d = np.abs(a[1] - b[1]).reshape(-1, 3)
+    assert np.minimum(d, L - d).max() < 1e-5
+    scale = np.abs(c).sum() * P.lx * P.ly * P.lz / w.V
+    assert abs((a[2] - a[3]) - (b[2] - b[3])) < 1e-12 * scale
+    with fipi.Simulation(P, "fp64") as s:
+        s.set_phase(c)
+        s.set_particles(p, r, ct)
+        s.step(2)
+        assert np.array_equal(s.get_phase(), b[0])
