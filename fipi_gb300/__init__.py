@@ -12,12 +12,15 @@ from .lib import (  # noqa: F401
     declared_symbols,
     load,
     reference_params,
+    free_energy_density,
     seed_particles,
     seed_phase,
+    vtk_write_field,
+    vtk_write_particles,
 )
 
 __all__ = [
     "FipiParams", "Workload", "WORKLOADS", "workload", "reference_head", "FipiError",
     "Simulation", "cell_geometry", "declared_symbols", "load", "reference_params",
-    "seed_particles", "seed_phase",
+    "seed_particles", "seed_phase", "vtk_write_field", "vtk_write_particles", "free_energy_density",
 ]

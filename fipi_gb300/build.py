@@ -24,6 +24,7 @@ UNITS = {
     "fields.cu": [],
     "adjoint.cu": [],
     "particles.cu": ["-fmad=false"],
+    "vtk.cu": ["-Xcompiler", "-ffp-contract=off"],
 }
 
 

@@ -437,6 +437,8 @@ fipi_status fipi_step_async(fipi_ctx* ctx, int nsteps) {
     if (!ctx) return set_error(ctx, FIPI_ERR_BAD_ARG, "ctx is NULL");
     if (nsteps < 0) return set_error(ctx, FIPI_ERR_BAD_ARG, "nsteps < 0");
     if (!ctx->have_phase) return set_error(ctx, FIPI_ERR_STATE, "fipi_set_phase must come before fipi_step");
+    if (ctx->substep != 0)
+        return set_error(ctx, FIPI_ERR_STATE, "an iteration begun with fipi_step_ch is not finished");
     FIPI_CUDA(ctx, cudaSetDevice(ctx->device));
     for (int s = 0; s < nsteps; ++s) {
         const bool spread_ready = ctx->pb.sp_prev_valid || ctx->pb.n == 0 || !ctx->P.switch_particle;
@@ -461,6 +463,39 @@ fipi_status fipi_sync(fipi_ctx* ctx) {
 fipi_status fipi_step(fipi_ctx* ctx, int nsteps) {
     fipi_status st = fipi_step_async(ctx, nsteps);
     if (st != FIPI_OK) return st;
+    return check_status(ctx);
+}
+
+// The three parts of one iteration (direct launches), in the order of
+// enqueue_step; fipi_step_particles ends the iteration.
+fipi_status fipi_step_ch(fipi_ctx* ctx) {
+    if (!ctx) return set_error(ctx, FIPI_ERR_BAD_ARG, "ctx is NULL");
+    if (!ctx->have_phase) return set_error(ctx, FIPI_ERR_STATE, "fipi_set_phase must come first");
+    if (ctx->substep != 0) return set_error(ctx, FIPI_ERR_STATE, "fipi_step_ch must start an iteration");
+    FIPI_CUDA(ctx, cudaSetDevice(ctx->device));
+    fields_step_ch(ctx, ctx->t);  // main.cpp:176-238
+    ctx->substep = 1;
+    return check_status(ctx);
+}
+
+fipi_status fipi_step_stokes(fipi_ctx* ctx) {
+    if (!ctx) return set_error(ctx, FIPI_ERR_BAD_ARG, "ctx is NULL");
+    if (ctx->substep != 1) return set_error(ctx, FIPI_ERR_STATE, "fipi_step_stokes must follow fipi_step_ch");
+    FIPI_CUDA(ctx, cudaSetDevice(ctx->device));
+    particles_spread(ctx);      // main.cpp:266
+    fields_step_stokes(ctx);    // main.cpp:243-278
+    ctx->substep = 2;
+    return check_status(ctx);
+}
+
+fipi_status fipi_step_particles(fipi_ctx* ctx) {
+    if (!ctx) return set_error(ctx, FIPI_ERR_BAD_ARG, "ctx is NULL");
+    if (ctx->substep != 2) return set_error(ctx, FIPI_ERR_STATE, "fipi_step_particles must follow fipi_step_stokes");
+    FIPI_CUDA(ctx, cudaSetDevice(ctx->device));
+    particles_step(ctx);        // main.cpp:283-316
+    step_tick(ctx);
+    ctx->t += 1;
+    ctx->substep = 0;
     return check_status(ctx);
 }
 
@@ -617,6 +652,12 @@ fipi_status fipi_advect(fipi_ctx* ctx, int stage, const double* f_pi, const doub
     if (ctx->pb.n == 0) return FIPI_OK;
     FIPI_CUDA(ctx, cudaSetDevice(ctx->device));
     return particles_advect(ctx, stage, f_pi, f_pp, r, p, p_old, u_old);
+}
+
+fipi_status fipi_wrap(fipi_ctx* ctx, double* p) {
+    if (!ctx || (!p && ctx->pb.n > 0)) return set_error(ctx, FIPI_ERR_BAD_ARG, "NULL argument");
+    FIPI_CUDA(ctx, cudaSetDevice(ctx->device));
+    return particles_wrap(ctx, p);
 }
 
 fipi_status fipi_spread(fipi_ctx* ctx, const double* p, const double* f_pp, double* out) {

@@ -185,6 +185,7 @@ struct fipi_ctx {
         long long launches = 0;
     } graphs[2];
     bool use_graphs = true;
+    int substep = 0;           // 1 after fipi_step_ch, 2 after fipi_step_stokes
     bool have_phase = false;
     bool track_tau = true;     // packing energy during the step (cluster.cpp:350-353)
     size_t device_bytes = 0;
@@ -212,6 +213,7 @@ fipi_status fields_get_velocity(fipi_ctx* ctx, double* u_host);
 void fields_step_ch(fipi_ctx* ctx, int t);        // conv, CH update, c, f
 void fields_step_stokes(fipi_ctx* ctx);           // mu, grad c, force, projection
 void fields_refresh_upre(fipi_ctx* ctx);          // after u_hat changed outside the step
+fipi_status fields_get_grad(fipi_ctx* ctx, double* g_host);  // grad c of the state, 3 x V
 fipi_status fields_mass(fipi_ctx* ctx, double* out);
 fipi_status fields_free_energy(fipi_ctx* ctx, double* out);
 // Fine-grained transforms on host arrays.
@@ -249,6 +251,8 @@ fipi_status particles_spread_host(fipi_ctx* ctx, const double* p, const double* 
                                   double* out);
 // Packing energy of the last contact-force evaluation.
 fipi_status particles_packing_tau(fipi_ctx* ctx, double* out);
+fipi_status particles_get_radii(fipi_ctx* ctx, double* r_host);
+fipi_status particles_wrap(fipi_ctx* ctx, double* p_host);
 
 // Reverse mode (adjoint.cu / particles.cu).
 void enqueue_step(fipi_ctx* ctx);  // one forward step, direct launches

@@ -621,6 +621,17 @@ template <typename T> static fipi_status get_velocity_t(fipi_ctx* ctx, double* u
     return download<T>(ctx, ur, u_host, (size_t)g.V * 3);
 }
 
+fipi_status fields_get_grad(fipi_ctx* ctx, double* g_host) {
+    const size_t V = (size_t)ctx->g.V;
+    for (int d = 0; d < 3; ++d) {
+        fipi_status st = ctx->prec == FIPI_MIXED
+                             ? download<float>(ctx, (const float*)ctx->fb.g[d], g_host + d * V, V)
+                             : download<double>(ctx, (const double*)ctx->fb.g[d], g_host + d * V, V);
+        if (st != FIPI_OK) return st;
+    }
+    return FIPI_OK;
+}
+
 fipi_status fields_get_velocity(fipi_ctx* ctx, double* u_host) {
     return ctx->prec == FIPI_MIXED ? get_velocity_t<float>(ctx, u_host) : get_velocity_t<double>(ctx, u_host);
 }

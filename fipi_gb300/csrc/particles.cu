@@ -1202,6 +1202,31 @@ static fipi_status read_status(fipi_ctx* ctx) {
     return FIPI_OK;
 }
 
+__global__ void k_wrap_many(PC pc, double* p) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= pc.n) return;
+    for (int a = 0; a < 3; ++a) p[3 * i + a] = fmod(p[3 * i + a] + pc.L[a], pc.L[a]);  // element.cpp:271-280
+}
+
+fipi_status particles_wrap(fipi_ctx* ctx, double* p_host) {
+    const int n = ctx->pb.n;
+    if (n == 0) return FIPI_OK;
+    DevScratch ds{ctx};
+    double* pd = ds.get<double>(3 * (size_t)n);
+    if (!pd) return set_error(ctx, FIPI_ERR_CUDA, "cudaMalloc failed");
+    FIPI_CUDA(ctx, h2d(ctx, pd, p_host, sizeof(double) * 3 * n));
+    const PC pc = make_pc(ctx);
+    { LaunchScope ls_(ctx, "wrap", 0.0); k_wrap_many<<<(n + kPT - 1) / kPT, kPT, 0, ctx->stream>>>(pc, pd); }
+    FIPI_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    FIPI_CUDA(ctx, d2h(ctx, p_host, pd, sizeof(double) * 3 * n));
+    return FIPI_OK;
+}
+
+fipi_status particles_get_radii(fipi_ctx* ctx, double* r_host) {
+    FIPI_CUDA(ctx, d2h(ctx, r_host, ctx->pb.r, sizeof(double) * ctx->pb.n));
+    return FIPI_OK;
+}
+
 fipi_status particles_cells_build(fipi_ctx* ctx, const double* p, int* keys, int* sorted, int* offsets) {
     ParticleBufs& b = ctx->pb;
     const int n = b.n;

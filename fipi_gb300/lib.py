@@ -57,6 +57,10 @@ _SIGS = {
     "fipi_get_time": (ctypes.c_int, [_vp, _ip]),
     "fipi_step": (ctypes.c_int, [_vp, ctypes.c_int]),
     "fipi_step_async": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "fipi_step_ch": (ctypes.c_int, [_vp]),
+    "fipi_step_stokes": (ctypes.c_int, [_vp]),
+    "fipi_step_particles": (ctypes.c_int, [_vp]),
+    "fipi_wrap": (ctypes.c_int, [_vp, _dp]),
     "fipi_sync": (ctypes.c_int, [_vp]),
     "fipi_stream": (ctypes.c_int, [_vp, ctypes.POINTER(_vp)]),
     "fipi_mass": (ctypes.c_int, [_vp, _dp]),
@@ -78,6 +82,12 @@ _SIGS = {
     "fipi_kernel_stats": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_char_p, ctypes.c_int,
                                          ctypes.POINTER(ctypes.c_longlong), _dp, _dp]),
     "fipi_launch_count": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_longlong)]),
+    "fipi_vtk_write_field": (ctypes.c_int, [ctypes.POINTER(FipiParams), ctypes.c_char_p, ctypes.c_char_p,
+                                            ctypes.c_int, _dp]),
+    "fipi_vtk_write_particles": (ctypes.c_int, [ctypes.POINTER(FipiParams), ctypes.c_char_p, ctypes.c_int, _dp,
+                                                _dp, _dp]),
+    "fipi_free_energy_density": (ctypes.c_int, [ctypes.POINTER(FipiParams), _dp, _dp, _dp]),
+    "fipi_write_vtk": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_char_p]),
     "fipi_checkpoint_reserve": (ctypes.c_int, [_vp, ctypes.c_int]),
     "fipi_checkpoint_bytes": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_size_t)]),
     "fipi_checkpoint_save": (ctypes.c_int, [_vp, ctypes.c_int]),
@@ -172,6 +182,28 @@ def seed_phase(params: FipiParams, seed: int, mean: float = 0.0, amp: float = 0.
     return c
 
 
+def vtk_write_field(params: FipiParams, path, name: str, values, components: int = 1):
+    """field::output_to_file of the reference (no device needed)."""
+    v = _f64(values, components * params.nx * params.ny * params.nz)
+    _check(load().fipi_vtk_write_field(ctypes.byref(params), str(path).encode(), name.encode(), components, _d(v)))
+
+
+def vtk_write_particles(params: FipiParams, path, p, r=None, f_pp=None):
+    """cluster::output of the reference (no device needed)."""
+    n = params.n_p
+    pp = _f64(p, 3 * n)
+    fp = _f64(f_pp if f_pp is not None else np.zeros(3 * n), 3 * n)
+    _check(load().fipi_vtk_write_particles(ctypes.byref(params), str(path).encode(), n, _d(pp),
+                                           _d(_f64(r, n)), _d(fp)))
+
+
+def free_energy_density(params: FipiParams, c, grad_c) -> np.ndarray:
+    V = params.nx * params.ny * params.nz
+    out = np.empty(V)
+    _check(load().fipi_free_energy_density(ctypes.byref(params), _d(_f64(c, V)), _d(_f64(grad_c, 3 * V)), _d(out)))
+    return out
+
+
 def seed_particles(params: FipiParams, seed: int, r_range=None, theta_range_deg=None,
                    allow_overlap: bool = False):
     n = params.n_p
@@ -253,6 +285,20 @@ class Simulation:
     def step(self, n: int = 1):
         _check(self.lib.fipi_step(self.h, n))
 
+    def step_ch(self):
+        _check(self.lib.fipi_step_ch(self.h))
+
+    def step_stokes(self):
+        _check(self.lib.fipi_step_stokes(self.h))
+
+    def step_particles(self):
+        _check(self.lib.fipi_step_particles(self.h))
+
+    def wrap(self, p) -> np.ndarray:
+        out = _f64(p, 3 * self.n).copy()
+        _check(self.lib.fipi_wrap(self.h, _d(out)))
+        return out
+
     def step_async(self, n: int = 1):
         _check(self.lib.fipi_step_async(self.h, n))
 
@@ -305,6 +351,11 @@ class Simulation:
         n = ctypes.c_longlong()
         _check(self.lib.fipi_launch_count(self.h, ctypes.byref(n)))
         return n.value
+
+    def write_vtk(self, what: str, path):
+        """VTK file of the current state: 'phase', 'free_energy', 'u' or 'particles'."""
+        code = {"phase": 0, "free_energy": 1, "u": 2, "particles": 3}[what]
+        _check(self.lib.fipi_write_vtk(self.h, code, str(path).encode()))
 
     # ---------------------------------------------------------------- checkpoints
     def checkpoint_reserve(self, slots: int):

@@ -136,6 +136,15 @@ fipi_status fipi_step(fipi_ctx* ctx, int nsteps);
  * fipi_sync, fipi_step or state read. */
 fipi_status fipi_step_async(fipi_ctx* ctx, int nsteps);
 fipi_status fipi_sync(fipi_ctx* ctx);
+/* The three parts of one iteration, for callers that interleave their own
+ * work between them: the Cahn-Hilliard update (main.cpp:176-238), the
+ * spreading and Stokes solve (main.cpp:243-278), the two particle stages
+ * (main.cpp:283-316, ending the iteration: t += 1).  In this order they give
+ * the same results as fipi_step(ctx, 1); any other order is
+ * FIPI_ERR_STATE, and so is fipi_step while an iteration is open. */
+fipi_status fipi_step_ch(fipi_ctx* ctx);
+fipi_status fipi_step_stokes(fipi_ctx* ctx);
+fipi_status fipi_step_particles(fipi_ctx* ctx);
 /* The CUDA stream the context runs on (as a void*: cudaStream_t). */
 fipi_status fipi_stream(const fipi_ctx* ctx, void** stream);
 
@@ -208,6 +217,9 @@ fipi_status fipi_f_pi(fipi_ctx* ctx, const double* c_loc, const double* dcdx, co
  * p, p_old, u_old are updated in place (n_p x 3). */
 fipi_status fipi_advect(fipi_ctx* ctx, int stage, const double* f_pi, const double* f_pp,
                         const double* r, double* p, double* p_old, double* u_old);
+/* element::enforce_bc (element.cpp:271-280) / cluster::enforce_bc:
+ * p = fmod(p + L, L) per axis, n_p x 3 in place. */
+fipi_status fipi_wrap(fipi_ctx* ctx, double* p);
 /* cluster::compute_f_r (cluster.cpp:438-504): trilinear spreading of
  * f_pp / (dx dy dz) onto the grid, out: 3 x V.  Deterministic: per grid
  * node the contributions are summed in ascending particle id. */
@@ -237,6 +249,30 @@ fipi_status fipi_spread(fipi_ctx* ctx, const double* p, const double* f_pp, doub
 #define FIPI_NOALLOC_MAX_PARTICLES 65536
 fipi_status fipi_cells_build_noalloc(const fipi_params* p, const double* d_pos, int* d_keys,
                                      int* d_sorted, int* d_offsets, void* stream);
+
+/* ------------------------------------------------------------- VTK output
+ * The reference's output step (main.cpp:225-238): legacy ASCII VTK files
+ * written by field::output_to_file (field.cpp:469-503) and cluster::output
+ * (cluster.cpp:415-456).  The host writers below produce, for the same
+ * values, the same bytes as the reference.  They need no device. */
+/* Structured-points field: components 1 (SCALARS, V values) or 3 (VECTORS,
+ * 3 x V values, component-major like field::v), named `name`. */
+fipi_status fipi_vtk_write_field(const fipi_params* p, const char* path, const char* name, int components,
+                                 const double* values);
+/* Particles: positions / dx, radii / dx (r NULL = r_p) and
+ * |f_pp| / A / pi / sigma / r_p; pos and f_pp are n x 3. */
+fipi_status fipi_vtk_write_particles(const fipi_params* p, const char* path, int n, const double* pos,
+                                     const double* r, const double* f_pp);
+/* The free-energy density field lambda (0.5 |grad c|^2 + 0.25/eps^2 (c^2-1)^2)
+ * of main.cpp:232 (c: V, grad_c: 3 x V, out: V). */
+fipi_status fipi_free_energy_density(const fipi_params* p, const double* c, const double* grad_c, double* out);
+/* The context's current state: the phase field ("phase"), the free-energy
+ * density ("free_energy"), the velocity ("u") or the particles. */
+#define FIPI_VTK_PHASE 0
+#define FIPI_VTK_FREE_ENERGY 1
+#define FIPI_VTK_VELOCITY 2
+#define FIPI_VTK_PARTICLES 3
+fipi_status fipi_write_vtk(fipi_ctx* ctx, int what, const char* path);
 
 /* ------------------------------------------------------------ checkpoints
  * No counterpart in the reference (it has no checkpoint or restart).  A

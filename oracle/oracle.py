@@ -250,6 +250,13 @@ def advect(params, stage, f_pi_, f_pp_, r, p, p_old, u_old):
     return p, p_old, u_old
 
 
+def enforce_bc(params, p):
+    """element::enforce_bc on n x 3 positions (a copy)."""
+    q = np.ascontiguousarray(p, np.float64).ravel().copy()
+    port_lib().oracle_enforce_bc(ctypes.byref(params), q.size // 3, _d(q))
+    return q
+
+
 def spread(params, p, f_pp_):
     n = len(p) // 3
     V = params.nx * params.ny * params.nz
@@ -288,6 +295,24 @@ class Ref:
         L.ref_f_pi.argtypes = [ctypes.c_int, _dp, _dp, _dp, _dp]
         L.ref_advect.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, _dp, _dp, _dp]
         L.ref_spread.argtypes = [_dp, _dp, _dp]
+        L.ref_write_field.argtypes = [_dp, ctypes.c_int, ctypes.c_char_p, ctypes.c_char_p]
+        L.ref_write_free_energy.argtypes = [_dp, _dp, ctypes.c_char_p]
+        L.ref_write_particles.argtypes = [_dp, _dp, _dp, ctypes.c_char_p]
+
+    def write_field(self, values, components, name, path):
+        v = np.ascontiguousarray(values, np.float64).ravel()
+        self.lib.ref_write_field(_d(v), components, name.encode(), str(path).encode())
+
+    def write_free_energy(self, c, g, path):
+        c = np.ascontiguousarray(c, np.float64).ravel()
+        g = np.ascontiguousarray(g, np.float64).ravel()
+        self.lib.ref_write_free_energy(_d(c), _d(g), str(path).encode())
+
+    def write_particles(self, p, r, f_pp, path):
+        p = np.ascontiguousarray(p, np.float64).ravel()
+        r = None if r is None else np.ascontiguousarray(r, np.float64).ravel()
+        f = np.ascontiguousarray(f_pp, np.float64).ravel()
+        self.lib.ref_write_particles(_d(p), _d(r), _d(f), str(path).encode())
 
     def config(self):
         out = np.zeros(27)

@@ -102,7 +102,9 @@ def build(name: str, force: bool = False) -> Path:
     hdr = OUT / f"cfg_{name}.hpp"
     text = config_header(w)
     lib = lib_path(name)
-    if lib.exists() and hdr.exists() and hdr.read_text() == text and not force:
+    deps = [HERE / "ref_harness.cpp", HERE / "fftw_shim.c", HERE / "fftw3.h", ORACLE / "fft_c2c.c", Path(__file__)]
+    fresh = lib.exists() and all(d.stat().st_mtime <= lib.stat().st_mtime for d in deps)
+    if fresh and hdr.exists() and hdr.read_text() == text and not force:
         return lib
     hdr.write_text(text)
     objdir = OUT / f"obj_{name}"

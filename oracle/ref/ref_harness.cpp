@@ -372,4 +372,43 @@ void ref_spread(const double* p, const double* f_pp, double* out) {
     for (int d = 0; d < 3; ++d) get_real(fr, d, out + d * V);
 }
 
+/* ------------------------------------------------------------ VTK output */
+/* field::output_to_file (field.cpp:469-503) of given values. */
+int ref_write_field(const double* values, int components, const char* name, const char* path) {
+    field a(components == 1 ? "SCALARS" : "VECTORS");
+    for (int d = 0; d < components; ++d)
+        for (long it = 0; it < V; ++it) {
+            a.v[d][it][0] = values[d * V + it];
+            a.v[d][it][1] = 0.0;
+        }
+    a.output_to_file(path, name);
+    return 0;
+}
+
+/* The free-energy field of main.cpp:232 from c and grad c, written like main.cpp:233. */
+int ref_write_free_energy(const double* c, const double* g, const char* path) {
+    field cc("SCALARS"), gc("VECTORS"), fe("SCALARS");
+    for (long it = 0; it < V; ++it) {
+        cc.v[0][it][0] = c[it];
+        cc.v[0][it][1] = 0.0;
+        for (int d = 0; d < 3; ++d) {
+            gc.v[d][it][0] = g[d * V + it];
+            gc.v[d][it][1] = 0.0;
+        }
+    }
+    fe = lambda * (0.5 * gc.power(2.0) + 0.25 / sqr(epsilon) * (cc.power(2.0) - 1.0).power(2.0));
+    fe.output_to_file(path, "free_energy");
+    return 0;
+}
+
+/* cluster::output (cluster.cpp:415-456) of given particles. */
+int ref_write_particles(const double* p, const double* r, const double* f_pp, const char* path) {
+    if (!g_sim) g_sim = new Sim();
+    load_particles(g_sim->suspension, p, r);
+    for (int it = 0; it < N_p; ++it)
+        g_sim->suspension.particle[it].f_pp.set_value(f_pp[3 * it], f_pp[3 * it + 1], f_pp[3 * it + 2]);
+    g_sim->suspension.output(path);
+    return 0;
+}
+
 }  // extern "C"

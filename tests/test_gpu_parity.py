@@ -281,3 +281,67 @@ def test_full_size_512_forms_agree(fipi):
         s.set_particles(p, r, ct)
         s.step(2)
         assert np.array_equal(s.get_phase(), b[0])
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_substeps_equal_step(fipi, prec):
+    """fipi_step_ch + fipi_step_stokes + fipi_step_particles == fipi_step(1),
+    bit for bit; out-of-order calls are refused."""
+    w = fipi.workload("t32")
+    P, c, p, r, ct = seeded_state(w, 31)
+    res = []
+    for split in (False, True):
+        with fipi.Simulation(P, prec) as s:
+            s.set_phase(c)
+            s.set_particles(p, r, ct)
+            for _ in range(3):
+                if split:
+                    s.step_ch()
+                    s.step_stokes()
+                    s.step_particles()
+                else:
+                    s.step(1)
+            res.append((s.get_phase(), s.get_velocity(), s.get_particles()[0], s.time))
+            if split:
+                with pytest.raises(fipi.FipiError):
+                    s.step_stokes()
+                s.step_ch()
+                with pytest.raises(fipi.FipiError):
+                    s.step(1)
+    for a, b in zip(res[0], res[1]):
+        assert np.array_equal(a, b)
+
+
+def test_wrap_matches_oracle(fipi, oracle_mod):
+    w = fipi.workload("t32")
+    P = w.params()
+    rng = np.random.default_rng(8)
+    p = (rng.random(3 * w.n_p) * 3 - 1) * 32.0  # inside and outside [0, L)
+    with fipi.Simulation(P, "fp64") as s:
+        got = s.wrap(p)
+    assert np.array_equal(got, oracle_mod.enforce_bc(P, p))
+
+
+def test_write_vtk_from_context(fipi, tmp_path):
+    w = fipi.workload("t32")
+    P, c, p, r, ct = seeded_state(w, 33)
+    with fipi.Simulation(P, "fp64") as s:
+        s.set_phase(c)
+        s.set_particles(p, r, ct)
+        s.write_vtk("phase", tmp_path / "a.vtk")
+        fipi.vtk_write_field(P, tmp_path / "b.vtk", "phase", c, 1)
+        assert (tmp_path / "a.vtk").read_bytes() == (tmp_path / "b.vtk").read_bytes()
+        s.step(2)
+        s.write_vtk("u", tmp_path / "u.vtk")
+        fipi.vtk_write_field(P, tmp_path / "u2.vtk", "u", s.get_velocity(), 3)
+        assert (tmp_path / "u.vtk").read_bytes() == (tmp_path / "u2.vtk").read_bytes()
+        s.write_vtk("particles", tmp_path / "p.vtk")
+        pos, fpp, _ = s.get_particles()
+        fipi.vtk_write_particles(P, tmp_path / "p2.vtk", pos, r, fpp)
+        assert (tmp_path / "p.vtk").read_bytes() == (tmp_path / "p2.vtk").read_bytes()
+        s.write_vtk("free_energy", tmp_path / "fe.vtk")
+        lines = (tmp_path / "fe.vtk").read_text().splitlines()
+        assert lines[9] == "SCALARS free_energy double" and len(lines) == 11 + w.V
+        vals = np.array([float(x) for x in lines[11:]])
+        dx = P.lx / P.nx
+        assert abs(vals.sum() * dx ** 3 - s.free_energy()) < 1e-4 * abs(s.free_energy())
