@@ -37,20 +37,6 @@
 namespace fipi {
 
 // ------------------------------------------------------------ X-pass ops
-// R2C of NF real fields.
-template <typename T, int NF> struct OpR2CN {
-    using C = cplx<T>;
-    const T* src[NF];
-    C* o[NF];
-    int nx, ny;
-    __device__ C* out(int f) const { return o[f]; }
-    __device__ const C* in(int) const { return nullptr; }
-    __device__ void point(int z, int y, int n, C* v) const {
-        const size_t row = ((size_t)z * ny + y) * nx;
-#pragma unroll
-        for (int f = 0; f < NF; ++f) v[f] = reinterpret_cast<const C*>(src[f] + row)[n];
-    }
-};
 
 // Stokes part reversed (see the file comment); in: lamF spectra (3),
 // out: R2C of [L_c, L_mu, L_g0, L_g1, L_g2]; lamF is also stored real.

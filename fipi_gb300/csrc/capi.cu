@@ -654,6 +654,20 @@ fipi_status fipi_advect(fipi_ctx* ctx, int stage, const double* f_pi, const doub
     return particles_advect(ctx, stage, f_pi, f_pp, r, p, p_old, u_old);
 }
 
+fipi_status fipi_interpolate2(fipi_ctx* ctx, const double* fields, int nfields, const double* p, double* out) {
+    if (!ctx || !fields || !out || nfields < 1 || (!p && ctx->pb.n > 0))
+        return set_error(ctx, FIPI_ERR_BAD_ARG, "bad argument");
+    FIPI_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (ctx->pb.n == 0) return FIPI_OK;
+    return particles_interpolate2(ctx, fields, nfields, p, out);
+}
+
+fipi_status fipi_div(fipi_ctx* ctx, const double* v, double* out) {
+    if (!ctx || !v || !out) return set_error(ctx, FIPI_ERR_BAD_ARG, "NULL argument");
+    FIPI_CUDA(ctx, cudaSetDevice(ctx->device));
+    return fields_div(ctx, v, out);
+}
+
 fipi_status fipi_wrap(fipi_ctx* ctx, double* p) {
     if (!ctx || (!p && ctx->pb.n > 0)) return set_error(ctx, FIPI_ERR_BAD_ARG, "NULL argument");
     FIPI_CUDA(ctx, cudaSetDevice(ctx->device));

@@ -220,6 +220,7 @@ fipi_status fields_free_energy(fipi_ctx* ctx, double* out);
 fipi_status fields_fft_r2c(fipi_ctx* ctx, const double* in, double* out);
 fipi_status fields_fft_c2r(fipi_ctx* ctx, const double* in, double* out);
 fipi_status fields_grad(fipi_ctx* ctx, const double* c, double* out);
+fipi_status fields_div(fipi_ctx* ctx, const double* v, double* out);
 // Device pointers of the real fields used by the particle side (T-typed).
 const void* fields_real_c(fipi_ctx* ctx);
 const void* fields_real_grad(fipi_ctx* ctx, int d);
@@ -243,6 +244,8 @@ fipi_status particles_pairs(fipi_ctx* ctx, const double* p, int* pairs, int max_
                             int* n_pairs);
 fipi_status particles_interpolate(fipi_ctx* ctx, const double* fields, int nfields,
                                   const double* p, double* out);
+fipi_status particles_interpolate2(fipi_ctx* ctx, const double* fields, int nfields,
+                                   const double* p, double* out);
 fipi_status particles_f_pi(fipi_ctx* ctx, const double* c_loc, const double* dcdx,
                            const double* r, const double* cth, double* f_pi);
 fipi_status particles_advect(fipi_ctx* ctx, int stage, const double* f_pi, const double* f_pp,

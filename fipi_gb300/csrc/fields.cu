@@ -821,6 +821,61 @@ fipi_status fields_grad(fipi_ctx* ctx, const double* c, double* out) {
     return ctx->prec == FIPI_MIXED ? grad_t<float>(ctx, c, out) : grad_t<double>(ctx, c, out);
 }
 
+// field::div (field.cpp:332-361) + field::ifft, real part: the divergence
+// of a real vector field.  The reference leaves the Nyquist index in; its
+// contribution to the inverse transform is purely imaginary (i k_d at the
+// self-conjugate Nyquist plane of d), so the real part equals the inverse
+// with that plane zeroed, which is what the round-trip Z pass forms.
+template <typename T> struct ZOpDivRt {
+    using C = cplx<T>;
+    const C* in[3];
+    C* out;
+    KTabs<T> kt;
+    int m, ny2, nz2;
+    __device__ const C* src(int f) const { return in[f]; }
+    __device__ void prologue() const {}
+    __device__ void load(int, int, int, size_t gi, C* v) const {
+        v[0] = in[0][gi];
+        v[1] = in[1][gi];
+        v[2] = in[2][gi];
+    }
+    __device__ void mid(int ix, int iy, int iz, size_t, const C* vi, C* vo) const {
+        const T k[3] = {ix == m ? T(0) : kt.kx[ix], iy == ny2 ? T(0) : kt.ky[iy], iz == nz2 ? T(0) : kt.kz[iz]};
+        T re = T(0), im = T(0);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            re += -k[d] * vi[d].y;
+            im += k[d] * vi[d].x;
+        }
+        vo[0] = mkc<C>(re, im);
+    }
+    __device__ void store2(int, int, int, size_t gi, const C* v) const { out[gi] = v[0]; }
+};
+
+template <typename T> static fipi_status div_t(fipi_ctx* ctx, const double* v, double* out) {
+    const Geom& g = ctx->g;
+    T* tmp = (T*)ctx->fb.ureal;
+    fipi_status st = upload<T>(ctx, v, tmp, (size_t)g.V * 3);
+    if (st != FIPI_OK) return st;
+    OpR2CN<T, 3> op{{tmp, tmp + g.V, tmp + 2 * g.V}, {F<T>::S(ctx, 0), F<T>::S(ctx, 1), F<T>::S(ctx, 2)}, g.nx, g.ny};
+    launch_x<T, 0, 3, false>(ctx, "X forward", 3, NoAcc<OpR2CN<T, 3>>{op});
+    void* s3[3] = {ctx->fb.S[0], ctx->fb.S[1], ctx->fb.S[2]};
+    launch_y<T>(ctx, 3, s3, s3, -1);
+    ZOpDivRt<T> zd{{F<T>::S(ctx, 0), F<T>::S(ctx, 1), F<T>::S(ctx, 2)}, F<T>::S(ctx, 3), F<T>::ktabs(ctx), g.m,
+                   g.ny / 2, g.nz / 2};
+    launch_zrt<T, 3, 1, -1, 16 / (sizeof(T) / 4), false>(ctx, "Z forward + div + inverse", 4, zd);
+    void* s1[1] = {ctx->fb.S[3]};
+    launch_y<T>(ctx, 1, s1, s1, +1);
+    OpC2RStore<T, 1> oc{{F<T>::S(ctx, 3)}, {tmp}, g.nx, g.ny};
+    launch_x<T, 1, 0, false>(ctx, "X inverse store", 1, NoAcc<OpC2RStore<T, 1>>{oc});
+    FIPI_CUDA(ctx, cudaGetLastError());
+    return download<T>(ctx, tmp, out, (size_t)g.V);
+}
+
+fipi_status fields_div(fipi_ctx* ctx, const double* v, double* out) {
+    return ctx->prec == FIPI_MIXED ? div_t<float>(ctx, v, out) : div_t<double>(ctx, v, out);
+}
+
 const void* fields_real_c(fipi_ctx* ctx) { return ctx->fb.c; }
 const void* fields_real_grad(fipi_ctx* ctx, int d) { return ctx->fb.g[d]; }
 void* fields_spread_target(fipi_ctx* ctx, int d) { return ctx->fb.fsp[d]; }

@@ -1335,7 +1335,26 @@ fipi_status particles_pairs(fipi_ctx* ctx, const double* p, int* pairs, int max_
     return FIPI_OK;
 }
 
-template <typename T>
+// field::interpolate2 (field.cpp:250-281): the trilinear products on the
+// fractions m/3 + 1/3 of a size-3 stencil whose corners are the nodes i + 1
+// and i + 2 (periodic), dead code in the reference's loop.
+template <typename TF, typename TA>
+__device__ __forceinline__ TA interp2(const PC& pc, double x, double y, double z, const TF* __restrict__ v) {
+    const int size = 3;
+    const double fx = floor(x / pc.dx), fy = floor(y / pc.dy), fz = floor(z / pc.dz);
+    const int i = (int)fx, j = (int)fy, k = (int)fz;
+    TA m = (TA)(x / pc.dx - fx), nn = (TA)(y / pc.dy - fy), o = (TA)(z / pc.dz - fz);
+    m = m / size + TA(1.0) / size;
+    nn = nn / size + TA(1.0) / size;
+    o = o / size + TA(1.0) / size;
+    const int Nx = pc.N[0], Ny = pc.N[1], Nz = pc.N[2];
+    const int i0 = wrapi(i + 1 + Nx, Nx), i1 = wrapi(i + 2, Nx);
+    const int j0 = wrapi(j + 1 + Ny, Ny), j1 = wrapi(j + 2, Ny);
+    const int k0 = wrapi(k + 1 + Nz, Nz), k1 = wrapi(k + 2, Nz);
+    return interp<TF, TA>(v, i0, j0, k0, i1, j1, k1, m, nn, o, Nx, Ny);
+}
+
+template <typename T, bool WIDE>
 __global__ void k_interp_many(PC pc, const T* __restrict__ fields, int nf, size_t V, const double* __restrict__ p,
                               double* out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1344,12 +1363,25 @@ __global__ void k_interp_many(PC pc, const T* __restrict__ fields, int nf, size_
     for (int f = 0; f < nf; ++f) {
         const T* fl[1] = {fields + (size_t)f * V};
         T v;
-        interp_fields<T, T>(pc, x, y, z, fl, 1, &v);
+        if (WIDE) v = interp2<T, T>(pc, x, y, z, fl[0]);
+        else interp_fields<T, T>(pc, x, y, z, fl, 1, &v);
         out[(size_t)i * nf + f] = (double)v;
     }
 }
 
+static fipi_status interpolate_impl(fipi_ctx* ctx, const double* fields, int nfields, const double* p, double* out,
+                                    bool wide);
+
 fipi_status particles_interpolate(fipi_ctx* ctx, const double* fields, int nfields, const double* p, double* out) {
+    return interpolate_impl(ctx, fields, nfields, p, out, false);
+}
+
+fipi_status particles_interpolate2(fipi_ctx* ctx, const double* fields, int nfields, const double* p, double* out) {
+    return interpolate_impl(ctx, fields, nfields, p, out, true);
+}
+
+static fipi_status interpolate_impl(fipi_ctx* ctx, const double* fields, int nfields, const double* p, double* out,
+                                    bool wide) {
     const int n = ctx->pb.n;
     const size_t V = (size_t)ctx->g.V;
     DevScratch ds{ctx};
@@ -1365,12 +1397,16 @@ fipi_status particles_interpolate(fipi_ctx* ctx, const double* fields, int nfiel
         float* fd = ds.get<float>(V * nfields);
         if (!fd) return set_error(ctx, FIPI_ERR_CUDA, "cudaMalloc failed");
         FIPI_CUDA(ctx, h2d(ctx, fd, hf.data(), sizeof(float) * V * nfields));
-        { LaunchScope ls_(ctx, "interpolate", 0.0); k_interp_many<float><<<(n + 255) / 256, 256, 0, ctx->stream>>>(pc, fd, nfields, V, pd, od); }
+        { LaunchScope ls_(ctx, "interpolate", 0.0);
+          if (wide) k_interp_many<float, true><<<(n + 255) / 256, 256, 0, ctx->stream>>>(pc, fd, nfields, V, pd, od);
+          else k_interp_many<float, false><<<(n + 255) / 256, 256, 0, ctx->stream>>>(pc, fd, nfields, V, pd, od); }
     } else {
         double* fd = ds.get<double>(V * nfields);
         if (!fd) return set_error(ctx, FIPI_ERR_CUDA, "cudaMalloc failed");
         FIPI_CUDA(ctx, h2d(ctx, fd, fields, sizeof(double) * V * nfields));
-        { LaunchScope ls_(ctx, "interpolate", 0.0); k_interp_many<double><<<(n + 255) / 256, 256, 0, ctx->stream>>>(pc, fd, nfields, V, pd, od); }
+        { LaunchScope ls_(ctx, "interpolate", 0.0);
+          if (wide) k_interp_many<double, true><<<(n + 255) / 256, 256, 0, ctx->stream>>>(pc, fd, nfields, V, pd, od);
+          else k_interp_many<double, false><<<(n + 255) / 256, 256, 0, ctx->stream>>>(pc, fd, nfields, V, pd, od); }
     }
     FIPI_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     FIPI_CUDA(ctx, d2h(ctx, out, od, sizeof(double) * n * nfields));

@@ -118,6 +118,21 @@ template <int NF, class Op> __device__ __forceinline__ auto out_sel(const Op& op
     return p;
 }
 
+// R2C of NF real fields.
+template <typename T, int NF> struct OpR2CN {
+    using C = cplx<T>;
+    const T* src[NF];
+    C* o[NF];
+    int nx, ny;
+    __device__ C* out(int f) const { return o[f]; }
+    __device__ const C* in(int) const { return nullptr; }
+    __device__ void point(int z, int y, int n, C* v) const {
+        const size_t row = ((size_t)z * ny + y) * nx;
+#pragma unroll
+        for (int f = 0; f < NF; ++f) v[f] = reinterpret_cast<const C*>(src[f] + row)[n];
+    }
+};
+
 // Adapter giving point() an accumulator when the op does not take one.
 template <class Op> struct NoAcc {
     Op op;

@@ -89,7 +89,7 @@ def loss_and_grad(sim: Simulation, c0: np.ndarray, init: InitialState, nsteps: i
     cT = PhaseTrajectory.apply(x, sim, init, nsteps, stride)
     L = structure_loss(cT, target, shape)
     L.backward()
-    return float(L), x.grad.numpy().copy()
+    return float(L.detach()), x.grad.numpy().copy()
 
 
 def loss_only(sim: Simulation, c0: np.ndarray, init: InitialState, nsteps: int, target: torch.Tensor) -> float:

@@ -61,6 +61,8 @@ _SIGS = {
     "fipi_step_stokes": (ctypes.c_int, [_vp]),
     "fipi_step_particles": (ctypes.c_int, [_vp]),
     "fipi_wrap": (ctypes.c_int, [_vp, _dp]),
+    "fipi_interpolate2": (ctypes.c_int, [_vp, _dp, ctypes.c_int, _dp, _dp]),
+    "fipi_div": (ctypes.c_int, [_vp, _dp, _dp]),
     "fipi_sync": (ctypes.c_int, [_vp]),
     "fipi_stream": (ctypes.c_int, [_vp, ctypes.POINTER(_vp)]),
     "fipi_mass": (ctypes.c_int, [_vp, _dp]),
@@ -293,6 +295,18 @@ class Simulation:
 
     def step_particles(self):
         _check(self.lib.fipi_step_particles(self.h))
+
+    def interpolate2(self, fields, p):
+        fields = _f64(fields)
+        nf = fields.size // self.V
+        out = np.empty(self.n * nf)
+        _check(self.lib.fipi_interpolate2(self.h, _d(fields), nf, _d(_f64(p, 3 * self.n)), _d(out)))
+        return out.reshape(self.n, nf)
+
+    def div(self, v) -> np.ndarray:
+        out = np.empty(self.V)
+        _check(self.lib.fipi_div(self.h, _d(_f64(v, 3 * self.V)), _d(out)))
+        return out
 
     def wrap(self, p) -> np.ndarray:
         out = _f64(p, 3 * self.n).copy()

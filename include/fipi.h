@@ -217,6 +217,12 @@ fipi_status fipi_f_pi(fipi_ctx* ctx, const double* c_loc, const double* dcdx, co
  * p, p_old, u_old are updated in place (n_p x 3). */
 fipi_status fipi_advect(fipi_ctx* ctx, int stage, const double* f_pi, const double* f_pp,
                         const double* r, double* p, double* p_old, double* u_old);
+/* field::interpolate2 (field.cpp:250-281; not called by the reference's
+ * loop): the size-3-stencil variant of fipi_interpolate, same layout. */
+fipi_status fipi_interpolate2(fipi_ctx* ctx, const double* fields, int nfields, const double* p, double* out);
+/* field::div (field.cpp:332-361) + field::ifft, real part (not called by the
+ * reference's loop): divergence of a real vector field v (3 x V) -> out (V). */
+fipi_status fipi_div(fipi_ctx* ctx, const double* v, double* out);
 /* element::enforce_bc (element.cpp:271-280) / cluster::enforce_bc:
  * p = fmod(p + L, L) per axis, n_p x 3 in place. */
 fipi_status fipi_wrap(fipi_ctx* ctx, double* p);

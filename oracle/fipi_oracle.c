@@ -273,6 +273,34 @@ void oracle_grad(const fipi_params* P, const double* c, double* out) {
     oracle_destroy(o);
 }
 
+/* field::div (field.cpp:332-361) of a real vector field v (3 x V): every
+ * component transformed (field::fft), -k_d Im + i k_d Re accumulated over d
+ * with no Nyquist zeroing, field::ifft, real part. */
+void oracle_div(const fipi_params* P, const double* v, double* out) {
+    oracle* o = oracle_create(P);
+    if (!o) return;
+    const long V = o->V;
+    double* acc = (double*)calloc((size_t)(2 * V), sizeof(double));
+    double* tmp = (double*)malloc(sizeof(double) * 2 * (size_t)V);
+    for (int d = 0; d < 3; ++d) {
+        for (long it = 0; it < V; ++it) {
+            tmp[2 * it] = v[d * V + it];
+            tmp[2 * it + 1] = 0.0;
+        }
+        fft(o, tmp);
+        for (long it = 0; it < V; ++it) {
+            const double k = d == 0 ? o->kx[IDX_I(o, it)] : (d == 1 ? o->ky[IDX_J(o, it)] : o->kz[IDX_K(o, it)]);
+            acc[2 * it] += -k * tmp[2 * it + 1];
+            acc[2 * it + 1] += k * tmp[2 * it];
+        }
+    }
+    ifft(o, acc);
+    for (long it = 0; it < V; ++it) out[it] = acc[2 * it];
+    free(tmp);
+    free(acc);
+    oracle_destroy(o);
+}
+
 /* f = (lambda/sqr(epsilon))*(c.power(3.0)-c)  (main.cpp:178, 250) */
 static void bulk_potential(oracle* o) {
     const double s = o->P.lambda / (o->P.epsilon * o->P.epsilon);
@@ -490,6 +518,40 @@ void oracle_interpolate(const fipi_params* P, const double* v, int n, const doub
         val += (1.0 - m) * nn * oo * v[i + j1 * Nx + k1 * Nx * Ny];
         val += m * (1.0 - nn) * oo * v[i1 + j * Nx + k1 * Nx * Ny];
         val += m * nn * oo * v[i1 + j1 * Nx + k1 * Nx * Ny];
+        out[q] = val;
+    }
+}
+
+/* field::interpolate2 (field.cpp:250-281): the same products as
+ * field::interpolate on the fractions m/3 + 1/3 of the size-3 stencil whose
+ * corners are the nodes i + 1 and i + 2 (indices as the reference forms
+ * them, periodic). */
+void oracle_interpolate2(const fipi_params* P, const double* v, int n, const double* pos, double* out) {
+    const int Nx = P->nx, Ny = P->ny, Nz = P->nz;
+    const double dx = P->lx / Nx, dy = P->ly / Ny, dz = P->lz / Nz;
+    const int size = 3;
+    for (int q = 0; q < n; ++q) {
+        const double x = pos[3 * q], y = pos[3 * q + 1], z = pos[3 * q + 2];
+        const int i = (int)floor(x / dx), j = (int)floor(y / dy), k = (int)floor(z / dz);
+        double m = x / dx - floor(x / dx);
+        double nn = y / dy - floor(y / dy);
+        double o = z / dz - floor(z / dz);
+        m = m / size + 1.0 / size;
+        nn = nn / size + 1.0 / size;
+        o = o / size + 1.0 / size;
+        const int i0 = (i - (1 - size) / 2 + Nx) % Nx, i1 = (i + (1 + size) / 2) % Nx;
+        const int j0 = (j - (1 - size) / 2 + Ny) % Ny, j1 = (j + (1 + size) / 2) % Ny;
+        const int k0 = (k - (1 - size) / 2 + Nz) % Nz, k1 = (k + (1 + size) / 2) % Nz;
+        const long sxy = (long)Nx * Ny;
+        double val;
+        val = (1.0 - m) * (1.0 - nn) * (1.0 - o) * v[i0 + j0 * Nx + k0 * sxy];
+        val += (1.0 - m) * nn * (1.0 - o) * v[i0 + j1 * Nx + k0 * sxy];
+        val += m * (1.0 - nn) * (1.0 - o) * v[i1 + j0 * Nx + k0 * sxy];
+        val += m * nn * (1.0 - o) * v[i1 + j1 * Nx + k0 * sxy];
+        val += (1.0 - m) * (1.0 - nn) * o * v[i0 + j0 * Nx + k1 * sxy];
+        val += (1.0 - m) * nn * o * v[i0 + j1 * Nx + k1 * sxy];
+        val += m * (1.0 - nn) * o * v[i1 + j0 * Nx + k1 * sxy];
+        val += m * nn * o * v[i1 + j1 * Nx + k1 * sxy];
         out[q] = val;
     }
 }

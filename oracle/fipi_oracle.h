@@ -52,6 +52,8 @@ int oracle_step(oracle* o);
 /* Fine-grained restatements (stateless w.r.t. the step). */
 void oracle_fft3(const fipi_params* P, double* data, int sign); /* C2C, unnormalised */
 void oracle_grad(const fipi_params* P, const double* c, double* out); /* 3 x V */
+void oracle_div(const fipi_params* P, const double* v, double* out);  /* 3 x V -> V */
+void oracle_interpolate2(const fipi_params* P, const double* field, int n, const double* p, double* out);
 int oracle_sorting(const fipi_params* P, int n, const double* p, int* keys, int* sorted,
                    int* offsets, int* it_mark);
 int oracle_f_pp(const fipi_params* P, int n, const double* p, int t, const double* f_pi,

@@ -80,6 +80,8 @@ def port_lib():
         lib.oracle_mass.argtypes = [ctypes.c_void_p]
         lib.oracle_fft3.argtypes = [P, _dp, ctypes.c_int]
         lib.oracle_grad.argtypes = [P, _dp, _dp]
+        lib.oracle_div.argtypes = [P, _dp, _dp]
+        lib.oracle_interpolate2.argtypes = [P, _dp, ctypes.c_int, _dp, _dp]
         lib.oracle_sorting.argtypes = [P, ctypes.c_int, _dp, _ip, _ip, _ip, _ip]
         lib.oracle_f_pp.argtypes = [P, ctypes.c_int, _dp, ctypes.c_int, _dp, _dp, _dp, _ip,
                                     ctypes.c_int, _ip]
@@ -185,6 +187,21 @@ def grad(params, c):
     V = params.nx * params.ny * params.nz
     out = np.zeros(3 * V)
     port_lib().oracle_grad(ctypes.byref(params), _d(np.ascontiguousarray(c, np.float64)), _d(out))
+    return out
+
+
+def div(params, v):
+    V = params.nx * params.ny * params.nz
+    out = np.zeros(V)
+    port_lib().oracle_div(ctypes.byref(params), _d(np.ascontiguousarray(v, np.float64).ravel()), _d(out))
+    return out
+
+
+def interpolate2(params, field, p):
+    n = len(p) // 3
+    out = np.zeros(n)
+    port_lib().oracle_interpolate2(ctypes.byref(params), _d(np.ascontiguousarray(field, np.float64)), n,
+                                   _d(np.ascontiguousarray(p, np.float64)), _d(out))
     return out
 
 
@@ -296,6 +313,20 @@ class Ref:
         L.ref_advect.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, _dp, _dp, _dp]
         L.ref_spread.argtypes = [_dp, _dp, _dp]
         L.ref_write_field.argtypes = [_dp, ctypes.c_int, ctypes.c_char_p, ctypes.c_char_p]
+        L.ref_div.argtypes = [_dp, _dp]
+        L.ref_interpolate2.argtypes = [_dp, ctypes.c_int, _dp, _dp]
+
+    def div(self, v):
+        out = np.zeros(self.V)
+        self.lib.ref_div(_d(np.ascontiguousarray(v, np.float64).ravel()), _d(out))
+        return out
+
+    def interpolate2(self, field, p):
+        n = len(p) // 3
+        out = np.zeros(n)
+        self.lib.ref_interpolate2(_d(np.ascontiguousarray(field, np.float64)), n,
+                                  _d(np.ascontiguousarray(p, np.float64)), _d(out))
+        return out
         L.ref_write_free_energy.argtypes = [_dp, _dp, ctypes.c_char_p]
         L.ref_write_particles.argtypes = [_dp, _dp, _dp, ctypes.c_char_p]
 

@@ -372,6 +372,28 @@ void ref_spread(const double* p, const double* f_pp, double* out) {
     for (int d = 0; d < 3; ++d) get_real(fr, d, out + d * V);
 }
 
+/* field::div (field.cpp:332-361) of a real vector field, then field::ifft, real part. */
+void ref_div(const double* v, double* out) {
+    if (!g_sim) g_sim = new Sim();
+    field a("VECTORS");
+    for (int d = 0; d < 3; ++d)
+        for (long it = 0; it < V; ++it) {
+            a.v[d][it][0] = v[d * V + it];
+            a.v[d][it][1] = 0.0;
+        }
+    a.fft(g_sim->p_forward);
+    field dv = a.div(g_sim->kf);
+    dv.ifft(g_sim->p_backward);
+    get_real(dv, 0, out);
+}
+
+/* field::interpolate2 (field.cpp:250-281) of one real field at n positions. */
+void ref_interpolate2(const double* vals, int n, const double* p, double* out) {
+    field a("SCALARS");
+    for (long it = 0; it < V; ++it) a.set_value(0, (int)it, vals[it]);
+    for (int q = 0; q < n; ++q) out[q] = a.interpolate2(vector(p[3 * q], p[3 * q + 1], p[3 * q + 2]), 0);
+}
+
 /* ------------------------------------------------------------ VTK output */
 /* field::output_to_file (field.cpp:469-503) of given values. */
 int ref_write_field(const double* values, int components, const char* name, const char* path) {

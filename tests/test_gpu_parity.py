@@ -345,3 +345,28 @@ def test_write_vtk_from_context(fipi, tmp_path):
         vals = np.array([float(x) for x in lines[11:]])
         dx = P.lx / P.nx
         assert abs(vals.sum() * dx ** 3 - s.free_energy()) < 1e-4 * abs(s.free_energy())
+
+
+@pytest.mark.parametrize("name", ["t16", "t32_aniso", "t32_2pi"])
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_div_and_interpolate2(fipi, oracle_mod, name, prec):
+    """field::div and field::interpolate2 (field API, not in the loop)."""
+    w = fipi.workload(name)
+    P = w.params()
+    if prec == "mixed" and P.ny < 16:
+        pytest.skip("mixed form needs ny >= 16")
+    rng = np.random.default_rng(12)
+    v = rng.standard_normal(3 * w.V)
+    fld = rng.standard_normal(w.V)
+    p = (rng.random((w.n_p, 3)) * np.array([P.lx, P.ly, P.lz])).ravel()
+    with fipi.Simulation(P, prec) as s:
+        d = s.div(v)
+        i2 = s.interpolate2(fld, p).ravel()
+    d_ref = oracle_mod.div(P, v)
+    i_ref = oracle_mod.interpolate2(P, fld, p)
+    if prec == "fp64":
+        assert rel_l2(d, d_ref) < 1e-12
+        assert np.array_equal(i2, i_ref)
+    else:
+        assert rel_l2(d, d_ref) < 1e-5
+        assert rel_l2(i2, i_ref) < 1e-6

@@ -175,3 +175,22 @@ def test_oracle_without_particles(oracle_mod):
     port.set_state(c0)
     assert port.step(2) == 0
     assert np.isfinite(port.phase()).all()
+
+
+@pytest.mark.parametrize("name", ["t16", "t32_aniso", "t32_2pi"])
+def test_div_and_interpolate2_bit_exact_with_reference(oracle_mod, name):
+    """field::div and field::interpolate2 (dead code in the reference's loop,
+    part of the field API): the C restatement equals the reference."""
+    if not oracle_mod.reference_available():
+        pytest.skip("reference sources absent")
+    import fipi_gb300 as F
+
+    w = F.workload(name)
+    P = w.params()
+    ref = oracle_mod.Ref(name)
+    rng = np.random.default_rng(6)
+    v = rng.standard_normal(3 * w.V)
+    assert np.array_equal(oracle_mod.div(P, v), ref.div(v))
+    fld = rng.standard_normal(w.V)
+    p = (rng.random((50, 3)) * np.array([P.lx, P.ly, P.lz])).ravel()
+    assert np.array_equal(oracle_mod.interpolate2(P, fld, p), ref.interpolate2(fld, p))
