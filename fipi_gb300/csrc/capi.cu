@@ -193,6 +193,10 @@ fipi_status fipi_create(const fipi_params* P, fipi_precision prec, int device, f
     if (st != FIPI_OK) return fail(st);
     st = particles_alloc(ctx);
     if (st != FIPI_OK) return fail(st);
+    if (ctx->pb.n > 0) {
+        e = cudaMallocHost((void**)&ctx->pin, sizeof(double) * 12 * (size_t)ctx->pb.n);
+        if (e != cudaSuccess) return fail(cuda_check(ctx, e, "cudaMallocHost(particle staging)"));
+    }
     e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return fail(cuda_check(ctx, e, "init"));
     // default particle radii r_p (element.cpp:119)
@@ -215,6 +219,7 @@ fipi_status fipi_destroy(fipi_ctx* ctx) {
     drain_timer(ctx);
     for (cudaEvent_t e : ctx->kt.pool) cudaEventDestroy(e);
     adjoint_free(ctx);
+    if (ctx->pin) cudaFreeHost(ctx->pin);
     fields_free(ctx);
     particles_free(ctx);
     if (ctx->status) cudaFree(ctx->status);
@@ -294,6 +299,18 @@ fipi_status fipi::download_soa(fipi_ctx* ctx, const double* d, double* h, int n)
 
 extern "C" {
 
+// Particle state in and out through the pinned staging buffer: the host
+// transposes (n x 3 <-> 3 x n) happen there, the copies are asynchronous and
+// each call synchronises once.
+static void to_soa(const double* h, double* s, int n) {
+    for (int i = 0; i < n; ++i)
+        for (int a = 0; a < 3; ++a) s[(size_t)a * n + i] = h[3 * i + a];
+}
+static void from_soa(const double* s, double* h, int n) {
+    for (int i = 0; i < n; ++i)
+        for (int a = 0; a < 3; ++a) h[3 * i + a] = s[(size_t)a * n + i];
+}
+
 fipi_status fipi_set_particles(fipi_ctx* ctx, const double* p, const double* r, const double* cos_theta,
                                const double* f_pp) {
     if (!ctx) return set_error(ctx, FIPI_ERR_BAD_ARG, "ctx is NULL");
@@ -301,23 +318,30 @@ fipi_status fipi_set_particles(fipi_ctx* ctx, const double* p, const double* r, 
     if (n == 0) return FIPI_OK;
     if (!p) return set_error(ctx, FIPI_ERR_BAD_ARG, "p is NULL");
     FIPI_CUDA(ctx, cudaSetDevice(ctx->device));
-    fipi_status st = upload_soa(ctx, p, ctx->pb.p, n);
-    if (st != FIPI_OK) return st;
-    FIPI_CUDA(ctx, cudaMemcpyAsync(ctx->pb.p_old, ctx->pb.p, sizeof(double) * 3 * n, cudaMemcpyDeviceToDevice,
+    FIPI_CUDA(ctx, cudaStreamSynchronize(ctx->stream));  // the staging buffer is free
+    double* pin = ctx->pin;
+    const size_t b3 = sizeof(double) * 3 * n, b1 = sizeof(double) * n;
+    to_soa(p, pin, n);
+    FIPI_CUDA(ctx, cudaMemcpyAsync(ctx->pb.p, pin, b3, cudaMemcpyHostToDevice, ctx->stream));
+    FIPI_CUDA(ctx, cudaMemcpyAsync(ctx->pb.p_old, ctx->pb.p, b3, cudaMemcpyDeviceToDevice,
                                    ctx->stream));  // cluster.cpp:182
-    std::vector<double> rr(n, ctx->P.r_p), cc(n, 0.0);
-    if (r) rr.assign(r, r + n);
-    if (cos_theta) cc.assign(cos_theta, cos_theta + n);
-    FIPI_CUDA(ctx, cudaMemcpyAsync(ctx->pb.r, rr.data(), sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
-    FIPI_CUDA(ctx, cudaMemcpyAsync(ctx->pb.cth, cc.data(), sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
-    if (f_pp) {
-        st = upload_soa(ctx, f_pp, ctx->pb.f_pp, n);
-        if (st != FIPI_OK) return st;
-    } else {
-        FIPI_CUDA(ctx, cudaMemsetAsync(ctx->pb.f_pp, 0, sizeof(double) * 3 * n, ctx->stream));
+    double* pr = pin + 3 * (size_t)n;
+    double* pc = pr + n;
+    for (int i = 0; i < n; ++i) {
+        pr[i] = r ? r[i] : ctx->P.r_p;
+        pc[i] = cos_theta ? cos_theta[i] : 0.0;
     }
-    FIPI_CUDA(ctx, cudaMemsetAsync(ctx->pb.f_pi, 0, sizeof(double) * 3 * n, ctx->stream));
-    FIPI_CUDA(ctx, cudaMemsetAsync(ctx->pb.u_old, 0, sizeof(double) * 3 * n, ctx->stream));
+    FIPI_CUDA(ctx, cudaMemcpyAsync(ctx->pb.r, pr, b1, cudaMemcpyHostToDevice, ctx->stream));
+    FIPI_CUDA(ctx, cudaMemcpyAsync(ctx->pb.cth, pc, b1, cudaMemcpyHostToDevice, ctx->stream));
+    if (f_pp) {
+        double* pf = pc + n;
+        to_soa(f_pp, pf, n);
+        FIPI_CUDA(ctx, cudaMemcpyAsync(ctx->pb.f_pp, pf, b3, cudaMemcpyHostToDevice, ctx->stream));
+    } else {
+        FIPI_CUDA(ctx, cudaMemsetAsync(ctx->pb.f_pp, 0, b3, ctx->stream));
+    }
+    FIPI_CUDA(ctx, cudaMemsetAsync(ctx->pb.f_pi, 0, b3, ctx->stream));
+    FIPI_CUDA(ctx, cudaMemsetAsync(ctx->pb.u_old, 0, b3, ctx->stream));
     return check_status(ctx);
 }
 
@@ -344,9 +368,16 @@ fipi_status fipi_get_particles(fipi_ctx* ctx, double* p, double* f_pp, double* f
     if (st != FIPI_OK) return st;
     const int n = ctx->pb.n;
     if (n == 0) return FIPI_OK;
-    if (p && (st = download_soa(ctx, ctx->pb.p, p, n)) != FIPI_OK) return st;
-    if (f_pp && (st = download_soa(ctx, ctx->pb.f_pp, f_pp, n)) != FIPI_OK) return st;
-    if (f_pi && (st = download_soa(ctx, ctx->pb.f_pi, f_pi, n)) != FIPI_OK) return st;
+    const size_t b3 = sizeof(double) * 3 * n;
+    double* dst[3] = {p, f_pp, f_pi};
+    const double* src[3] = {ctx->pb.p, ctx->pb.f_pp, ctx->pb.f_pi};
+    for (int k = 0; k < 3; ++k)
+        if (dst[k])
+            FIPI_CUDA(ctx, cudaMemcpyAsync(ctx->pin + 3 * (size_t)n * k, src[k], b3, cudaMemcpyDeviceToHost,
+                                           ctx->stream));
+    FIPI_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    for (int k = 0; k < 3; ++k)
+        if (dst[k]) from_soa(ctx->pin + 3 * (size_t)n * k, dst[k], n);
     return FIPI_OK;
 }
 
