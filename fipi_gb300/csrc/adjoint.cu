@@ -274,7 +274,7 @@ fipi_status adjoint_alloc(fipi_ctx* ctx) {
 // ------------------------------------------------------------ checkpoints
 // Payload regions, each 256-byte aligned.
 struct CkLayout {
-    size_t c, g, spec, uhat, k0, p, fpp, r, cth, bytes;
+    size_t c, g, spec, upre, k0, p, fpp, r, cth, bytes;
 };
 
 size_t up256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -291,7 +291,7 @@ CkLayout ck_layout(const fipi_ctx* ctx) {
     o = up256(o + 3 * ts * V);
     L.spec = o;  // chat, chat_old, fhat, fhat_old, Chat_old
     o = up256(o + 5 * 2 * ts * SH);
-    L.uhat = o;
+    L.upre = o;
     o = up256(o + 3 * 2 * ts * SH);
     L.k0 = o;
     o = up256(o + 6 * sizeof(double));
@@ -324,7 +324,7 @@ std::vector<CkCopy> ck_regions(fipi_ctx* ctx, unsigned char* base) {
     for (int d = 0; d < 3; ++d) r.push_back({base + L.g + d * ts * V, b.g[d], ts * V});
     void* specs[5] = {b.chat, b.chat_old, b.fhat, b.fhat_old, b.Chat_old};
     for (int i = 0; i < 5; ++i) r.push_back({base + L.spec + i * 2 * ts * SH, specs[i], 2 * ts * SH});
-    for (int d = 0; d < 3; ++d) r.push_back({base + L.uhat + d * 2 * ts * SH, b.uhat[d], 2 * ts * SH});
+    for (int d = 0; d < 3; ++d) r.push_back({base + L.upre + d * 2 * ts * SH, b.upre[d], 2 * ts * SH});
     r.push_back({base + L.k0, ctx->k0, 6 * sizeof(double)});
     if (n > 0) {
         r.push_back({base + L.p, ctx->pb.p, 3 * n * sizeof(double)});
@@ -385,7 +385,6 @@ fipi_status ck_load(fipi_ctx* ctx, int slot) {
         FIPI_CUDA(ctx, cudaMemcpyAsync(c.ctxbuf, c.slot, c.bytes, cudaMemcpyDeviceToDevice, ctx->stream));
     ctx->t = ctx->ck.t[slot];
     set_tick(ctx, ctx->t);
-    fields_refresh_upre(ctx);
     ctx->pb.tau_valid = false;
     ctx->have_phase = true;
     return FIPI_OK;

@@ -31,8 +31,7 @@ struct FieldBufs {
     void* fhat = nullptr;
     void* fhat_old = nullptr;
     void* Chat_old = nullptr;
-    void* uhat[3] = {};
-    void* upre[3] = {};  // Z inverse of u_hat (the first pass of u = C2R(u_hat)), kept by the step
+    void* upre[3] = {};  // velocity state: Z^-1 u_hat (the first pass of u = C2R(u_hat))
     void* S[4] = {};  // scratch
 };
 
@@ -213,7 +212,6 @@ fipi_status fields_get_velocity(fipi_ctx* ctx, double* u_host);
 // The three grid sub-steps of one iteration (enqueue only).
 void fields_step_ch(fipi_ctx* ctx, int t);        // conv, CH update, c, f
 void fields_step_stokes(fipi_ctx* ctx);           // mu, grad c, force, projection
-void fields_refresh_upre(fipi_ctx* ctx);          // after u_hat changed outside the step
 fipi_status fields_get_grad(fipi_ctx* ctx, double* g_host);  // grad c of the state, 3 x V
 fipi_status fields_mass(fipi_ctx* ctx, double* out);
 fipi_status fields_free_energy(fipi_ctx* ctx, double* out);

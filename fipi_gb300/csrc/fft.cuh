@@ -112,6 +112,11 @@ template <typename T> inline size_t ypass_smem(const Geom& g) {
 // tile, the last stage stores straight to global memory.  `fields` fields of
 // rows are processed in one launch.
 constexpr int kYStages = 2;  // 3 measured no faster on GB300 (more registers)
+// FFT rounds per Y tile: FP32 tiles of 2 x 8 rows (32 KB at ny = 256) keep
+// more bytes in flight per SM; FP64 rows are twice as large already.
+template <typename T> struct YGroups {
+    static constexpr int value = sizeof(T) == 4 ? 2 : 1;
+};
 
 template <typename T, int DIR, int N>
 __global__ void __launch_bounds__(kThreads) k_ypass_tma(Geom g, const cplx<T>* __restrict__ twy, FieldPtrs<T> fp,
@@ -120,8 +125,11 @@ __global__ void __launch_bounds__(kThreads) k_ypass_tma(Geom g, const cplx<T>* _
     using IO = FftIO<T, DIR, N>;
     constexpr int S = kYStages;
     constexpr int Tn = FftPlan<N, FftE<T>::value>::Tn;
-    constexpr int RB = kThreads / Tn;
-    constexpr int BUF = RB * ((N + (N >> 4) + 15) & ~15);  // padded rows, 128-byte multiple for FP32/FP64
+    constexpr int RG = kThreads / Tn;           // rows per FFT round (all threads)
+    constexpr int G = YGroups<T>::value;        // rounds per tile: G * RG rows per bulk copy
+    constexpr int RB = G * RG;
+    constexpr int PITCH = (N + (N >> 4) + 15) & ~15;  // >= padded_len(N); 128-byte multiple for FP32/FP64
+    constexpr int BUF = RB * PITCH;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* buf0 = reinterpret_cast<C*>(smem_raw);
     __shared__ __align__(8) uint64_t bar[S];
@@ -166,17 +174,11 @@ __global__ void __launch_bounds__(kThreads) k_ypass_tma(Geom g, const cplx<T>* _
             abort_flag = 1;
         }
         C* in = buf0 + b * BUF;
-        const int row = tid / Tn, t = tid - row * Tn;
-        const bool act = row < rows;
-        C v[IO::E];
-        if (act && ok) {
-#pragma unroll
-            for (int i = 0; i < IO::E; ++i) v[i] = in[row * N + IO::in_elem(t, i)];
-        }
+        const int rl = tid / Tn, t = tid - rl * Tn;
         // generic-proxy accesses of the previous tile's buffer are ordered
         // before the bulk copy that will overwrite it
         fence_proxy_async_smem();
-        __syncthreads();  // this tile is in registers; the previous tile is finished
+        __syncthreads();  // this tile has landed; the previous tile is finished
         if (abort_flag) {
             if (tid == 0) {
                 atomicOr(status, ERR_TMA_TIMEOUT);
@@ -187,11 +189,24 @@ __global__ void __launch_bounds__(kThreads) k_ypass_tma(Geom g, const cplx<T>* _
         }
         const long long next = tile + (long long)(S - 1) * gridDim.x;
         if (tid == 0 && next < ntiles) issue(next, (b + S - 1) % S);
-        smem_fft2<T, DIR, N, true, true>(in, xidx, row, t, act, twy, 1, v);
-        if (act) {
-            C* out = fp.pick(fp.out, f) + (r0 + row) * N;
+        // rounds in descending order: round gr exchanges through padded rows
+        // [gr RG, (gr + 1) RG), which lie past the natural rows of the rounds
+        // still to come (PITCH >= N)
+        for (int gr = G - 1; gr >= 0; --gr) {
+            const int row = gr * RG + rl;
+            const bool act = row < rows;
+            C v[IO::E];
+            if (act) {
 #pragma unroll
-            for (int i = 0; i < IO::E; ++i) out[IO::out_elem(t, i)] = v[i];
+                for (int i = 0; i < IO::E; ++i) v[i] = in[row * N + IO::in_elem(t, i)];
+            }
+            __syncthreads();  // the round's exchange rows overlap its natural rows
+            smem_fft2<T, DIR, N, true, true>(in + gr * RG * PITCH, xidx, rl, t, act, twy, 1, v);
+            if (act) {
+                C* out = fp.pick(fp.out, f) + (r0 + row) * N;
+#pragma unroll
+                for (int i = 0; i < IO::E; ++i) out[IO::out_elem(t, i)] = v[i];
+            }
         }
         b = (b + 1) % S;
     }
@@ -199,10 +214,11 @@ __global__ void __launch_bounds__(kThreads) k_ypass_tma(Geom g, const cplx<T>* _
 
 template <typename T> inline size_t ypass_tma_smem(const Geom& g) {
     const int tn = fft_threads_per_row<T>(g.ny);
-    const int rb = kThreads / tn;
+    const int rb = YGroups<T>::value * (kThreads / tn);
     const int row = (g.ny + (g.ny >> 4) + 15) & ~15;
     return (size_t)kYStages * rb * row * sizeof(cplx<T>);
 }
+template <typename T> inline int ypass_tile_rows(int ny) { return YGroups<T>::value * ypass_rows<T>(ny); }
 
 // ----------------------------------------------------------------- Z pass
 // One block = kx = blockIdx.x, ky in [blockIdx.y*TZ, +TZ), all kz, NF fields

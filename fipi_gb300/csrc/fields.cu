@@ -331,8 +331,9 @@ template <typename T> struct ZOpFRt {
 };
 
 // Round trip C -> next A (NF = NB = 3): the Leray projection of ZOpProj in
-// the forward Z pass (u_hat stored), then the inverse Z transform of u_hat
-// into upre, which the next step's conv pass starts from.
+// the forward Z pass, then the inverse Z transform of u_hat into upre — the
+// velocity state the next step's conv pass starts from (u_hat itself is
+// never stored).
 template <typename T> struct ZOpProjRt {
     using C = cplx<T>;
     ZOpProj<T> pj;
@@ -344,12 +345,7 @@ template <typename T> struct ZOpProjRt {
         v[1] = pj.in[1][gi];
         v[2] = pj.in[2][gi];
     }
-    __device__ void mid(int ix, int iy, int iz, size_t gi, const C* vi, C* vo) const {
-        pj.compute(ix, iy, iz, vi, vo);
-        pj.out[0][gi] = vo[0];
-        pj.out[1][gi] = vo[1];
-        pj.out[2][gi] = vo[2];
-    }
+    __device__ void mid(int ix, int iy, int iz, size_t, const C* vi, C* vo) const { pj.compute(ix, iy, iz, vi, vo); }
     __device__ void store2(int, int, int, size_t gi, const C* v) const {
         upre[0][gi] = v[0];
         upre[1][gi] = v[1];
@@ -458,8 +454,6 @@ template <typename T> static fipi_status alloc_fields_t(fipi_ctx* ctx) {
         FIPI_CUDA(ctx, A(&b.g[d], sizeof(T) * V));
         FIPI_CUDA(ctx, A(&b.fsp[d], sizeof(T) * V));
         FIPI_CUDA(ctx, cudaMemsetAsync(b.fsp[d], 0, sizeof(T) * V, ctx->stream));
-        FIPI_CUDA(ctx, A(&b.uhat[d], sizeof(C) * SH));
-        FIPI_CUDA(ctx, cudaMemsetAsync(b.uhat[d], 0, sizeof(C) * SH, ctx->stream));
         FIPI_CUDA(ctx, A(&b.upre[d], sizeof(C) * SH));
         FIPI_CUDA(ctx, cudaMemsetAsync(b.upre[d], 0, sizeof(C) * SH, ctx->stream));
     }
@@ -526,8 +520,7 @@ void fields_free(fipi_ctx* ctx) {
     FieldBufs& b = ctx->fb;
     void* all[] = {b.twx, b.twy, b.twz, b.kx, b.ky, b.kz, b.c, b.ureal, b.chat, b.chat_old, b.fhat,
                    b.fhat_old, b.Chat_old, b.S[0], b.S[1], b.S[2], b.S[3], b.g[0], b.g[1], b.g[2],
-                   b.fsp[0], b.fsp[1], b.fsp[2], b.uhat[0], b.uhat[1], b.uhat[2], b.upre[0], b.upre[1],
-                   b.upre[2], ctx->partials, ctx->k0};
+                   b.fsp[0], b.fsp[1], b.fsp[2], b.upre[0], b.upre[1], b.upre[2], ctx->partials, ctx->k0};
     for (void* p : all)
         if (p) cudaFree(p);
     b = FieldBufs{};
@@ -571,29 +564,27 @@ fipi_status fields_set_phase(fipi_ctx* ctx, const double* c_host) {
     return ctx->prec == FIPI_MIXED ? set_phase_t<float>(ctx, c_host) : set_phase_t<double>(ctx, c_host);
 }
 
-// upre = Z inverse of u_hat (after u_hat changed outside the step).
-template <typename T> static void refresh_upre_t(fipi_ctx* ctx) {
-    FieldBufs& b = ctx->fb;
-    ZOpStore<T, 3> zs{{F<T>::sp(b.uhat[0]), F<T>::sp(b.uhat[1]), F<T>::sp(b.uhat[2])},
-                      {F<T>::sp(b.upre[0]), F<T>::sp(b.upre[1]), F<T>::sp(b.upre[2])}, 0};
-    launch_z<T, 3, +1>(ctx, "Z inverse copy", 6, zs);
-}
-
-// u_hat = R2C(u): the step only needs the spectrum of the velocity.
+// The velocity state is upre = Z^-1 u_hat (the first pass of the inverse
+// transform u = C2R(u_hat), which is what the next step starts from);
+// u_hat itself is not kept.  set_velocity: u_hat = R2C(u), then Z^-1.
 template <typename T> static fipi_status set_velocity_t(fipi_ctx* ctx, const double* u_host) {
     const Geom& g = ctx->g;
     for (int d = 0; d < 3; ++d) {
         T* tmp = (T*)ctx->fb.ureal + (size_t)d * g.V;
         fipi_status st = upload<T>(ctx, u_host + (size_t)d * g.V, tmp, (size_t)g.V);
         if (st != FIPI_OK) return st;
-        OpR2C<T> op{tmp, F<T>::S(ctx, 0), g.nx, g.ny};
+        OpR2C<T> op{tmp, F<T>::S(ctx, d), g.nx, g.ny};
         launch_x<T, 0, 1, false>(ctx, "X forward", 1, NoAcc<OpR2C<T>>{op});
-        void* sp[1] = {ctx->fb.S[0]};
-        launch_y<T>(ctx, 1, sp, sp, -1);
-        ZOpStore<T, 1> zs{{F<T>::S(ctx, 0)}, {F<T>::sp(ctx->fb.uhat[d])}, 0};
-        launch_z<T, 1, -1>(ctx, "Z forward store", 2, zs);
     }
-    refresh_upre_t<T>(ctx);
+    void* s3[3] = {ctx->fb.S[0], ctx->fb.S[1], ctx->fb.S[2]};
+    launch_y<T>(ctx, 3, s3, s3, -1);
+    ZOpStore<T, 3> zf{{F<T>::S(ctx, 0), F<T>::S(ctx, 1), F<T>::S(ctx, 2)},
+                      {F<T>::S(ctx, 0), F<T>::S(ctx, 1), F<T>::S(ctx, 2)}, 0};
+    launch_z<T, 3, -1>(ctx, "Z forward store", 6, zf);
+    FieldBufs& b = ctx->fb;
+    ZOpStore<T, 3> zi{{F<T>::S(ctx, 0), F<T>::S(ctx, 1), F<T>::S(ctx, 2)},
+                      {F<T>::sp(b.upre[0]), F<T>::sp(b.upre[1]), F<T>::sp(b.upre[2])}, 0};
+    launch_z<T, 3, +1>(ctx, "Z inverse copy", 6, zi);
     FIPI_CUDA(ctx, cudaGetLastError());
     return FIPI_OK;
 }
@@ -609,11 +600,9 @@ fipi_status fields_get_phase(fipi_ctx* ctx, double* c_host) {
 
 template <typename T> static fipi_status get_velocity_t(fipi_ctx* ctx, double* u_host) {
     const Geom& g = ctx->g;
-    ZOpStore<T, 3> zs{{F<T>::sp(ctx->fb.uhat[0]), F<T>::sp(ctx->fb.uhat[1]), F<T>::sp(ctx->fb.uhat[2])},
-                      {F<T>::S(ctx, 0), F<T>::S(ctx, 1), F<T>::S(ctx, 2)}, 0};
-    launch_z<T, 3, +1>(ctx, "Z inverse copy", 6, zs);
+    void* up[3] = {ctx->fb.upre[0], ctx->fb.upre[1], ctx->fb.upre[2]};
     void* sp[3] = {ctx->fb.S[0], ctx->fb.S[1], ctx->fb.S[2]};
-    launch_y<T>(ctx, 3, sp, sp, +1);
+    launch_y<T>(ctx, 3, up, sp, +1);
     T* ur = (T*)ctx->fb.ureal;
     OpC2RStore<T, 3> op{{F<T>::S(ctx, 0), F<T>::S(ctx, 1), F<T>::S(ctx, 2)}, {ur, ur + g.V, ur + 2 * g.V}, g.nx, g.ny};
     launch_x<T, 3, 0, false>(ctx, "X inverse store", 3, NoAcc<OpC2RStore<T, 3>>{op});
@@ -703,16 +692,12 @@ template <typename T> static void step_stokes_t(fipi_ctx* ctx) {
     launch_x<T, 4, 3, false>(ctx, "X inverse mu,grad, force, forward", nreal, of);
     void* s3[3] = {b.S[0], b.S[1], b.S[2]};
     launch_y<T>(ctx, 3, s3, s3, -1);
-    ZOpProj<T> zp{{F<T>::S(ctx, 0), F<T>::S(ctx, 1), F<T>::S(ctx, 2)},
-                  {F<T>::sp(b.uhat[0]), F<T>::sp(b.uhat[1]), F<T>::sp(b.uhat[2])}, kt, k.mu, g.m, g.ny / 2, g.nz / 2};
+    ZOpProj<T> zp{{F<T>::S(ctx, 0), F<T>::S(ctx, 1), F<T>::S(ctx, 2)}, {nullptr, nullptr, nullptr}, kt, k.mu, g.m,
+                  g.ny / 2, g.nz / 2};
     ZOpProjRt<T> zpr{zp, {F<T>::sp(b.upre[0]), F<T>::sp(b.upre[1]), F<T>::sp(b.upre[2])}};
-    launch_zrt<T, 3, 3, -1, 16 / (sizeof(T) / 4), false>(ctx, "Z forward + projection + inverse", 9, zpr);
+    launch_zrt<T, 3, 3, -1, 16 / (sizeof(T) / 4), false>(ctx, "Z forward + projection + inverse", 6, zpr);
 }
 
-void fields_refresh_upre(fipi_ctx* ctx) {
-    if (ctx->prec == FIPI_MIXED) refresh_upre_t<float>(ctx);
-    else refresh_upre_t<double>(ctx);
-}
 
 void fields_step_stokes(fipi_ctx* ctx) {
     if (ctx->prec == FIPI_MIXED) step_stokes_t<float>(ctx);

@@ -397,7 +397,7 @@ template <typename T> void launch_y(fipi_ctx* ctx, int nf, void* const* in, void
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm[di], kern, kThreads, smem);
             if (blocks_per_sm[di] < 1) blocks_per_sm[di] = 1;
         }
-        const int rb = ypass_rows<T>(g.ny);
+        const int rb = ypass_tile_rows<T>(g.ny);
         const long long tiles = ((long long)g.nz * g.h + rb - 1) / rb * nf;
         long long grid = (long long)ctx->num_sms * blocks_per_sm[di];
         if (grid > tiles) grid = tiles;

@@ -284,7 +284,8 @@ fipi_status fipi_write_vtk(fipi_ctx* ctx, int what, const char* path);
  * No counterpart in the reference (it has no checkpoint or restart).  A
  * checkpoint is a device-resident copy of everything one step reads from
  * the previous one: c, grad c, the spectra c_hat, f_hat and the SBDF2
- * histories c_hat_old, f_hat_old, C_hat_old, u_hat, particle positions,
+ * histories c_hat_old, f_hat_old, C_hat_old, the velocity spectrum (kept
+ * after its inverse z pass, the form the step starts from), positions,
  * radii, cos(theta) and f_pp (spread at the next step, cluster.cpp:452),
  * the step index t (the contact ramp depends on it) and, in the mixed form,
  * the FP64 k = 0 record.  Slots live in HBM so the sqrt(N) schedule of the
