@@ -1,6 +1,6 @@
 // Reverse mode of the FP64 step, device-resident checkpoints and the
 // sqrt(N)-checkpointed trajectory gradient.  The reference has neither; the
-// step being differentiated is main.cpp:172-316 (CH update, Stokes
+// step being differentiated is main.cpp:75-219 (CH update, Stokes
 // projection, two Heun particle stages) as the forward path computes it.
 //
 // Cotangents of the Eulerian state are kept as half spectra of the real
@@ -129,7 +129,7 @@ template <typename C, typename T> __device__ __forceinline__ void sub_ik(C& acc,
 
 // ------------------------------------------------------------ Z-pass ops
 // Last forward Z pass of the Stokes part: forms L, the cotangent of
-// c_hat^{n+1}, and reverses the CH update (main.cpp:192-235).  Writes
+// c_hat^{n+1}, and reverses the CH update (main.cpp:95-138).  Writes
 // lam_f (S[0]) and lam_C (S[1]) and the cotangents of c^n (partial) and of
 // the start state's histories.
 template <typename T> struct ZOpAdjC {

@@ -1,5 +1,5 @@
 // C ABI of the FIPI GB300 library: context lifecycle, state I/O, the step
-// driver (main.cpp:172-316 of the reference) and the fine-grained parity
+// driver (main.cpp:75-219 of the reference) and the fine-grained parity
 // entry points.  Errors are returned as fipi_status codes; the reference
 // printed a message and called exit(0).
 #include <cuda_runtime.h>
@@ -153,7 +153,7 @@ fipi_status fipi_cell_geometry(const fipi_params* P, int n_cell[3], double d_cel
     if (!P || !n_cell || !d_cell) return set_error(nullptr, FIPI_ERR_BAD_ARG, "NULL argument");
     const double L[3] = {P->lx, P->ly, P->lz};
     for (int a = 0; a < 3; ++a) {
-        n_cell[a] = (int)std::floor(L[a] / P->r_c + 2 * P->margin / P->r_c);  // cluster.cpp:120-122
+        n_cell[a] = (int)std::floor(L[a] / P->r_c + 2 * P->margin / P->r_c);  // cluster.cpp:26-28
         d_cell[a] = n_cell[a] > 0 ? std::fmod(L[a] + 2 * P->margin, P->r_c) / n_cell[a] + P->r_c : 0.0;
     }
     return FIPI_OK;
@@ -199,7 +199,7 @@ fipi_status fipi_create(const fipi_params* P, fipi_precision prec, int device, f
     }
     e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return fail(cuda_check(ctx, e, "init"));
-    // default particle radii r_p (element.cpp:119)
+    // default particle radii r_p (element.cpp:25)
     if (ctx->pb.n > 0) {
         std::vector<double> r(ctx->pb.n, P->r_p);
         e = h2d(ctx, ctx->pb.r, r.data(), sizeof(double) * r.size());
@@ -245,7 +245,7 @@ fipi_status fipi::check_status(fipi_ctx* ctx) {
         FIPI_CUDA(ctx, cudaMemsetAsync(ctx->status, 0, sizeof(int), ctx->stream));
         if (st & ERR_TMA_TIMEOUT) return set_error(ctx, FIPI_ERR_CUDA, "a bulk-copy wait timed out in an FFT pass");
         if (st & ERR_NONFINITE) return set_error(ctx, FIPI_ERR_NONFINITE, "non-finite particle position");
-        return set_error(ctx, FIPI_ERR_OUT_OF_RANGE, "particle out of sorting range (cluster.cpp:238-257)");
+        return set_error(ctx, FIPI_ERR_OUT_OF_RANGE, "particle out of sorting range (cluster.cpp:144-163)");
     }
     return FIPI_OK;
 }
@@ -324,7 +324,7 @@ fipi_status fipi_set_particles(fipi_ctx* ctx, const double* p, const double* r, 
     to_soa(p, pin, n);
     FIPI_CUDA(ctx, cudaMemcpyAsync(ctx->pb.p, pin, b3, cudaMemcpyHostToDevice, ctx->stream));
     FIPI_CUDA(ctx, cudaMemcpyAsync(ctx->pb.p_old, ctx->pb.p, b3, cudaMemcpyDeviceToDevice,
-                                   ctx->stream));  // cluster.cpp:182
+                                   ctx->stream));  // cluster.cpp:88
     double* pr = pin + 3 * (size_t)n;
     double* pc = pr + n;
     for (int i = 0; i < n; ++i) {
@@ -397,13 +397,13 @@ void fipi::graphs_reset(fipi_ctx* ctx) {
 }
 
 
-// One iteration of main.cpp:172-316, enqueued on the context stream.
+// One iteration of main.cpp:75-219, enqueued on the context stream.
 void fipi::enqueue_step(fipi_ctx* ctx) {
     const int t = ctx->t;
-    fields_step_ch(ctx, t);      // main.cpp:176-238
-    particles_spread(ctx);       // main.cpp:266 (compute_f_r of the previous step's state)
-    fields_step_stokes(ctx);     // main.cpp:243-278
-    particles_step(ctx);         // main.cpp:283-316
+    fields_step_ch(ctx, t);      // main.cpp:79-141
+    particles_spread(ctx);       // main.cpp:169 (compute_f_r of the previous step's state)
+    fields_step_stokes(ctx);     // main.cpp:146-181
+    particles_step(ctx);         // main.cpp:186-219
     step_tick(ctx);
     ctx->t = t + 1;
 }
@@ -504,7 +504,7 @@ fipi_status fipi_step_ch(fipi_ctx* ctx) {
     if (!ctx->have_phase) return set_error(ctx, FIPI_ERR_STATE, "fipi_set_phase must come first");
     if (ctx->substep != 0) return set_error(ctx, FIPI_ERR_STATE, "fipi_step_ch must start an iteration");
     FIPI_CUDA(ctx, cudaSetDevice(ctx->device));
-    fields_step_ch(ctx, ctx->t);  // main.cpp:176-238
+    fields_step_ch(ctx, ctx->t);  // main.cpp:79-141
     ctx->substep = 1;
     return check_status(ctx);
 }
@@ -513,8 +513,8 @@ fipi_status fipi_step_stokes(fipi_ctx* ctx) {
     if (!ctx) return set_error(ctx, FIPI_ERR_BAD_ARG, "ctx is NULL");
     if (ctx->substep != 1) return set_error(ctx, FIPI_ERR_STATE, "fipi_step_stokes must follow fipi_step_ch");
     FIPI_CUDA(ctx, cudaSetDevice(ctx->device));
-    particles_spread(ctx);      // main.cpp:266
-    fields_step_stokes(ctx);    // main.cpp:243-278
+    particles_spread(ctx);      // main.cpp:169
+    fields_step_stokes(ctx);    // main.cpp:146-181
     ctx->substep = 2;
     return check_status(ctx);
 }
@@ -523,7 +523,7 @@ fipi_status fipi_step_particles(fipi_ctx* ctx) {
     if (!ctx) return set_error(ctx, FIPI_ERR_BAD_ARG, "ctx is NULL");
     if (ctx->substep != 2) return set_error(ctx, FIPI_ERR_STATE, "fipi_step_particles must follow fipi_step_stokes");
     FIPI_CUDA(ctx, cudaSetDevice(ctx->device));
-    particles_step(ctx);        // main.cpp:283-316
+    particles_step(ctx);        // main.cpp:186-219
     step_tick(ctx);
     ctx->t += 1;
     ctx->substep = 0;

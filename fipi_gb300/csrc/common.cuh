@@ -32,7 +32,7 @@ template <typename C> __device__ __forceinline__ C cmul_i(C a, int dir) {
 
 // Device error word bits (read back by the host after each step).
 enum : int {
-    ERR_OUT_OF_RANGE = 1,  // particle outside the cell grid (cluster.cpp:238-257)
+    ERR_OUT_OF_RANGE = 1,  // particle outside the cell grid (cluster.cpp:144-163)
     ERR_NONFINITE = 2,     // NaN/Inf seen in a particle position
     ERR_TMA_TIMEOUT = 4,   // a bounded wait for a bulk copy gave up
 };

@@ -187,7 +187,7 @@ struct fipi_ctx {
     int substep = 0;           // 1 after fipi_step_ch, 2 after fipi_step_stokes
     double* pin = nullptr;     // pinned host staging of the particle state, 12 n doubles
     bool have_phase = false;
-    bool track_tau = true;     // packing energy during the step (cluster.cpp:350-353)
+    bool track_tau = true;     // packing energy during the step (cluster.cpp:256-259)
     size_t device_bytes = 0;
     std::string last_error;
     fipi::KTimer kt;

@@ -1,5 +1,5 @@
 // Eulerian side of the FIPI step on sm_103a: the pseudo-spectral
-// Cahn-Hilliard update and the Stokes projection (main.cpp:176-278 of the
+// Cahn-Hilliard update and the Stokes projection (main.cpp:79-181 of the
 // reference), as 3-pass R2C/C2R FFTs with the element-wise work fused into
 // the passes.  Per step (13 transforms):
 //
@@ -55,7 +55,7 @@ template <typename T> struct OpR2C {
 };
 
 
-// Step A: u (3 inverse) . grad c -> conv (1 forward).  main.cpp:188-189
+// Step A: u (3 inverse) . grad c -> conv (1 forward).  main.cpp:91-92
 template <typename T, bool MIXED> struct OpConv {
     using C = cplx<T>;
     const C* uS[3];
@@ -111,7 +111,7 @@ template <typename T, bool MIXED> struct OpCF {
 };
 
 // Step C: mu, grad c (4 inverse) -> F = mu grad c + spread + buoyancy (3 forward).
-// main.cpp:246-269; the spread term is cluster::compute_f_r.
+// main.cpp:149-172; the spread term is cluster::compute_f_r.
 template <typename T> struct OpForce {
     using C = cplx<T>;
     const C* S[4];
@@ -159,7 +159,7 @@ template <typename T> struct OpForce {
 };
 
 // ------------------------------------------------------------ Z-pass ops
-// Z forward with the Cahn-Hilliard update (main.cpp:192-235) fused.
+// Z forward with the Cahn-Hilliard update (main.cpp:95-138) fused.
 // The conv spectrum C^n is the transformed input; c_hat^{n+1} is written
 // over c_hat^{n-1} and C^n over C^{n-1} at the same index.
 template <typename T, bool MIXED> struct ZOpCH {
@@ -289,7 +289,7 @@ template <typename T, bool MIXED> struct ZOpCHRt {
 };
 
 // Round trip B -> C (NF = 1, NB = 4): the forward Z transform of f gives
-// f_hat^{n+1} (stored); mu_hat = lambda k^2 c_hat + f_hat (main.cpp:254) and
+// f_hat^{n+1} (stored); mu_hat = lambda k^2 c_hat + f_hat (main.cpp:157) and
 // i k_d c_hat with the Nyquist index of d zeroed (field.cpp:288-328) are
 // transformed back along z into out[0..3] (the inverses of mu and grad c).
 template <typename T> struct ZOpFRt {
@@ -353,7 +353,7 @@ template <typename T> struct ZOpProjRt {
     }
 };
 
-// Z inverse prologue: mu_hat = lambda k^2 c_hat + f_hat (main.cpp:254).
+// Z inverse prologue: mu_hat = lambda k^2 c_hat + f_hat (main.cpp:157).
 template <typename T> struct ZOpMu {
     using C = cplx<T>;
     const C* chat;
@@ -393,7 +393,7 @@ template <typename T> struct ZOpGrad {
 
 
 
-// FP64 per-block sums for mass and free energy (main.cpp:329, field.cpp:507-516).
+// FP64 per-block sums for mass and free energy (main.cpp:232, field.cpp:507-516).
 template <typename T>
 __global__ void k_diag(const T* __restrict__ c, const T* __restrict__ g0, const T* __restrict__ g1,
                        const T* __restrict__ g2, size_t V, double lam, double e2, double dv,
@@ -529,7 +529,7 @@ void fields_free(fipi_ctx* ctx) {
 }
 
 
-// t = 0 state: c, c_hat, f_hat, grad c (everything main.cpp:178-189 needs).
+// t = 0 state: c, c_hat, f_hat, grad c (everything main.cpp:81-92 needs).
 template <typename T> static fipi_status set_phase_t(fipi_ctx* ctx, const double* c_host) {
     const Geom& g = ctx->g;
     const bool mixed = ctx->prec == FIPI_MIXED;

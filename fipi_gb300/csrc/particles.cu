@@ -1,18 +1,18 @@
-// Lagrangian side of the FIPI step on sm_103a (main.cpp:283-316 and
+// Lagrangian side of the FIPI step on sm_103a (main.cpp:186-219 and
 // cluster.cpp / element.cpp of the reference).
 //
 //  - cell list: key = i + j n + k n^2 with i = floor(p/d_cell + margin/d_cell)
-//    (cluster.cpp:234-259), a stable LSD radix sort of (key, particle id) and
+//    (cluster.cpp:140-165), a stable LSD radix sort of (key, particle id) and
 //    offsets by binary search; ids inside a cell are ascending, which is the
 //    order the reference's linked lists hold them in (linked_list.cpp:30-43);
-//  - contact forces one warp per home cell (cluster.cpp:268-369): each lane
+//  - contact forces one warp per home cell (cluster.cpp:174-275): each lane
 //    owns one particle of the cell and walks the 27 neighbour cells in the
 //    reference's (k, j, i) order; every pair is evaluated from the lower id's
 //    side exactly as the reference does and the result is applied with the
 //    reference's sign, so forces are deterministic and atomic-free;
 //  - interpolation, attachment force, Heun advection and periodic wrap per
-//    particle (field.cpp:223-248, element.cpp:149-280);
-//  - spreading (cluster.cpp:438-504) as a sorted segmented reduction: the
+//    particle (field.cpp:223-248, element.cpp:55-185);
+//  - spreading (cluster.cpp:344-410) as a sorted segmented reduction: the
 //    8 corner records of every particle are radix-sorted by grid node,
 //    stable in particle id, and each node sums its records in ascending id,
 //    the order in which the reference's loop adds them.
@@ -47,7 +47,7 @@ struct PC {
     double r_eq, k_n, r_p, A, sigma, epsilon, pi, mu, dt;
     double dx, dy, dz;
     int N[3];
-    double tanh2;  // tanh(2.0), element.cpp:178
+    double tanh2;  // tanh(2.0), element.cpp:84
 };
 
 static PC make_pc(const fipi_ctx* ctx) {
@@ -81,7 +81,7 @@ static PC make_pc(const fipi_ctx* ctx) {
     return c;
 }
 
-// ramp (primitive.cpp:205-212)
+// ramp (primitive.cpp:122-129)
 static double ramp(double t, double thr) {
     if (t < 0) return 0.0;
     if (t >= 0 && t < thr) return t / thr;
@@ -195,10 +195,10 @@ static int bits_for(long long maxval) {
 
 // ------------------------------------------------------------ cell list
 __device__ __forceinline__ int cell_coord(double x, double dcell, double margin) {
-    return (int)floor(x / dcell + margin / dcell);  // cluster.cpp:234-236
+    return (int)floor(x / dcell + margin / dcell);  // cluster.cpp:140-142
 }
 
-// Cell key of one position (cluster.cpp:234-257); out-of-range or
+// Cell key of one position (cluster.cpp:140-163); out-of-range or
 // non-finite positions are clamped and reported through the error word.
 __device__ __forceinline__ unsigned cell_key(const PC& pc, double x, double y, double z, int* status) {
     int c[3] = {cell_coord(x, pc.dc[0], pc.margin), cell_coord(y, pc.dc[1], pc.margin),
@@ -238,9 +238,9 @@ __global__ void k_cell_offsets(const unsigned* __restrict__ keys, int n, int* of
 // slot from atomicAdd is arbitrary), an exclusive scan of the counts (the
 // offsets), placement at offset + slot, then one warp per cell ranks its
 // ids so each cell lists its particles in ascending id — the order of the
-// stable sort of cluster::sorting (cluster.cpp:210-263).  The result does
+// stable sort of cluster::sorting (cluster.cpp:116-169).  The result does
 // not depend on the order of the atomics.  With `ymax` the same kernels
-// find it_mark of cluster.cpp:222-232 (the first id with the largest
+// find it_mark of cluster.cpp:128-138 (the first id with the largest
 // p_y > 0; unchanged when there is none).
 __global__ void k_cells_count(PC pc, const double* __restrict__ p, unsigned* keys, unsigned* slot, int* cnt,
                               unsigned long long* ymax, int* status) {
@@ -356,7 +356,7 @@ static bool build_cells(fipi_ctx* ctx, const double* p_dev, bool want_it_mark = 
 
 // ------------------------------------------------------------ contact forces
 // Separation of exactly coincident particles: the reference draws
-// rand()%1000/1e3*2 r_p - r_p per component (cluster.cpp:328-336); here the
+// rand()%1000/1e3*2 r_p - r_p per component (cluster.cpp:234-242); here the
 // same 1e-3 lattice is drawn from a hash of the pair (lower id first).
 __device__ __forceinline__ void coincident_d(int a, int b, double r_p, double d[3]) {
     unsigned long long h = ((unsigned long long)(unsigned)a << 32) ^ (unsigned long long)(unsigned)b;
@@ -429,7 +429,7 @@ __global__ void k_f_pp(PC pc, const double* __restrict__ p, const unsigned* __re
                             d[1] = yj - yi;
                             d[2] = zj - zi;
                         }
-                        // cluster.cpp:319-326
+                        // cluster.cpp:225-232
                         if (d[0] > T0) d[0] = d[0] - pc.L[0];
                         else if (d[0] < -T0) d[0] = d[0] + pc.L[0];
                         if (d[1] > T1) d[1] = d[1] - pc.L[1];
@@ -485,7 +485,7 @@ __global__ void k_f_pp(PC pc, const double* __restrict__ p, const unsigned* __re
 
 // Mixed-form contact forces when every axis has at least 4 cells.  Then
 // the reference's minimum-image rule (shift d by L when |d| exceeds
-// d_cell (n_cell - 2), cluster.cpp:319-326) shifts exactly the pairs whose
+// d_cell (n_cell - 2), cluster.cpp:225-232) shifts exactly the pairs whose
 // neighbour cell was reached through the periodic wrap, so d can be formed
 // from cell-relative FP32 coordinates plus the neighbour cell's offset
 // (di, dj, dk) d_cell, with no per-pair test.  A warp owns a home cell;
@@ -608,7 +608,7 @@ __global__ void __launch_bounds__(32 * kFppRows) k_f_pp_fast(PC pc, const float4
     }
 }
 
-// it_mark of cluster::sorting (cluster.cpp:222-232): the first index of
+// it_mark of cluster::sorting (cluster.cpp:128-138): the first index of
 // the largest p_y, kept from the previous call when no p_y > 0.  For
 // non-negative doubles the bit pattern orders like the value, so the
 // maximum is an integer atomicMax and the first index an atomicMin.
@@ -689,7 +689,7 @@ __device__ __forceinline__ void interp_fields(const PC& pc, double x, double y, 
     for (int q = 0; q < nf; ++q) out[q] = interp<TF, TA>(f[q], i, j, k, i1, j1, k1, m, nn, o, pc.N[0], pc.N[1]);
 }
 
-// element::get_f_pi (element.cpp:169-191) with f_mag = -A pi (d - r cos_theta) sigma.
+// element::get_f_pi (element.cpp:75-97) with f_mag = -A pi (d - r cos_theta) sigma.
 __device__ __forceinline__ void f_pi_of(const PC& pc, double phi, double gx, double gy, double gz, double r, double ct,
                                         double* f) {
     const double gn = sqrt(gx * gx + gy * gy + gz * gz);
@@ -706,7 +706,7 @@ __device__ __forceinline__ void f_pi_of(const PC& pc, double phi, double gx, dou
     }
 }
 
-// element::advect (element.cpp:250-267) and enforce_bc (element.cpp:271-280)
+// element::advect (element.cpp:156-173) and enforce_bc (element.cpp:177-185)
 // for one particle; uf = 0 and f_ext = 0 as in the reference.
 __device__ __forceinline__ void advect_one(const PC& pc, int stage, const double* fpi, const double* fpp, double r,
                                            double* p, double* po, double* uo) {
@@ -802,7 +802,7 @@ __global__ void k_stage_advect(PC pc, int stage, double* p, double* p_old, doubl
 }
 
 // ------------------------------------------------------------ spreading
-// Corner order of cluster.cpp:462-500: (0,0,0) (1,0,0) (1,1,0) (1,0,1) (1,1,1) (0,0,1) (0,1,0) (0,1,1).
+// Corner order of cluster.cpp:368-406: (0,0,0) (1,0,0) (1,1,0) (1,0,1) (1,1,1) (0,0,1) (0,1,0) (0,1,1).
 __constant__ int c_corner[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {1, 0, 1}, {1, 1, 1}, {0, 0, 1}, {0, 1, 0}, {0, 1, 1}};
 
 __device__ __forceinline__ void cell_and_frac(const PC& pc, double X, double Y, double Z, int* ix, double* fr) {
@@ -817,7 +817,7 @@ __device__ __forceinline__ void cell_and_frac(const PC& pc, double X, double Y, 
 
 // Per particle: the 8 corner records (node, particle*8 + corner), the force
 // density f = (f_pp + f_ext)/dx/dy/dz and the fractions (o, p, q) of
-// cluster.cpp:452-460, computed once here instead of once per record.
+// cluster.cpp:358-366, computed once here instead of once per record.
 template <typename TA>
 __global__ void k_spread_records(PC pc, const double* __restrict__ p, const double* __restrict__ f_pp,
                                  unsigned* keys, unsigned* vals, TA* __restrict__ fw) {
@@ -850,7 +850,7 @@ __global__ void k_spread_clear(const unsigned* __restrict__ nodes, int m, TF* f0
     f2[nd] = TF(0);
 }
 
-// Weight products of cluster.cpp:463-500 for corner c, left to right from f.
+// Weight products of cluster.cpp:369-406 for corner c, left to right from f.
 template <typename TA>
 __device__ __forceinline__ TA corner_value(TA f, int c, TA o, TA pp, TA q) {
     switch (c) {
@@ -912,7 +912,7 @@ static void spread_t(fipi_ctx* ctx, const double* p, const double* f_pp, T* cons
 }
 
 // Mixed-form spreading of the step: the 8 FP32 corner contributions of each
-// particle (the weight products of cluster.cpp:463-500) are added as 64-bit
+// particle (the weight products of cluster.cpp:369-406) are added as 64-bit
 // fixed-point integers (units of 2^-32) with atomics.  Integer addition is
 // associative, so the sums do not depend on the order of the atomics (the
 // result is deterministic) and no sort is needed; the touched nodes are
@@ -997,7 +997,7 @@ void particles_spread(fipi_ctx* ctx) {
     }
 }
 
-// compute_f_pp; with `tau` the packing energy of cluster.cpp:350-353 is
+// compute_f_pp; with `tau` the packing energy of cluster.cpp:256-259 is
 // accumulated per particle and summed in a fixed order.  TA = float with
 // at least 4 cells per axis takes the FP32 cell-relative path.
 // it_mark for the packing energy: the first index of the largest p_y.
@@ -1009,7 +1009,7 @@ static void it_mark_launch(fipi_ctx* ctx, const double* p) {
     { LaunchScope ls_(ctx, "it_mark argmax", 0.0); k_ymax_resolve<<<1, 1, 0, ctx->stream>>>(b.ymax, b.it_mark); }
 }
 
-// compute_f_pp; with `tau` the packing energy of cluster.cpp:350-353 is
+// compute_f_pp; with `tau` the packing energy of cluster.cpp:256-259 is
 // accumulated per particle (tau_part) and summed when it is asked for.
 // TA = float with at least 4 cells per axis takes the FP32 cell-relative path.
 static bool f_pp_fast_path(const fipi_ctx* ctx, bool fp32) {
@@ -1060,7 +1060,7 @@ template <typename T> static void step_t(fipi_ctx* ctx) {
     float4* spos = f_pp_fast_path(ctx, sizeof(T) == sizeof(float)) ? b.spos : nullptr;
     // per stage: interpolate_local_variables, sorting, compute_f_pi,
     // compute_f_pp(t+1), compute_f_ext (zero), advect, enforce_bc
-    // (main.cpp:295-314); the ramp(t+1, 0.2 t_end) factor is kept on the
+    // (main.cpp:198-217); the ramp(t+1, 0.2 t_end) factor is kept on the
     // device (step_tick).  Stage 1's advection and stage 2's interpolation
     // run in one kernel.
     { LaunchScope ls_(ctx, "stage interpolate + f_pi", 0.0); k_stage_fpi<T, T><<<nb, kPT, 0, ctx->stream>>>(pc, c, g0, g1, g2, b.p, b.f_pi, b.r, b.cth); }
@@ -1085,7 +1085,7 @@ void particles_step(fipi_ctx* ctx) {
 }
 
 // End of a step: t += 1 and the next step's ramp(t + 1, 0.2 t_end)
-// (compute_f_pp(t+1), main.cpp:299; primitive.cpp:205-212).
+// (compute_f_pp(t+1), main.cpp:202; primitive.cpp:122-129).
 __global__ void k_step_tick(int* d_t, double* d_rmp, double thr) {
     const int t = ++(*d_t);
     const double x = (double)(t + 1);
@@ -1198,14 +1198,14 @@ static fipi_status read_status(fipi_ctx* ctx) {
     FIPI_CUDA(ctx, cudaMemsetAsync(ctx->status, 0, sizeof(int), ctx->stream));
     if (st & ERR_NONFINITE) return set_error(ctx, FIPI_ERR_NONFINITE, "non-finite particle position");
     if (st & ERR_OUT_OF_RANGE)
-        return set_error(ctx, FIPI_ERR_OUT_OF_RANGE, "particle out of sorting range (cluster.cpp:238-257)");
+        return set_error(ctx, FIPI_ERR_OUT_OF_RANGE, "particle out of sorting range (cluster.cpp:144-163)");
     return FIPI_OK;
 }
 
 __global__ void k_wrap_many(PC pc, double* p) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= pc.n) return;
-    for (int a = 0; a < 3; ++a) p[3 * i + a] = fmod(p[3 * i + a] + pc.L[a], pc.L[a]);  // element.cpp:271-280
+    for (int a = 0; a < 3; ++a) p[3 * i + a] = fmod(p[3 * i + a] + pc.L[a], pc.L[a]);  // element.cpp:177-185
 }
 
 fipi_status particles_wrap(fipi_ctx* ctx, double* p_host) {
@@ -1524,9 +1524,9 @@ void set_tick(fipi_ctx* ctx, int t) {
 }
 
 // ------------------------------------------------------------ adjoint
-// Reverse mode of the two Heun stages (element.cpp:250-280,
-// cluster.cpp:268-369, element.cpp:169-191, field.cpp:223-248) and of the
-// spreading (cluster.cpp:438-504), FP64.  Branches (interpolation cell,
+// Reverse mode of the two Heun stages (element.cpp:156-185,
+// cluster.cpp:174-275, element.cpp:75-97, field.cpp:223-248) and of the
+// spreading (cluster.cpp:344-410), FP64.  Branches (interpolation cell,
 // |phi| <= tanh 2, |d| < r, |d| < r_eq) are those of the forward step.
 
 // Trilinear value and position gradient of v at (x, y, z) (field.cpp:223-248).
@@ -1648,7 +1648,7 @@ __global__ void k_adj_stage(PC pc, int stage, const double* __restrict__ p, cons
 }
 
 // Adjoint of compute_f_pp with respect to positions: for every pair of the
-// forward evaluation (same cells, minimum-image rule of cluster.cpp:319-326
+// forward evaluation (same cells, minimum-image rule of cluster.cpp:225-232
 // and |d| < r_eq test), lam_p[i] += J(d) (lamF[i] - lamF[j]) with
 // J = ramp k_n ((r_eq/|d| - 1) I - r_eq d d^T / |d|^3), which is even in d.
 // Warp per home cell, lane per home particle as in k_f_pp; coincident pairs
@@ -1981,6 +1981,6 @@ extern "C" fipi_status fipi_cells_build_noalloc(const fipi_params* P, const doub
     if (e != cudaSuccess) return set_error(nullptr, FIPI_ERR_CUDA, std::string("sync: ") + cudaGetErrorString(e));
     if (hst & ERR_NONFINITE) return set_error(nullptr, FIPI_ERR_NONFINITE, "non-finite particle position");
     if (hst & ERR_OUT_OF_RANGE)
-        return set_error(nullptr, FIPI_ERR_OUT_OF_RANGE, "particle out of sorting range (cluster.cpp:238-257)");
+        return set_error(nullptr, FIPI_ERR_OUT_OF_RANGE, "particle out of sorting range (cluster.cpp:144-163)");
     return FIPI_OK;
 }

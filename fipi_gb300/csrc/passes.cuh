@@ -14,13 +14,13 @@ namespace fipi {
 
 // ------------------------------------------------------------ constants
 template <typename T> struct StepConsts {
-    T lam_eps;    // lambda/sqr(epsilon)              main.cpp:178
+    T lam_eps;    // lambda/sqr(epsilon)              main.cpp:81
     T lam;        // lambda
     T dt;
-    T s1, s2;     // t = 0: dt*M, dt*M*lambda          main.cpp:203-210
-    T s4, s2m;    // t > 0: 4 dt M, 2 dt M             main.cpp:215-216
-    T s4c, s2c;   // 4 dt, 2 dt                        main.cpp:220-221
-    T s3;         // 2 dt M lambda                     main.cpp:224
+    T s1, s2;     // t = 0: dt*M, dt*M*lambda          main.cpp:106-113
+    T s4, s2m;    // t > 0: 4 dt M, 2 dt M             main.cpp:118-119
+    T s4c, s2c;   // 4 dt, 2 dt                        main.cpp:123-124
+    T s3;         // 2 dt M lambda                     main.cpp:127
     T mu;
     T rho1, rho2, gravity;
     int ny2, nz2, m;  // Nyquist indices
@@ -258,7 +258,7 @@ __global__ void __launch_bounds__(NT, XMinBlocks<T, (NIN > NOUT ? NIN : NOUT), N
     }
 }
 
-// Z forward with the Leray projection (main.cpp:274-275) fused:
+// Z forward with the Leray projection (main.cpp:177-178) fused:
 // u_hat = (F - k (k.F)/k^2) / (mu k^2), 0 at k = 0.  At modes with a Nyquist
 // index the reference's C2C inverse keeps only the real part of a
 // non-Hermitian spectrum; that equals the inverse of the average of the

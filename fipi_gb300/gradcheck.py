@@ -10,7 +10,7 @@ The harness checks the result against central finite differences of the
 FP64 forward path.
 
 The reference has no adjoint; the differentiated step is the loop body of
-main.cpp:172-316 as the library computes it.
+main.cpp:75-219 as the library computes it.
 """
 from __future__ import annotations
 

@@ -45,7 +45,7 @@ typedef enum fipi_status {
     FIPI_ERR_BAD_ARG = 2,       /* NULL pointer, bad size or stage name       */
     FIPI_ERR_CUDA = 3,          /* a CUDA runtime call failed                 */
     FIPI_ERR_OUT_OF_RANGE = 4,  /* particle outside the sorting range:
-                                   cluster.cpp:238-257 printed and exit(0)    */
+                                   cluster.cpp:144-163 printed and exit(0)    */
     FIPI_ERR_NONFINITE = 5,     /* NaN/Inf detected in the state              */
     FIPI_ERR_NO_DEVICE = 6,     /* no CUDA device visible                     */
     FIPI_ERR_STATE = 7,         /* call out of order (e.g. step before state) */
@@ -101,7 +101,7 @@ fipi_status fipi_cell_geometry(const fipi_params* p, int n_cell[3], double d_cel
 
 /* ------------------------------------------------------------- lifecycle */
 /* Allocates every device buffer of the step on `device`.  Replaces the field
- * constructors of main.cpp:126-155 and cluster::cluster (cluster.cpp:21-40). */
+ * constructors of main.cpp:29-58 and cluster::cluster (cluster.cpp:21-40). */
 fipi_status fipi_create(const fipi_params* p, fipi_precision prec, int device, fipi_ctx** out);
 fipi_status fipi_destroy(fipi_ctx* ctx);
 /* Bytes of device memory held by the context. */
@@ -109,26 +109,26 @@ fipi_status fipi_device_bytes(const fipi_ctx* ctx, size_t* out);
 
 /* ----------------------------------------------------------------- state */
 /* Initial phase field (field.cpp:85-99 drew it from rand()); resets t = 0
- * and the SBDF2 history, like entering main.cpp:172 with t = 0. */
+ * and the SBDF2 history, like entering main.cpp:75 with t = 0. */
 fipi_status fipi_set_phase(fipi_ctx* ctx, const double* c);
-/* Velocity field u (3 x V).  The reference starts from u = 0 (main.cpp:146). */
+/* Velocity field u (3 x V).  The reference starts from u = 0 (main.cpp:49). */
 fipi_status fipi_set_velocity(fipi_ctx* ctx, const double* u);
 /* Particle state (cluster::distribute, cluster.cpp:53-92, drew p from rand()).
- * p: n_p x 3 positions in [0, L).  r: n_p radii or NULL (= r_p, element.cpp:119).
+ * p: n_p x 3 positions in [0, L).  r: n_p radii or NULL (= r_p, element.cpp:25).
  * cos_theta: n_p wettabilities or NULL (= 0, the reference's 90 degree form).
  * f_pp: n_p x 3 contact forces of the previous step or NULL (= 0); they are
- * spread at the next step (cluster.cpp:452). */
+ * spread at the next step (cluster.cpp:358). */
 fipi_status fipi_set_particles(fipi_ctx* ctx, const double* p, const double* r,
                                const double* cos_theta, const double* f_pp);
 fipi_status fipi_get_phase(fipi_ctx* ctx, double* c);
 fipi_status fipi_get_velocity(fipi_ctx* ctx, double* u);
 /* Any output pointer may be NULL.  f_pi is the attachment force of the last
- * stage (element.cpp:169-191). */
+ * stage (element.cpp:75-97). */
 fipi_status fipi_get_particles(fipi_ctx* ctx, double* p, double* f_pp, double* f_pi);
 fipi_status fipi_get_time(const fipi_ctx* ctx, int* t);
 
 /* ------------------------------------------------------------------ step */
-/* Advances `nsteps` iterations of the loop body of main.cpp:172-316
+/* Advances `nsteps` iterations of the loop body of main.cpp:75-219
  * (Cahn-Hilliard, Stokes, two Heun particle stages). */
 fipi_status fipi_step(fipi_ctx* ctx, int nsteps);
 /* Enqueues the steps without waiting for them; errors raised on the device
@@ -137,9 +137,9 @@ fipi_status fipi_step(fipi_ctx* ctx, int nsteps);
 fipi_status fipi_step_async(fipi_ctx* ctx, int nsteps);
 fipi_status fipi_sync(fipi_ctx* ctx);
 /* The three parts of one iteration, for callers that interleave their own
- * work between them: the Cahn-Hilliard update (main.cpp:176-238), the
- * spreading and Stokes solve (main.cpp:243-278), the two particle stages
- * (main.cpp:283-316, ending the iteration: t += 1).  In this order they give
+ * work between them: the Cahn-Hilliard update (main.cpp:79-141), the
+ * spreading and Stokes solve (main.cpp:146-181), the two particle stages
+ * (main.cpp:186-219, ending the iteration: t += 1).  In this order they give
  * the same results as fipi_step(ctx, 1); any other order is
  * FIPI_ERR_STATE, and so is fipi_step while an iteration is open. */
 fipi_status fipi_step_ch(fipi_ctx* ctx);
@@ -153,14 +153,14 @@ fipi_status fipi_stream(const fipi_ctx* ctx, void** stream);
  * field; mixed form: the FP64 k = 0 mode.  Not in the reference. */
 fipi_status fipi_mass(fipi_ctx* ctx, double* out);
 /* Total free energy sum lambda (0.5|grad c|^2 + 0.25/eps^2 (c^2-1)^2) dx^3
- * (main.cpp:329 + field.cpp:507-516), compensated sum. */
+ * (main.cpp:232 + field.cpp:507-516), compensated sum. */
 fipi_status fipi_free_energy(fipi_ctx* ctx, double* out);
-/* Packing energy tau of the last contact-force evaluation (cluster.cpp:283-353). */
+/* Packing energy tau of the last contact-force evaluation (cluster.cpp:189-259). */
 fipi_status fipi_packing_tau(fipi_ctx* ctx, double* out);
 
 /* -------------------------------------------------------- instrumentation
  * Not in the reference (its only timing is clock() around the whole run,
- * main.cpp:122-123, 345-346).  Every kernel launch of the library is
+ * main.cpp:25-26, 248-249).  Every kernel launch of the library is
  * counted; with timing enabled each launch is bracketed by CUDA events on
  * the context stream and accumulated per kernel class together with the
  * kernel's algorithmic bytes per launch (arrays it must read and write). */
@@ -181,19 +181,19 @@ fipi_status fipi_launch_count(const fipi_ctx* ctx, long long* n);
  * spectrum with kx in [0, nx/2], ky fastest. */
 fipi_status fipi_fft_r2c(fipi_ctx* ctx, const double* in, double* out);
 /* Inverse of the above, normalised by 1/V like field::ifft + normalize
- * (field.cpp:446-455, primitive.cpp:137-145): real part of the inverse DFT
+ * (field.cpp:446-455, primitive.cpp:54-62): real part of the inverse DFT
  * of the Hermitian completion of the half spectrum. */
 fipi_status fipi_fft_c2r(fipi_ctx* ctx, const double* in, double* out);
 /* grad c = ifft(i k c_hat) with the Nyquist index of each component zeroed
  * (field::grad, field.cpp:288-328, then ifft).  c: V reals, out: 3 x V. */
 fipi_status fipi_grad(fipi_ctx* ctx, const double* c, double* grad_out);
-/* cluster::sorting (cluster.cpp:210-263): cell key of every particle,
+/* cluster::sorting (cluster.cpp:116-169): cell key of every particle,
  * particle ids sorted by (cell, id), cell offsets (n_cells + 1 entries).
  * Any output may be NULL.  Returns FIPI_ERR_OUT_OF_RANGE like the reference's
  * out-of-range exit. */
 fipi_status fipi_cells_build(fipi_ctx* ctx, const double* p, int* keys, int* sorted_ids,
                              int* cell_offsets);
-/* cluster::compute_f_pp(t) (cluster.cpp:268-369): contact forces, n_p x 3.
+/* cluster::compute_f_pp(t) (cluster.cpp:174-275): contact forces, n_p x 3.
  * f_pi (n_p x 3, may be NULL = all zero) only feeds the packing energy tau. */
 fipi_status fipi_f_pp(fipi_ctx* ctx, const double* p, int t, const double* f_pi,
                       double* f_pp, double* tau);
@@ -202,17 +202,17 @@ fipi_status fipi_f_pp(fipi_ctx* ctx, const double* p, int t, const double* f_pi,
  * NULL to query the count; max_pairs bounds what is written. */
 fipi_status fipi_pairs(fipi_ctx* ctx, const double* p, int* pairs, int max_pairs, int* n_pairs);
 /* element::get_local_c / get_local_dcdx via field::interpolate
- * (element.cpp:149-165, field.cpp:223-248): trilinear values of `fields`
+ * (element.cpp:55-71, field.cpp:223-248): trilinear values of `fields`
  * (nfields x V reals) at the particles -> out (n_p x nfields). */
 fipi_status fipi_interpolate(fipi_ctx* ctx, const double* fields, int nfields, const double* p,
                              double* out);
-/* element::get_f_pi (element.cpp:169-191) for every particle, with the
+/* element::get_f_pi (element.cpp:75-97) for every particle, with the
  * contact-angle extension f_mag = -A pi (d - r cos_theta) sigma
  * (cos_theta = 0 is the reference).  c_loc: n_p, dcdx: n_p x 3. */
 fipi_status fipi_f_pi(fipi_ctx* ctx, const double* c_loc, const double* dcdx, const double* r,
                       const double* cos_theta, double* f_pi);
-/* element::advect (element.cpp:250-267) + element::enforce_bc
- * (element.cpp:271-280).  stage 1: u_old = F/(6 pi mu r), p_old = p,
+/* element::advect (element.cpp:156-173) + element::enforce_bc
+ * (element.cpp:177-185).  stage 1: u_old = F/(6 pi mu r), p_old = p,
  * p += dt u_old; stage 2: u = F/(6 pi mu r), p = p_old + dt/2 (u_old + u).
  * p, p_old, u_old are updated in place (n_p x 3). */
 fipi_status fipi_advect(fipi_ctx* ctx, int stage, const double* f_pi, const double* f_pp,
@@ -223,10 +223,10 @@ fipi_status fipi_interpolate2(fipi_ctx* ctx, const double* fields, int nfields, 
 /* field::div (field.cpp:332-361) + field::ifft, real part (not called by the
  * reference's loop): divergence of a real vector field v (3 x V) -> out (V). */
 fipi_status fipi_div(fipi_ctx* ctx, const double* v, double* out);
-/* element::enforce_bc (element.cpp:271-280) / cluster::enforce_bc:
+/* element::enforce_bc (element.cpp:177-185) / cluster::enforce_bc:
  * p = fmod(p + L, L) per axis, n_p x 3 in place. */
 fipi_status fipi_wrap(fipi_ctx* ctx, double* p);
-/* cluster::compute_f_r (cluster.cpp:438-504): trilinear spreading of
+/* cluster::compute_f_r (cluster.cpp:344-410): trilinear spreading of
  * f_pp / (dx dy dz) onto the grid, out: 3 x V.  Deterministic: per grid
  * node the contributions are summed in ascending particle id. */
 fipi_status fipi_spread(fipi_ctx* ctx, const double* p, const double* f_pp, double* out);
@@ -286,7 +286,7 @@ fipi_status fipi_write_vtk(fipi_ctx* ctx, int what, const char* path);
  * the previous one: c, grad c, the spectra c_hat, f_hat and the SBDF2
  * histories c_hat_old, f_hat_old, C_hat_old, the velocity spectrum (kept
  * after its inverse z pass, the form the step starts from), positions,
- * radii, cos(theta) and f_pp (spread at the next step, cluster.cpp:452),
+ * radii, cos(theta) and f_pp (spread at the next step, cluster.cpp:358),
  * the step index t (the contact ramp depends on it) and, in the mixed form,
  * the FP64 k = 0 record.  Slots live in HBM so the sqrt(N) schedule of the
  * adjoint costs device copies only.  Resuming from a slot is bit-exact. */
@@ -309,8 +309,8 @@ fipi_status fipi_checkpoint_import(fipi_ctx* ctx, int slot, const void* blob, si
  * field; c_hat, f_hat and grad c of that state are functions of c), the
  * real-field equivalents of the three SBDF2 histories, u, the positions and
  * f_pp.  Branches of the step (floor of the interpolation cell, the
- * |phi| <= tanh 2 and |d| < r tests of element.cpp:175-182, the pair test
- * |d| < r_eq of cluster.cpp:327) are held fixed: the derivative is the one
+ * |phi| <= tanh 2 and |d| < r tests of element.cpp:84-89, the pair test
+ * |d| < r_eq of cluster.cpp:246) are held fixed: the derivative is the one
  * of the branch the forward step took. */
 /* Sets the cotangent of the context's current state (any pointer NULL =
  * zero): dc V reals, du 3 x V, dp and df_pp n_p x 3. */
@@ -341,7 +341,7 @@ fipi_status fipi_trajectory_backward(fipi_ctx* ctx, const double* dc, const doub
 
 /* ------------------------------------------------ seeded synthetic inputs
  * Host-only helpers (no device needed).  The reference draws its initial
- * state from unseeded rand() (field.cpp:96, cluster.cpp:153-183); these draw
+ * state from unseeded rand() (field.cpp:96, cluster.cpp:59-89); these draw
  * from a splitmix64 stream so runs are reproducible. */
 /* c[i] = mean + amp * U(-1, 1), V values. */
 fipi_status fipi_seed_phase(const fipi_params* p, uint64_t seed, double mean, double amp, double* c);
@@ -349,7 +349,7 @@ fipi_status fipi_seed_phase(const fipi_params* p, uint64_t seed, double mean, do
  * contact angles U[theta_min, theta_max] degrees returned as cos(theta).
  * Without allow_overlap the spheres are placed by random sequential
  * addition with the periodic minimum-image distance >= r_i + r_j
- * (the reference's check_overlap, cluster.cpp:192-207, ignores periodic
+ * (the reference's check_overlap, cluster.cpp:98-113, ignores periodic
  * images).  r and cos_theta may be NULL. */
 fipi_status fipi_seed_particles(const fipi_params* p, uint64_t seed, double r_min, double r_max,
                                 double theta_min_deg, double theta_max_deg, int allow_overlap,

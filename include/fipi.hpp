@@ -1,6 +1,6 @@
 // fipi.hpp — header-only C++ view of the C ABI in fipi.h, in the
 // reference's vocabulary.  `fipi::simulation` owns a context (the fields of
-// main.cpp:126-155 and the `cluster` of cluster.cpp:21-40 on the GPU);
+// main.cpp:29-58 and the `cluster` of cluster.cpp:21-40 on the GPU);
 // its members are named after the reference calls they replace.  Errors
 // throw fipi::error (the reference printed and called exit(0)).
 #ifndef FIPI_HPP
@@ -67,7 +67,7 @@ public:
         return p;
     }
 
-    // ---- the loop body of main.cpp:172-316
+    // ---- the loop body of main.cpp:75-219
     void step(int n = 1) { check(fipi_step(ctx_, n)); }
     int time() const {
         int t = 0;

@@ -5,7 +5,7 @@
  * row-major dims (n0 slowest ... n2 fastest), forward sign -1, backward
  * sign +1, unnormalised.  The reference executes exactly this transform
  * through fftw_plan_dft_3d(Nz, Ny, Nx, ...) / fftw_execute_dft
- * (main.cpp:167-170, field.cpp:441,451).  Power-of-two sizes only.
+ * (main.cpp:70-73, field.cpp:441,451).  Power-of-two sizes only.
  */
 #ifndef ORACLE_FFT_C2C_H
 #define ORACLE_FFT_C2C_H

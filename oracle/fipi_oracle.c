@@ -13,8 +13,8 @@
  * Where the reference is undefined or random, the oracle picks a defined
  * behaviour and the GPU library picks the same one:
  *  - grid index floor(x/dx) == N (x within an ulp of L) wraps to 0
- *    (field.cpp:229-245 and cluster.cpp:454-497 read out of bounds);
- *  - coincident particles (|d| == 0, cluster.cpp:328-336 draws rand())
+ *    (field.cpp:229-245 and cluster.cpp:360-403 read out of bounds);
+ *  - coincident particles (|d| == 0, cluster.cpp:234-242 draws rand())
  *    get the separation of coincident_d() below.
  */
 #include "fipi_oracle.h"
@@ -73,7 +73,7 @@ oracle* oracle_create(const fipi_params* P) {
     oracle* o = (oracle*)calloc(1, sizeof(oracle));
     o->P = *P;
     o->V = (long)P->nx * P->ny * P->nz;
-    o->plan = offt_create(P->nz, P->ny, P->nx); /* main.cpp:169-170 plan dims (Nz,Ny,Nx) */
+    o->plan = offt_create(P->nz, P->ny, P->nx); /* main.cpp:72-73 plan dims (Nz,Ny,Nx) */
     if (!o->plan) {
         free(o);
         return NULL;
@@ -111,8 +111,8 @@ oracle* oracle_create(const fipi_params* P) {
     o->r = (double*)calloc(n3 / 3, sizeof(double));
     o->cth = (double*)calloc(n3 / 3, sizeof(double));
     for (int i = 0; i < n; ++i) {
-        o->r[i] = P->r_p;  /* element.cpp:119 */
-        o->c_loc[i] = 1.0; /* element.cpp:128 */
+        o->r[i] = P->r_p;  /* element.cpp:25 */
+        o->c_loc[i] = 1.0; /* element.cpp:34 */
     }
     int nc[3];
     double dc[3];
@@ -120,7 +120,7 @@ oracle* oracle_create(const fipi_params* P) {
     o->keys = (int*)calloc(n3 / 3, sizeof(int));
     o->sorted = (int*)calloc(n3 / 3, sizeof(int));
     o->offsets = (int*)calloc((size_t)nc[0] * nc[1] * nc[2] + 1, sizeof(int));
-    o->it_mark = -1; /* cluster.cpp:133 */
+    o->it_mark = -1; /* cluster.cpp:39 */
     o->tau = 0.0;
     o->t = 0;
     return o;
@@ -169,7 +169,7 @@ int oracle_set_particles(oracle* o, const double* p, const double* r, const doub
     for (int i = 0; i < o->n; ++i) {
         for (int a = 0; a < 3; ++a) {
             o->p[3 * i + a] = p[3 * i + a];
-            o->p_old[3 * i + a] = p[3 * i + a]; /* cluster.cpp:182 */
+            o->p_old[3 * i + a] = p[3 * i + a]; /* cluster.cpp:88 */
             o->f_pp[3 * i + a] = f_pp ? f_pp[3 * i + a] : 0.0;
         }
         o->r[i] = r ? r[i] : o->P.r_p;
@@ -211,7 +211,7 @@ void oracle_fft3(const fipi_params* P, double* data, int sign) {
 /* field::fft (field.cpp:438-443) */
 static void fft(oracle* o, double* a) { offt_execute(o->plan, a, -1); }
 
-/* field::ifft + normalize (field.cpp:446-455, primitive.cpp:137-145) */
+/* field::ifft + normalize (field.cpp:446-455, primitive.cpp:54-62) */
 static void ifft(oracle* o, double* a) {
     offt_execute(o->plan, a, +1);
     const int nn = o->P.nx * o->P.ny * o->P.nz;
@@ -230,7 +230,7 @@ static double (*volatile field_pow)(double, double) = pow;
 #define IDX_J(o, it) ((int)(((it) / (o)->P.nx) % (o)->P.ny))
 #define IDX_K(o, it) ((int)((it) / ((long)(o)->P.nx * (o)->P.ny)))
 
-/* kf2 = kf.power(2.0) (main.cpp:128, field.cpp:408-431): sum of squares
+/* kf2 = kf.power(2.0) (main.cpp:31, field.cpp:408-431): sum of squares
  * accumulated from 0.0 in component order. */
 static inline double kf2_at(const oracle* o, long it) {
     double kx = o->kx[IDX_I(o, it)], ky = o->ky[IDX_J(o, it)], kz = o->kz[IDX_K(o, it)];
@@ -261,7 +261,7 @@ static void grad_spectral(oracle* o, const double* a, double* g[3]) {
     }
 }
 
-/* c.fft; grad_c = c.grad(kf); grad_c.ifft  (main.cpp:287-289) on a real c. */
+/* c.fft; grad_c = c.grad(kf); grad_c.ifft  (main.cpp:190-192) on a real c. */
 void oracle_grad(const fipi_params* P, const double* c, double* out) {
     oracle* o = oracle_create(P);
     if (!o) return;
@@ -301,7 +301,7 @@ void oracle_div(const fipi_params* P, const double* v, double* out) {
     oracle_destroy(o);
 }
 
-/* f = (lambda/sqr(epsilon))*(c.power(3.0)-c)  (main.cpp:178, 250) */
+/* f = (lambda/sqr(epsilon))*(c.power(3.0)-c)  (main.cpp:81, 153) */
 static void bulk_potential(oracle* o) {
     const double s = o->P.lambda / (o->P.epsilon * o->P.epsilon);
     for (long it = 0; it < o->V; ++it) {
@@ -315,7 +315,7 @@ static void bulk_potential(oracle* o) {
 
 /* ------------------------------------------------------------- particles */
 void oracle_cell_geometry(const fipi_params* P, int nc[3], double dc[3]) {
-    /* cluster.cpp:120-126 */
+    /* cluster.cpp:26-32 */
     const double L[3] = {P->lx, P->ly, P->lz};
     for (int a = 0; a < 3; ++a) {
         nc[a] = (int)floor(L[a] / P->r_c + 2 * P->margin / P->r_c);
@@ -324,7 +324,7 @@ void oracle_cell_geometry(const fipi_params* P, int nc[3], double dc[3]) {
 }
 
 static inline int cell_coord(double x, double dcell, double margin) {
-    return (int)floor(x / dcell + margin / dcell); /* cluster.cpp:234-236, 291-293 */
+    return (int)floor(x / dcell + margin / dcell); /* cluster.cpp:140-142, 197-199 */
 }
 
 int oracle_sorting(const fipi_params* P, int n, const double* p, int* keys, int* sorted,
@@ -333,10 +333,10 @@ int oracle_sorting(const fipi_params* P, int n, const double* p, int* keys, int*
     double dc[3];
     oracle_cell_geometry(P, nc, dc);
     const int ncells = nc[0] * nc[1] * nc[2];
-    double y_max = 0.0; /* cluster.cpp:222 */
+    double y_max = 0.0; /* cluster.cpp:128 */
     int status = FIPI_OK;
     for (int it = 0; it < n; ++it) {
-        if (p[3 * it + 1] > y_max) { /* cluster.cpp:228-232 */
+        if (p[3 * it + 1] > y_max) { /* cluster.cpp:134-138 */
             y_max = p[3 * it + 1];
             if (it_mark) *it_mark = it;
         }
@@ -344,11 +344,11 @@ int oracle_sorting(const fipi_params* P, int n, const double* p, int* keys, int*
         const int j = cell_coord(p[3 * it + 1], dc[1], P->margin);
         const int k = cell_coord(p[3 * it + 2], dc[2], P->margin);
         if (i < 0 || i >= nc[0] || j < 0 || j >= nc[1] || k < 0 || k >= nc[2]) {
-            status = FIPI_ERR_OUT_OF_RANGE; /* cluster.cpp:238-257 */
+            status = FIPI_ERR_OUT_OF_RANGE; /* cluster.cpp:144-163 */
             keys[it] = -1;
             continue;
         }
-        keys[it] = i + j * nc[0] + k * nc[0] * nc[1]; /* cluster.cpp:259 */
+        keys[it] = i + j * nc[0] + k * nc[0] * nc[1]; /* cluster.cpp:165 */
     }
     if (status != FIPI_OK) return status;
     /* Appending ids in ascending order to per-cell lists (linked_list.cpp:30-43)
@@ -363,7 +363,7 @@ int oracle_sorting(const fipi_params* P, int n, const double* p, int* keys, int*
     return FIPI_OK;
 }
 
-/* primitive.cpp:205-212 */
+/* primitive.cpp:122-129 */
 static double ramp(double t, double thr) {
     if (t < 0) return 0.0;
     else if (t >= 0 && t < thr) return t / thr;
@@ -376,7 +376,7 @@ static inline double vnorm(double x, double y, double z) {
 }
 
 /* Separation used when two particles coincide exactly.  The reference
- * draws rand()%1000/1e3*2 r_p - r_p per component (cluster.cpp:328-336);
+ * draws rand()%1000/1e3*2 r_p - r_p per component (cluster.cpp:234-242);
  * this draws the same 1e-3 lattice from a hash of the pair, so the
  * oracle and the GPU agree.  Not pinned to the reference (its rand()). */
 void oracle_coincident_d(int a, int b, double r_p, double d[3]) {
@@ -422,10 +422,10 @@ int oracle_f_pp(const fipi_params* P, int n, const double* p, int t, const doubl
     }
     pair_t* plist = NULL;
     long np_cap = 0, np_cnt = 0;
-    const double bx = P->lx, by = P->ly, bz = P->lz; /* bc_x, bc_y, bc_z (cluster.cpp:279-281) */
+    const double bx = P->lx, by = P->ly, bz = P->lz; /* bc_x, bc_y, bc_z (cluster.cpp:185-187) */
     const double rmp = ramp((double)t, 0.2 * P->t_end);
     double tau = 0.0;
-    for (int it = 0; it < 3 * n; ++it) f_pp[it] = 0.0; /* cluster.cpp:285 */
+    for (int it = 0; it < 3 * n; ++it) f_pp[it] = 0.0; /* cluster.cpp:191 */
     for (int it = 0; it < n; ++it) {
         const int o_ = cell_coord(p[3 * it], dc[0], P->margin);
         const int p_ = cell_coord(p[3 * it + 1], dc[1], P->margin);
@@ -438,10 +438,10 @@ int oracle_f_pp(const fipi_params* P, int n, const double* p, int t, const doubl
                     co += (k + nc[2]) % nc[2] * nc[0] * nc[1];
                     for (int s = offsets[co]; s < offsets[co + 1]; ++s) {
                         const int id = sorted[s];
-                        if (!(id > it)) continue; /* cluster.cpp:314 */
+                        if (!(id > it)) continue; /* cluster.cpp:220 */
                         double d[3] = {p[3 * it] - p[3 * id], p[3 * it + 1] - p[3 * id + 1],
                                        p[3 * it + 2] - p[3 * id + 2]};
-                        /* cluster.cpp:319-326 */
+                        /* cluster.cpp:225-232 */
                         if (d[0] > dc[0] * (nc[0] - 2)) d[0] = d[0] - bx;
                         else if (d[0] < -dc[0] * (nc[0] - 2)) d[0] = d[0] + bx;
                         if (d[1] > dc[1] * (nc[1] - 2)) d[1] = d[1] - by;
@@ -450,7 +450,7 @@ int oracle_f_pp(const fipi_params* P, int n, const double* p, int t, const doubl
                         else if (d[2] < -dc[2] * (nc[2] - 2)) d[2] = d[2] + bz;
                         if (vnorm(d[0], d[1], d[2]) == 0.0) oracle_coincident_d(it, id, P->r_p, d);
                         const double dn = vnorm(d[0], d[1], d[2]);
-                        if (dn < P->r_eq) { /* cluster.cpp:340-356 */
+                        if (dn < P->r_eq) { /* cluster.cpp:246-262 */
                             const double s_ = (P->r_eq - dn) * rmp * P->k_n;
                             double fn[3];
                             for (int a = 0; a < 3; ++a) fn[a] = (d[a] / dn) * s_;
@@ -556,7 +556,7 @@ void oracle_interpolate2(const fipi_params* P, const double* v, int n, const dou
     }
 }
 
-/* element::get_f_pi (element.cpp:169-191) with the contact-angle extension:
+/* element::get_f_pi (element.cpp:75-97) with the contact-angle extension:
  * f_mag = -A pi (d - r cos_theta) sigma; cos_theta = 0 is the reference. */
 void oracle_f_pi(const fipi_params* P, int n, const double* c_loc, const double* dcdx,
                  const double* r, const double* cth, double* f_pi) {
@@ -581,8 +581,8 @@ void oracle_f_pi(const fipi_params* P, int n, const double* c_loc, const double*
     }
 }
 
-/* element::advect (element.cpp:250-267); f_ext = 0 (element.cpp:194-198)
- * and uf = 0 (get_local_u, element.cpp:132-146). */
+/* element::advect (element.cpp:156-173); f_ext = 0 (element.cpp:100-104)
+ * and uf = 0 (get_local_u, element.cpp:38-52). */
 void oracle_advect(const fipi_params* P, int n, int stage, const double* f_pi,
                    const double* f_pp, const double* r, double* p, double* p_old,
                    double* u_old) {
@@ -608,7 +608,7 @@ void oracle_advect(const fipi_params* P, int n, int stage, const double* f_pi,
     }
 }
 
-/* element::enforce_bc (element.cpp:271-280) */
+/* element::enforce_bc (element.cpp:177-185) */
 void oracle_enforce_bc(const fipi_params* P, int n, double* p) {
     for (int q = 0; q < n; ++q) {
         p[3 * q] = fmod(p[3 * q] + P->lx, P->lx);
@@ -617,7 +617,7 @@ void oracle_enforce_bc(const fipi_params* P, int n, double* p) {
     }
 }
 
-/* cluster::compute_f_r (cluster.cpp:438-504) into out (3 x V reals, zeroed here). */
+/* cluster::compute_f_r (cluster.cpp:344-410) into out (3 x V reals, zeroed here). */
 void oracle_spread(const fipi_params* P, int n, const double* pos, const double* f_pp,
                    double* out) {
     const int Nx = P->nx, Ny = P->ny, Nz = P->nz;
@@ -636,7 +636,7 @@ void oracle_spread(const fipi_params* P, int n, const double* pos, const double*
         y %= Ny;
         z %= Nz;
         const int x1 = (x + 1) % Nx, y1 = (y + 1) % Ny, z1 = (z + 1) % Nz;
-        /* corner order and weight products of cluster.cpp:462-500 */
+        /* corner order and weight products of cluster.cpp:368-406 */
         const long co[8] = {x + y * Nx + (long)z * Nx * Ny,    x1 + y * Nx + (long)z * Nx * Ny,
                             x1 + y1 * Nx + (long)z * Nx * Ny,  x1 + y * Nx + (long)z1 * Nx * Ny,
                             x1 + y1 * Nx + (long)z1 * Nx * Ny, x + y * Nx + (long)z1 * Nx * Ny,
@@ -660,7 +660,7 @@ static void particle_stage(oracle* o, int stage) {
     const fipi_params* P = &o->P;
     const int n = o->n;
     const long V = o->V;
-    /* interpolate_local_variables (cluster.cpp:401-417) */
+    /* interpolate_local_variables (cluster.cpp:307-323) */
     if (P->switch_ch) {
         double* tmp = (double*)malloc(sizeof(double) * (size_t)V);
         double* vals = (double*)malloc(sizeof(double) * (size_t)(n > 0 ? n : 1));
@@ -674,13 +674,13 @@ static void particle_stage(oracle* o, int stage) {
         free(tmp);
         free(vals);
     }
-    /* sorting (cluster.cpp:210-263) */
+    /* sorting (cluster.cpp:116-169) */
     (void)oracle_sorting(P, n, o->p, o->keys, o->sorted, o->offsets, &o->it_mark);
-    /* compute_f_pi (cluster.cpp:380-384) */
+    /* compute_f_pi (cluster.cpp:286-290) */
     oracle_f_pi(P, n, o->c_loc, o->dcdx, o->r, o->cth, o->f_pi);
-    /* compute_f_pp(t+1) (main.cpp:299, 310) */
+    /* compute_f_pp(t+1) (main.cpp:202, 213) */
     oracle_f_pp(P, n, o->p, o->t + 1, o->f_pi, o->f_pp, &o->tau, NULL, 0, NULL);
-    /* compute_f_ext: zero (element.cpp:194-198); advect; enforce_bc */
+    /* compute_f_ext: zero (element.cpp:100-104); advect; enforce_bc */
     oracle_advect(P, n, stage, o->f_pi, o->f_pp, o->r, o->p, o->p_old, o->u_old);
     oracle_enforce_bc(P, n, o->p);
 }
@@ -707,13 +707,13 @@ int oracle_step(oracle* o) {
         if (st != FIPI_OK) return st;
     }
 
-    /* ------------------------------------------- Phase field (main.cpp:176-238) */
+    /* ------------------------------------------- Phase field (main.cpp:79-141) */
     if (P->switch_ch) {
-        bulk_potential(o); /* main.cpp:178 */
-        fft(o, o->f);      /* main.cpp:180 */
-        fft(o, o->c);      /* main.cpp:181 */
+        bulk_potential(o); /* main.cpp:81 */
+        fft(o, o->f);      /* main.cpp:83 */
+        fft(o, o->c);      /* main.cpp:84 */
         if (P->switch_ns) {
-            grad_spectral(o, o->c, o->grad); /* main.cpp:185 */
+            grad_spectral(o, o->c, o->grad); /* main.cpp:88 */
             for (int d = 0; d < 3; ++d) ifft(o, o->grad[d]);
             for (long it = 0; it < V; ++it) { /* conv_c = u.dot(grad_c) (field.cpp:388-401) */
                 double s = 0.0;
@@ -721,9 +721,9 @@ int oracle_step(oracle* o) {
                 o->conv[2 * it] = s;
                 o->conv[2 * it + 1] = 0.0;
             }
-            fft(o, o->conv); /* main.cpp:189 */
+            fft(o, o->conv); /* main.cpp:92 */
         }
-        if (t == 0) { /* main.cpp:192-211 */
+        if (t == 0) { /* main.cpp:95-114 */
             memcpy(o->c_old, o->c, sizeof(double) * 2 * (size_t)V);
             memcpy(o->f_old, o->f, sizeof(double) * 2 * (size_t)V);
             if (P->switch_ns) memcpy(o->conv_old, o->conv, sizeof(double) * 2 * (size_t)V);
@@ -743,7 +743,7 @@ int oracle_step(oracle* o) {
                 o->c[2 * it] /= den;
                 o->c[2 * it + 1] /= den;
             }
-        } else { /* main.cpp:212-235 */
+        } else { /* main.cpp:115-138 */
             const double s4 = 4.0 * dt * M, s2m = 2.0 * dt * M;
             const double s4c = 4.0 * dt, s2c = 2.0 * dt, s3 = 2.0 * dt * M * lam;
             for (long it = 0; it < V; ++it) {
@@ -767,7 +767,7 @@ int oracle_step(oracle* o) {
                 o->c_new[2 * it] = re / den;
                 o->c_new[2 * it + 1] = im / den;
             }
-            /* c_old = c; f_old = f; conv_c_old = conv_c; c = c_new (main.cpp:226-234) */
+            /* c_old = c; f_old = f; conv_c_old = conv_c; c = c_new (main.cpp:129-137) */
             double* tmp = o->c_old;
             o->c_old = o->c;
             o->c = o->c_new;
@@ -781,26 +781,26 @@ int oracle_step(oracle* o) {
                 o->conv = tmp;
             }
         }
-        ifft(o, o->c); /* main.cpp:237 */
+        ifft(o, o->c); /* main.cpp:140 */
     }
 
-    /* ------------------------------------------- Fluid velocity (main.cpp:243-278) */
+    /* ------------------------------------------- Fluid velocity (main.cpp:146-181) */
     if (P->switch_ns) {
         for (int d = 0; d < 3; ++d) memset(o->ftot[d], 0, sizeof(double) * 2 * (size_t)V);
         if (P->switch_ch) {
-            bulk_potential(o); /* main.cpp:250 */
+            bulk_potential(o); /* main.cpp:153 */
             fft(o, o->f);
             fft(o, o->c);
-            for (long it = 0; it < V; ++it) { /* pch = lambda*kf2*c + f (main.cpp:254) */
+            for (long it = 0; it < V; ++it) { /* pch = lambda*kf2*c + f (main.cpp:157) */
                 const double a = kf2_at(o, it) * lam;
                 o->pch[2 * it] = a * o->c[2 * it] + o->f[2 * it];
                 o->pch[2 * it + 1] = a * o->c[2 * it + 1] + o->f[2 * it + 1];
             }
             ifft(o, o->pch);
-            grad_spectral(o, o->c, o->grad); /* main.cpp:257-259 */
+            grad_spectral(o, o->c, o->grad); /* main.cpp:160-162 */
             for (int d = 0; d < 3; ++d) ifft(o, o->grad[d]);
             ifft(o, o->c);
-            for (int d = 0; d < 3; ++d) /* f_total += pch*grad_c (main.cpp:261) */
+            for (int d = 0; d < 3; ++d) /* f_total += pch*grad_c (main.cpp:164) */
                 for (long it = 0; it < V; ++it) {
                     o->ftot[d][2 * it] += o->pch[2 * it] * o->grad[d][2 * it];
                     o->ftot[d][2 * it + 1] = 0.0;
@@ -816,7 +816,7 @@ int oracle_step(oracle* o) {
                 }
             free(sp);
         }
-        for (long it = 0; it < V; ++it) { /* buoyancy (main.cpp:269) */
+        for (long it = 0; it < V; ++it) { /* buoyancy (main.cpp:172) */
             const double cr = o->c[2 * it];
             double a = cr + 1.0;
             a = a / 2.0;
@@ -830,8 +830,8 @@ int oracle_step(oracle* o) {
             o->ftot[2][2 * it] += s * P->gravity;
             for (int d = 0; d < 3; ++d) o->ftot[d][2 * it + 1] = 0.0;
         }
-        for (int d = 0; d < 3; ++d) fft(o, o->ftot[d]); /* main.cpp:272 */
-        /* u = f_total - kf*(kf.dot(f_total))/kf2; u /= mu*kf2 (main.cpp:274-275) */
+        for (int d = 0; d < 3; ++d) fft(o, o->ftot[d]); /* main.cpp:175 */
+        /* u = f_total - kf*(kf.dot(f_total))/kf2; u /= mu*kf2 (main.cpp:177-178) */
         for (long it = 0; it < V; ++it) {
             const double kv[3] = {o->kx[IDX_I(o, it)], o->ky[IDX_J(o, it)], o->kz[IDX_K(o, it)]};
             const double k2 = kf2_at(o, it);
@@ -863,13 +863,13 @@ int oracle_step(oracle* o) {
                 o->u[d][2 * it + 1] = uim;
             }
         }
-        for (int d = 0; d < 3; ++d) ifft(o, o->u[d]); /* main.cpp:276 */
+        for (int d = 0; d < 3; ++d) ifft(o, o->u[d]); /* main.cpp:179 */
     }
 
-    /* ------------------------------------------- Particles (main.cpp:283-316) */
+    /* ------------------------------------------- Particles (main.cpp:186-219) */
     if (P->switch_particle && o->n > 0) {
         if (P->switch_ch) {
-            fft(o, o->c); /* main.cpp:287-290 */
+            fft(o, o->c); /* main.cpp:190-193 */
             grad_spectral(o, o->c, o->grad);
             for (int d = 0; d < 3; ++d) ifft(o, o->grad[d]);
             ifft(o, o->c);
@@ -881,7 +881,7 @@ int oracle_step(oracle* o) {
     return FIPI_OK;
 }
 
-/* main.cpp:329 with field.cpp:507-516: sum of
+/* main.cpp:232 with field.cpp:507-516: sum of
  * lambda*(0.5 |grad c|^2 + 0.25/eps^2 (c^2-1)^2) * dx^3. */
 double oracle_free_energy(const oracle* o) {
     const fipi_params* P = &o->P;

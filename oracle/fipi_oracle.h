@@ -2,7 +2,7 @@
  * TEST INFRASTRUCTURE ONLY (oracle).  Only tests/, __graft_entry__.smoke()
  * and bench.py's CPU-baseline leg may load this; the product never does.
  *
- * A plain-C, FP64 restatement of the reference FIPI step (main.cpp:172-316)
+ * A plain-C, FP64 restatement of the reference FIPI step (main.cpp:75-219)
  * and of the field / cluster / element calls it makes, using full complex
  * C2C fields exactly as the reference does (field.cpp:41-46), so that it
  * reproduces the reference's arithmetic, its Nyquist handling and its
@@ -25,9 +25,9 @@ typedef struct oracle oracle;
  * (non power-of-two grid, fewer than 3 cells per axis with particles on). */
 oracle* oracle_create(const fipi_params* p);
 int oracle_params_ok(const fipi_params* p);
-/* cluster.cpp:120-126 */
+/* cluster.cpp:26-32 */
 void oracle_cell_geometry(const fipi_params* p, int nc[3], double dc[3]);
-/* deterministic stand-in for the rand() separation of cluster.cpp:328-336 */
+/* deterministic stand-in for the rand() separation of cluster.cpp:234-242 */
 void oracle_coincident_d(int a, int b, double r_p, double d[3]);
 void oracle_destroy(oracle* o);
 void oracle_set_threads(int n);
@@ -45,8 +45,8 @@ void oracle_get_particles(const oracle* o, double* p, double* f_pp, double* f_pi
 double oracle_tau(const oracle* o);
 int oracle_time(const oracle* o);
 
-/* One iteration of the main.cpp:172-316 loop body; returns FIPI_OK or
- * FIPI_ERR_OUT_OF_RANGE (the reference's cluster.cpp:238-257 exit). */
+/* One iteration of the main.cpp:75-219 loop body; returns FIPI_OK or
+ * FIPI_ERR_OUT_OF_RANGE (the reference's cluster.cpp:144-163 exit). */
 int oracle_step(oracle* o);
 
 /* Fine-grained restatements (stateless w.r.t. the step). */

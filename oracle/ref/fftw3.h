@@ -1,7 +1,7 @@
 /*
  * TEST INFRASTRUCTURE ONLY (oracle recipe).
  *
- * The subset of the FFTW3 API that the reference calls (main.cpp:167-170,
+ * The subset of the FFTW3 API that the reference calls (main.cpp:70-73,
  * field.cpp:41-46, 441, 451, 461), declared from FFTW3's public
  * documentation and implemented by fftw_shim.c on top of the oracle's own
  * C2C transform.  FFTW3 is an external dependency of the reference

@@ -3,10 +3,10 @@
  *
  * Harness around the reference's own objects (field, cluster, element),
  * compiled together with the reference sources where they lie.  main.cpp is
- * not compiled: its set-up (main.cpp:126-170) and loop body
- * (main.cpp:172-316) are restated call for call below, with seeded initial
+ * not compiled: its set-up (main.cpp:29-73) and loop body
+ * (main.cpp:75-219) are restated call for call below, with seeded initial
  * conditions injected after construction (replacing rand() in
- * field.cpp:96 and cluster.cpp:153-183) and the VTK output skipped.
+ * field.cpp:96 and cluster.cpp:59-89) and the VTK output skipped.
  *
  * The generated configuration header (pre-included) defines the HEAD guard,
  * every constant of head.hpp and `private` as `public`, so the harness can
@@ -40,16 +40,16 @@ struct Sim {
     int t = 0;
 
     Sim() {
-        kf2 = kf.power(2.0); /* main.cpp:128 */
+        kf2 = kf.power(2.0); /* main.cpp:31 */
         fftw_init_threads();
-        fftw_plan_with_nthreads(4); /* main.cpp:167 */
+        fftw_plan_with_nthreads(4); /* main.cpp:70 */
         fftw_complex* dummy = (fftw_complex*)fftw_malloc(sizeof(fftw_complex) * Nx * Ny * Nz);
         p_forward = fftw_plan_dft_3d(Nz, Ny, Nx, dummy, dummy, FFTW_FORWARD, FFTW_ESTIMATE);
         p_backward = fftw_plan_dft_3d(Nz, Ny, Nx, dummy, dummy, FFTW_BACKWARD, FFTW_ESTIMATE);
         fftw_free(dummy);
     }
 
-    /* Loop body of main.cpp:172-316 for the current t. */
+    /* Loop body of main.cpp:75-219 for the current t. */
     void step() {
         if (switch_ch) {
             f = (lambda / sqr(epsilon)) * (c.power(3.0) - c);
@@ -134,7 +134,7 @@ Sim* g_sim = nullptr;
 const long V = (long)Nx * Ny * Nz;
 
 /* cluster::sorting exits the process on an out-of-range particle
- * (cluster.cpp:238-257); check the same expression first. */
+ * (cluster.cpp:144-163); check the same expression first. */
 bool in_sorting_range(const cluster& s, const double* p, int n) {
     for (int it = 0; it < n; ++it) {
         int i = int(floor(p[3 * it] / s.dx_cell + margin / s.dx_cell));
@@ -237,7 +237,7 @@ void ref_get_particles(double* p, double* f_pp, double* f_pi) {
 }
 double ref_tau(void) { return g_sim->suspension.tau; }
 
-/* main.cpp:329 free energy, summed like field.cpp:507-516. */
+/* main.cpp:232 free energy, summed like field.cpp:507-516. */
 double ref_free_energy(void) {
     field fe("SCALARS");
     fe = lambda * (0.5 * g_sim->grad_c.power(2.0) +
@@ -260,7 +260,7 @@ void ref_fft(double* data, int sign, int normalise) {
     std::memcpy(data, a.v[0], sizeof(fftw_complex) * V);
 }
 
-/* c.fft; grad_c = c.grad(kf); grad_c.ifft  (main.cpp:287-289) */
+/* c.fft; grad_c = c.grad(kf); grad_c.ifft  (main.cpp:190-192) */
 void ref_grad(const double* c, double* out) {
     if (!g_sim) g_sim = new Sim();
     field a("SCALARS");

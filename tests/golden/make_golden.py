@@ -33,7 +33,7 @@ def inputs(name, seed):
     k = rng.integers(0, 1000, w.V).astype(np.uint16)
     c0 = k.astype(np.float64) / 1e3 * 0.2 - 0.1
     L = np.array([w.lx, w.ly, w.lz])
-    u = rng.integers(0, 1000, (w.n_p, 3)).astype(np.float64) / 1e3  # cluster.cpp:157-166 lattice
+    u = rng.integers(0, 1000, (w.n_p, 3)).astype(np.float64) / 1e3  # cluster.cpp:63-72 lattice
     p0 = (u * L).ravel()
     return w, k, c0, p0
 

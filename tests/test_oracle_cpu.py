@@ -150,7 +150,7 @@ def test_oracle_out_of_range_particle(oracle_mod):
     w = workload("t32")
     P = w.params()
     p = np.full(3 * w.n_p, 1.0)
-    p[5] = w.lx + 1.0  # outside the cell grid: the reference exits (cluster.cpp:238-257)
+    p[5] = w.lx + 1.0  # outside the cell grid: the reference exits (cluster.cpp:144-163)
     st, *_ = oracle_mod.sorting(P, p)
     assert st == 4
     port = oracle_mod.Port(P)
