@@ -150,6 +150,75 @@ template <typename T, int NRF> struct XGlobalRow {
     }
 };
 
+// Split processing of the half-length complex transforms of the X pass
+// (N = 2M real points as M complex pairs), W_k = twx[k] = exp(-2 pi i k / N).
+// Each thread keeps one k (its twiddles in registers) and walks rows; the
+// self-paired k = M/2 of every row follows, one row per thread.
+// C2R pre-processing: Z_k = (X_k + conj X_{M-k}) + i conj(W_k) (X_k - conj X_{M-k});
+// only the real parts of X_0 and X_M enter.
+template <typename T, int M, int ROWS, int NT, class Idx>
+__device__ __forceinline__ void c2r_pre(cplx<T>* s, const Idx& idx, const cplx<T>* __restrict__ twx, int tid) {
+    using C = cplx<T>;
+    constexpr int HM = M / 2;
+    constexpr int L = HM < NT ? HM : NT;  // lanes per row
+    constexpr int RG = NT / L;            // rows in flight
+    const int lane = tid % L, rg = tid / L;
+    auto pair = [&](int row, int k, const C Wk, const C Wm) {
+        const int km = M - k;
+        const C Xk = s[idx(row, k)], Xm = s[idx(row, km)];
+        const C A = cadd(Xk, cconj(Xm)), B = csub(Xk, cconj(Xm));
+        const C A2 = cadd(Xm, cconj(Xk)), B2 = csub(Xm, cconj(Xk));
+        s[idx(row, k)] = cadd(A, cmul_i(cmul(B, cconj(Wk)), +1));
+        if (km != k) s[idx(row, km)] = cadd(A2, cmul_i(cmul(B2, cconj(Wm)), +1));
+    };
+    for (int k = lane; k < HM; k += L) {
+        const C Wk = twx[k], Wm = twx[M - k];
+        for (int row = rg; row < ROWS; row += RG) {
+            if (k == 0) {
+                const T a = s[idx(row, 0)].x, c = s[idx(row, M)].x;
+                s[idx(row, 0)] = mkc<C>(a + c, a - c);
+            } else {
+                pair(row, k, Wk, Wm);
+            }
+        }
+    }
+    const C Wh = twx[HM];
+    for (int row = tid; row < ROWS; row += NT) pair(row, HM, Wh, Wh);
+}
+
+// R2C post-processing: X_k = (E - i W_k D) / 2 with E = Z_k + conj Z_{M-k},
+// D = Z_k - conj Z_{M-k}; X_0 and X_M from Z_0; X_M lands at index M.
+template <typename T, int M, int ROWS, int NT, class Idx>
+__device__ __forceinline__ void r2c_post(cplx<T>* s, const Idx& idx, const cplx<T>* __restrict__ twx, int tid) {
+    using C = cplx<T>;
+    constexpr int HM = M / 2;
+    constexpr int L = HM < NT ? HM : NT;
+    constexpr int RG = NT / L;
+    const int lane = tid % L, rg = tid / L;
+    auto pair = [&](int row, int k, const C Wk, const C Wm) {
+        const int km = M - k;
+        const C Zk = s[idx(row, k)], Zm = s[idx(row, km)];
+        const C E1 = cadd(Zk, cconj(Zm)), D1 = csub(Zk, cconj(Zm));
+        const C E2 = cadd(Zm, cconj(Zk)), D2 = csub(Zm, cconj(Zk));
+        s[idx(row, k)] = cscale(csub(E1, cmul_i(cmul(Wk, D1), +1)), T(0.5));
+        if (km != k) s[idx(row, km)] = cscale(csub(E2, cmul_i(cmul(Wm, D2), +1)), T(0.5));
+    };
+    for (int k = lane; k < HM; k += L) {
+        const C Wk = twx[k], Wm = twx[M - k];
+        for (int row = rg; row < ROWS; row += RG) {
+            if (k == 0) {
+                const C Z0 = s[idx(row, 0)];
+                s[idx(row, 0)] = mkc<C>(Z0.x + Z0.y, T(0));
+                s[idx(row, M)] = mkc<C>(Z0.x - Z0.y, T(0));
+            } else {
+                pair(row, k, Wk, Wm);
+            }
+        }
+    }
+    const C Wh = twx[HM];
+    for (int row = tid; row < ROWS; row += NT) pair(row, HM, Wh, Wh);
+}
+
 // X pass: one block = TY consecutive rows y0..y0+TY-1 of plane z, NIN
 // spectral inputs (transposed runs of TY along y, C2R) and NOUT spectral
 // outputs (R2C, transposed store); point() does the fused real-space work
@@ -173,36 +242,24 @@ __global__ void __launch_bounds__(NT, XMinBlocks<T, (NIN > NOUT ? NIN : NOUT), N
     constexpr int H = M + 1;
     const IdxPadded idx{xpass_pitch(M)};
     const int z = blockIdx.y, y0 = blockIdx.x * TY;
-    const int tid = threadIdx.x, nthr = blockDim.x;
-    constexpr int halfM = M / 2;
+    const int tid = threadIdx.x;
     constexpr int Tn = FftPlan<M, FftE<T>::value>::Tn;
     constexpr int rpr = NT / Tn;  // row FFTs per round
+    // Loads and stores walk the tile field by field with ty fastest (a
+    // run of TY along y per kx): each thread keeps one ty and steps kx.
+    constexpr int KS = NT / TY;
+    const int tyl = tid % TY, kx0 = tid / TY;
+    const size_t gbase = (size_t)z * H * g.ny + y0 + tyl;
     if constexpr (NIN > 0) {
         // every element of the tile is requested before any is waited for
-        const int n = NIN * H * TY;
-        for (int i = tid; i < n; i += NT) {
-            const int ty = i % TY, rest = i / TY, kx = rest % H, f = rest / H;
-            cp_async<sizeof(C)>(&s[idx(f * TY + ty, kx)], in_sel<NIN>(op, f) + ((size_t)z * H + kx) * g.ny + y0 + ty);
+#pragma unroll
+        for (int f = 0; f < NIN; ++f) {
+            const C* src = op.in(f) + gbase;
+            for (int kx = kx0; kx < H; kx += KS) cp_async<sizeof(C)>(&s[idx(f * TY + tyl, kx)], src + (size_t)kx * g.ny);
         }
         cp_async_wait_all();
         __syncthreads();
-        // C2R split pre-processing (only the real parts of X_0 and X_M enter).
-        for (int i = tid; i < NIN * TY * (halfM + 1); i += nthr) {
-            const int k = i % (halfM + 1);
-            const int row = i / (halfM + 1);
-            if (k == 0) {
-                const T a = s[idx(row, 0)].x, c = s[idx(row, M)].x;
-                s[idx(row, 0)] = mkc<C>(a + c, a - c);
-            } else {
-                const int km = M - k;
-                const C Xk = s[idx(row, k)], Xm = s[idx(row, km)];
-                const C Wk = twx[k], Wm = twx[km];
-                const C A = cadd(Xk, cconj(Xm)), B = csub(Xk, cconj(Xm));
-                const C A2 = cadd(Xm, cconj(Xk)), B2 = csub(Xm, cconj(Xk));
-                s[idx(row, k)] = cadd(A, cmul_i(cmul(B, cconj(Wk)), +1));
-                if (km != k) s[idx(row, km)] = cadd(A2, cmul_i(cmul(B2, cconj(Wm)), +1));
-            }
-        }
+        c2r_pre<T, M, NIN * TY, NT>(s, idx, twx, tid);
         __syncthreads();
         for (int r0 = 0; r0 < NIN * TY; r0 += rpr) {
             const int row = r0 + tid / Tn;
@@ -211,7 +268,7 @@ __global__ void __launch_bounds__(NT, XMinBlocks<T, (NIN > NOUT ? NIN : NOUT), N
     }
     const T invV = T(1) / T(g.V);
     T acc = T(0);  // per-thread partial sum in the arithmetic type (FP64 only per block)
-    for (int i = tid; i < TY * M; i += nthr) {
+    for (int i = tid; i < TY * M; i += NT) {
         const int n = i % M;
         const int ty = i / M;
         C v[NF];
@@ -231,29 +288,12 @@ __global__ void __launch_bounds__(NT, XMinBlocks<T, (NIN > NOUT ? NIN : NOUT), N
             const int row = r0 + tid / Tn;
             smem_fft2<T, -1, M>(s, idx, row, tid % Tn, row < NOUT * TY, twx, 2);
         }
-        // R2C split post-processing; X_M lands at index M.
-        for (int i = tid; i < NOUT * TY * (halfM + 1); i += nthr) {
-            const int k = i % (halfM + 1);
-            const int row = i / (halfM + 1);
-            if (k == 0) {
-                const C Z0 = s[idx(row, 0)];
-                s[idx(row, 0)] = mkc<C>(Z0.x + Z0.y, T(0));
-                s[idx(row, M)] = mkc<C>(Z0.x - Z0.y, T(0));
-            } else {
-                const int km = M - k;
-                const C Zk = s[idx(row, k)], Zm = s[idx(row, km)];
-                const C Wk = twx[k], Wm = twx[km];
-                const C E1 = cadd(Zk, cconj(Zm)), D1 = csub(Zk, cconj(Zm));
-                const C E2 = cadd(Zm, cconj(Zk)), D2 = csub(Zm, cconj(Zk));
-                s[idx(row, k)] = cscale(csub(E1, cmul_i(cmul(Wk, D1), +1)), T(0.5));
-                if (km != k) s[idx(row, km)] = cscale(csub(E2, cmul_i(cmul(Wm, D2), +1)), T(0.5));
-            }
-        }
+        r2c_post<T, M, NOUT * TY, NT>(s, idx, twx, tid);
         __syncthreads();
-        const int n = NOUT * H * TY;
-        for (int i = tid; i < n; i += nthr) {
-            const int ty = i % TY, rest = i / TY, kx = rest % H, f = rest / H;
-            out_sel<NOUT>(op, f)[((size_t)z * H + kx) * g.ny + y0 + ty] = s[idx(f * TY + ty, kx)];
+#pragma unroll
+        for (int f = 0; f < NOUT; ++f) {
+            C* dst = op.out(f) + gbase;
+            for (int kx = kx0; kx < H; kx += KS) dst[(size_t)kx * g.ny] = s[idx(f * TY + tyl, kx)];
         }
     }
 }
