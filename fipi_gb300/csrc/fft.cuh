@@ -470,6 +470,66 @@ __global__ void __launch_bounds__(kThreads) k_zpass_rt_t(Geom g, const cplx<T>* 
     }
 }
 
+// Round trip held in registers (the FP32 passes): each thread loads its
+// column's modes straight into the first FFT stage, the mid operation runs
+// on the last stage's outputs (FftIO: the same modes the inverse's first
+// stage takes), and every inverse transform is stored from registers.
+// Shared memory only carries the exchanges between FFT stages, one field
+// at a time through a single tile.  The op supplies State (what a mode
+// keeps between the transforms), rr_mid (NF transformed values -> State),
+// rr_out (output b of a State) and rr_store (output b at gi).
+template <typename T, int NF, int NB, int DIR, int N, int COLS, class Op>
+__global__ void __launch_bounds__(kThreads, 2) k_zpass_rr(Geom g, const cplx<T>* __restrict__ twz, Op op) {
+    using C = cplx<T>;
+    using SH = ZRtShapeT<T, N, COLS>;
+    using IOF = FftIO<T, DIR, N>;
+    using IOI = FftIO<T, -DIR, N>;
+    constexpr int E = SH::E, TZ = SH::TZ;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C* s = reinterpret_cast<C*>(smem_raw);
+    const int kx = blockIdx.x, ky0 = blockIdx.y * TZ;
+    const int c = threadIdx.x % TZ, t = threadIdx.x / TZ;
+    const int ky = ky0 + c;
+    const size_t zstride = (size_t)g.h * g.ny;
+    const size_t base = (size_t)kx * g.ny + ky;
+    const IdxColumns idx{TZ};
+    op.prologue();
+    typename Op::State st[E];
+    {
+        C v[NF][E];
+#pragma unroll
+        for (int i = 0; i < E; ++i) {
+            const int z = IOF::in_elem(t, i);
+            C w[NF];
+            op.load(kx, ky, z, base + z * zstride, w);
+#pragma unroll
+            for (int f = 0; f < NF; ++f) v[f][i] = w[f];
+        }
+#pragma unroll
+        for (int f = 0; f < NF; ++f) smem_fft2<T, DIR, N, true, true>(s, idx, c, t, true, twz, 1, v[f]);
+#pragma unroll
+        for (int i = 0; i < E; ++i) {
+            const int z = IOF::out_elem(t, i);
+            C w[NF];
+#pragma unroll
+            for (int f = 0; f < NF; ++f) w[f] = v[f][i];
+            op.rr_mid(kx, ky, z, base + z * zstride, w, st[i]);
+        }
+    }
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+        C v[E];
+#pragma unroll
+        for (int i = 0; i < E; ++i) v[i] = op.rr_out(b, kx, ky, IOF::out_elem(t, i), st[i]);
+        smem_fft2<T, -DIR, N, true, true>(s, idx, c, t, true, twz, 1, v);
+#pragma unroll
+        for (int i = 0; i < E; ++i) {
+            const int z = IOI::out_elem(t, i);
+            op.rr_store(b, base + z * zstride, v[i]);
+        }
+    }
+}
+
 template <typename T, int NF>
 inline size_t zpass_smem(const Geom& g) {
     return (size_t)NF * zpass_cols<T>(g.nz) * g.nz * sizeof(cplx<T>);

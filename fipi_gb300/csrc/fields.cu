@@ -286,6 +286,17 @@ template <typename T, bool MIXED> struct ZOpCHRt {
         mid(ix, iy, iz, gi, vi, vo, p);
     }
     __device__ void store2(int, int, int, size_t gi, const C* v) const { out[gi] = v[0]; }
+    // register round trip (k_zpass_rr)
+    struct State {
+        C c;
+    };
+    __device__ void rr_mid(int ix, int iy, int iz, size_t gi, const C* w, State& st) const {
+        PreT p;
+        ch.pre(gi, p);
+        st.c = ch.update(ix, iy, iz, gi, w[0], p);
+    }
+    __device__ C rr_out(int, int, int, int, const State& st) const { return st.c; }
+    __device__ void rr_store(int, size_t gi, C v) const { out[gi] = v; }
 };
 
 // Round trip B -> C (NF = 1, NB = 4): the forward Z transform of f gives
@@ -328,6 +339,26 @@ template <typename T> struct ZOpFRt {
 #pragma unroll
         for (int b = 0; b < 4; ++b) out[b][gi] = v[b];
     }
+    // register round trip (k_zpass_rr): the outputs are formed one at a time
+    struct State {
+        C f, c;
+    };
+    __device__ void rr_mid(int, int, int, size_t gi, const C* w, State& st) const {
+        fhat_out[gi] = w[0];
+        st.f = w[0];
+        st.c = chat[gi];
+    }
+    __device__ C rr_out(int b, int ix, int iy, int iz, const State& st) const {
+        const C c = st.c;
+        if (b == 0) {
+            const T a = kt.k2(ix, iy, iz) * lam;
+            return mkc<C>(a * c.x + st.f.x, a * c.y + st.f.y);
+        }
+        const T kd = b == 1 ? kt.kx[ix] : b == 2 ? kt.ky[iy] : kt.kz[iz];
+        const bool nyq = b == 1 ? ix == m : b == 2 ? iy == ny2 : iz == nz2;
+        return nyq ? mkc<C>(T(0), T(0)) : mkc<C>(-kd * c.y, kd * c.x);
+    }
+    __device__ void rr_store(int b, size_t gi, C v) const { out[b][gi] = v; }
 };
 
 // Round trip C -> next A (NF = NB = 3): the Leray projection of ZOpProj in
@@ -351,6 +382,13 @@ template <typename T> struct ZOpProjRt {
         upre[1][gi] = v[1];
         upre[2][gi] = v[2];
     }
+    // register round trip (k_zpass_rr)
+    struct State {
+        C u[3];
+    };
+    __device__ void rr_mid(int ix, int iy, int iz, size_t, const C* w, State& st) const { pj.compute(ix, iy, iz, w, st.u); }
+    __device__ C rr_out(int b, int, int, int, const State& st) const { return st.u[b]; }
+    __device__ void rr_store(int b, size_t gi, C v) const { upre[b][gi] = v; }
 };
 
 // Z inverse prologue: mu_hat = lambda k^2 c_hat + f_hat (main.cpp:157).
@@ -835,6 +873,13 @@ template <typename T> struct ZOpDivRt {
         vo[0] = mkc<C>(re, im);
     }
     __device__ void store2(int, int, int, size_t gi, const C* v) const { out[gi] = v[0]; }
+    // register round trip (k_zpass_rr)
+    struct State {
+        C o;
+    };
+    __device__ void rr_mid(int ix, int iy, int iz, size_t gi, const C* w, State& st) const { mid(ix, iy, iz, gi, w, &st.o); }
+    __device__ C rr_out(int, int, int, int, const State& st) const { return st.o; }
+    __device__ void rr_store(int, size_t gi, C v) const { out[gi] = v; }
 };
 
 template <typename T> static fipi_status div_t(fipi_ctx* ctx, const double* v, double* out) {

@@ -324,10 +324,21 @@ template <typename T> struct ZOpProj {
             dre += kv[d] * F[d].x;
             dim += kv[d] * F[d].y;
         }
+        if constexpr (sizeof(T) == sizeof(float)) {
+            // mixed form: two reciprocals instead of twelve divisions
+            const T r1 = T(1) / k2, r2 = T(1) / mk2;
 #pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            const T qre = (kv[d] * dre) / k2, qim = (kv[d] * dim) / k2;
-            u[d] = mkc<C>((F[d].x - qre) / mk2, (F[d].y - qim) / mk2);
+            for (int d = 0; d < 3; ++d) {
+                const T qre = (kv[d] * dre) * r1, qim = (kv[d] * dim) * r1;
+                u[d] = mkc<C>((F[d].x - qre) * r2, (F[d].y - qim) * r2);
+            }
+        } else {
+            // FP64: the reference's evaluation order (main.cpp:177-178)
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                const T qre = (kv[d] * dre) / k2, qim = (kv[d] * dim) / k2;
+                u[d] = mkc<C>((F[d].x - qre) / mk2, (F[d].y - qim) / mk2);
+            }
         }
     }
     __device__ void store(int ix, int iy, int iz, size_t gi, const C* F) const {
@@ -461,6 +472,10 @@ template <typename T, int NF, int DIR, class Op> void launch_z(fipi_ctx* ctx, co
     });
 }
 
+// FP32 round trips that run as k_zpass_rr (measured faster there than the
+// shared-memory tiles of k_zpass_rt / k_zpass_rt_t).
+template <int NF, int NB> constexpr bool zrt_in_registers = (NF == 1 && NB == 4);
+
 // Round-trip Z pass: NF fields in, NB fields out; WIDE: k_zpass_rt with
 // tiles of COLS ky columns (COLS <= 16 for FP32, whose grids have
 // ny >= 16, and <= 8 for FP64, ny >= 8), else k_zpass_rt_t.
@@ -468,6 +483,20 @@ template <typename T, int NF, int NB, int DIR, int COLS, bool WIDE, class Op>
 void launch_zrt(fipi_ctx* ctx, const char* name, int nspec, const Op& op) {
     const Geom& g = ctx->g;
     LaunchScope ls(ctx, name, (double)nspec * g.SH * sizeof(cplx<T>));
+    if constexpr (sizeof(T) == sizeof(float) && zrt_in_registers<NF, NB>) {
+        // FP32: the round trip held in registers
+        dispatch_pow2(g.nz, [&](auto NC) {
+            constexpr int N = decltype(NC)::value;
+            using SHP = ZRtShapeT<T, N, 16>;
+            const size_t smem = (size_t)SHP::TZ * N * sizeof(cplx<T>);
+            dim3 grid(g.h, g.ny / SHP::TZ);
+            auto kern = k_zpass_rr<T, NF, NB, DIR, N, 16, Op>;
+            static size_t granted = 48 * 1024;
+            ensure_smem(kern, smem, granted);
+            kern<<<grid, SHP::TZ * SHP::Tn, smem, ctx->stream>>>(g, (const cplx<T>*)ctx->fb.twz, op);
+        });
+        return;
+    }
     if constexpr (!WIDE) {
         dispatch_pow2(g.nz, [&](auto NC) {
             constexpr int N = decltype(NC)::value;
