@@ -11,6 +11,7 @@ from .lib import (  # noqa: F401
     cell_geometry,
     declared_symbols,
     load,
+    reference_initial_state,
     reference_params,
     free_energy_density,
     seed_particles,
@@ -22,5 +23,5 @@ from .lib import (  # noqa: F401
 __all__ = [
     "FipiParams", "Workload", "WORKLOADS", "workload", "reference_head", "FipiError",
     "Simulation", "cell_geometry", "declared_symbols", "load", "reference_params",
-    "seed_particles", "seed_phase", "vtk_write_field", "vtk_write_particles", "free_energy_density",
+    "reference_initial_state", "seed_particles", "seed_phase", "vtk_write_field", "vtk_write_particles", "free_energy_density",
 ]

@@ -25,6 +25,7 @@ UNITS = {
     "adjoint.cu": [],
     "particles.cu": ["-fmad=false"],
     "vtk.cu": ["-Xcompiler", "-ffp-contract=off"],
+    "initial.cu": ["-Xcompiler", "-ffp-contract=off"],
 }
 
 

@@ -104,6 +104,7 @@ _SIGS = {
     "fipi_trajectory_backward": (ctypes.c_int, [_vp, _dp, _dp, _dp, _dp]),
     "fipi_seed_phase": (ctypes.c_int, [ctypes.POINTER(FipiParams), ctypes.c_uint64, ctypes.c_double,
                                        ctypes.c_double, _dp]),
+    "fipi_reference_initial_state": (ctypes.c_int, [ctypes.POINTER(FipiParams), ctypes.c_uint, _dp, _dp]),
     "fipi_seed_particles": (ctypes.c_int, [ctypes.POINTER(FipiParams), ctypes.c_uint64,
                                            ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                            ctypes.c_double, ctypes.c_int, _dp, _dp, _dp]),
@@ -204,6 +205,17 @@ def free_energy_density(params: FipiParams, c, grad_c) -> np.ndarray:
     out = np.empty(V)
     _check(load().fipi_free_energy_density(ctypes.byref(params), _d(_f64(c, V)), _d(_f64(grad_c, 3 * V)), _d(out)))
     return out
+
+
+def reference_initial_state(params: FipiParams, seed: int, phase: bool = True):
+    """The reference's own set-up draws for srand(seed): the phase field
+    (field.cpp:85-99) and cluster::distribute (cluster.cpp:53-113).  Returns
+    (c or None, positions n_p x 3 flattened)."""
+    V = params.nx * params.ny * params.nz
+    c = np.empty(V) if phase else None
+    pos = np.empty(3 * max(params.n_p, 0))
+    _check(load().fipi_reference_initial_state(ctypes.byref(params), seed, _d(c) if phase else None, _d(pos)))
+    return c, pos
 
 
 def seed_particles(params: FipiParams, seed: int, r_range=None, theta_range_deg=None,

@@ -355,6 +355,18 @@ fipi_status fipi_seed_particles(const fipi_params* p, uint64_t seed, double r_mi
                                 double theta_min_deg, double theta_max_deg, int allow_overlap,
                                 double* pos, double* r, double* cos_theta);
 
+/* The reference's own initial state for a given seed (host only): srand(seed)
+ * (main.cpp:24 seeds from the clock), then the phase field's V draws
+ * c = (rand()%1000)/1e3*0.2 - 0.1 in index order (field.cpp:85-99) and,
+ * when switch_particle, cluster::distribute (cluster.cpp:53-113): per
+ * particle, candidates p = L (rand()%1000)/1e3 (3 draws) until none of the
+ * earlier particles lies closer than 2 r_p (check_overlap, cluster.cpp:98-113,
+ * no periodic images).  rand() is glibc's generator, restated so every host
+ * draws the same values.  c: V values or NULL (drawn either way); pos:
+ * n_p x 3 or NULL.  FIPI_ERR_BAD_PARAMS when a particle finds no place in
+ * 1e7 candidates (the reference would loop forever). */
+fipi_status fipi_reference_initial_state(const fipi_params* p, unsigned int seed, double* c, double* pos);
+
 #ifdef __cplusplus
 }
 #endif

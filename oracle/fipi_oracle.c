@@ -910,3 +910,82 @@ double oracle_mass(const oracle* o) {
     for (long it = 0; it < o->V; ++it) s += o->c[2 * it];
     return s * dv;
 }
+
+/* ------------------------------------------------ the reference's initial state
+ * glibc's rand() (random() with the default TYPE_3 state of 31 words):
+ * state r[0] = seed (1 if 0), r[i] = 16807 r[i-1] mod (2^31 - 1) for i < 31
+ * (Schrage's decomposition), front index 3 and rear index 0, then 310
+ * discarded outputs; each output adds the rear word into the front word
+ * (mod 2^32) and returns it shifted right by one. */
+typedef struct {
+    int32_t r[31];
+    int f, b;
+} glibc_rand;
+
+static int glibc_next(glibc_rand* g) {
+    const uint32_t v = (uint32_t)g->r[g->f] + (uint32_t)g->r[g->b];
+    g->r[g->f] = (int32_t)v;
+    g->f = (g->f + 1) % 31;
+    g->b = (g->b + 1) % 31;
+    return (int)(v >> 1);
+}
+
+static void glibc_srand(glibc_rand* g, unsigned int seed) {
+    int32_t word = (int32_t)(seed ? seed : 1u);
+    g->r[0] = word;
+    for (int i = 1; i < 31; ++i) {
+        const int32_t hi = word / 127773, lo = word % 127773;
+        word = 16807 * lo - 2836 * hi;
+        if (word < 0) word += 2147483647;
+        g->r[i] = word;
+    }
+    g->f = 3;
+    g->b = 0;
+    for (int i = 0; i < 310; ++i) glibc_next(g);
+}
+
+/* vector::norm (primitive.hpp:58) */
+static double ref_norm3(double x, double y, double z) {
+    return pow(pow(x, 2) + pow(y, 2) + pow(z, 2), 0.5);
+}
+
+int oracle_reference_initial_state(const fipi_params* P, unsigned int seed, double* c, double* pos,
+                                   long max_candidates) {
+    glibc_rand g;
+    glibc_srand(&g, seed); /* srand (main.cpp:24) */
+    const long V = (long)P->nx * P->ny * P->nz;
+    for (long it = 0; it < V; ++it) { /* field("SCALARS","phase_field") (field.cpp:85-99) */
+        const double v = (double)(glibc_next(&g) % 1000) / 1e3 * 0.2 - 0.1;
+        if (c) c[it] = v;
+    }
+    if (!P->switch_particle || P->n_p <= 0) return FIPI_OK;
+    const int n = P->n_p;
+    double* p = (double*)malloc(sizeof(double) * 3 * (size_t)n);
+    for (int it = 0; it < n; ++it) { /* cluster::distribute (cluster.cpp:53-92) */
+        long cand = 0;
+        for (;;) {
+            const double r1 = (double)(glibc_next(&g) % 1000) / 1e3;
+            const double r2 = (double)(glibc_next(&g) % 1000) / 1e3;
+            const double r3 = (double)(glibc_next(&g) % 1000) / 1e3;
+            p[3 * it] = P->lx * r1;
+            p[3 * it + 1] = P->ly * r2;
+            p[3 * it + 2] = P->lz * r3;
+            int overlap = 0; /* check_overlap (cluster.cpp:98-113) */
+            for (int j = 0; j < it; ++j) {
+                if (ref_norm3(p[3 * j] - p[3 * it], p[3 * j + 1] - p[3 * it + 1], p[3 * j + 2] - p[3 * it + 2]) <
+                    2.0 * P->r_p) {
+                    overlap = 1;
+                    break;
+                }
+            }
+            if (!overlap) break;
+            if (++cand >= max_candidates) {
+                free(p);
+                return FIPI_ERR_BAD_PARAMS;
+            }
+        }
+    }
+    if (pos) memcpy(pos, p, sizeof(double) * 3 * (size_t)n);
+    free(p);
+    return FIPI_OK;
+}

@@ -68,6 +68,11 @@ void oracle_advect(const fipi_params* P, int n, int stage, const double* f_pi,
 void oracle_enforce_bc(const fipi_params* P, int n, double* p);
 void oracle_spread(const fipi_params* P, int n, const double* p, const double* f_pp,
                    double* out);
+/* srand(seed) (main.cpp:24), the phase field's draws (field.cpp:85-99) and
+ * cluster::distribute (cluster.cpp:53-113) with glibc's rand(); returns
+ * FIPI_ERR_BAD_PARAMS when a particle exceeds max_candidates draws. */
+int oracle_reference_initial_state(const fipi_params* P, unsigned int seed, double* c, double* pos,
+                                   long max_candidates);
 double oracle_free_energy(const oracle* o);
 double oracle_mass(const oracle* o);
 

@@ -91,6 +91,7 @@ def port_lib():
         lib.oracle_enforce_bc.argtypes = [P, ctypes.c_int, _dp]
         lib.oracle_spread.argtypes = [P, ctypes.c_int, _dp, _dp, _dp]
         lib.oracle_cell_geometry.argtypes = [P, _ip, _dp]
+        lib.oracle_reference_initial_state.argtypes = [P, ctypes.c_uint, _dp, _dp, ctypes.c_long]
         lib.oracle_params_ok.argtypes = [P]
         _port_lib = lib
     return _port_lib
@@ -205,6 +206,15 @@ def interpolate2(params, field, p):
     return out
 
 
+def reference_initial_state(params, seed: int, max_candidates: int = 10**7):
+    """The reference's seeded set-up draws (oracle restatement): c, positions."""
+    V = params.nx * params.ny * params.nz
+    c = np.zeros(V)
+    pos = np.zeros(3 * max(params.n_p, 0))
+    st = port_lib().oracle_reference_initial_state(ctypes.byref(params), seed, _d(c), _d(pos), max_candidates)
+    return st, c, pos
+
+
 def sorting(params, p):
     n = len(p) // 3
     nc, _ = cell_geometry(params)
@@ -315,6 +325,16 @@ class Ref:
         L.ref_write_field.argtypes = [_dp, ctypes.c_int, ctypes.c_char_p, ctypes.c_char_p]
         L.ref_div.argtypes = [_dp, _dp]
         L.ref_interpolate2.argtypes = [_dp, ctypes.c_int, _dp, _dp]
+        L.ref_write_free_energy.argtypes = [_dp, _dp, ctypes.c_char_p]
+        L.ref_write_particles.argtypes = [_dp, _dp, _dp, ctypes.c_char_p]
+        L.ref_initial_state.argtypes = [ctypes.c_uint, _dp, _dp]
+
+    def initial_state(self, seed: int):
+        """srand(seed); the phase field's draws; cluster::distribute."""
+        c = np.zeros(self.V)
+        pos = np.zeros(3 * max(self.n, 0))
+        self.lib.ref_initial_state(seed, _d(c), _d(pos))
+        return c, pos
 
     def div(self, v):
         out = np.zeros(self.V)
@@ -327,8 +347,6 @@ class Ref:
         self.lib.ref_interpolate2(_d(np.ascontiguousarray(field, np.float64)), n,
                                   _d(np.ascontiguousarray(p, np.float64)), _d(out))
         return out
-        L.ref_write_free_energy.argtypes = [_dp, _dp, ctypes.c_char_p]
-        L.ref_write_particles.argtypes = [_dp, _dp, _dp, ctypes.c_char_p]
 
     def write_field(self, values, components, name, path):
         v = np.ascontiguousarray(values, np.float64).ravel()

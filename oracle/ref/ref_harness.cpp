@@ -433,4 +433,22 @@ int ref_write_particles(const double* p, const double* r, const double* f_pp, co
     return 0;
 }
 
+/* srand(seed) (main.cpp:24), field c("SCALARS","phase_field") (main.cpp:34)
+ * and cluster::distribute (main.cpp:58-66) with the C library's rand(). */
+int ref_initial_state(unsigned int seed, double* c, double* pos) {
+    srand(seed);
+    field cf("SCALARS", "phase_field");
+    for (long it = 0; it < V; ++it) c[it] = cf.v[0][it][0];
+    if (switch_particle && N_p > 0) {
+        cluster s;
+        s.distribute();
+        for (int it = 0; it < N_p; ++it) {
+            pos[3 * it] = s.particle[it].p.get_x();
+            pos[3 * it + 1] = s.particle[it].p.get_y();
+            pos[3 * it + 2] = s.particle[it].p.get_z();
+        }
+    }
+    return 0;
+}
+
 }  // extern "C"
