@@ -497,6 +497,9 @@ fipi_status adjoint_seed_impl(fipi_ctx* ctx, const double* dc, const double* du,
                               const double* dfpp) {
     if (ctx->prec != FIPI_FP64)
         return set_error(ctx, FIPI_ERR_UNSUPPORTED, "the adjoint is built for FIPI_FP64 contexts");
+    if (ctx->couple_u || ctx->brown_kt > 0.0)
+        return set_error(ctx, FIPI_ERR_UNSUPPORTED, "the adjoint is built for the reference's particle model "
+                                                    "(fluid coupling and Brownian force off)");
     if (!ctx->have_phase) return set_error(ctx, FIPI_ERR_STATE, "fipi_set_phase must come first");
     fipi_status st = adjoint_alloc(ctx);
     if (st != FIPI_OK) return st;
@@ -537,6 +540,9 @@ fipi_status adjoint_seed_impl(fipi_ctx* ctx, const double* dc, const double* du,
 fipi_status adjoint_ready(fipi_ctx* ctx) {
     if (ctx->prec != FIPI_FP64)
         return set_error(ctx, FIPI_ERR_UNSUPPORTED, "the adjoint is built for FIPI_FP64 contexts");
+    if (ctx->couple_u || ctx->brown_kt > 0.0)
+        return set_error(ctx, FIPI_ERR_UNSUPPORTED, "the adjoint is built for the reference's particle model "
+                                                    "(fluid coupling and Brownian force off)");
     if (!ctx->ad.ready) return set_error(ctx, FIPI_ERR_STATE, "fipi_adjoint_seed must come first");
     return FIPI_OK;
 }

@@ -596,6 +596,29 @@ fipi_status fipi_launch_count(const fipi_ctx* ctx, long long* n) {
 #define NEED(x) \
     if (!(x)) return set_error(ctx, FIPI_ERR_BAD_ARG, "NULL argument: " #x)
 
+// ---------------------------------------------------------------- extensions
+fipi_status fipi_set_fluid_coupling(fipi_ctx* ctx, int on) {
+    NEED(ctx);
+    if (ctx->substep != 0) return set_error(ctx, FIPI_ERR_STATE, "extensions change between iterations only");
+    FIPI_CUDA(ctx, cudaSetDevice(ctx->device));
+    FIPI_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->couple_u = on ? 1 : 0;
+    graphs_reset(ctx);
+    return particles_ext_alloc(ctx);
+}
+
+fipi_status fipi_set_brownian(fipi_ctx* ctx, double kt, uint64_t seed) {
+    NEED(ctx);
+    if (!(kt >= 0.0) || !std::isfinite(kt)) return set_error(ctx, FIPI_ERR_BAD_ARG, "kt must be finite and >= 0");
+    if (ctx->substep != 0) return set_error(ctx, FIPI_ERR_STATE, "extensions change between iterations only");
+    FIPI_CUDA(ctx, cudaSetDevice(ctx->device));
+    FIPI_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->brown_kt = kt;
+    ctx->noise_seed = seed;
+    graphs_reset(ctx);
+    return particles_ext_alloc(ctx);
+}
+
 fipi_status fipi_fft_r2c(fipi_ctx* ctx, const double* in, double* out) {
     NEED(ctx);
     NEED(in);

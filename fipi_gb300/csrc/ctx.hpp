@@ -75,6 +75,10 @@ struct ParticleBufs {
     bool tau_valid = false;
     int* it_mark = nullptr;      // 1
     double* tau = nullptr;       // 1
+    // extensions (off by default): fluid velocity at the particle and the
+    // Brownian force of the current step
+    double* uf = nullptr;      // 3 x n
+    double* f_rand = nullptr;  // 3 x n
 };
 
 // Device-resident checkpoints of the step state (one allocation, `slots`
@@ -187,6 +191,9 @@ struct fipi_ctx {
     int substep = 0;           // 1 after fipi_step_ch, 2 after fipi_step_stokes
     double* pin = nullptr;     // pinned host staging of the particle state, 12 n doubles
     bool have_phase = false;
+    int couple_u = 0;          // fluid coupling: uf = u interpolated at the particle
+    double brown_kt = 0.0;     // Brownian force strength kT (0: off)
+    uint64_t noise_seed = 0;   // Philox key of the Brownian force
     bool track_tau = true;     // packing energy during the step (cluster.cpp:256-259)
     size_t device_bytes = 0;
     std::string last_error;
@@ -232,6 +239,8 @@ void particles_free(fipi_ctx* ctx);
 void particles_spread(fipi_ctx* ctx);
 // Two Heun stages (enqueue); the ramp factor is read from ctx->d_rmp.
 void particles_step(fipi_ctx* ctx);
+fipi_status particles_ext_alloc(fipi_ctx* ctx);
+void fields_velocity_real(fipi_ctx* ctx);  // fb.ureal = u (the fluid-coupling extension)
 // t += 1 on the device and the next step's ramp factor.
 void step_tick(fipi_ctx* ctx);
 // Fine-grained parity entry points (synchronous, host arrays).

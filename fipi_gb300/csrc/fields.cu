@@ -636,7 +636,8 @@ fipi_status fields_get_phase(fipi_ctx* ctx, double* c_host) {
     return download<double>(ctx, (const double*)ctx->fb.c, c_host, (size_t)ctx->g.V);
 }
 
-template <typename T> static fipi_status get_velocity_t(fipi_ctx* ctx, double* u_host) {
+// Real velocity u (3 x V) into fb.ureal from the velocity state.
+template <typename T> static void velocity_real_t(fipi_ctx* ctx) {
     const Geom& g = ctx->g;
     void* up[3] = {ctx->fb.upre[0], ctx->fb.upre[1], ctx->fb.upre[2]};
     void* sp[3] = {ctx->fb.S[0], ctx->fb.S[1], ctx->fb.S[2]};
@@ -644,8 +645,17 @@ template <typename T> static fipi_status get_velocity_t(fipi_ctx* ctx, double* u
     T* ur = (T*)ctx->fb.ureal;
     OpC2RStore<T, 3> op{{F<T>::S(ctx, 0), F<T>::S(ctx, 1), F<T>::S(ctx, 2)}, {ur, ur + g.V, ur + 2 * g.V}, g.nx, g.ny};
     launch_x<T, 3, 0, false>(ctx, "X inverse store", 3, NoAcc<OpC2RStore<T, 3>>{op});
+}
+
+void fields_velocity_real(fipi_ctx* ctx) {
+    if (ctx->prec == FIPI_MIXED) velocity_real_t<float>(ctx);
+    else velocity_real_t<double>(ctx);
+}
+
+template <typename T> static fipi_status get_velocity_t(fipi_ctx* ctx, double* u_host) {
+    velocity_real_t<T>(ctx);
     FIPI_CUDA(ctx, cudaGetLastError());
-    return download<T>(ctx, ur, u_host, (size_t)g.V * 3);
+    return download<T>(ctx, (T*)ctx->fb.ureal, u_host, (size_t)ctx->g.V * 3);
 }
 
 fipi_status fields_get_grad(fipi_ctx* ctx, double* g_host) {

@@ -706,15 +706,83 @@ __device__ __forceinline__ void f_pi_of(const PC& pc, double phi, double gx, dou
     }
 }
 
+// ------------------------------------------------------------ extensions
+// Philox-4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as
+// easy as 1, 2, 3", SC 2011): ten rounds of two 32x32 -> 64-bit products
+// with a Weyl-sequence key schedule.
+__host__ __device__ inline void philox4x32(const unsigned ctr_in[4], unsigned k0, unsigned k1, unsigned out[4]) {
+    unsigned c0 = ctr_in[0], c1 = ctr_in[1], c2 = ctr_in[2], c3 = ctr_in[3];
+    for (int r = 0; r < 10; ++r) {
+        if (r > 0) {
+            k0 += 0x9E3779B9u;
+            k1 += 0xBB67AE85u;
+        }
+        const unsigned long long p0 = 0xD2511F53ull * c0, p1 = 0xCD9E8D57ull * c2;
+        const unsigned hi0 = (unsigned)(p0 >> 32), lo0 = (unsigned)p0;
+        const unsigned hi1 = (unsigned)(p1 >> 32), lo1 = (unsigned)p1;
+        c0 = hi1 ^ c1 ^ k0;
+        c1 = lo1;
+        c2 = hi0 ^ c3 ^ k1;
+        c3 = lo0;
+    }
+    out[0] = c0;
+    out[1] = c1;
+    out[2] = c2;
+    out[3] = c3;
+}
+
+// Three standard normals the way element::get_f_rand draws them
+// (element.cpp:109-144): Box-Muller on uniforms (k mod 1000)/1000, redrawn
+// while |g| > 5 (only r1 = 0 is), here from the Philox stream of
+// (particle, step) instead of rand(); at most 64 draws per normal (then 0).
+__host__ __device__ inline void brownian_normals(unsigned long long seed, unsigned id, unsigned t, double pi,
+                                                 double g[3]) {
+    unsigned buf[4];
+    int used = 4;
+    unsigned blk = 0;
+    auto next = [&]() -> unsigned {
+        if (used == 4) {
+            const unsigned ctr[4] = {id, t, blk++, 0u};
+            philox4x32(ctr, (unsigned)seed, (unsigned)(seed >> 32), buf);
+            used = 0;
+        }
+        return buf[used++];
+    };
+    for (int a = 0; a < 3; ++a) {
+        double v = 0.0;
+        for (int k = 0; k < 64; ++k) {
+            const double r1 = double(next() % 1000u) / 1000;
+            const double r2 = double(next() % 1000u) / 1000;
+            v = sqrt(-2 * log(r1)) * cos(2 * pi * r2);
+            if (fabs(v) <= 5.0) break;
+            v = 0.0;
+        }
+        g[a] = v;
+    }
+}
+
+// Per-step extension inputs of the stage kernels (all off: the reference's step).
+struct PExt {
+    const void* u[3];           // real fluid velocity (T), or NULL: uf = 0
+    double* uf;                 // 3 x n: uf of the current stage
+    double* f_rand;             // 3 x n: f_rand of the step, or NULL
+    const int* d_t;             // step index (Philox counter)
+    unsigned long long seed;
+    double kt;
+};
+
 // element::advect (element.cpp:156-173) and enforce_bc (element.cpp:177-185)
-// for one particle; uf = 0 and f_ext = 0 as in the reference.
+// for one particle; f_ext = 0 as in the reference, uf = 0 unless fluid
+// coupling is on, and f_rand only with a Brownian force.
 __device__ __forceinline__ void advect_one(const PC& pc, int stage, const double* fpi, const double* fpp, double r,
-                                           double* p, double* po, double* uo) {
+                                           double* p, double* po, double* uo, const double* uf = nullptr,
+                                           const double* fr = nullptr) {
     double v[3];
     for (int a = 0; a < 3; ++a) {
         double F = fpi[a] + 0.0;
         F = F + fpp[a];
-        v[a] = 0.0 + F / 6.0 / pc.pi / pc.mu / r;
+        if (fr) F = F + fr[a];
+        v[a] = (uf ? uf[a] : 0.0) + F / 6.0 / pc.pi / pc.mu / r;
     }
     if (stage == 1) {
         for (int a = 0; a < 3; ++a) {
@@ -729,12 +797,48 @@ __device__ __forceinline__ void advect_one(const PC& pc, int stage, const double
     for (int a = 0; a < 3; ++a) p[a] = fmod(p[a] + pc.L[a], pc.L[a]);
 }
 
+// Extension work of a stage for particle i at (x, y, z): uf from the fluid
+// velocity (get_local_u with its interpolation, element.cpp:38-52) and, at
+// the first stage of a step, the step's Brownian force
+// sqrt(12 pi r mu kt / dt) g (element.cpp:138-143 with the particle's radius).
+template <typename TF, typename TA>
+__device__ __forceinline__ void stage_ext(const PC& pc, const PExt& ex, int i, double x, double y, double z, double r,
+                                          bool first) {
+    const int n = pc.n;
+    if (ex.u[0]) {
+        const TF* fl[3] = {(const TF*)ex.u[0], (const TF*)ex.u[1], (const TF*)ex.u[2]};
+        TA uv[3];
+        interp_fields<TF, TA>(pc, x, y, z, fl, 3, uv);
+        for (int a = 0; a < 3; ++a) ex.uf[a * n + i] = (double)uv[a];
+    }
+    if (first && ex.f_rand) {
+        double g[3];
+        brownian_normals(ex.seed, (unsigned)i, (unsigned)*ex.d_t, pc.pi, g);
+        const double s = sqrt(12.0 * pc.pi * r * pc.mu * ex.kt / pc.dt);
+        for (int a = 0; a < 3; ++a) ex.f_rand[a * n + i] = s * g[a];
+    }
+}
+
+__device__ __forceinline__ void ext_load(const PExt& ex, int n, int i, double* uf, double* fr, const double*& puf,
+                                         const double*& pfr) {
+    puf = nullptr;
+    pfr = nullptr;
+    if (ex.u[0]) {
+        for (int a = 0; a < 3; ++a) uf[a] = ex.uf[a * n + i];
+        puf = uf;
+    }
+    if (ex.f_rand) {
+        for (int a = 0; a < 3; ++a) fr[a] = ex.f_rand[a * n + i];
+        pfr = fr;
+    }
+}
+
 // Stage part 1: interpolate c, grad c at the stage-start positions and form
 // f_pi (cluster::interpolate_local_variables + compute_f_pi).
 template <typename TF, typename TA>
 __global__ void k_stage_fpi(PC pc, const TF* __restrict__ c, const TF* __restrict__ g0, const TF* __restrict__ g1,
                             const TF* __restrict__ g2, const double* __restrict__ p, double* f_pi,
-                            const double* __restrict__ r, const double* __restrict__ cth) {
+                            const double* __restrict__ r, const double* __restrict__ cth, PExt ex) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = pc.n;
     if (i >= n) return;
@@ -744,6 +848,7 @@ __global__ void k_stage_fpi(PC pc, const TF* __restrict__ c, const TF* __restric
     double fpi[3];
     f_pi_of(pc, (double)vals[0], (double)vals[1], (double)vals[2], (double)vals[3], r[i], cth[i], fpi);
     for (int a = 0; a < 3; ++a) f_pi[a * n + i] = fpi[a];
+    stage_ext<TF, TA>(pc, ex, i, p[i], p[n + i], p[2 * n + i], r[i], true);
 }
 
 // Stage 1's advection and wrap followed, for the same particle, by stage 2's
@@ -754,7 +859,7 @@ __global__ void k_stage_advect1_fpi2(PC pc, double* p, double* p_old, double* u_
                                      const double* __restrict__ f_pp, const double* __restrict__ r,
                                      const double* __restrict__ cth, const TF* __restrict__ c,
                                      const TF* __restrict__ g0, const TF* __restrict__ g1,
-                                     const TF* __restrict__ g2, int* status) {
+                                     const TF* __restrict__ g2, int* status, PExt ex) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = pc.n;
     if (i >= n) return;
@@ -762,7 +867,10 @@ __global__ void k_stage_advect1_fpi2(PC pc, double* p, double* p_old, double* u_
     double po[3], uo[3];
     const double fpi[3] = {f_pi[i], f_pi[n + i], f_pi[2 * n + i]};
     const double fpp[3] = {f_pp[i], f_pp[n + i], f_pp[2 * n + i]};
-    advect_one(pc, 1, fpi, fpp, r[i], pp, po, uo);
+    double ufv[3], frv[3];
+    const double *puf, *pfr;
+    ext_load(ex, n, i, ufv, frv, puf, pfr);
+    advect_one(pc, 1, fpi, fpp, r[i], pp, po, uo, puf, pfr);
     for (int a = 0; a < 3; ++a) {
         p[a * n + i] = pp[a];
         p_old[a * n + i] = po[a];
@@ -778,12 +886,13 @@ __global__ void k_stage_advect1_fpi2(PC pc, double* p, double* p_old, double* u_
     double f2[3];
     f_pi_of(pc, (double)vals[0], (double)vals[1], (double)vals[2], (double)vals[3], r[i], cth[i], f2);
     for (int a = 0; a < 3; ++a) f_pi[a * n + i] = f2[a];
+    stage_ext<TF, TA>(pc, ex, i, pp[0], pp[1], pp[2], r[i], false);
 }
 
 // Stage part 2: advect with this stage's f_pi + f_pp, then wrap.
 __global__ void k_stage_advect(PC pc, int stage, double* p, double* p_old, double* u_old,
                                const double* __restrict__ f_pi, const double* __restrict__ f_pp,
-                               const double* __restrict__ r, int* status) {
+                               const double* __restrict__ r, int* status, PExt ex) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = pc.n;
     if (i >= n) return;
@@ -792,7 +901,10 @@ __global__ void k_stage_advect(PC pc, int stage, double* p, double* p_old, doubl
     double uo[3] = {u_old[i], u_old[n + i], u_old[2 * n + i]};
     const double fpi[3] = {f_pi[i], f_pi[n + i], f_pi[2 * n + i]};
     const double fpp[3] = {f_pp[i], f_pp[n + i], f_pp[2 * n + i]};
-    advect_one(pc, stage, fpi, fpp, r[i], pp, po, uo);
+    double ufv[3], frv[3];
+    const double *puf, *pfr;
+    ext_load(ex, n, i, ufv, frv, puf, pfr);
+    advect_one(pc, stage, fpi, fpp, r[i], pp, po, uo, puf, pfr);
     for (int a = 0; a < 3; ++a) {
         p[a * n + i] = pp[a];
         p_old[a * n + i] = po[a];
@@ -1048,6 +1160,35 @@ fipi_status particles_packing_tau(fipi_ctx* ctx, double* out) {
     return FIPI_OK;
 }
 
+static PExt particle_ext(const fipi_ctx* ctx) {
+    PExt ex{};
+    if (ctx->couple_u) {
+        const size_t es = ctx->prec == FIPI_MIXED ? sizeof(float) : sizeof(double);
+        for (int a = 0; a < 3; ++a) ex.u[a] = (const char*)ctx->fb.ureal + a * (size_t)ctx->g.V * es;
+        ex.uf = ctx->pb.uf;
+    }
+    if (ctx->brown_kt > 0.0) {
+        ex.f_rand = ctx->pb.f_rand;
+        ex.kt = ctx->brown_kt;
+        ex.seed = ctx->noise_seed;
+    }
+    ex.d_t = ctx->d_t;
+    return ex;
+}
+
+// Buffers of the extensions, allocated when one is switched on.
+fipi_status particles_ext_alloc(fipi_ctx* ctx) {
+    ParticleBufs& b = ctx->pb;
+    const size_t bytes = sizeof(double) * 3 * (size_t)(b.n > 0 ? b.n : 1);
+    if ((ctx->couple_u || ctx->brown_kt > 0.0) && !b.uf) {
+        FIPI_CUDA(ctx, cudaMalloc((void**)&b.uf, bytes));
+        FIPI_CUDA(ctx, cudaMalloc((void**)&b.f_rand, bytes));
+        FIPI_CUDA(ctx, cudaMemset(b.uf, 0, bytes));
+        FIPI_CUDA(ctx, cudaMemset(b.f_rand, 0, bytes));
+    }
+    return FIPI_OK;
+}
+
 template <typename T> static void step_t(fipi_ctx* ctx) {
     ParticleBufs& b = ctx->pb;
     const PC pc = make_pc(ctx);
@@ -1063,23 +1204,26 @@ template <typename T> static void step_t(fipi_ctx* ctx) {
     // (main.cpp:198-217); the ramp(t+1, 0.2 t_end) factor is kept on the
     // device (step_tick).  Stage 1's advection and stage 2's interpolation
     // run in one kernel.
-    { LaunchScope ls_(ctx, "stage interpolate + f_pi", 0.0); k_stage_fpi<T, T><<<nb, kPT, 0, ctx->stream>>>(pc, c, g0, g1, g2, b.p, b.f_pi, b.r, b.cth); }
+    const PExt ex = particle_ext(ctx);
+    { LaunchScope ls_(ctx, "stage interpolate + f_pi", 0.0); k_stage_fpi<T, T><<<nb, kPT, 0, ctx->stream>>>(pc, c, g0, g1, g2, b.p, b.f_pi, b.r, b.cth, ex); }
     for (int stage = 1; stage <= 2; ++stage) {
         const bool im = build_cells(ctx, b.p, ctx->track_tau, spos);
         f_pp_launch<T>(ctx, b.p, ctx->d_rmp, b.f_pi, b.f_pp, ctx->track_tau, im, spos != nullptr);
         if (stage == 1) {
             LaunchScope ls_(ctx, "stage advect + interpolate + f_pi", 0.0);
             k_stage_advect1_fpi2<T, T><<<nb, kPT, 0, ctx->stream>>>(pc, b.p, b.p_old, b.u_old, b.f_pi, b.f_pp, b.r,
-                                                                     b.cth, c, g0, g1, g2, ctx->status);
+                                                                     b.cth, c, g0, g1, g2, ctx->status, ex);
         } else {
             LaunchScope ls_(ctx, "stage advect + wrap", 0.0);
-            k_stage_advect<<<nb, kPT, 0, ctx->stream>>>(pc, 2, b.p, b.p_old, b.u_old, b.f_pi, b.f_pp, b.r, ctx->status);
+            k_stage_advect<<<nb, kPT, 0, ctx->stream>>>(pc, 2, b.p, b.p_old, b.u_old, b.f_pi, b.f_pp, b.r, ctx->status,
+                                                        ex);
         }
     }
 }
 
 void particles_step(fipi_ctx* ctx) {
     if (ctx->pb.n <= 0 || !ctx->P.switch_particle) return;
+    if (ctx->couple_u) fields_velocity_real(ctx);  // u^{n+1} at the particles (get_local_u)
     if (ctx->prec == FIPI_MIXED) step_t<float>(ctx);
     else step_t<double>(ctx);
 }
@@ -1154,7 +1298,7 @@ void particles_free(fipi_ctx* ctx) {
     ParticleBufs& b = ctx->pb;
     void* all[] = {b.p, b.p_old, b.u_old, b.f_pp, b.f_pi, b.r, b.cth, b.keys, b.keys_alt, b.ids, b.ids_alt,
                    b.cell_off, b.cell_cnt, b.sp_keys, b.sp_keys_alt, b.sp_vals, b.sp_vals_alt, b.sp_prev,
-                   b.hist, b.tau_part, b.it_mark, b.tau, b.spos, b.sp_fw, b.ymax, b.sp_acc};
+                   b.hist, b.tau_part, b.it_mark, b.tau, b.spos, b.sp_fw, b.ymax, b.sp_acc, b.uf, b.f_rand};
     for (void* p : all)
         if (p) cudaFree(p);
     b = ParticleBufs{};

@@ -61,6 +61,8 @@ _SIGS = {
     "fipi_step_stokes": (ctypes.c_int, [_vp]),
     "fipi_step_particles": (ctypes.c_int, [_vp]),
     "fipi_wrap": (ctypes.c_int, [_vp, _dp]),
+    "fipi_set_fluid_coupling": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "fipi_set_brownian": (ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_uint64]),
     "fipi_interpolate2": (ctypes.c_int, [_vp, _dp, ctypes.c_int, _dp, _dp]),
     "fipi_div": (ctypes.c_int, [_vp, _dp, _dp]),
     "fipi_sync": (ctypes.c_int, [_vp]),
@@ -319,6 +321,15 @@ class Simulation:
         out = np.empty(self.V)
         _check(self.lib.fipi_div(self.h, _d(_f64(v, 3 * self.V)), _d(out)))
         return out
+
+    def set_fluid_coupling(self, on: bool = True):
+        """Particles advected with the interpolated fluid velocity (off: the
+        reference's uf = 0)."""
+        _check(self.lib.fipi_set_fluid_coupling(self.h, 1 if on else 0))
+
+    def set_brownian(self, kt: float, seed: int = 0):
+        """Brownian force sqrt(12 pi r mu kt / dt) g per step (kt = 0: off)."""
+        _check(self.lib.fipi_set_brownian(self.h, kt, seed))
 
     def wrap(self, p) -> np.ndarray:
         out = _f64(p, 3 * self.n).copy()

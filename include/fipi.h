@@ -355,6 +355,29 @@ fipi_status fipi_seed_particles(const fipi_params* p, uint64_t seed, double r_mi
                                 double theta_min_deg, double theta_max_deg, int allow_overlap,
                                 double* pos, double* r, double* cos_theta);
 
+/* ------------------------------------------------ particle-model extensions
+ * The reference carries a fluid-to-particle coupling and a Brownian force
+ * that its step never uses: get_local_u sets uf = 0 with the interpolation
+ * commented out (element.cpp:38-52), and get_f_rand / get_f_drag
+ * (element.cpp:109-150) are never called.  Both are off by default (the
+ * step is then the reference's); the adjoint rejects contexts with either on.
+ *
+ * fipi_set_fluid_coupling(ctx, 1): every stage interpolates the fluid
+ * velocity u^{n+1} at the particle (field::interpolate per component, the
+ * commented-out body of get_local_u) and advects with
+ * uf + (f_pi + f_ext + f_pp)/(6 pi mu r) (element.cpp:163, 170).  The drag
+ * f_drag = -6 pi r mu (u - uf) of element.cpp:147-150 then balances the
+ * other forces exactly and is not stored.
+ *
+ * fipi_set_brownian(ctx, kt, seed): kt > 0 adds to both stages of step t
+ * f_rand = sqrt(12 pi r mu kt / dt) g (element.cpp:138-143, with the
+ * particle's radius), g three standard normals drawn as get_f_rand draws
+ * them -- Box-Muller on uniforms (k mod 1000)/1000, redrawn while |g| > 5 --
+ * from Philox-4x32-10 keyed by seed with counter (particle, t, block, 0)
+ * instead of rand().  kt = 0 switches it off. */
+fipi_status fipi_set_fluid_coupling(fipi_ctx* ctx, int on);
+fipi_status fipi_set_brownian(fipi_ctx* ctx, double kt, uint64_t seed);
+
 /* The reference's own initial state for a given seed (host only): srand(seed)
  * (main.cpp:24 seeds from the clock), then the phase field's V draws
  * c = (rand()%1000)/1e3*0.2 - 0.1 in index order (field.cpp:85-99) and,

@@ -41,6 +41,11 @@ struct oracle {
     int it_mark;
     double tau;
     int t;
+    /* extensions (off: the reference's particle model) */
+    int couple;
+    double kt;
+    unsigned long long seed;
+    double *uf, *f_rand; /* n x 3 */
 };
 
 void oracle_set_threads(int n) { offt_set_threads(n); }
@@ -103,6 +108,8 @@ oracle* oracle_create(const fipi_params* P) {
     o->p_old = (double*)calloc(n3, sizeof(double));
     o->up = (double*)calloc(n3, sizeof(double));
     o->u_old = (double*)calloc(n3, sizeof(double));
+    o->uf = (double*)calloc(n3, sizeof(double));
+    o->f_rand = (double*)calloc(n3, sizeof(double));
     o->f_pp = (double*)calloc(n3, sizeof(double));
     o->f_pi = (double*)calloc(n3, sizeof(double));
     o->f_ext = (double*)calloc(n3, sizeof(double));
@@ -131,7 +138,7 @@ void oracle_destroy(oracle* o) {
     offt_destroy(o->plan);
     double* all[] = {o->c, o->c_new, o->c_old, o->f, o->f_old, o->conv, o->conv_old, o->pch,
                      o->kx, o->ky, o->kz, o->p, o->p_old, o->up, o->u_old, o->f_pp, o->f_pi,
-                     o->f_ext, o->c_loc, o->dcdx, o->r, o->cth};
+                     o->f_ext, o->c_loc, o->dcdx, o->r, o->cth, o->uf, o->f_rand};
     for (size_t i = 0; i < sizeof(all) / sizeof(all[0]); ++i) free(all[i]);
     for (int d = 0; d < 3; ++d) {
         free(o->grad[d]);
@@ -655,6 +662,91 @@ void oracle_spread(const fipi_params* P, int n, const double* pos, const double*
     }
 }
 
+/* ------------------------------------------------ particle-model extensions
+ * Philox-4x32-10 (Salmon, Moraes, Dror, Shaw, SC 2011). */
+void oracle_philox4x32(const unsigned ctr_in[4], unsigned k0, unsigned k1, unsigned out[4]) {
+    unsigned c0 = ctr_in[0], c1 = ctr_in[1], c2 = ctr_in[2], c3 = ctr_in[3];
+    for (int r = 0; r < 10; ++r) {
+        if (r > 0) {
+            k0 += 0x9E3779B9u;
+            k1 += 0xBB67AE85u;
+        }
+        const unsigned long long p0 = 0xD2511F53ull * c0, p1 = 0xCD9E8D57ull * c2;
+        const unsigned hi0 = (unsigned)(p0 >> 32), lo0 = (unsigned)p0;
+        const unsigned hi1 = (unsigned)(p1 >> 32), lo1 = (unsigned)p1;
+        c0 = hi1 ^ c1 ^ k0;
+        c1 = lo1;
+        c2 = hi0 ^ c3 ^ k1;
+        c3 = lo0;
+    }
+    out[0] = c0;
+    out[1] = c1;
+    out[2] = c2;
+    out[3] = c3;
+}
+
+/* element::get_f_rand's draw (element.cpp:109-144) with the Philox stream of
+ * (particle, step) in place of rand(): Box-Muller on (k mod 1000)/1000,
+ * redrawn while |g| > 5, at most 64 draws per normal (then 0). */
+void oracle_brownian_normals(unsigned long long seed, unsigned id, unsigned t, double pi, double g[3]) {
+    unsigned buf[4];
+    int used = 4;
+    unsigned blk = 0;
+    for (int a = 0; a < 3; ++a) {
+        double v = 0.0;
+        for (int k = 0; k < 64; ++k) {
+            unsigned x[2];
+            for (int q = 0; q < 2; ++q) {
+                if (used == 4) {
+                    const unsigned ctr[4] = {id, t, blk++, 0u};
+                    oracle_philox4x32(ctr, (unsigned)seed, (unsigned)(seed >> 32), buf);
+                    used = 0;
+                }
+                x[q] = buf[used++];
+            }
+            const double r1 = (double)(x[0] % 1000u) / 1000;
+            const double r2 = (double)(x[1] % 1000u) / 1000;
+            v = sqrt(-2 * log(r1)) * cos(2 * pi * r2);
+            if (fabs(v) <= 5.0) break;
+            v = 0.0;
+        }
+        g[a] = v;
+    }
+}
+
+void oracle_set_extensions(oracle* o, int couple, double kt, unsigned long long seed) {
+    o->couple = couple;
+    o->kt = kt;
+    o->seed = seed;
+}
+
+/* element::advect (element.cpp:156-173) with uf (fluid coupling) and the
+ * Brownian force added to f_pi + f_ext + f_pp. */
+static void advect_ext(const oracle* o, int stage) {
+    const fipi_params* P = &o->P;
+    for (int q = 0; q < o->n; ++q) {
+        const double rq = o->r[q];
+        double v[3];
+        for (int a = 0; a < 3; ++a) {
+            double F = o->f_pi[3 * q + a] + 0.0;
+            F = F + o->f_pp[3 * q + a];
+            if (o->kt > 0.0) F = F + o->f_rand[3 * q + a];
+            v[a] = (o->couple ? o->uf[3 * q + a] : 0.0) + F / 6.0 / P->pi / P->mu / rq;
+        }
+        if (stage == 1) {
+            for (int a = 0; a < 3; ++a) {
+                o->u_old[3 * q + a] = v[a];
+                o->p_old[3 * q + a] = o->p[3 * q + a];
+                o->p[3 * q + a] = o->p[3 * q + a] + v[a] * P->dt;
+            }
+        } else {
+            const double hdt = 0.5 * P->dt;
+            for (int a = 0; a < 3; ++a)
+                o->p[3 * q + a] = o->p_old[3 * q + a] + (o->u_old[3 * q + a] + v[a]) * hdt;
+        }
+    }
+}
+
 /* ------------------------------------------------------------------ step */
 static void particle_stage(oracle* o, int stage) {
     const fipi_params* P = &o->P;
@@ -674,6 +766,24 @@ static void particle_stage(oracle* o, int stage) {
         free(tmp);
         free(vals);
     }
+    if (o->couple) { /* get_local_u with its interpolation (element.cpp:38-52) */
+        double* tmp = (double*)malloc(sizeof(double) * (size_t)V);
+        double* vals = (double*)malloc(sizeof(double) * (size_t)(n > 0 ? n : 1));
+        for (int d = 0; d < 3; ++d) {
+            for (long it = 0; it < V; ++it) tmp[it] = o->u[d][2 * it];
+            oracle_interpolate(P, tmp, n, o->p, vals);
+            for (int q = 0; q < n; ++q) o->uf[3 * q + d] = vals[q];
+        }
+        free(tmp);
+        free(vals);
+    }
+    if (o->kt > 0.0 && stage == 1) /* the step's Brownian force (element.cpp:138-143) */
+        for (int q = 0; q < n; ++q) {
+            double g[3];
+            oracle_brownian_normals(o->seed, (unsigned)q, (unsigned)o->t, P->pi, g);
+            const double s = sqrt(12.0 * P->pi * o->r[q] * P->mu * o->kt / P->dt);
+            for (int a = 0; a < 3; ++a) o->f_rand[3 * q + a] = s * g[a];
+        }
     /* sorting (cluster.cpp:116-169) */
     (void)oracle_sorting(P, n, o->p, o->keys, o->sorted, o->offsets, &o->it_mark);
     /* compute_f_pi (cluster.cpp:286-290) */
@@ -681,7 +791,8 @@ static void particle_stage(oracle* o, int stage) {
     /* compute_f_pp(t+1) (main.cpp:202, 213) */
     oracle_f_pp(P, n, o->p, o->t + 1, o->f_pi, o->f_pp, &o->tau, NULL, 0, NULL);
     /* compute_f_ext: zero (element.cpp:100-104); advect; enforce_bc */
-    oracle_advect(P, n, stage, o->f_pi, o->f_pp, o->r, o->p, o->p_old, o->u_old);
+    if (o->couple || o->kt > 0.0) advect_ext(o, stage);
+    else oracle_advect(P, n, stage, o->f_pi, o->f_pp, o->r, o->p, o->p_old, o->u_old);
     oracle_enforce_bc(P, n, o->p);
 }
 

@@ -68,6 +68,12 @@ void oracle_advect(const fipi_params* P, int n, int stage, const double* f_pi,
 void oracle_enforce_bc(const fipi_params* P, int n, double* p);
 void oracle_spread(const fipi_params* P, int n, const double* p, const double* f_pp,
                    double* out);
+/* Particle-model extensions (off by default): fluid coupling (uf = u
+ * interpolated, element.cpp:38-52) and the Brownian force of
+ * element.cpp:109-144 drawn from Philox-4x32-10. */
+void oracle_set_extensions(oracle* o, int couple, double kt, unsigned long long seed);
+void oracle_philox4x32(const unsigned ctr[4], unsigned k0, unsigned k1, unsigned out[4]);
+void oracle_brownian_normals(unsigned long long seed, unsigned id, unsigned t, double pi, double g[3]);
 /* srand(seed) (main.cpp:24), the phase field's draws (field.cpp:85-99) and
  * cluster::distribute (cluster.cpp:53-113) with glibc's rand(); returns
  * FIPI_ERR_BAD_PARAMS when a particle exceeds max_candidates draws. */

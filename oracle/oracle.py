@@ -78,6 +78,11 @@ def port_lib():
         lib.oracle_free_energy.argtypes = [ctypes.c_void_p]
         lib.oracle_mass.restype = ctypes.c_double
         lib.oracle_mass.argtypes = [ctypes.c_void_p]
+        lib.oracle_set_extensions.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_ulonglong]
+        lib.oracle_philox4x32.argtypes = [ctypes.POINTER(ctypes.c_uint), ctypes.c_uint, ctypes.c_uint,
+                                          ctypes.POINTER(ctypes.c_uint)]
+        lib.oracle_brownian_normals.argtypes = [ctypes.c_ulonglong, ctypes.c_uint, ctypes.c_uint, ctypes.c_double,
+                                                _dp]
         lib.oracle_fft3.argtypes = [P, _dp, ctypes.c_int]
         lib.oracle_grad.argtypes = [P, _dp, _dp]
         lib.oracle_div.argtypes = [P, _dp, _dp]
@@ -132,6 +137,9 @@ class Port:
             arrs = [None if a is None else np.ascontiguousarray(a, np.float64).ravel()
                     for a in (p, r, cos_theta, f_pp)]
             self.lib.oracle_set_particles(self.h, *[_d(a) for a in arrs])
+
+    def set_extensions(self, couple: bool = False, kt: float = 0.0, seed: int = 0):
+        self.lib.oracle_set_extensions(self.h, 1 if couple else 0, kt, seed)
 
     def step(self, n: int = 1):
         for _ in range(n):
@@ -204,6 +212,20 @@ def interpolate2(params, field, p):
     port_lib().oracle_interpolate2(ctypes.byref(params), _d(np.ascontiguousarray(field, np.float64)), n,
                                    _d(np.ascontiguousarray(p, np.float64)), _d(out))
     return out
+
+
+def philox4x32(ctr, key):
+    """Philox-4x32-10 of a 4-word counter and a 2-word key (4 words out)."""
+    c = (ctypes.c_uint * 4)(*ctr)
+    out = (ctypes.c_uint * 4)()
+    port_lib().oracle_philox4x32(c, key[0], key[1], out)
+    return list(out)
+
+
+def brownian_normals(seed: int, pid: int, t: int, pi: float):
+    g = np.zeros(3)
+    port_lib().oracle_brownian_normals(seed, pid, t, pi, _d(g))
+    return g
 
 
 def reference_initial_state(params, seed: int, max_candidates: int = 10**7):
