@@ -65,43 +65,14 @@ template <typename T> struct FieldPtrs {
     }
 };
 
-// Rows per Y-pass block: 256 threads, Tn = fft_threads_per_row(ny) per row.
-template <typename T> __host__ __device__ inline int ypass_rows(int ny) { return kThreads / fft_threads_per_row<T>(ny); }
-
-// C2C along contiguous rows of length ny; blockIdx.y selects the field.
-// Rows are staged in shared memory with one pad slot per 16 elements.
-template <typename T, int DIR, int N>
-__global__ void __launch_bounds__(kThreads) k_ypass(Geom g, const cplx<T>* __restrict__ twy, FieldPtrs<T> fp) {
-    using C = cplx<T>;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    C* s = reinterpret_cast<C*>(smem_raw);
-    constexpr int Tn = FftPlan<N, FftE<T>::value>::Tn;
-    const int rpb = kThreads / Tn;
-    const long long total_rows = (long long)g.nz * g.h;
-    const long long r0 = (long long)blockIdx.x * rpb;
-    const int rows = (int)min((long long)rpb, total_rows - r0);
-    const C* in = fp.in[blockIdx.y] + r0 * N;
-    C* out = fp.out[blockIdx.y] + r0 * N;
-    const IdxPadded idx{padded_len(N)};
-    using IO = FftIO<T, DIR, N>;
-    const int tid = threadIdx.x;
-    const int row = tid / Tn, t = tid - row * Tn;
-    const bool act = row < rows;
-    // first stage straight from global memory, last stage straight back
-    C v[IO::E];
-    if (act) {
-#pragma unroll
-        for (int i = 0; i < IO::E; ++i) v[i] = in[(size_t)row * N + IO::in_elem(t, i)];
-    }
-    smem_fft2<T, DIR, N, true, true>(s, idx, row, t, act, twy, 1, v);
-    if (act) {
-#pragma unroll
-        for (int i = 0; i < IO::E; ++i) out[(size_t)row * N + IO::out_elem(t, i)] = v[i];
-    }
-}
-
-template <typename T> inline size_t ypass_smem(const Geom& g) {
-    return (size_t)ypass_rows<T>(g.ny) * padded_len(g.ny) * sizeof(cplx<T>);
+// Elements per thread of the Y pass: radix-16 register codelets in FP32
+// (N = 256 in two stages, one shared-memory exchange), 8 in FP64.
+template <typename T> struct YE {
+    static constexpr int value = sizeof(T) == 4 ? 16 : 8;
+};
+// Rows per FFT round of a Y-pass block: 256 threads, N / min(N, YE) per row.
+template <typename T> __host__ __device__ inline int ypass_rows(int ny) {
+    return kThreads / (ny / (ny < YE<T>::value ? ny : YE<T>::value));
 }
 
 // Persistent Y pass: each block streams tiles of RB consecutive rows
@@ -112,19 +83,19 @@ template <typename T> inline size_t ypass_smem(const Geom& g) {
 // tile, the last stage stores straight to global memory.  `fields` fields of
 // rows are processed in one launch.
 constexpr int kYStages = 2;  // 3 measured no faster on GB300 (more registers)
-// FFT rounds per Y tile: FP32 tiles of 2 x 8 rows (32 KB at ny = 256) keep
-// more bytes in flight per SM; FP64 rows are twice as large already.
+// FFT rounds per Y tile (one: 16 FP32 or 8 FP64 rows of 256, 32 KB per copy).
 template <typename T> struct YGroups {
-    static constexpr int value = sizeof(T) == 4 ? 2 : 1;
+    static constexpr int value = 1;
 };
 
 template <typename T, int DIR, int N>
 __global__ void __launch_bounds__(kThreads) k_ypass_tma(Geom g, const cplx<T>* __restrict__ twy, FieldPtrs<T> fp,
                                                        int fields, int* status) {
     using C = cplx<T>;
-    using IO = FftIO<T, DIR, N>;
+    constexpr int EM = YE<T>::value;
+    using IO = FftIO<T, DIR, N, EM>;
     constexpr int S = kYStages;
-    constexpr int Tn = FftPlan<N, FftE<T>::value>::Tn;
+    constexpr int Tn = FftPlan<N, EM>::Tn;
     constexpr int RG = kThreads / Tn;           // rows per FFT round (all threads)
     constexpr int G = YGroups<T>::value;        // rounds per tile: G * RG rows per bulk copy
     constexpr int RB = G * RG;
@@ -201,7 +172,7 @@ __global__ void __launch_bounds__(kThreads) k_ypass_tma(Geom g, const cplx<T>* _
                 for (int i = 0; i < IO::E; ++i) v[i] = in[row * N + IO::in_elem(t, i)];
             }
             __syncthreads();  // the round's exchange rows overlap its natural rows
-            smem_fft2<T, DIR, N, true, true>(in + gr * RG * PITCH, xidx, rl, t, act, twy, 1, v);
+            smem_fft2<T, DIR, N, true, true, EM>(in + gr * RG * PITCH, xidx, rl, t, act, twy, 1, v);
             if (act) {
                 C* out = fp.pick(fp.out, f) + (r0 + row) * N;
 #pragma unroll
@@ -213,8 +184,7 @@ __global__ void __launch_bounds__(kThreads) k_ypass_tma(Geom g, const cplx<T>* _
 }
 
 template <typename T> inline size_t ypass_tma_smem(const Geom& g) {
-    const int tn = fft_threads_per_row<T>(g.ny);
-    const int rb = YGroups<T>::value * (kThreads / tn);
+    const int rb = YGroups<T>::value * ypass_rows<T>(g.ny);
     const int row = (g.ny + (g.ny >> 4) + 15) & ~15;
     return (size_t)kYStages * rb * row * sizeof(cplx<T>);
 }

@@ -162,10 +162,10 @@ template <int N, int EM> struct FftPlan {
 // (row, t); E/R groups per thread.  With IN the stage's inputs are already
 // in v (slot q*R + m holds element g + m N/R, g = t + Tn q); with OUT its
 // outputs stay in v (slot q*R + j holds element (g - k) R + k + j p).
-template <typename T, int R, int DIR, int N, int P, bool IN, bool OUT, class Idx>
+template <typename T, int R, int DIR, int N, int P, bool IN, bool OUT, int EM, class Idx>
 __device__ __forceinline__ void fft_stage(cplx<T>* s, const Idx& idx, int row, int t, bool act,
                                           const cplx<T>* __restrict__ tw, int ts, cplx<T>* v) {
-    using PL = FftPlan<N, FftE<T>::value>;
+    using PL = FftPlan<N, EM>;
     constexpr int G = PL::E / R;
     constexpr int NR = N / R;
     if constexpr (!IN) {
@@ -200,21 +200,21 @@ __device__ __forceinline__ void fft_stage(cplx<T>* s, const Idx& idx, int row, i
     if constexpr (!OUT) __syncthreads();
 }
 
-template <typename T, int DIR, int N, int S, int P, bool IN, bool OUT, class Idx>
+template <typename T, int DIR, int N, int S, int P, bool IN, bool OUT, int EM, class Idx>
 __device__ __forceinline__ void fft_stages(cplx<T>* s, const Idx& idx, int row, int t, bool act,
                                            const cplx<T>* __restrict__ tw, int ts, cplx<T>* v) {
-    using PL = FftPlan<N, FftE<T>::value>;
+    using PL = FftPlan<N, EM>;
     if constexpr (S < PL::NS) {
         constexpr int R = PL::radix(S, DIR);
-        fft_stage<T, R, DIR, N, P, IN && S == 0, OUT && S == PL::NS - 1>(s, idx, row, t, act, tw, ts, v);
-        fft_stages<T, DIR, N, S + 1, P * R, IN, OUT>(s, idx, row, t, act, tw, ts, v);
+        fft_stage<T, R, DIR, N, P, IN && S == 0, OUT && S == PL::NS - 1, EM>(s, idx, row, t, act, tw, ts, v);
+        fft_stages<T, DIR, N, S + 1, P * R, IN, OUT, EM>(s, idx, row, t, act, tw, ts, v);
     }
 }
 
 // Element indices of the register slots of the first stage (inputs) and
 // of the last stage (outputs) for thread t of a row.
-template <typename T, int DIR, int N> struct FftIO {
-    using PL = FftPlan<N, FftE<T>::value>;
+template <typename T, int DIR, int N, int EM = FftE<T>::value> struct FftIO {
+    using PL = FftPlan<N, EM>;
     static constexpr int E = PL::E;
     static constexpr int R0 = PL::radix(0, DIR);
     static constexpr int RL = PL::radix(PL::NS - 1, DIR);
@@ -231,16 +231,16 @@ template <typename T, int DIR, int N> struct FftIO {
 // Every thread of the block must call it (it contains block barriers).
 // IN: the first stage's inputs are in v (FftIO::in_elem order) instead of
 // shared memory; OUT: the results stay in v (FftIO::out_elem order).
-template <typename T, int DIR, int N, bool IN = false, bool OUT = false, class Idx>
+template <typename T, int DIR, int N, bool IN = false, bool OUT = false, int EM = FftE<T>::value, class Idx>
 __device__ __forceinline__ void smem_fft2(cplx<T>* s, const Idx& idx, int row, int t, bool act,
                                           const cplx<T>* __restrict__ tw, int ts, cplx<T>* v) {
-    fft_stages<T, DIR, N, 0, 1, IN, OUT>(s, idx, row, t, act, tw, ts, v);
+    fft_stages<T, DIR, N, 0, 1, IN, OUT, EM>(s, idx, row, t, act, tw, ts, v);
 }
-template <typename T, int DIR, int N, class Idx>
+template <typename T, int DIR, int N, int EM = FftE<T>::value, class Idx>
 __device__ __forceinline__ void smem_fft2(cplx<T>* s, const Idx& idx, int row, int t, bool act,
                                           const cplx<T>* __restrict__ tw, int ts) {
-    cplx<T> v[FftPlan<N, FftE<T>::value>::E];
-    fft_stages<T, DIR, N, 0, 1, false, false>(s, idx, row, t, act, tw, ts, v);
+    cplx<T> v[FftPlan<N, EM>::E];
+    fft_stages<T, DIR, N, 0, 1, false, false, EM>(s, idx, row, t, act, tw, ts, v);
 }
 
 // Calls f(std::integral_constant<int, n>) for a power of two n in [8, 512].
