@@ -292,8 +292,8 @@ __global__ void __launch_bounds__(kThreads) k_zpass(Geom g, const cplx<T>* __res
 // inverse Z pass that read its output again (one write and one read of
 // every intermediate spectrum less).  COLS ky columns per block (a run of
 // COLS complex values per kz).
-template <typename T, int N, int COLS> struct ZRtShape {
-    static constexpr int E = N < FftE<T>::value ? N : FftE<T>::value;
+template <typename T, int N, int COLS, int EM = FftE<T>::value> struct ZRtShape {
+    static constexpr int E = N < EM ? N : EM;
     static constexpr int Tn = N / E;                                      // threads per column FFT
     static constexpr int RC = COLS * Tn <= kThreads ? COLS : kThreads / Tn;  // columns per FFT round
     static constexpr int THREADS = RC * Tn;
@@ -304,10 +304,10 @@ template <typename T, int N, int COLS> struct ZRtShape {
 // of all kz; the column FFTs run in rounds of RC columns, while loads, the
 // mid operation and stores walk the tile with ky fastest (full runs per
 // warp).  Tiles whose load() only copies arrays (src()) arrive by cp.async.
-template <typename T, int NF, int NB, int DIR, int N, int COLS, class Op>
+template <typename T, int NF, int NB, int DIR, int N, int COLS, class Op, int EM = FftE<T>::value>
 __global__ void __launch_bounds__(kThreads) k_zpass_rt(Geom g, const cplx<T>* __restrict__ twz, Op op) {
     using C = cplx<T>;
-    using SH = ZRtShape<T, N, COLS>;
+    using SH = ZRtShape<T, N, COLS, EM>;
     constexpr int RC = SH::RC, P = SH::P, NT = SH::THREADS;
     constexpr int ELEMS = COLS * N;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -342,7 +342,7 @@ __global__ void __launch_bounds__(kThreads) k_zpass_rt(Geom g, const cplx<T>* __
     const int cl = tid % RC, t = tid / RC;
 #pragma unroll
     for (int f = 0; f < NF; ++f)
-        for (int r = 0; r < COLS; r += RC) smem_fft2<T, DIR, N>(s + f * fstride + r, idx, cl, t, true, twz, 1);
+        for (int r = 0; r < COLS; r += RC) smem_fft2<T, DIR, N, EM>(s + f * fstride + r, idx, cl, t, true, twz, 1);
     __syncthreads();
     for (int e = tid; e < ELEMS; e += NT) {
         const int c = e % COLS, z = e / COLS;
@@ -356,7 +356,7 @@ __global__ void __launch_bounds__(kThreads) k_zpass_rt(Geom g, const cplx<T>* __
     __syncthreads();
 #pragma unroll
     for (int b = 0; b < NB; ++b)
-        for (int r = 0; r < COLS; r += RC) smem_fft2<T, -DIR, N>(s + b * fstride + r, idx, cl, t, true, twz, 1);
+        for (int r = 0; r < COLS; r += RC) smem_fft2<T, -DIR, N, EM>(s + b * fstride + r, idx, cl, t, true, twz, 1);
     __syncthreads();
     for (int e = tid; e < ELEMS; e += NT) {
         const int c = e % COLS, z = e / COLS;
@@ -372,16 +372,16 @@ __global__ void __launch_bounds__(kThreads) k_zpass_rt(Geom g, const cplx<T>* __
 // each thread's mid and store work is on the modes its last FFT stage
 // produced.  Measured faster than k_zpass_rt for three or more fields
 // (smaller tiles, more blocks per SM); k_zpass_rt is faster for one.
-template <typename T, int N, int COLS> struct ZRtShapeT {
-    static constexpr int E = N < FftE<T>::value ? N : FftE<T>::value;
+template <typename T, int N, int COLS, int EM = FftE<T>::value> struct ZRtShapeT {
+    static constexpr int E = N < EM ? N : EM;
     static constexpr int Tn = N / E;
     static constexpr int TZ = COLS * Tn <= kThreads ? COLS : kThreads / Tn;
 };
 
-template <typename T, int NF, int NB, int DIR, int N, int COLS, class Op>
+template <typename T, int NF, int NB, int DIR, int N, int COLS, class Op, int EM = FftE<T>::value>
 __global__ void __launch_bounds__(kThreads) k_zpass_rt_t(Geom g, const cplx<T>* __restrict__ twz, Op op) {
     using C = cplx<T>;
-    using SH = ZRtShapeT<T, N, COLS>;
+    using SH = ZRtShapeT<T, N, COLS, EM>;
     constexpr int E = SH::E, Tn = SH::Tn, TZ = SH::TZ;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* s = reinterpret_cast<C*>(smem_raw);
@@ -415,7 +415,7 @@ __global__ void __launch_bounds__(kThreads) k_zpass_rt_t(Geom g, const cplx<T>* 
     }
     __syncthreads();
 #pragma unroll
-    for (int f = 0; f < NF; ++f) smem_fft2<T, DIR, N>(s + f * fstride, idx, c, t, true, twz, 1);
+    for (int f = 0; f < NF; ++f) smem_fft2<T, DIR, N, EM>(s + f * fstride, idx, c, t, true, twz, 1);
     // each thread's outputs of the last stage are the modes z = t + Tn i
 #pragma unroll 2
     for (int i = 0; i < E; ++i) {
@@ -429,7 +429,7 @@ __global__ void __launch_bounds__(kThreads) k_zpass_rt_t(Geom g, const cplx<T>* 
     }
     __syncthreads();
 #pragma unroll
-    for (int b = 0; b < NB; ++b) smem_fft2<T, -DIR, N>(s + b * fstride, idx, c, t, true, twz, 1);
+    for (int b = 0; b < NB; ++b) smem_fft2<T, -DIR, N, EM>(s + b * fstride, idx, c, t, true, twz, 1);
 #pragma unroll 4
     for (int i = 0; i < E; ++i) {
         const int z = t + Tn * i;
@@ -448,12 +448,12 @@ __global__ void __launch_bounds__(kThreads) k_zpass_rt_t(Geom g, const cplx<T>* 
 // at a time through a single tile.  The op supplies State (what a mode
 // keeps between the transforms), rr_mid (NF transformed values -> State),
 // rr_out (output b of a State) and rr_store (output b at gi).
-template <typename T, int NF, int NB, int DIR, int N, int COLS, class Op>
+template <typename T, int NF, int NB, int DIR, int N, int COLS, class Op, int EM = FftE<T>::value>
 __global__ void __launch_bounds__(kThreads, 2) k_zpass_rr(Geom g, const cplx<T>* __restrict__ twz, Op op) {
     using C = cplx<T>;
-    using SH = ZRtShapeT<T, N, COLS>;
-    using IOF = FftIO<T, DIR, N>;
-    using IOI = FftIO<T, -DIR, N>;
+    using SH = ZRtShapeT<T, N, COLS, EM>;
+    using IOF = FftIO<T, DIR, N, EM>;
+    using IOI = FftIO<T, -DIR, N, EM>;
     constexpr int E = SH::E, TZ = SH::TZ;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* s = reinterpret_cast<C*>(smem_raw);
@@ -476,7 +476,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_zpass_rr(Geom g, const cplx<T>*
             for (int f = 0; f < NF; ++f) v[f][i] = w[f];
         }
 #pragma unroll
-        for (int f = 0; f < NF; ++f) smem_fft2<T, DIR, N, true, true>(s, idx, c, t, true, twz, 1, v[f]);
+        for (int f = 0; f < NF; ++f) smem_fft2<T, DIR, N, true, true, EM>(s, idx, c, t, true, twz, 1, v[f]);
 #pragma unroll
         for (int i = 0; i < E; ++i) {
             const int z = IOF::out_elem(t, i);
@@ -491,7 +491,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_zpass_rr(Geom g, const cplx<T>*
         C v[E];
 #pragma unroll
         for (int i = 0; i < E; ++i) v[i] = op.rr_out(b, kx, ky, IOF::out_elem(t, i), st[i]);
-        smem_fft2<T, -DIR, N, true, true>(s, idx, c, t, true, twz, 1, v);
+        smem_fft2<T, -DIR, N, true, true, EM>(s, idx, c, t, true, twz, 1, v);
 #pragma unroll
         for (int i = 0; i < E; ++i) {
             const int z = IOI::out_elem(t, i);

@@ -475,6 +475,10 @@ template <typename T, int NF, int DIR, class Op> void launch_z(fipi_ctx* ctx, co
 // FP32 round trips that run as k_zpass_rr (measured faster there than the
 // shared-memory tiles of k_zpass_rt / k_zpass_rt_t).
 template <int NF, int NB> constexpr bool zrt_in_registers = (NF == 1 && NB == 4);
+// Elements per thread (radix of the register codelets) of the Z round trips:
+// 16 in FP32 (N = 256 in two stages, one shared-memory exchange; measured
+// 10 % faster than radix 8 for the one-field round trips), 8 in FP64.
+template <typename T, int NF, int NB> constexpr int zrt_elems = sizeof(T) == 4 ? 16 : 8;
 
 // Round-trip Z pass: NF fields in, NB fields out; WIDE: k_zpass_rt with
 // tiles of COLS ky columns (COLS <= 16 for FP32, whose grids have
@@ -483,14 +487,15 @@ template <typename T, int NF, int NB, int DIR, int COLS, bool WIDE, class Op>
 void launch_zrt(fipi_ctx* ctx, const char* name, int nspec, const Op& op) {
     const Geom& g = ctx->g;
     LaunchScope ls(ctx, name, (double)nspec * g.SH * sizeof(cplx<T>));
+    constexpr int EM = zrt_elems<T, NF, NB>;
     if constexpr (sizeof(T) == sizeof(float) && zrt_in_registers<NF, NB>) {
         // FP32: the round trip held in registers
         dispatch_pow2(g.nz, [&](auto NC) {
             constexpr int N = decltype(NC)::value;
-            using SHP = ZRtShapeT<T, N, 16>;
+            using SHP = ZRtShapeT<T, N, 16, EM>;
             const size_t smem = (size_t)SHP::TZ * N * sizeof(cplx<T>);
             dim3 grid(g.h, g.ny / SHP::TZ);
-            auto kern = k_zpass_rr<T, NF, NB, DIR, N, 16, Op>;
+            auto kern = k_zpass_rr<T, NF, NB, DIR, N, 16, Op, EM>;
             static size_t granted = 48 * 1024;
             ensure_smem(kern, smem, granted);
             kern<<<grid, SHP::TZ * SHP::Tn, smem, ctx->stream>>>(g, (const cplx<T>*)ctx->fb.twz, op);
@@ -500,11 +505,11 @@ void launch_zrt(fipi_ctx* ctx, const char* name, int nspec, const Op& op) {
     if constexpr (!WIDE) {
         dispatch_pow2(g.nz, [&](auto NC) {
             constexpr int N = decltype(NC)::value;
-            using SHP = ZRtShapeT<T, N, COLS>;
+            using SHP = ZRtShapeT<T, N, COLS, EM>;
             constexpr int NS = NF > NB ? NF : NB;
             const size_t smem = (size_t)NS * SHP::TZ * N * sizeof(cplx<T>);
             dim3 grid(g.h, g.ny / SHP::TZ);
-            auto kern = k_zpass_rt_t<T, NF, NB, DIR, N, COLS, Op>;
+            auto kern = k_zpass_rt_t<T, NF, NB, DIR, N, COLS, Op, EM>;
             static size_t granted = 48 * 1024;
             ensure_smem(kern, smem, granted);
             kern<<<grid, SHP::TZ * SHP::Tn, smem, ctx->stream>>>(g, (const cplx<T>*)ctx->fb.twz, op);
@@ -513,11 +518,11 @@ void launch_zrt(fipi_ctx* ctx, const char* name, int nspec, const Op& op) {
     } else
     dispatch_pow2(g.nz, [&](auto NC) {
         constexpr int N = decltype(NC)::value;
-        using SHP = ZRtShape<T, N, COLS>;
+        using SHP = ZRtShape<T, N, COLS, EM>;
         constexpr int NS = NF > NB ? NF : NB;
         const size_t smem = (size_t)NS * SHP::P * N * sizeof(cplx<T>);
         dim3 grid(g.h, g.ny / COLS);
-        auto kern = k_zpass_rt<T, NF, NB, DIR, N, COLS, Op>;
+        auto kern = k_zpass_rt<T, NF, NB, DIR, N, COLS, Op, EM>;
         static size_t granted = 48 * 1024;
         ensure_smem(kern, smem, granted);
         kern<<<grid, SHP::THREADS, smem, ctx->stream>>>(g, (const cplx<T>*)ctx->fb.twz, op);
