@@ -85,6 +85,29 @@ template <typename T, bool MIXED> struct OpConv {
         v[0] = mkc<C>(s0, s1);
         if (MIXED) acc += s0 + s1;  // per-thread FP32 partial; FP64 from the block sum on
     }
+    // k_xpass_stream: u_f . (grad c)_f accumulated field by field
+    struct State {
+        C s;
+    };
+    static constexpr int emit_after(int f) { return f == 2 ? 0 : -1; }
+    struct Pre {};  // grad c is read in take (measured faster than fetching it ahead)
+    template <int F> __device__ void fetch(int, int, int, Pre&) const {}
+    template <int F, class A> __device__ C take(int z, int y, int n, C v, const Pre&, State& st, A& acc) const {
+        const size_t row = ((size_t)z * ny + y) * nx;
+        if (tape_u[0]) reinterpret_cast<C*>(tape_u[F] + row)[n] = v;
+        const C gg = reinterpret_cast<const C*>(g[F] + row)[n];
+        if (F == 0) {
+            T s0 = T(0), s1 = T(0);
+            s0 += v.x * gg.x;
+            s1 += v.y * gg.y;
+            st.s = mkc<C>(s0, s1);
+        } else {
+            st.s.x += v.x * gg.x;
+            st.s.y += v.y * gg.y;
+        }
+        if (F == 2 && MIXED) acc += st.s.x + st.s.y;
+        return st.s;
+    }
 };
 
 // Step B: c = C2R(c_hat) (+ FP64 mean in the mixed form), f = (lambda/eps^2)(c^3 - c).
@@ -107,6 +130,15 @@ template <typename T, bool MIXED> struct OpCF {
         }
         reinterpret_cast<C*>(c + ((size_t)z * ny + y) * nx)[n] = cc;
         v[0] = mkc<C>((cc.x * cc.x * cc.x - cc.x) * lam_eps, (cc.y * cc.y * cc.y - cc.y) * lam_eps);
+    }
+    // k_xpass_stream
+    struct State {};
+    static constexpr int emit_after(int f) { return f == 0 ? 0 : -1; }
+    struct Pre {};
+    template <int F> __device__ void fetch(int, int, int, Pre&) const {}
+    template <int F, class A> __device__ C take(int z, int y, int n, C v, const Pre&, State&, A& acc) const {
+        point(z, y, n, &v, acc);
+        return v;
     }
 };
 
@@ -688,7 +720,7 @@ template <typename T, bool MIXED> static void step_ch_t(fipi_ctx* ctx, int t) {
     OpConv<T, MIXED> oc{{F<T>::S(ctx, 0), F<T>::S(ctx, 1), F<T>::S(ctx, 2)},
                         {(const T*)b.g[0], (const T*)b.g[1], (const T*)b.g[2]}, F<T>::S(ctx, 3), ctx->partials,
                         {(T*)ctx->tape_u[0], (T*)ctx->tape_u[1], (T*)ctx->tape_u[2]}, g.nx, g.ny};
-    launch_x<T, 3, 1, MIXED>(ctx, "X inverse u, conv, forward", 3, oc, ctx->partials);
+    launch_xs<T, 3, 1, MIXED>(ctx, "X inverse u, conv, forward", 3, oc, ctx->partials);
     void* s1[1] = {b.S[3]};
     launch_y<T>(ctx, 1, s1, s1, -1);
     ZOpCH<T, MIXED> zc{F<T>::S(ctx, 3), F<T>::sp(b.chat), F<T>::sp(b.chat_old), F<T>::sp(b.fhat),
@@ -704,7 +736,7 @@ template <typename T, bool MIXED> static void step_ch_t(fipi_ctx* ctx, int t) {
     launch_y<T>(ctx, 1, s0, s0, +1);
     OpCF<T, MIXED> ocf{F<T>::S(ctx, 0), (T*)b.c, F<T>::S(ctx, 1), reinterpret_cast<const float*>(ctx->k0 + 4),
                        k.lam_eps, g.nx, g.ny};
-    launch_x<T, 1, 1, false>(ctx, "X inverse c, f, forward", 1, ocf);
+    launch_xs<T, 1, 1, false>(ctx, "X inverse c, f, forward", 1, ocf);
     void* s1b[1] = {b.S[1]};
     launch_y<T>(ctx, 1, s1b, s1b, -1);
     ZOpFRt<T> zf{F<T>::S(ctx, 1), F<T>::sp(b.fhat_old), F<T>::sp(b.chat),
@@ -743,7 +775,7 @@ template <typename T> static void step_stokes_t(fipi_ctx* ctx) {
     ZOpProj<T> zp{{F<T>::S(ctx, 0), F<T>::S(ctx, 1), F<T>::S(ctx, 2)}, {nullptr, nullptr, nullptr}, kt, k.mu, g.m,
                   g.ny / 2, g.nz / 2};
     ZOpProjRt<T> zpr{zp, {F<T>::sp(b.upre[0]), F<T>::sp(b.upre[1]), F<T>::sp(b.upre[2])}};
-    launch_zrt<T, 3, 3, -1, 16 / (sizeof(T) / 4), false>(ctx, "Z forward + projection + inverse", 6, zpr);
+    launch_zrt<T, 3, 3, -1, 16 / (sizeof(T) / 4), true>(ctx, "Z forward + projection + inverse", 6, zpr);
 }
 
 

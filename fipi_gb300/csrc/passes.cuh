@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <type_traits>
 
 #include "ctx.hpp"
 
@@ -227,6 +228,9 @@ __device__ __forceinline__ void r2c_post(cplx<T>* s, const Idx& idx, const cplx<
 // transposed column accesses are conflict-free); X_M sits at index M.
 // Blocks per SM the register budget is set for: FP32 4 (3 with four
 // fields), FP64 3 (2).  512-thread blocks measured slower.
+// Elements per thread (radix of the register codelets) of the X pass.
+template <typename T, int NIN, int NOUT> constexpr int x_elems = FftE<T>::value;
+
 template <typename T, int NF, int NT> struct XMinBlocks {
     static constexpr int value = sizeof(T) == 4 ? (NF <= 3 ? 4 : 3) : (NF <= 3 ? 3 : 2);
 };
@@ -243,7 +247,8 @@ __global__ void __launch_bounds__(NT, XMinBlocks<T, (NIN > NOUT ? NIN : NOUT), N
     const IdxPadded idx{xpass_pitch(M)};
     const int z = blockIdx.y, y0 = blockIdx.x * TY;
     const int tid = threadIdx.x;
-    constexpr int Tn = FftPlan<M, FftE<T>::value>::Tn;
+    constexpr int EM = x_elems<T, NIN, NOUT>;
+    constexpr int Tn = FftPlan<M, EM>::Tn;
     constexpr int rpr = NT / Tn;  // row FFTs per round
     // Loads and stores walk the tile field by field with ty fastest (a
     // run of TY along y per kx): each thread keeps one ty and steps kx.
@@ -263,7 +268,7 @@ __global__ void __launch_bounds__(NT, XMinBlocks<T, (NIN > NOUT ? NIN : NOUT), N
         __syncthreads();
         for (int r0 = 0; r0 < NIN * TY; r0 += rpr) {
             const int row = r0 + tid / Tn;
-            smem_fft2<T, +1, M>(s, idx, row, tid % Tn, row < NIN * TY, twx, 2);
+            smem_fft2<T, +1, M, EM>(s, idx, row, tid % Tn, row < NIN * TY, twx, 2);
         }
     }
     const T invV = T(1) / T(g.V);
@@ -286,7 +291,7 @@ __global__ void __launch_bounds__(NT, XMinBlocks<T, (NIN > NOUT ? NIN : NOUT), N
     if constexpr (NOUT > 0) {
         for (int r0 = 0; r0 < NOUT * TY; r0 += rpr) {
             const int row = r0 + tid / Tn;
-            smem_fft2<T, -1, M>(s, idx, row, tid % Tn, row < NOUT * TY, twx, 2);
+            smem_fft2<T, -1, M, EM>(s, idx, row, tid % Tn, row < NOUT * TY, twx, 2);
         }
         r2c_post<T, M, NOUT * TY, NT>(s, idx, twx, tid);
         __syncthreads();
@@ -295,6 +300,97 @@ __global__ void __launch_bounds__(NT, XMinBlocks<T, (NIN > NOUT ? NIN : NOUT), N
             C* dst = op.out(f) + gbase;
             for (int kx = kx0; kx < H; kx += KS) dst[(size_t)kx * g.ny] = s[idx(f * TY + tyl, kx)];
         }
+    }
+}
+
+template <int I, int N, class F> __device__ __forceinline__ void static_for(F&& f) {
+    if constexpr (I < N) {
+        f(std::integral_constant<int, I>{});
+        static_for<I + 1, N>(f);
+    }
+}
+
+// X pass with the point operation on registers: one FFT round per field
+// (TY rows x Tn threads = the block), the inverse transform of input f ends
+// in registers (its last stage's modes), op.take<f> consumes them and, when
+// op.emit_after(f) names an output d, returns that output's values, whose
+// forward transform starts from the registers, exchanging through the tile
+// of field d (already consumed).  Against k_xpass_acc this drops the point
+// loop's shared-memory round trip and one exchange per field.  The op keeps
+// a State per mode between the rounds; op.fetch<f> requests the round's
+// real-space inputs (Pre) before its transform.
+template <typename T, int M> struct XStreamShape {
+    static constexpr int TY = Tiles<T>::TY;
+    static constexpr int E = FftPlan<M, FftE<T>::value>::E;
+    static constexpr int Tn = FftPlan<M, FftE<T>::value>::Tn;
+    static constexpr int NT = TY * Tn;
+    // blocks per SM the register budget is set for: three (two in FP64)
+    // 256-thread blocks' worth (the State of a mode stays live across rounds)
+    template <int NF> static constexpr int minb() {
+        const int b = (sizeof(T) == 4 ? 3 : 2) * 256 / NT;
+        return b < 1 ? 1 : (b > 8 ? 8 : b);
+    }
+};
+
+template <typename T, int NIN, int NOUT, bool REDUCE, int M, class Op>
+__global__ void __launch_bounds__(XStreamShape<T, M>::NT,
+                                  XStreamShape<T, M>::template minb<(NIN > NOUT ? NIN : NOUT)>())
+    k_xpass_stream(Geom g, const cplx<T>* __restrict__ twx, Op op, double* partials) {
+    using C = cplx<T>;
+    using SH = XStreamShape<T, M>;
+    constexpr int TY = SH::TY, E = SH::E, Tn = SH::Tn, NT = SH::NT;
+    constexpr int EM = FftE<T>::value;
+    constexpr int H = M + 1;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C* s = reinterpret_cast<C*>(smem_raw);
+    const IdxPadded idx{xpass_pitch(M)};
+    const int z = blockIdx.y, y0 = blockIdx.x * TY;
+    const int tid = threadIdx.x;
+    {
+        const int tyl = tid % TY, kx0 = tid / TY;
+        const size_t gbase = (size_t)z * H * g.ny + y0 + tyl;
+#pragma unroll
+        for (int f = 0; f < NIN; ++f) {
+            const C* src = op.in(f) + gbase;
+            for (int kx = kx0; kx < H; kx += NT / TY) cp_async<sizeof(C)>(&s[idx(f * TY + tyl, kx)], src + (size_t)kx * g.ny);
+        }
+        cp_async_wait_all();
+        __syncthreads();
+        c2r_pre<T, M, NIN * TY, NT>(s, idx, twx, tid);
+        __syncthreads();
+    }
+    const int ty = tid / Tn, t = tid % Tn;
+    using IO = FftIO<T, +1, M, EM>;
+    const T invV = T(1) / T(g.V);
+    T acc = T(0);
+    typename Op::State st[E];
+    static_for<0, NIN>([&](auto FC) {
+        constexpr int f = decltype(FC)::value;
+        // the real-space inputs of this round are requested before its transform
+        typename Op::Pre pre[E];
+#pragma unroll
+        for (int i = 0; i < E; ++i) op.template fetch<f>(z, y0 + ty, IO::out_elem(t, i), pre[i]);
+        C v[E];
+        smem_fft2<T, +1, M, false, true, EM>(s, idx, f * TY + ty, t, true, twx, 2, v);
+#pragma unroll
+        for (int i = 0; i < E; ++i)
+            v[i] = op.template take<f>(z, y0 + ty, IO::out_elem(t, i), cscale(v[i], invV), pre[i], st[i], acc);
+        constexpr int d = Op::emit_after(f);
+        if constexpr (d >= 0) smem_fft2<T, -1, M, true, false, EM>(s, idx, d * TY + ty, t, true, twx, 2, v);
+    });
+    if constexpr (REDUCE) {
+        const double bs = block_sum((double)acc);
+        if (tid == 0) partials[(size_t)blockIdx.y * gridDim.x + blockIdx.x] = bs;
+    }
+    __syncthreads();
+    r2c_post<T, M, NOUT * TY, NT>(s, idx, twx, tid);
+    __syncthreads();
+    const int tyl = tid % TY, kx0 = tid / TY;
+    const size_t gbase = (size_t)z * H * g.ny + y0 + tyl;
+#pragma unroll
+    for (int f = 0; f < NOUT; ++f) {
+        C* dst = op.out(f) + gbase;
+        for (int kx = kx0; kx < H; kx += NT / TY) dst[(size_t)kx * g.ny] = s[idx(f * TY + tyl, kx)];
     }
 }
 
@@ -423,6 +519,38 @@ void launch_x(fipi_ctx* ctx, const char* name, int nreal, const Op& op, double* 
         ensure_smem(kern, smem, granted);
         kern<<<grid, NT, smem, ctx->stream>>>(g, (const cplx<T>*)ctx->fb.twx, op, partials);
     });
+}
+
+// FP32: k_xpass_stream (ops with take) for rows up to 256 points; otherwise
+// and in FP64: k_xpass_acc.  The force pass stays on k_xpass_acc (measured
+// faster there: its streamed form holds mu and the force inputs across rounds).
+template <typename T, int NIN, int NOUT, bool REDUCE, class Op>
+void launch_xs(fipi_ctx* ctx, const char* name, int nreal, const Op& op, double* partials = nullptr) {
+    if constexpr (sizeof(T) != sizeof(float)) {
+        launch_x<T, NIN, NOUT, REDUCE>(ctx, name, nreal, op, partials);
+    } else {
+        const Geom& g = ctx->g;
+        LaunchScope ls(ctx, name,
+                       (double)(NIN + NOUT) * g.SH * sizeof(cplx<T>) + (double)nreal * g.V * sizeof(T));
+        constexpr int NF = NIN > NOUT ? NIN : NOUT;
+        const size_t smem = (size_t)NF * Tiles<T>::TY * xpass_pitch(g.m) * sizeof(cplx<T>);
+        dim3 grid(g.ny / Tiles<T>::TY, g.nz);
+        dispatch_pow2(g.m, [&](auto MC) {
+            constexpr int M = decltype(MC)::value;
+            if constexpr (XStreamShape<T, M>::NT <= kThreads) {
+                auto kern = k_xpass_stream<T, NIN, NOUT, REDUCE, M, Op>;
+                static size_t granted = 48 * 1024;
+                ensure_smem(kern, smem, granted);
+                kern<<<grid, XStreamShape<T, M>::NT, smem, ctx->stream>>>(g, (const cplx<T>*)ctx->fb.twx, op,
+                                                                          partials);
+            } else {  // rows of more than 256 points: one round per field would need > 256 threads
+                auto kern = k_xpass_acc<T, NIN, NOUT, REDUCE, M, Op>;
+                static size_t granted = 48 * 1024;
+                ensure_smem(kern, smem, granted);
+                kern<<<grid, kThreads, smem, ctx->stream>>>(g, (const cplx<T>*)ctx->fb.twx, op, partials);
+            }
+        });
+    }
 }
 
 template <typename T> void launch_y(fipi_ctx* ctx, int nf, void* const* in, void* const* out, int dir) {
