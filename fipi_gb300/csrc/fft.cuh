@@ -46,8 +46,6 @@ template <typename T> struct Tiles {
     static constexpr int TZ = 128 / (2 * sizeof(T));
 };
 
-// A Z-pass operation whose load() only copies NF spectral arrays declares
-// src(f) (the array of field f); its tiles are then fetched with cp.async.
 // A Z-pass operation that declares PreT and pre() has global reads in its
 // mid operation that can be issued ahead (k_zpass_rt batches ZU modes; two
 // measured fastest, more raise register pressure).
@@ -55,6 +53,8 @@ template <class O, class = void> struct HasPre : std::false_type {};
 template <class O> struct HasPre<O, std::void_t<typename O::PreT>> : std::true_type {};
 constexpr int ZU = 2;
 
+// A Z-pass operation whose load() only copies NF spectral arrays declares
+// src(f) (the array of field f); its tiles are then fetched with cp.async.
 template <class O, class = void> struct HasSrc : std::false_type {};
 template <class O> struct HasSrc<O, std::void_t<decltype(std::declval<const O&>().src(0))>> : std::true_type {};
 
