@@ -325,9 +325,10 @@ template <typename T, int M> struct XStreamShape {
     static constexpr int Tn = FftPlan<M, FftE<T>::value>::Tn;
     static constexpr int NT = TY * Tn;
     // blocks per SM the register budget is set for: three (two in FP64)
-    // 256-thread blocks' worth (the State of a mode stays live across rounds)
+    // 256-thread blocks' worth (the State of a mode stays live across
+    // rounds), four for a single field
     template <int NF> static constexpr int minb() {
-        const int b = (sizeof(T) == 4 ? 3 : 2) * 256 / NT;
+        const int b = (sizeof(T) == 4 ? (NF == 1 ? 4 : 3) : 2) * 256 / NT;
         return b < 1 ? 1 : (b > 8 ? 8 : b);
     }
 };
