@@ -90,15 +90,15 @@ template <typename T> __host__ __device__ inline int ypass_rows(int ny) {
 // tile, the last stage stores straight to global memory.  `fields` fields of
 // rows are processed in one launch.
 constexpr int kYStages = 2;  // 3 measured no faster on GB300 (more registers)
-// Three blocks per SM (<= 85 registers) measured 6 % faster than two with the
-// radix-16 codelets.
+// FP32: three blocks per SM (<= 85 registers) measured 6 % faster than two
+// with the radix-16 codelets; FP64 keeps two (its codelets need ~124).
 // FFT rounds per Y tile (one: 16 FP32 or 8 FP64 rows of 256, 32 KB per copy).
 template <typename T> struct YGroups {
     static constexpr int value = 1;
 };
 
 template <typename T, int DIR, int N>
-__global__ void __launch_bounds__(kThreads, 3) k_ypass_tma(Geom g, const cplx<T>* __restrict__ twy, FieldPtrs<T> fp,
+__global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 3 : 2) k_ypass_tma(Geom g, const cplx<T>* __restrict__ twy, FieldPtrs<T> fp,
                                                        int fields, int* status) {
     using C = cplx<T>;
     constexpr int EM = YE<T>::value;
