@@ -725,7 +725,7 @@ template <typename T, bool MIXED> static void step_ch_t(fipi_ctx* ctx, int t) {
     launch_y<T>(ctx, 1, s1, s1, -1);
     ZOpCH<T, MIXED> zc{F<T>::S(ctx, 3), F<T>::sp(b.chat), F<T>::sp(b.chat_old), F<T>::sp(b.fhat),
                        F<T>::sp(b.fhat_old), F<T>::sp(b.Chat_old), kt, k, t == 0 ? 1 : 0};
-    ZOpCHRt<T, MIXED> zcr{zc, F<T>::S(ctx, 0), ctx->k0, ctx->partials, (g.ny / Tiles<T>::TY) * g.nz,
+    ZOpCHRt<T, MIXED> zcr{zc, F<T>::S(ctx, 0), ctx->k0, ctx->partials, (g.ny / x_rows_of(sizeof(T), g.m)) * g.nz,
                           ctx->P.dt, 1.0 / (double)g.V};
     launch_zrt<T, 1, 1, -1, 16 / (sizeof(T) / 4), true>(ctx, t == 0 ? "Z forward + IMEX update + inverse" : "Z forward + SBDF2 update + inverse",
                                 t == 0 ? 6 : 9, zcr);

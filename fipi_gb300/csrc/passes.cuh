@@ -228,6 +228,14 @@ __device__ __forceinline__ void r2c_post(cplx<T>* s, const Idx& idx, const cplx<
 // transposed column accesses are conflict-free); X_M sits at index M.
 // Blocks per SM the register budget is set for: FP32 4 (3 with four
 // fields), FP64 3 (2).  512-thread blocks measured slower.
+// Rows per X-pass tile: 16 FP32 rows (8 FP64) keep 128-byte runs along y;
+// FP32 rows of 512 points take 8 so that the tile of four fields fits
+// three blocks per SM.
+__host__ __device__ constexpr int x_rows_of(int elem_bytes, int m) {
+    return elem_bytes == 4 ? (m >= 256 ? 8 : 16) : 8;
+}
+template <typename T, int M> constexpr int x_rows = x_rows_of(sizeof(T), M);
+
 // Elements per thread (radix of the register codelets) of the X pass.
 template <typename T, int NIN, int NOUT> constexpr int x_elems = FftE<T>::value;
 
@@ -239,7 +247,7 @@ template <typename T, int NIN, int NOUT, bool REDUCE, int M, class Op, int NT = 
 __global__ void __launch_bounds__(NT, XMinBlocks<T, (NIN > NOUT ? NIN : NOUT), NT>::value)
     k_xpass_acc(Geom g, const cplx<T>* __restrict__ twx, Op op, double* partials) {
     using C = cplx<T>;
-    constexpr int TY = Tiles<T>::TY;
+    constexpr int TY = x_rows<T, M>;
     constexpr int NF = NIN > NOUT ? NIN : NOUT;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* s = reinterpret_cast<C*>(smem_raw);
@@ -320,7 +328,7 @@ template <int I, int N, class F> __device__ __forceinline__ void static_for(F&& 
 // a State per mode between the rounds; op.fetch<f> requests the round's
 // real-space inputs (Pre) before its transform.
 template <typename T, int M> struct XStreamShape {
-    static constexpr int TY = Tiles<T>::TY;
+    static constexpr int TY = x_rows<T, M>;
     static constexpr int E = FftPlan<M, FftE<T>::value>::E;
     static constexpr int Tn = FftPlan<M, FftE<T>::value>::Tn;
     static constexpr int NT = TY * Tn;
@@ -504,17 +512,18 @@ template <typename T> struct F {
 };
 
 // nreal: real (V-sized) arrays the fused point operation reads or writes.
-// One block per tile of Tiles<T>::TY rows; NT threads per block.
+// One block per tile of x_rows<T, M> rows; NT threads per block.
 template <typename T, int NIN, int NOUT, bool REDUCE, class Op, int NT = kThreads>
 void launch_x(fipi_ctx* ctx, const char* name, int nreal, const Op& op, double* partials = nullptr) {
     const Geom& g = ctx->g;
     LaunchScope ls(ctx, name,
                    (double)(NIN + NOUT) * g.SH * sizeof(cplx<T>) + (double)nreal * g.V * sizeof(T));
     constexpr int NF = NIN > NOUT ? NIN : NOUT;
-    const size_t smem = (size_t)NF * Tiles<T>::TY * xpass_pitch(g.m) * sizeof(cplx<T>);
-    dim3 grid(g.ny / Tiles<T>::TY, g.nz);
     dispatch_pow2(g.m, [&](auto MC) {
         constexpr int M = decltype(MC)::value;
+        constexpr int TY = x_rows<T, M>;
+        const size_t smem = (size_t)NF * TY * xpass_pitch(g.m) * sizeof(cplx<T>);
+        dim3 grid(g.ny / TY, g.nz);
         auto kern = k_xpass_acc<T, NIN, NOUT, REDUCE, M, Op, NT>;
         static size_t granted = 48 * 1024;
         ensure_smem(kern, smem, granted);
@@ -534,10 +543,11 @@ void launch_xs(fipi_ctx* ctx, const char* name, int nreal, const Op& op, double*
         LaunchScope ls(ctx, name,
                        (double)(NIN + NOUT) * g.SH * sizeof(cplx<T>) + (double)nreal * g.V * sizeof(T));
         constexpr int NF = NIN > NOUT ? NIN : NOUT;
-        const size_t smem = (size_t)NF * Tiles<T>::TY * xpass_pitch(g.m) * sizeof(cplx<T>);
-        dim3 grid(g.ny / Tiles<T>::TY, g.nz);
         dispatch_pow2(g.m, [&](auto MC) {
             constexpr int M = decltype(MC)::value;
+            constexpr int TY = x_rows<T, M>;
+            const size_t smem = (size_t)NF * TY * xpass_pitch(g.m) * sizeof(cplx<T>);
+            dim3 grid(g.ny / TY, g.nz);
             if constexpr (XStreamShape<T, M>::NT <= kThreads) {
                 auto kern = k_xpass_stream<T, NIN, NOUT, REDUCE, M, Op>;
                 static size_t granted = 48 * 1024;
@@ -647,11 +657,13 @@ void launch_zrt(fipi_ctx* ctx, const char* name, int nspec, const Op& op) {
     } else
     dispatch_pow2(g.nz, [&](auto NC) {
         constexpr int N = decltype(NC)::value;
-        using SHP = ZRtShape<T, N, COLS, EM>;
         constexpr int NS = NF > NB ? NF : NB;
+        // columns of 512 modes with three or more fields: half the tile (two blocks per SM)
+        constexpr int CW = (N >= 512 && NS >= 3 && COLS > 8) ? COLS / 2 : COLS;
+        using SHP = ZRtShape<T, N, CW, EM>;
         const size_t smem = (size_t)NS * SHP::P * N * sizeof(cplx<T>);
-        dim3 grid(g.h, g.ny / COLS);
-        auto kern = k_zpass_rt<T, NF, NB, DIR, N, COLS, Op, EM>;
+        dim3 grid(g.h, g.ny / CW);
+        auto kern = k_zpass_rt<T, NF, NB, DIR, N, CW, Op, EM>;
         static size_t granted = 48 * 1024;
         ensure_smem(kern, smem, granted);
         kern<<<grid, SHP::THREADS, smem, ctx->stream>>>(g, (const cplx<T>*)ctx->fb.twz, op);
