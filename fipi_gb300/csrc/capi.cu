@@ -196,6 +196,8 @@ fipi_status fipi_create(const fipi_params* P, fipi_precision prec, int device, f
     if (ctx->pb.n > 0) {
         e = cudaMallocHost((void**)&ctx->pin, sizeof(double) * 12 * (size_t)ctx->pb.n);
         if (e != cudaSuccess) return fail(cuda_check(ctx, e, "cudaMallocHost(particle staging)"));
+        e = cudaHostGetDevicePointer((void**)&ctx->pin_dev, ctx->pin, 0);
+        if (e != cudaSuccess) return fail(cuda_check(ctx, e, "cudaHostGetDevicePointer(particle staging)"));
     }
     e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return fail(cuda_check(ctx, e, "init"));
@@ -237,10 +239,11 @@ fipi_status fipi_device_bytes(const fipi_ctx* ctx, size_t* out) {
 }  // extern "C"
 
 fipi_status fipi::check_status(fipi_ctx* ctx) {
-    FIPI_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    FIPI_CUDA(ctx, cudaGetLastError());
+    // the copy of the error word is ordered after all enqueued work, so one
+    // synchronisation covers both
     int st = 0;
     FIPI_CUDA(ctx, d2h(ctx, &st, ctx->status, sizeof(int)));
+    FIPI_CUDA(ctx, cudaGetLastError());
     if (st) {
         FIPI_CUDA(ctx, cudaMemsetAsync(ctx->status, 0, sizeof(int), ctx->stream));
         if (st & ERR_TMA_TIMEOUT) return set_error(ctx, FIPI_ERR_CUDA, "a bulk-copy wait timed out in an FFT pass");
@@ -300,17 +303,51 @@ fipi_status fipi::download_soa(fipi_ctx* ctx, const double* d, double* h, int n)
 extern "C" {
 
 // Particle state in and out through the pinned staging buffer: the host
-// transposes (n x 3 <-> 3 x n) happen there, the copies are asynchronous and
-// each call synchronises once.
-static void to_soa(const double* h, double* s, int n) {
-    for (int i = 0; i < n; ++i)
-        for (int a = 0; a < 3; ++a) s[(size_t)a * n + i] = h[3 * i + a];
-}
-static void from_soa(const double* s, double* h, int n) {
-    for (int i = 0; i < n; ++i)
-        for (int a = 0; a < 3; ++a) h[3 * i + a] = s[(size_t)a * n + i];
-}
+// side is plain copies into and out of it; the AoS (n x 3, the reference's
+// particle[i].p) <-> SoA (3 x n) transposes run on the device and read or
+// write the mapped staging buffer directly (no separate copy); a call
+// synchronises at most once.
+}  // extern "C"
 
+namespace {
+// The whole particle state from the staging buffer (AoS p, f_pp; r, cos theta)
+// into the SoA state arrays; p_old = p (cluster.cpp:88), f_pi = u_old = 0.
+__global__ void k_state_in(const double* __restrict__ stage, int n, int has_fpp, double* p, double* p_old,
+                           double* f_pp, double* r, double* cth, double* f_pi, double* u_old) {
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < 3 * n; j += gridDim.x * blockDim.x) {
+        const int i = j / 3, a = j - 3 * i;
+        const size_t s = (size_t)a * n + i;
+        const double x = stage[j];
+        p[s] = x;
+        p_old[s] = x;
+        f_pp[s] = has_fpp ? stage[3 * (size_t)n + j] : 0.0;
+        f_pi[s] = 0.0;
+        u_old[s] = 0.0;
+        if (j < n) {
+            r[j] = stage[6 * (size_t)n + j];
+            cth[j] = stage[7 * (size_t)n + j];
+        }
+    }
+}
+// SoA arrays (up to three, NULL to skip) into AoS runs of the staging buffer.
+__global__ void k_state_out(const double* __restrict__ a0, const double* __restrict__ a1,
+                            const double* __restrict__ a2, int n, double* stage) {
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < 3 * n; j += gridDim.x * blockDim.x) {
+        const int i = j / 3, a = j - 3 * i;
+        const size_t s = (size_t)a * n + i;
+        if (a0) stage[j] = a0[s];
+        if (a1) stage[3 * (size_t)n + j] = a1[s];
+        if (a2) stage[6 * (size_t)n + j] = a2[s];
+    }
+}
+inline int transpose_blocks(int n) { return (3 * n + 255) / 256 < 1024 ? (3 * n + 255) / 256 : 1024; }
+}  // namespace
+
+extern "C" {
+
+// The copies are enqueued on the context stream (nothing is waited for at
+// the end: the next call that reads results synchronises); the caller's
+// arrays are consumed before the call returns.
 fipi_status fipi_set_particles(fipi_ctx* ctx, const double* p, const double* r, const double* cos_theta,
                                const double* f_pp) {
     if (!ctx) return set_error(ctx, FIPI_ERR_BAD_ARG, "ctx is NULL");
@@ -321,28 +358,23 @@ fipi_status fipi_set_particles(fipi_ctx* ctx, const double* p, const double* r, 
     FIPI_CUDA(ctx, cudaStreamSynchronize(ctx->stream));  // the staging buffer is free
     double* pin = ctx->pin;
     const size_t b3 = sizeof(double) * 3 * n, b1 = sizeof(double) * n;
-    to_soa(p, pin, n);
-    FIPI_CUDA(ctx, cudaMemcpyAsync(ctx->pb.p, pin, b3, cudaMemcpyHostToDevice, ctx->stream));
-    FIPI_CUDA(ctx, cudaMemcpyAsync(ctx->pb.p_old, ctx->pb.p, b3, cudaMemcpyDeviceToDevice,
-                                   ctx->stream));  // cluster.cpp:88
-    double* pr = pin + 3 * (size_t)n;
+    std::memcpy(pin, p, b3);
+    if (f_pp) std::memcpy(pin + 3 * (size_t)n, f_pp, b3);
+    double* pr = pin + 6 * (size_t)n;
     double* pc = pr + n;
-    for (int i = 0; i < n; ++i) {
-        pr[i] = r ? r[i] : ctx->P.r_p;
-        pc[i] = cos_theta ? cos_theta[i] : 0.0;
+    if (r) std::memcpy(pr, r, b1);
+    else
+        for (int i = 0; i < n; ++i) pr[i] = ctx->P.r_p;
+    if (cos_theta) std::memcpy(pc, cos_theta, b1);
+    else std::memset(pc, 0, b1);
+    {  // one kernel reads the pinned staging buffer directly (mapped host memory)
+        LaunchScope ls(ctx, "particle state in", 0.0);
+        k_state_in<<<transpose_blocks(n), 256, 0, ctx->stream>>>(ctx->pin_dev, n, f_pp ? 1 : 0, ctx->pb.p,
+                                                                  ctx->pb.p_old, ctx->pb.f_pp, ctx->pb.r,
+                                                                  ctx->pb.cth, ctx->pb.f_pi, ctx->pb.u_old);
     }
-    FIPI_CUDA(ctx, cudaMemcpyAsync(ctx->pb.r, pr, b1, cudaMemcpyHostToDevice, ctx->stream));
-    FIPI_CUDA(ctx, cudaMemcpyAsync(ctx->pb.cth, pc, b1, cudaMemcpyHostToDevice, ctx->stream));
-    if (f_pp) {
-        double* pf = pc + n;
-        to_soa(f_pp, pf, n);
-        FIPI_CUDA(ctx, cudaMemcpyAsync(ctx->pb.f_pp, pf, b3, cudaMemcpyHostToDevice, ctx->stream));
-    } else {
-        FIPI_CUDA(ctx, cudaMemsetAsync(ctx->pb.f_pp, 0, b3, ctx->stream));
-    }
-    FIPI_CUDA(ctx, cudaMemsetAsync(ctx->pb.f_pi, 0, b3, ctx->stream));
-    FIPI_CUDA(ctx, cudaMemsetAsync(ctx->pb.u_old, 0, b3, ctx->stream));
-    return check_status(ctx);
+    FIPI_CUDA(ctx, cudaGetLastError());
+    return FIPI_OK;
 }
 
 fipi_status fipi_get_phase(fipi_ctx* ctx, double* c) {
@@ -364,20 +396,20 @@ fipi_status fipi_get_velocity(fipi_ctx* ctx, double* u) {
 fipi_status fipi_get_particles(fipi_ctx* ctx, double* p, double* f_pp, double* f_pi) {
     if (!ctx) return set_error(ctx, FIPI_ERR_BAD_ARG, "ctx is NULL");
     FIPI_CUDA(ctx, cudaSetDevice(ctx->device));
-    fipi_status st = check_status(ctx);
-    if (st != FIPI_OK) return st;
     const int n = ctx->pb.n;
-    if (n == 0) return FIPI_OK;
+    if (n == 0) return check_status(ctx);
     const size_t b3 = sizeof(double) * 3 * n;
     double* dst[3] = {p, f_pp, f_pi};
     const double* src[3] = {ctx->pb.p, ctx->pb.f_pp, ctx->pb.f_pi};
+    if (p || f_pp || f_pi) {
+        LaunchScope ls(ctx, "particle state out", 0.0);
+        k_state_out<<<transpose_blocks(n), 256, 0, ctx->stream>>>(p ? src[0] : nullptr, f_pp ? src[1] : nullptr,
+                                                                   f_pi ? src[2] : nullptr, n, ctx->pin_dev);
+    }
+    fipi_status st = check_status(ctx);  // the one synchronisation of the call
+    if (st != FIPI_OK) return st;
     for (int k = 0; k < 3; ++k)
-        if (dst[k])
-            FIPI_CUDA(ctx, cudaMemcpyAsync(ctx->pin + 3 * (size_t)n * k, src[k], b3, cudaMemcpyDeviceToHost,
-                                           ctx->stream));
-    FIPI_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    for (int k = 0; k < 3; ++k)
-        if (dst[k]) from_soa(ctx->pin + 3 * (size_t)n * k, dst[k], n);
+        if (dst[k]) std::memcpy(dst[k], ctx->pin + 3 * (size_t)n * k, b3);
     return FIPI_OK;
 }
 

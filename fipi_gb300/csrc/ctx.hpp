@@ -190,6 +190,7 @@ struct fipi_ctx {
     bool use_graphs = true;
     int substep = 0;           // 1 after fipi_step_ch, 2 after fipi_step_stokes
     double* pin = nullptr;     // pinned host staging of the particle state, 12 n doubles
+    double* pin_dev = nullptr; // the same buffer as a device pointer (mapped pinned memory)
     bool have_phase = false;
     int couple_u = 0;          // fluid coupling: uf = u interpolated at the particle
     double brown_kt = 0.0;     // Brownian force strength kT (0: off)

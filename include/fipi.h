@@ -117,7 +117,8 @@ fipi_status fipi_set_velocity(fipi_ctx* ctx, const double* u);
  * p: n_p x 3 positions in [0, L).  r: n_p radii or NULL (= r_p, element.cpp:25).
  * cos_theta: n_p wettabilities or NULL (= 0, the reference's 90 degree form).
  * f_pp: n_p x 3 contact forces of the previous step or NULL (= 0); they are
- * spread at the next step (cluster.cpp:358). */
+ * spread at the next step (cluster.cpp:358).  The arrays are consumed before
+ * the call returns; the upload completes in stream order (nothing waits). */
 fipi_status fipi_set_particles(fipi_ctx* ctx, const double* p, const double* r,
                                const double* cos_theta, const double* f_pp);
 fipi_status fipi_get_phase(fipi_ctx* ctx, double* c);
