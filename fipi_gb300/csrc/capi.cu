@@ -255,11 +255,11 @@ fipi_status fipi::check_status(fipi_ctx* ctx) {
 
 extern "C" {
 
-fipi_status fipi_set_phase(fipi_ctx* ctx, const double* c) {
+static fipi_status set_phase_impl(fipi_ctx* ctx, const double* c, bool dev) {
     if (!ctx || !c) return set_error(ctx, FIPI_ERR_BAD_ARG, "NULL argument");
     FIPI_CUDA(ctx, cudaSetDevice(ctx->device));
     graphs_reset(ctx);
-    fipi_status st = fields_set_phase(ctx, c);
+    fipi_status st = fields_set_phase(ctx, c, dev);
     if (st != FIPI_OK) return st;
     ctx->t = 0;
     // device step counter and ramp(t + 1, 0.2 t_end) for t = 0
@@ -272,13 +272,18 @@ fipi_status fipi_set_phase(fipi_ctx* ctx, const double* c) {
     return check_status(ctx);
 }
 
-fipi_status fipi_set_velocity(fipi_ctx* ctx, const double* u) {
+fipi_status fipi_set_phase(fipi_ctx* ctx, const double* c) { return set_phase_impl(ctx, c, false); }
+fipi_status fipi_set_phase_device(fipi_ctx* ctx, const double* d_c) { return set_phase_impl(ctx, d_c, true); }
+
+static fipi_status set_velocity_impl(fipi_ctx* ctx, const double* u, bool dev) {
     if (!ctx || !u) return set_error(ctx, FIPI_ERR_BAD_ARG, "NULL argument");
     FIPI_CUDA(ctx, cudaSetDevice(ctx->device));
-    fipi_status st = fields_set_velocity(ctx, u);
+    fipi_status st = fields_set_velocity(ctx, u, dev);
     if (st != FIPI_OK) return st;
     return check_status(ctx);
 }
+fipi_status fipi_set_velocity(fipi_ctx* ctx, const double* u) { return set_velocity_impl(ctx, u, false); }
+fipi_status fipi_set_velocity_device(fipi_ctx* ctx, const double* d_u) { return set_velocity_impl(ctx, d_u, true); }
 
 }  // extern "C"
 
@@ -310,34 +315,37 @@ extern "C" {
 }  // extern "C"
 
 namespace {
-// The whole particle state from the staging buffer (AoS p, f_pp; r, cos theta)
-// into the SoA state arrays; p_old = p (cluster.cpp:88), f_pi = u_old = 0.
-__global__ void k_state_in(const double* __restrict__ stage, int n, int has_fpp, double* p, double* p_old,
-                           double* f_pp, double* r, double* cth, double* f_pi, double* u_old) {
+// The whole particle state from AoS sources (p, f_pp: n x 3; r, cos theta:
+// n; NULL f_pp / r / cos theta: 0 / r_default / 0) into the SoA state
+// arrays; p_old = p (cluster.cpp:88), f_pi = u_old = 0.
+__global__ void k_state_in(const double* __restrict__ ap, const double* __restrict__ afpp,
+                           const double* __restrict__ ar, const double* __restrict__ acth, double r_default, int n,
+                           double* p, double* p_old, double* f_pp, double* r, double* cth, double* f_pi,
+                           double* u_old) {
     for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < 3 * n; j += gridDim.x * blockDim.x) {
         const int i = j / 3, a = j - 3 * i;
         const size_t s = (size_t)a * n + i;
-        const double x = stage[j];
+        const double x = ap[j];
         p[s] = x;
         p_old[s] = x;
-        f_pp[s] = has_fpp ? stage[3 * (size_t)n + j] : 0.0;
+        f_pp[s] = afpp ? afpp[j] : 0.0;
         f_pi[s] = 0.0;
         u_old[s] = 0.0;
         if (j < n) {
-            r[j] = stage[6 * (size_t)n + j];
-            cth[j] = stage[7 * (size_t)n + j];
+            r[j] = ar ? ar[j] : r_default;
+            cth[j] = acth ? acth[j] : 0.0;
         }
     }
 }
-// SoA arrays (up to three, NULL to skip) into AoS runs of the staging buffer.
+// SoA arrays into AoS destinations (NULL pairs are skipped).
 __global__ void k_state_out(const double* __restrict__ a0, const double* __restrict__ a1,
-                            const double* __restrict__ a2, int n, double* stage) {
+                            const double* __restrict__ a2, int n, double* o0, double* o1, double* o2) {
     for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < 3 * n; j += gridDim.x * blockDim.x) {
         const int i = j / 3, a = j - 3 * i;
         const size_t s = (size_t)a * n + i;
-        if (a0) stage[j] = a0[s];
-        if (a1) stage[3 * (size_t)n + j] = a1[s];
-        if (a2) stage[6 * (size_t)n + j] = a2[s];
+        if (o0) o0[j] = a0[s];
+        if (o1) o1[j] = a1[s];
+        if (o2) o2[j] = a2[s];
     }
 }
 inline int transpose_blocks(int n) { return (3 * n + 255) / 256 < 1024 ? (3 * n + 255) / 256 : 1024; }
@@ -368,13 +376,31 @@ fipi_status fipi_set_particles(fipi_ctx* ctx, const double* p, const double* r, 
     if (cos_theta) std::memcpy(pc, cos_theta, b1);
     else std::memset(pc, 0, b1);
     {  // one kernel reads the pinned staging buffer directly (mapped host memory)
+        const double* st = ctx->pin_dev;
         LaunchScope ls(ctx, "particle state in", 0.0);
-        k_state_in<<<transpose_blocks(n), 256, 0, ctx->stream>>>(ctx->pin_dev, n, f_pp ? 1 : 0, ctx->pb.p,
-                                                                  ctx->pb.p_old, ctx->pb.f_pp, ctx->pb.r,
-                                                                  ctx->pb.cth, ctx->pb.f_pi, ctx->pb.u_old);
+        k_state_in<<<transpose_blocks(n), 256, 0, ctx->stream>>>(
+            st, f_pp ? st + 3 * (size_t)n : nullptr, st + 6 * (size_t)n, st + 7 * (size_t)n, ctx->P.r_p, n,
+            ctx->pb.p, ctx->pb.p_old, ctx->pb.f_pp, ctx->pb.r, ctx->pb.cth, ctx->pb.f_pi, ctx->pb.u_old);
     }
     FIPI_CUDA(ctx, cudaGetLastError());
     return FIPI_OK;
+}
+
+fipi_status fipi_set_particles_device(fipi_ctx* ctx, const double* d_p, const double* d_r,
+                                      const double* d_cos_theta, const double* d_f_pp) {
+    if (!ctx) return set_error(ctx, FIPI_ERR_BAD_ARG, "ctx is NULL");
+    const int n = ctx->pb.n;
+    if (n == 0) return FIPI_OK;
+    if (!d_p) return set_error(ctx, FIPI_ERR_BAD_ARG, "p is NULL");
+    FIPI_CUDA(ctx, cudaSetDevice(ctx->device));
+    {
+        LaunchScope ls(ctx, "particle state in", 0.0);
+        k_state_in<<<transpose_blocks(n), 256, 0, ctx->stream>>>(d_p, d_f_pp, d_r, d_cos_theta, ctx->P.r_p, n,
+                                                                  ctx->pb.p, ctx->pb.p_old, ctx->pb.f_pp,
+                                                                  ctx->pb.r, ctx->pb.cth, ctx->pb.f_pi,
+                                                                  ctx->pb.u_old);
+    }
+    return check_status(ctx);  // the caller's arrays may be reused on return
 }
 
 fipi_status fipi_get_phase(fipi_ctx* ctx, double* c) {
@@ -402,15 +428,45 @@ fipi_status fipi_get_particles(fipi_ctx* ctx, double* p, double* f_pp, double* f
     double* dst[3] = {p, f_pp, f_pi};
     const double* src[3] = {ctx->pb.p, ctx->pb.f_pp, ctx->pb.f_pi};
     if (p || f_pp || f_pi) {
+        double* st = ctx->pin_dev;
         LaunchScope ls(ctx, "particle state out", 0.0);
-        k_state_out<<<transpose_blocks(n), 256, 0, ctx->stream>>>(p ? src[0] : nullptr, f_pp ? src[1] : nullptr,
-                                                                   f_pi ? src[2] : nullptr, n, ctx->pin_dev);
+        k_state_out<<<transpose_blocks(n), 256, 0, ctx->stream>>>(
+            src[0], src[1], src[2], n, p ? st : nullptr, f_pp ? st + 3 * (size_t)n : nullptr,
+            f_pi ? st + 6 * (size_t)n : nullptr);
     }
     fipi_status st = check_status(ctx);  // the one synchronisation of the call
     if (st != FIPI_OK) return st;
     for (int k = 0; k < 3; ++k)
         if (dst[k]) std::memcpy(dst[k], ctx->pin + 3 * (size_t)n * k, b3);
     return FIPI_OK;
+}
+
+fipi_status fipi_get_particles_device(fipi_ctx* ctx, double* d_p, double* d_f_pp, double* d_f_pi) {
+    if (!ctx) return set_error(ctx, FIPI_ERR_BAD_ARG, "ctx is NULL");
+    FIPI_CUDA(ctx, cudaSetDevice(ctx->device));
+    const int n = ctx->pb.n;
+    if (n > 0 && (d_p || d_f_pp || d_f_pi)) {
+        LaunchScope ls(ctx, "particle state out", 0.0);
+        k_state_out<<<transpose_blocks(n), 256, 0, ctx->stream>>>(ctx->pb.p, ctx->pb.f_pp, ctx->pb.f_pi, n, d_p,
+                                                                   d_f_pp, d_f_pi);
+    }
+    return check_status(ctx);
+}
+
+fipi_status fipi_get_phase_device(fipi_ctx* ctx, double* d_c) {
+    if (!ctx || !d_c) return set_error(ctx, FIPI_ERR_BAD_ARG, "NULL argument");
+    FIPI_CUDA(ctx, cudaSetDevice(ctx->device));
+    fipi_status st = fields_get_phase(ctx, d_c, true);
+    if (st != FIPI_OK) return st;
+    return check_status(ctx);
+}
+
+fipi_status fipi_get_velocity_device(fipi_ctx* ctx, double* d_u) {
+    if (!ctx || !d_u) return set_error(ctx, FIPI_ERR_BAD_ARG, "NULL argument");
+    FIPI_CUDA(ctx, cudaSetDevice(ctx->device));
+    fipi_status st = fields_get_velocity(ctx, d_u, true);
+    if (st != FIPI_OK) return st;
+    return check_status(ctx);
 }
 
 fipi_status fipi_get_time(const fipi_ctx* ctx, int* t) {

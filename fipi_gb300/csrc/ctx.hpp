@@ -213,10 +213,11 @@ namespace fipi {
 fipi_status fields_alloc(fipi_ctx* ctx);
 void fields_free(fipi_ctx* ctx);
 // Set c^0 (host doubles) and derive c_hat, f_hat, grad c (t = 0 state).
-fipi_status fields_set_phase(fipi_ctx* ctx, const double* c_host);
-fipi_status fields_set_velocity(fipi_ctx* ctx, const double* u_host);
-fipi_status fields_get_phase(fipi_ctx* ctx, double* c_host);
-fipi_status fields_get_velocity(fipi_ctx* ctx, double* u_host);
+// State I/O from / to host memory, or with `dev` device memory (no host copy).
+fipi_status fields_set_phase(fipi_ctx* ctx, const double* c, bool dev = false);
+fipi_status fields_set_velocity(fipi_ctx* ctx, const double* u, bool dev = false);
+fipi_status fields_get_phase(fipi_ctx* ctx, double* c, bool dev = false);
+fipi_status fields_get_velocity(fipi_ctx* ctx, double* u, bool dev = false);
 // The three grid sub-steps of one iteration (enqueue only).
 void fields_step_ch(fipi_ctx* ctx, int t);        // conv, CH update, c, f
 void fields_step_stokes(fipi_ctx* ctx);           // mu, grad c, force, projection

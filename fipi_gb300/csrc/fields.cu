@@ -600,16 +600,77 @@ void fields_free(fipi_ctx* ctx) {
 
 
 // t = 0 state: c, c_hat, f_hat, grad c (everything main.cpp:81-92 needs).
-template <typename T> static fipi_status set_phase_t(fipi_ctx* ctx, const double* c_host) {
+// FP64 values into a T field from host memory or, with `dev`, from device
+// memory of the context's device (no host copy).
+template <typename T> static fipi_status load_real(fipi_ctx* ctx, const double* src, T* dst, size_t n, bool dev) {
+    if (!dev) return upload<T>(ctx, src, dst, n);
+    if (sizeof(T) == sizeof(double)) {
+        FIPI_CUDA(ctx, cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+    } else {
+        LaunchScope ls(ctx, "convert", 0.0);
+        k_convert<double, T><<<1024, 256, 0, ctx->stream>>>(src, dst, n);
+    }
+    return FIPI_OK;
+}
+template <typename T> static fipi_status store_real(fipi_ctx* ctx, const T* src, double* dst, size_t n, bool dev) {
+    if (!dev) return download<T>(ctx, src, dst, n);
+    if (sizeof(T) == sizeof(double)) {
+        FIPI_CUDA(ctx, cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+    } else {
+        LaunchScope ls(ctx, "convert", 0.0);
+        k_convert<T, double><<<1024, 256, 0, ctx->stream>>>(src, dst, n);
+    }
+    FIPI_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return FIPI_OK;
+}
+
+// Compensated (Neumaier) FP64 sum of device values in a fixed order:
+// kSumBlocks x 256 strided partial sums, then one thread over the partials.
+constexpr int kSumBlocks = 1024;
+__device__ __forceinline__ void neumaier_add(double& s, double& c, double x) {
+    const double t = s + x;
+    c += (fabs(s) >= fabs(x)) ? (s - t) + x : (x - t) + s;
+    s = t;
+}
+__global__ void k_sum_partials(const double* __restrict__ x, size_t n, double* part) {
+    __shared__ double sh[256];
+    double s = 0.0, c = 0.0;
+    for (size_t i = (size_t)blockIdx.x * 256 + threadIdx.x; i < n; i += (size_t)kSumBlocks * 256) neumaier_add(s, c, x[i]);
+    sh[threadIdx.x] = s + c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double bs = 0.0, bc = 0.0;
+        for (int k = 0; k < 256; ++k) neumaier_add(bs, bc, sh[k]);
+        part[blockIdx.x] = bs + bc;
+    }
+}
+// k0 = {sum, sum, 0, 0}: the mixed form's FP64 k = 0 record of a new phase field
+__global__ void k_sum_k0(const double* __restrict__ part, double* k0) {
+    double s = 0.0, c = 0.0;
+    for (int k = 0; k < kSumBlocks; ++k) neumaier_add(s, c, part[k]);
+    k0[0] = k0[1] = s + c;
+    k0[2] = k0[3] = 0.0;
+}
+
+template <typename T> static fipi_status set_phase_t(fipi_ctx* ctx, const double* c_src, bool dev) {
     const Geom& g = ctx->g;
     const bool mixed = ctx->prec == FIPI_MIXED;
-    fipi_status st = upload<T>(ctx, c_host, (T*)ctx->fb.c, (size_t)g.V);
+    fipi_status st = load_real<T>(ctx, c_src, (T*)ctx->fb.c, (size_t)g.V, dev);
     if (st != FIPI_OK) return st;
-    if (mixed) {
+    if (mixed && dev) {
+        double* part = nullptr;
+        FIPI_CUDA(ctx, cudaMallocAsync((void**)&part, sizeof(double) * kSumBlocks, ctx->stream));
+        {
+            LaunchScope ls(ctx, "phase sum", 0.0);
+            k_sum_partials<<<kSumBlocks, 256, 0, ctx->stream>>>(c_src, (size_t)g.V, part);
+            k_sum_k0<<<1, 1, 0, ctx->stream>>>(part, ctx->k0);
+        }
+        FIPI_CUDA(ctx, cudaFreeAsync(part, ctx->stream));
+    } else if (mixed) {
         // FP64 k = 0 mode: sum of c (Neumaier)
         double s = 0.0, comp = 0.0;
         for (long long i = 0; i < g.V; ++i) {
-            const double x = c_host[i];
+            const double x = c_src[i];
             const double t = s + x;
             comp += (fabs(s) >= fabs(x)) ? (s - t) + x : (x - t) + s;
             s = t;
@@ -630,18 +691,18 @@ template <typename T> static fipi_status set_phase_t(fipi_ctx* ctx, const double
     return FIPI_OK;
 }
 
-fipi_status fields_set_phase(fipi_ctx* ctx, const double* c_host) {
-    return ctx->prec == FIPI_MIXED ? set_phase_t<float>(ctx, c_host) : set_phase_t<double>(ctx, c_host);
+fipi_status fields_set_phase(fipi_ctx* ctx, const double* c, bool dev) {
+    return ctx->prec == FIPI_MIXED ? set_phase_t<float>(ctx, c, dev) : set_phase_t<double>(ctx, c, dev);
 }
 
 // The velocity state is upre = Z^-1 u_hat (the first pass of the inverse
 // transform u = C2R(u_hat), which is what the next step starts from);
 // u_hat itself is not kept.  set_velocity: u_hat = R2C(u), then Z^-1.
-template <typename T> static fipi_status set_velocity_t(fipi_ctx* ctx, const double* u_host) {
+template <typename T> static fipi_status set_velocity_t(fipi_ctx* ctx, const double* u_src, bool dev) {
     const Geom& g = ctx->g;
     for (int d = 0; d < 3; ++d) {
         T* tmp = (T*)ctx->fb.ureal + (size_t)d * g.V;
-        fipi_status st = upload<T>(ctx, u_host + (size_t)d * g.V, tmp, (size_t)g.V);
+        fipi_status st = load_real<T>(ctx, u_src + (size_t)d * g.V, tmp, (size_t)g.V, dev);
         if (st != FIPI_OK) return st;
         OpR2C<T> op{tmp, F<T>::S(ctx, d), g.nx, g.ny};
         launch_x<T, 0, 1, false>(ctx, "X forward", 1, NoAcc<OpR2C<T>>{op});
@@ -659,13 +720,13 @@ template <typename T> static fipi_status set_velocity_t(fipi_ctx* ctx, const dou
     return FIPI_OK;
 }
 
-fipi_status fields_set_velocity(fipi_ctx* ctx, const double* u_host) {
-    return ctx->prec == FIPI_MIXED ? set_velocity_t<float>(ctx, u_host) : set_velocity_t<double>(ctx, u_host);
+fipi_status fields_set_velocity(fipi_ctx* ctx, const double* u, bool dev) {
+    return ctx->prec == FIPI_MIXED ? set_velocity_t<float>(ctx, u, dev) : set_velocity_t<double>(ctx, u, dev);
 }
 
-fipi_status fields_get_phase(fipi_ctx* ctx, double* c_host) {
-    if (ctx->prec == FIPI_MIXED) return download<float>(ctx, (const float*)ctx->fb.c, c_host, (size_t)ctx->g.V);
-    return download<double>(ctx, (const double*)ctx->fb.c, c_host, (size_t)ctx->g.V);
+fipi_status fields_get_phase(fipi_ctx* ctx, double* c, bool dev) {
+    if (ctx->prec == FIPI_MIXED) return store_real<float>(ctx, (const float*)ctx->fb.c, c, (size_t)ctx->g.V, dev);
+    return store_real<double>(ctx, (const double*)ctx->fb.c, c, (size_t)ctx->g.V, dev);
 }
 
 // Real velocity u (3 x V) into fb.ureal from the velocity state.
@@ -684,10 +745,10 @@ void fields_velocity_real(fipi_ctx* ctx) {
     else velocity_real_t<double>(ctx);
 }
 
-template <typename T> static fipi_status get_velocity_t(fipi_ctx* ctx, double* u_host) {
+template <typename T> static fipi_status get_velocity_t(fipi_ctx* ctx, double* u, bool dev) {
     velocity_real_t<T>(ctx);
     FIPI_CUDA(ctx, cudaGetLastError());
-    return download<T>(ctx, (T*)ctx->fb.ureal, u_host, (size_t)ctx->g.V * 3);
+    return store_real<T>(ctx, (T*)ctx->fb.ureal, u, (size_t)ctx->g.V * 3, dev);
 }
 
 fipi_status fields_get_grad(fipi_ctx* ctx, double* g_host) {
@@ -701,8 +762,8 @@ fipi_status fields_get_grad(fipi_ctx* ctx, double* g_host) {
     return FIPI_OK;
 }
 
-fipi_status fields_get_velocity(fipi_ctx* ctx, double* u_host) {
-    return ctx->prec == FIPI_MIXED ? get_velocity_t<float>(ctx, u_host) : get_velocity_t<double>(ctx, u_host);
+fipi_status fields_get_velocity(fipi_ctx* ctx, double* u, bool dev) {
+    return ctx->prec == FIPI_MIXED ? get_velocity_t<float>(ctx, u, dev) : get_velocity_t<double>(ctx, u, dev);
 }
 
 // ------------------------------------------------------------ the step

@@ -62,6 +62,12 @@ _SIGS = {
     "fipi_step_particles": (ctypes.c_int, [_vp]),
     "fipi_wrap": (ctypes.c_int, [_vp, _dp]),
     "fipi_set_fluid_coupling": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "fipi_set_phase_device": (ctypes.c_int, [_vp, _vp]),
+    "fipi_set_velocity_device": (ctypes.c_int, [_vp, _vp]),
+    "fipi_set_particles_device": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp]),
+    "fipi_get_phase_device": (ctypes.c_int, [_vp, _vp]),
+    "fipi_get_velocity_device": (ctypes.c_int, [_vp, _vp]),
+    "fipi_get_particles_device": (ctypes.c_int, [_vp, _vp, _vp, _vp]),
     "fipi_set_brownian": (ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_uint64]),
     "fipi_interpolate2": (ctypes.c_int, [_vp, _dp, ctypes.c_int, _dp, _dp]),
     "fipi_div": (ctypes.c_int, [_vp, _dp, _dp]),
@@ -152,6 +158,22 @@ def _check(code: int):
 
 def _d(a):
     return None if a is None else a.ctypes.data_as(_dp)
+
+
+def _dev(x, n=None):
+    """Device address of an FP64 device array: an int, or an object with
+    data_ptr() (a contiguous float64 torch CUDA tensor); None stays None."""
+    if x is None:
+        return None
+    if hasattr(x, "data_ptr"):
+        if str(getattr(x, "dtype", "torch.float64")) != "torch.float64":
+            raise TypeError("device arrays must be float64")
+        if hasattr(x, "is_contiguous") and not x.is_contiguous():
+            raise ValueError("device arrays must be contiguous")
+        if n is not None and hasattr(x, "numel") and x.numel() != n:
+            raise ValueError(f"expected {n} values, got {x.numel()}")
+        return ctypes.c_void_p(x.data_ptr())
+    return ctypes.c_void_p(int(x))
 
 
 def _i(a):
@@ -321,6 +343,28 @@ class Simulation:
         out = np.empty(self.V)
         _check(self.lib.fipi_div(self.h, _d(_f64(v, 3 * self.V)), _d(out)))
         return out
+
+    # device-pointer variants: no host copies (torch CUDA tensors or raw addresses)
+    def set_phase_device(self, c):
+        _check(self.lib.fipi_set_phase_device(self.h, _dev(c, self.V)))
+
+    def set_velocity_device(self, u):
+        _check(self.lib.fipi_set_velocity_device(self.h, _dev(u, 3 * self.V)))
+
+    def set_particles_device(self, p, r=None, cos_theta=None, f_pp=None):
+        n = self.n
+        _check(self.lib.fipi_set_particles_device(self.h, _dev(p, 3 * n), _dev(r, n), _dev(cos_theta, n),
+                                                  _dev(f_pp, 3 * n)))
+
+    def get_phase_device(self, out):
+        _check(self.lib.fipi_get_phase_device(self.h, _dev(out, self.V)))
+
+    def get_velocity_device(self, out):
+        _check(self.lib.fipi_get_velocity_device(self.h, _dev(out, 3 * self.V)))
+
+    def get_particles_device(self, p=None, f_pp=None, f_pi=None):
+        n = self.n
+        _check(self.lib.fipi_get_particles_device(self.h, _dev(p, 3 * n), _dev(f_pp, 3 * n), _dev(f_pi, 3 * n)))
 
     def set_fluid_coupling(self, on: bool = True):
         """Particles advected with the interpolated fluid velocity (off: the

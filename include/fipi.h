@@ -126,6 +126,17 @@ fipi_status fipi_get_velocity(fipi_ctx* ctx, double* u);
 /* Any output pointer may be NULL.  f_pi is the attachment force of the last
  * stage (element.cpp:75-97). */
 fipi_status fipi_get_particles(fipi_ctx* ctx, double* p, double* f_pp, double* f_pi);
+/* Device-pointer variants (zero host copies): the same FP64 layouts as the
+ * host calls above, in device memory of the context's device (e.g. a torch
+ * CUDA tensor's data pointer).  They return once the arrays have been read
+ * or written (the context stream is synchronised). */
+fipi_status fipi_set_phase_device(fipi_ctx* ctx, const double* d_c);
+fipi_status fipi_set_velocity_device(fipi_ctx* ctx, const double* d_u);
+fipi_status fipi_set_particles_device(fipi_ctx* ctx, const double* d_p, const double* d_r,
+                                      const double* d_cos_theta, const double* d_f_pp);
+fipi_status fipi_get_phase_device(fipi_ctx* ctx, double* d_c);
+fipi_status fipi_get_velocity_device(fipi_ctx* ctx, double* d_u);
+fipi_status fipi_get_particles_device(fipi_ctx* ctx, double* d_p, double* d_f_pp, double* d_f_pi);
 fipi_status fipi_get_time(const fipi_ctx* ctx, int* t);
 
 /* ------------------------------------------------------------------ step */
