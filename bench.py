@@ -16,6 +16,8 @@ Printed JSON line (rank 0):
   error        mixed vs FP64 after `--err-steps` steps from the same state
   roofline     dominant kernel: algorithmic bytes per launch / CUDA-event
                duration against the measured HBM copy bandwidth
+  step_roofline  the whole step: the ideal fused pipeline's 44 field passes
+               and this design's pass traffic, times steps/s, against it
   cpu_baseline the CPU oracle timed on this host on a bounded sample
 
 `--impl reference` times the reference's CPU path (the oracle) instead.
@@ -400,6 +402,20 @@ def run_gpu(args):
                 "share_of_step": dom["ms"] / sum(k["ms"] for k in ks),
                 "top_kernel_overall": top["name"] if top else None}
 
+    # ---- the whole step against the HBM roofline: the ideal fused pipeline
+    # (44 full-grid field passes of V FP32 words per step, one read and one
+    # write per transform) and the pass traffic of this design (the
+    # algorithmic bytes of every grid-pass launch of a step)
+    step_roof = None
+    if ks:
+        per_rep = value / ws
+        ideal = 44 * w.V * 4
+        design = sum(k["bytes"] * k["launches"] for k in ks) / args.kernel_steps
+        step_roof = {"model": "44 field passes x V x 4 B per step", "bytes_per_step": ideal,
+                     "achieved": ideal * per_rep / 1e9, "frac": ideal * per_rep / 1e9 / hbm,
+                     "pass_bytes_per_step": design, "pass_achieved": design * per_rep / 1e9,
+                     "pass_frac": design * per_rep / 1e9 / hbm, "unit": "GB/s", "peak": hbm}
+
     # ---- adjoint / forward (FP64 form)
     adj = None
     if args.adj_steps > 0:
@@ -426,6 +442,7 @@ def run_gpu(args):
             "e2e": {"value": e2e_val, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,
             "roofline": roof,
+            "step_roofline": step_roof,
             "kernels": sorted([{"name": k["name"], "launches": k["launches"], "ms": round(k["ms"], 4),
                                 "gbs": (k["bytes"] * k["launches"] / (k["ms"] / 1e3) / 1e9) if k["ms"] > 0 else None}
                                for k in ks], key=lambda k: -k["ms"]),

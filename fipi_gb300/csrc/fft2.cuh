@@ -1,7 +1,8 @@
 // Shared-memory row FFT with radix-16 register codelets (sm_103a).
 //
 // A row of N = 2^L complex values is transformed by Tn = N/E threads that
-// hold E = min(16, N) values each (8 in FP64).  Stages follow the Stockham autosort
+// hold E = min(EM, N) values each (EM = 16 or 8, chosen per pass: FftPlan,
+// smem_fft2's EM parameter).  Stages follow the Stockham autosort
 // recursion: with p the length of the sub-transforms already done, the
 // group g of a stage of radix R reads x[g + m N/R] (m < R), multiplies by
 // W_{Rp}^{m (g mod p)}, does a DFT-R in registers and writes
@@ -128,8 +129,9 @@ struct IdxColumns {  // element e of column `row` at e*cols + row (column index 
 };
 __host__ __device__ __forceinline__ int padded_len(int n) { return n + (n >> 4); }
 
-// Elements per thread (radix <= 8): keeps the pass kernels near 64
-// registers, so several blocks share an SM.
+// Default elements per thread (radix <= 8): keeps the pass kernels near 64
+// registers, so several blocks share an SM; the FP32 Y and Z passes take 16
+// (YE, zrt_elems).
 template <typename T> struct FftE {
     static constexpr int value = 8;
 };
