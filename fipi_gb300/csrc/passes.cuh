@@ -81,9 +81,16 @@ __device__ __forceinline__ double block_sum(double v) {
     return s;  // valid in thread 0
 }
 
-// Row pitch of the X pass: padded M plus the X_M slot, kept odd.
+// X-pass tiles: rows of M complex pairs with one pad slot per 2^kXPad
+// elements, the X_M slot at the end, an odd pitch (the transposed
+// tile loads and stores walk rows).
+constexpr int kXPad = 4;
+struct IdxX {
+    int pitch;
+    __device__ __forceinline__ int operator()(int row, int e) const { return row * pitch + e + (e >> kXPad); }
+};
 __host__ __device__ inline int xpass_pitch(int M) {
-    const int p = padded_len(M) + 1;
+    const int p = M + (M >> kXPad) + 1;
     return (p & 1) ? p : p + 1;
 }
 
@@ -252,7 +259,7 @@ __global__ void __launch_bounds__(NT, XMinBlocks<T, (NIN > NOUT ? NIN : NOUT), N
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* s = reinterpret_cast<C*>(smem_raw);
     constexpr int H = M + 1;
-    const IdxPadded idx{xpass_pitch(M)};
+    const IdxX idx{xpass_pitch(M)};
     const int z = blockIdx.y, y0 = blockIdx.x * TY;
     const int tid = threadIdx.x;
     constexpr int EM = x_elems<T, NIN, NOUT>;
@@ -352,7 +359,7 @@ __global__ void __launch_bounds__(XStreamShape<T, M>::NT,
     constexpr int H = M + 1;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* s = reinterpret_cast<C*>(smem_raw);
-    const IdxPadded idx{xpass_pitch(M)};
+    const IdxX idx{xpass_pitch(M)};
     const int z = blockIdx.y, y0 = blockIdx.x * TY;
     const int tid = threadIdx.x;
     {
