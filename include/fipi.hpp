@@ -153,6 +153,41 @@ public:
         return v;
     }
 
+    // ---- the three parts of an iteration, the output step, checkpoints
+    void step_ch() { check(fipi_step_ch(ctx_)); }
+    void step_stokes() { check(fipi_step_stokes(ctx_)); }
+    void step_particles() { check(fipi_step_particles(ctx_)); }
+    void write_vtk(int what, const char* path) { check(fipi_write_vtk(ctx_, what, path)); }
+    void checkpoint_reserve(int slots) { check(fipi_checkpoint_reserve(ctx_, slots)); }
+    void checkpoint_save(int slot) { check(fipi_checkpoint_save(ctx_, slot)); }
+    void checkpoint_load(int slot) { check(fipi_checkpoint_load(ctx_, slot)); }
+
+    // ---- reverse mode (FIPI_FP64 contexts): gradient of a trajectory's
+    // final-state functional with respect to its first state
+    void trajectory_forward(int nsteps, int stride = 0) { check(fipi_trajectory_forward(ctx_, nsteps, stride)); }
+    std::vector<double> trajectory_backward_phase(const std::vector<double>& dc_final) {
+        need(dc_final, grid_size());
+        check(fipi_trajectory_backward(ctx_, dc_final.data(), nullptr, nullptr, nullptr));
+        std::vector<double> dc(grid_size());
+        check(fipi_adjoint_get(ctx_, dc.data(), nullptr, nullptr, nullptr));
+        return dc;
+    }
+
+    // ---- particle-model extensions (off by default)
+    void set_fluid_coupling(bool on) { check(fipi_set_fluid_coupling(ctx_, on ? 1 : 0)); }
+    void set_brownian(double kt, uint64_t seed) { check(fipi_set_brownian(ctx_, kt, seed)); }
+
+    // ---- device-pointer state I/O (FP64 device arrays, no host copies)
+    void set_phase_device(const double* d_c) { check(fipi_set_phase_device(ctx_, d_c)); }
+    void get_phase_device(double* d_c) { check(fipi_get_phase_device(ctx_, d_c)); }
+    void set_particles_device(const double* d_p, const double* d_r = nullptr, const double* d_cos_theta = nullptr,
+                              const double* d_f_pp = nullptr) {
+        check(fipi_set_particles_device(ctx_, d_p, d_r, d_cos_theta, d_f_pp));
+    }
+    void get_particles_device(double* d_p, double* d_f_pp = nullptr, double* d_f_pi = nullptr) {
+        check(fipi_get_particles_device(ctx_, d_p, d_f_pp, d_f_pi));
+    }
+
 private:
     static void need(const std::vector<double>& v, size_t n) {
         if (v.size() != n) throw error(FIPI_ERR_BAD_ARG, "array size does not match the grid / particle count");
