@@ -53,6 +53,12 @@ template <class O, class = void> struct HasPre : std::false_type {};
 template <class O> struct HasPre<O, std::void_t<typename O::PreT>> : std::true_type {};
 constexpr int ZU = 2;
 
+// A register round trip (k_zpass_rr) whose mid operation reads one more
+// spectral array declares aux() (that array); its tile is then staged in
+// shared memory with cp.async and handed to rr_mid.
+template <class O, class = void> struct HasAux : std::false_type {};
+template <class O> struct HasAux<O, std::void_t<decltype(std::declval<const O&>().aux())>> : std::true_type {};
+
 // A Z-pass operation whose load() only copies NF spectral arrays declares
 // src(f) (the array of field f); its tiles are then fetched with cp.async.
 template <class O, class = void> struct HasSrc : std::false_type {};
@@ -498,6 +504,16 @@ __global__ void __launch_bounds__(kThreads, 2) k_zpass_rr(Geom g, const cplx<T>*
     const size_t base = (size_t)kx * g.ny + ky;
     const IdxColumns idx{TZ};
     op.prologue();
+    // the mid operation's extra spectral input (op.aux()) is staged with
+    // cp.async behind the exchange tile while the forward transform runs
+    C* sa = s + (size_t)TZ * N;
+    if constexpr (HasAux<Op>::value) {
+        const C* aux = op.aux() + (size_t)kx * g.ny + ky0;
+        for (int e = threadIdx.x; e < TZ * N; e += blockDim.x) {
+            const int cc = e % TZ, z = e / TZ;
+            cp_async<sizeof(C)>(&sa[(size_t)z * TZ + cc], aux + cc + z * zstride);
+        }
+    }
     typename Op::State st[E];
     {
         C v[NF][E];
@@ -511,13 +527,18 @@ __global__ void __launch_bounds__(kThreads, 2) k_zpass_rr(Geom g, const cplx<T>*
         }
 #pragma unroll
         for (int f = 0; f < NF; ++f) smem_fft2<T, DIR, N, true, true, EM>(s, idx, c, t, true, twz, 1, v[f]);
+        if constexpr (HasAux<Op>::value) {
+            cp_async_wait_all();
+            __syncthreads();
+        }
 #pragma unroll
         for (int i = 0; i < E; ++i) {
             const int z = IOF::out_elem(t, i);
             C w[NF];
 #pragma unroll
             for (int f = 0; f < NF; ++f) w[f] = v[f][i];
-            op.rr_mid(kx, ky, z, base + z * zstride, w, st[i]);
+            if constexpr (HasAux<Op>::value) op.rr_mid(kx, ky, z, base + z * zstride, w, sa[(size_t)z * TZ + c], st[i]);
+            else op.rr_mid(kx, ky, z, base + z * zstride, w, st[i]);
         }
     }
 #pragma unroll

@@ -375,10 +375,11 @@ template <typename T> struct ZOpFRt {
     struct State {
         C f, c;
     };
-    __device__ void rr_mid(int, int, int, size_t gi, const C* w, State& st) const {
+    __device__ const C* aux() const { return chat; }
+    __device__ void rr_mid(int, int, int, size_t gi, const C* w, C c_hat, State& st) const {
         fhat_out[gi] = w[0];
         st.f = w[0];
-        st.c = chat[gi];
+        st.c = c_hat;
     }
     __device__ C rr_out(int b, int ix, int iy, int iz, const State& st) const {
         const C c = st.c;

@@ -639,7 +639,7 @@ void launch_zrt(fipi_ctx* ctx, const char* name, int nspec, const Op& op) {
         dispatch_pow2(g.nz, [&](auto NC) {
             constexpr int N = decltype(NC)::value;
             using SHP = ZRtShapeT<T, N, 16, EM>;
-            const size_t smem = (size_t)SHP::TZ * N * sizeof(cplx<T>);
+            const size_t smem = (size_t)(HasAux<Op>::value ? 2 : 1) * SHP::TZ * N * sizeof(cplx<T>);
             dim3 grid(g.h, g.ny / SHP::TZ);
             auto kern = k_zpass_rr<T, NF, NB, DIR, N, 16, Op, EM>;
             static size_t granted = 48 * 1024;
