@@ -90,12 +90,12 @@ template <typename T, bool MIXED> struct OpConv {
         C s;
     };
     static constexpr int emit_after(int f) { return f == 2 ? 0 : -1; }
-    struct Pre {};  // grad c is read in take (measured faster than fetching it ahead)
-    template <int F> __device__ void fetch(int, int, int, Pre&) const {}
-    template <int F, class A> __device__ C take(int z, int y, int n, C v, const Pre&, State& st, A& acc) const {
+    // grad_F c arrives through the staged tile of round F
+    static constexpr bool kStaged = true;
+    template <int F> __device__ const T* staged_src() const { return g[F]; }
+    template <int F, class A> __device__ C take(int z, int y, int n, C v, C gg, State& st, A& acc) const {
         const size_t row = ((size_t)z * ny + y) * nx;
         if (tape_u[0]) reinterpret_cast<C*>(tape_u[F] + row)[n] = v;
-        const C gg = reinterpret_cast<const C*>(g[F] + row)[n];
         if (F == 0) {
             T s0 = T(0), s1 = T(0);
             s0 += v.x * gg.x;
@@ -134,9 +134,9 @@ template <typename T, bool MIXED> struct OpCF {
     // k_xpass_stream
     struct State {};
     static constexpr int emit_after(int f) { return f == 0 ? 0 : -1; }
-    struct Pre {};
-    template <int F> __device__ void fetch(int, int, int, Pre&) const {}
-    template <int F, class A> __device__ C take(int z, int y, int n, C v, const Pre&, State&, A& acc) const {
+    static constexpr bool kStaged = false;
+    template <int F> __device__ const T* staged_src() const { return nullptr; }
+    template <int F, class A> __device__ C take(int z, int y, int n, C v, C, State&, A& acc) const {
         point(z, y, n, &v, acc);
         return v;
     }

@@ -332,8 +332,7 @@ template <int I, int N, class F> __device__ __forceinline__ void static_for(F&& 
 // forward transform starts from the registers, exchanging through the tile
 // of field d (already consumed).  Against k_xpass_acc this drops the point
 // loop's shared-memory round trip and one exchange per field.  The op keeps
-// a State per mode between the rounds; op.fetch<f> requests the round's
-// real-space inputs (Pre) before its transform.
+// a State per mode between the rounds.
 template <typename T, int M> struct XStreamShape {
     static constexpr int TY = x_rows<T, M>;
     static constexpr int E = FftPlan<M, FftE<T>::value>::E;
@@ -355,6 +354,7 @@ __global__ void __launch_bounds__(XStreamShape<T, M>::NT,
     using C = cplx<T>;
     using SH = XStreamShape<T, M>;
     constexpr int TY = SH::TY, E = SH::E, Tn = SH::Tn, NT = SH::NT;
+    constexpr int NF = NIN > NOUT ? NIN : NOUT;
     constexpr int EM = FftE<T>::value;
     constexpr int H = M + 1;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -380,19 +380,34 @@ __global__ void __launch_bounds__(XStreamShape<T, M>::NT,
     const T invV = T(1) / T(g.V);
     T acc = T(0);
     typename Op::State st[E];
+    // a real-space input of each round (op.staged_src<f>()) is copied with
+    // cp.async into a tile behind the spectral tiles while the round's
+    // inverse transform runs
+    C* sr = s + (size_t)NF * TY * xpass_pitch(M);
     static_for<0, NIN>([&](auto FC) {
         constexpr int f = decltype(FC)::value;
-        // the real-space inputs of this round are requested before its transform
-        typename Op::Pre pre[E];
-#pragma unroll
-        for (int i = 0; i < E; ++i) op.template fetch<f>(z, y0 + ty, IO::out_elem(t, i), pre[i]);
+        if constexpr (Op::kStaged) {
+            const C* src = reinterpret_cast<const C*>(op.template staged_src<f>() + ((size_t)z * g.ny + y0) * g.nx);
+            for (int e = tid; e < TY * M; e += NT) {
+                const int r = e / M, n = e - r * M;
+                cp_async<sizeof(C)>(&sr[e], src + (size_t)r * (g.nx / 2) + n);
+            }
+        }
         C v[E];
         smem_fft2<T, +1, M, false, true, EM>(s, idx, f * TY + ty, t, true, twx, 2, v);
+        if constexpr (Op::kStaged) {
+            cp_async_wait_all();
+            __syncthreads();
+        }
 #pragma unroll
-        for (int i = 0; i < E; ++i)
-            v[i] = op.template take<f>(z, y0 + ty, IO::out_elem(t, i), cscale(v[i], invV), pre[i], st[i], acc);
+        for (int i = 0; i < E; ++i) {
+            const int n = IO::out_elem(t, i);
+            const C in2 = Op::kStaged ? sr[ty * M + n] : C{};
+            v[i] = op.template take<f>(z, y0 + ty, n, cscale(v[i], invV), in2, st[i], acc);
+        }
         constexpr int d = Op::emit_after(f);
         if constexpr (d >= 0) smem_fft2<T, -1, M, true, false, EM>(s, idx, d * TY + ty, t, true, twx, 2, v);
+        if constexpr (Op::kStaged) __syncthreads();  // the tile is read before the next copy overwrites it
     });
     if constexpr (REDUCE) {
         const double bs = block_sum((double)acc);
@@ -556,11 +571,12 @@ void launch_xs(fipi_ctx* ctx, const char* name, int nreal, const Op& op, double*
             const size_t smem = (size_t)NF * TY * xpass_pitch(g.m) * sizeof(cplx<T>);
             dim3 grid(g.ny / TY, g.nz);
             if constexpr (XStreamShape<T, M>::NT <= kThreads) {
+                const size_t smem_s = smem + (Op::kStaged ? (size_t)TY * M * sizeof(cplx<T>) : 0);
                 auto kern = k_xpass_stream<T, NIN, NOUT, REDUCE, M, Op>;
                 static size_t granted = 48 * 1024;
-                ensure_smem(kern, smem, granted);
-                kern<<<grid, XStreamShape<T, M>::NT, smem, ctx->stream>>>(g, (const cplx<T>*)ctx->fb.twx, op,
-                                                                          partials);
+                ensure_smem(kern, smem_s, granted);
+                kern<<<grid, XStreamShape<T, M>::NT, smem_s, ctx->stream>>>(g, (const cplx<T>*)ctx->fb.twx, op,
+                                                                            partials);
             } else {  // rows of more than 256 points: one round per field would need > 256 threads
                 auto kern = k_xpass_acc<T, NIN, NOUT, REDUCE, M, Op>;
                 static size_t granted = 48 * 1024;
