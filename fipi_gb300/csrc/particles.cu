@@ -540,8 +540,15 @@ __global__ void __launch_bounds__(32 * kFppRows) k_f_pp_fast(PC pc, const float4
         if (m >= 0) mark_ok = f_pi[m] != 0.0 || f_pi[n + m] != 0.0 || f_pi[2 * n + m] != 0.0;
     }
     const int rowbase = (cj + dj + pc.nc[1]) % pc.nc[1] * pc.nc[0] + (ck + dk + pc.nc[2]) % pc.nc[2] * pc.nc[0] * pc.nc[1];
-    for (int base = beg; base < end; base += 32) {
-        const int s = base + lane;
+    // L lanes per home particle when the cell holds few (L = 1, 2 or 4): the
+    // L lanes take every L-th candidate and their sums meet by shuffles in a
+    // fixed order (deterministic)
+    const int cnt_home = end - beg;
+    const int L = cnt_home <= 8 ? 4 : (cnt_home <= 16 ? 2 : 1);
+    const int P = 32 / L;
+    const int hl = lane / L, sub = lane % L;
+    for (int base = beg; base < end; base += P) {
+        const int s = base + hl;
         const bool active = s < end;
         const float4 h = active ? spos[s] : make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
         const int i = __float_as_int(h.w);
@@ -559,7 +566,7 @@ __global__ void __launch_bounds__(32 * kFppRows) k_f_pp_fast(PC pc, const float4
                 __syncwarp();
                 const int cnt = min(32, qe - q0);
                 if (!active) continue;
-                for (int q = 0; q < cnt; ++q) {
+                for (int q = sub; q < cnt; q += L) {
                     const float4 cd = buf[q];
                     const int j = __float_as_int(cd.w);
                     float dx = hx - cd.x, dy = hy - cd.y, dz = hz - cd.z;
@@ -585,19 +592,27 @@ __global__ void __launch_bounds__(32 * kFppRows) k_f_pp_fast(PC pc, const float4
                 }
             }
         }
-        part[w][0][lane] = ax;
-        part[w][1][lane] = ay;
-        part[w][2][lane] = az;
-        part[w][3][lane] = tau;
+        for (int o = 1; o < L; o <<= 1) {
+            ax += __shfl_xor_sync(0xffffffffu, ax, o);
+            ay += __shfl_xor_sync(0xffffffffu, ay, o);
+            az += __shfl_xor_sync(0xffffffffu, az, o);
+            tau += __shfl_xor_sync(0xffffffffu, tau, o);
+        }
+        if (sub == 0) {
+            part[w][0][hl] = ax;
+            part[w][1][hl] = ay;
+            part[w][2][hl] = az;
+            part[w][3][hl] = tau;
+        }
         __syncthreads();
-        if (w == 0 && active) {
+        if (w == 0 && active && sub == 0) {
             float sx = 0.f, sy = 0.f, sz = 0.f, st = 0.f;
 #pragma unroll
             for (int r = 0; r < kFppRows; ++r) {
-                sx += part[r][0][lane];
-                sy += part[r][1][lane];
-                sz += part[r][2][lane];
-                st += part[r][3][lane];
+                sx += part[r][0][hl];
+                sy += part[r][1][hl];
+                sz += part[r][2][hl];
+                st += part[r][3][hl];
             }
             f_pp[i] = (double)sx;
             f_pp[n + i] = (double)sy;
