@@ -348,7 +348,7 @@ __global__ void k_state_out(const double* __restrict__ a0, const double* __restr
         if (o2) o2[j] = a2[s];
     }
 }
-inline int transpose_blocks(int n) { return (3 * n + 255) / 256 < 1024 ? (3 * n + 255) / 256 : 1024; }
+inline int state_blocks(int n) { return (3 * n + 255) / 256 < 1024 ? (3 * n + 255) / 256 : 1024; }
 }  // namespace
 
 extern "C" {
@@ -378,7 +378,7 @@ fipi_status fipi_set_particles(fipi_ctx* ctx, const double* p, const double* r, 
     {  // one kernel reads the pinned staging buffer directly (mapped host memory)
         const double* st = ctx->pin_dev;
         LaunchScope ls(ctx, "particle state in", 0.0);
-        k_state_in<<<transpose_blocks(n), 256, 0, ctx->stream>>>(
+        k_state_in<<<state_blocks(n), 256, 0, ctx->stream>>>(
             st, f_pp ? st + 3 * (size_t)n : nullptr, st + 6 * (size_t)n, st + 7 * (size_t)n, ctx->P.r_p, n,
             ctx->pb.p, ctx->pb.p_old, ctx->pb.f_pp, ctx->pb.r, ctx->pb.cth, ctx->pb.f_pi, ctx->pb.u_old);
     }
@@ -395,7 +395,7 @@ fipi_status fipi_set_particles_device(fipi_ctx* ctx, const double* d_p, const do
     FIPI_CUDA(ctx, cudaSetDevice(ctx->device));
     {
         LaunchScope ls(ctx, "particle state in", 0.0);
-        k_state_in<<<transpose_blocks(n), 256, 0, ctx->stream>>>(d_p, d_f_pp, d_r, d_cos_theta, ctx->P.r_p, n,
+        k_state_in<<<state_blocks(n), 256, 0, ctx->stream>>>(d_p, d_f_pp, d_r, d_cos_theta, ctx->P.r_p, n,
                                                                   ctx->pb.p, ctx->pb.p_old, ctx->pb.f_pp,
                                                                   ctx->pb.r, ctx->pb.cth, ctx->pb.f_pi,
                                                                   ctx->pb.u_old);
@@ -430,7 +430,7 @@ fipi_status fipi_get_particles(fipi_ctx* ctx, double* p, double* f_pp, double* f
     if (p || f_pp || f_pi) {
         double* st = ctx->pin_dev;
         LaunchScope ls(ctx, "particle state out", 0.0);
-        k_state_out<<<transpose_blocks(n), 256, 0, ctx->stream>>>(
+        k_state_out<<<state_blocks(n), 256, 0, ctx->stream>>>(
             src[0], src[1], src[2], n, p ? st : nullptr, f_pp ? st + 3 * (size_t)n : nullptr,
             f_pi ? st + 6 * (size_t)n : nullptr);
     }
@@ -447,7 +447,7 @@ fipi_status fipi_get_particles_device(fipi_ctx* ctx, double* d_p, double* d_f_pp
     const int n = ctx->pb.n;
     if (n > 0 && (d_p || d_f_pp || d_f_pi)) {
         LaunchScope ls(ctx, "particle state out", 0.0);
-        k_state_out<<<transpose_blocks(n), 256, 0, ctx->stream>>>(ctx->pb.p, ctx->pb.f_pp, ctx->pb.f_pi, n, d_p,
+        k_state_out<<<state_blocks(n), 256, 0, ctx->stream>>>(ctx->pb.p, ctx->pb.f_pp, ctx->pb.f_pi, n, d_p,
                                                                    d_f_pp, d_f_pi);
     }
     return check_status(ctx);

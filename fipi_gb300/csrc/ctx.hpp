@@ -232,7 +232,6 @@ fipi_status fields_div(fipi_ctx* ctx, const double* v, double* out);
 // Device pointers of the real fields used by the particle side (T-typed).
 const void* fields_real_c(fipi_ctx* ctx);
 const void* fields_real_grad(fipi_ctx* ctx, int d);
-void* fields_spread_target(fipi_ctx* ctx, int d);
 
 // particles.cu
 fipi_status particles_alloc(fipi_ctx* ctx);

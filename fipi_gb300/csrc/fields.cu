@@ -1012,6 +1012,5 @@ fipi_status fields_div(fipi_ctx* ctx, const double* v, double* out) {
 
 const void* fields_real_c(fipi_ctx* ctx) { return ctx->fb.c; }
 const void* fields_real_grad(fipi_ctx* ctx, int d) { return ctx->fb.g[d]; }
-void* fields_spread_target(fipi_ctx* ctx, int d) { return ctx->fb.fsp[d]; }
 
 }  // namespace fipi
