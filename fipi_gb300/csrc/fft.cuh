@@ -316,9 +316,9 @@ template <typename T, int N, int COLS, int EM = FftE<T>::value> struct ZRtShape 
 };
 
 // The tile is COLS columns (a 128-byte run of ky per kz for FP32 and FP64)
-// of all kz; the column FFTs run in rounds of RC columns, while loads, the
-// mid operation and stores walk the tile with ky fastest (full runs per
-// warp).  Tiles whose load() only copies arrays (src()) arrive by cp.async.
+// of all kz; the column FFTs run in rounds of RC columns, while loads and
+// the mid operation walk the tile with ky fastest (full runs per warp).
+// Tiles whose load() only copies arrays (src()) arrive by cp.async.
 template <typename T, int NF, int NB, int DIR, int N, int COLS, class Op, int EM = FftE<T>::value>
 __global__ void __launch_bounds__(kThreads) k_zpass_rt(Geom g, const cplx<T>* __restrict__ twz, Op op) {
     using C = cplx<T>;
@@ -335,6 +335,8 @@ __global__ void __launch_bounds__(kThreads) k_zpass_rt(Geom g, const cplx<T>* __
     constexpr size_t fstride = (size_t)N * P;
     op.prologue();
     if constexpr (HasSrc<Op>::value) {
+        // one cp.async group per field: the transform of field f starts once
+        // its own tile has landed, while the later fields are still in flight
 #pragma unroll
         for (int f = 0; f < NF; ++f) {
             const C* src = op.src(f);
@@ -342,8 +344,8 @@ __global__ void __launch_bounds__(kThreads) k_zpass_rt(Geom g, const cplx<T>* __
                 const int c = e % COLS, z = e / COLS;
                 cp_async<sizeof(C)>(&s[f * fstride + z * P + c], src + base + c + z * zstride);
             }
+            cp_async_commit();
         }
-        cp_async_wait_all();
     } else {
         for (int e = tid; e < ELEMS; e += NT) {
             const int c = e % COLS, z = e / COLS;
@@ -352,12 +354,17 @@ __global__ void __launch_bounds__(kThreads) k_zpass_rt(Geom g, const cplx<T>* __
 #pragma unroll
             for (int f = 0; f < NF; ++f) s[f * fstride + z * P + c] = v[f];
         }
+        __syncthreads();
     }
-    __syncthreads();
     const int cl = tid % RC, t = tid / RC;
 #pragma unroll
-    for (int f = 0; f < NF; ++f)
+    for (int f = 0; f < NF; ++f) {
+        if constexpr (HasSrc<Op>::value) {
+            cp_async_wait_pending(NF - 1 - f);
+            __syncthreads();
+        }
         for (int r = 0; r < COLS; r += RC) smem_fft2<T, DIR, N, EM>(s + f * fstride + r, idx, cl, t, true, twz, 1);
+    }
     __syncthreads();
     if constexpr (HasPre<Op>::value) {
         // the mid operation's global reads of ZU modes are issued before any is used
@@ -394,17 +401,18 @@ __global__ void __launch_bounds__(kThreads) k_zpass_rt(Geom g, const cplx<T>* __
         }
     }
     __syncthreads();
+    // the inverse transforms' last stages store from registers: for each
+    // slot a warp writes RC consecutive columns of Tn-strided modes (full
+    // 128-byte runs), field by field while the next field is transformed
+    using IO = FftIO<T, -DIR, N, EM>;
 #pragma unroll
     for (int b = 0; b < NB; ++b)
-        for (int r = 0; r < COLS; r += RC) smem_fft2<T, -DIR, N, EM>(s + b * fstride + r, idx, cl, t, true, twz, 1);
-    __syncthreads();
-    for (int e = tid; e < ELEMS; e += NT) {
-        const int c = e % COLS, z = e / COLS;
-        C v[NB];
+        for (int r = 0; r < COLS; r += RC) {
+            C v[SH::E];
+            smem_fft2<T, -DIR, N, false, true, EM>(s + b * fstride + r, idx, cl, t, true, twz, 1, v);
 #pragma unroll
-        for (int b = 0; b < NB; ++b) v[b] = s[b * fstride + z * P + c];
-        op.store2(kx, ky0 + c, z, base + c + z * zstride, v);
-    }
+            for (int i = 0; i < SH::E; ++i) op.rr_store(b, base + r + cl + (size_t)IO::out_elem(t, i) * zstride, v[i]);
+        }
 }
 
 // Round trip with the column-per-thread-group mapping of k_zpass: the tile

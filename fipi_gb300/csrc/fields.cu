@@ -156,6 +156,17 @@ template <typename T> struct OpForce {
     int nx, ny;
     __device__ const C* in(int f) const { return S[f]; }
     __device__ C* out(int f) const { return const_cast<C*>(S[f]); }
+    // the rows of c and of the spread force are contiguous per tile
+    __device__ void prefetch_rows(int z, int y0, int rows) const {
+        const size_t row = ((size_t)z * ny + y0) * nx;
+        const uint32_t bytes = (uint32_t)((size_t)rows * nx * sizeof(T));
+        auto pf = [&](const T* a) {
+            if ((((uintptr_t)(a + row)) | bytes) % 16 == 0) prefetch_l2_bulk(a + row, bytes);
+        };
+        if (gravity != T(0)) pf(c);
+        if (spread)
+            for (int d = 0; d < 3; ++d) pf(fsp[d]);
+    }
     template <class A> __device__ void point(int z, int y, int n, C* v, A& acc) const {
         point(z, y, n, v, acc, XGlobalRow<T, 4>{{c, fsp[0], fsp[1], fsp[2]}, ((size_t)z * ny + y) * nx});
     }

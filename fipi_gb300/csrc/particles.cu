@@ -1045,26 +1045,27 @@ static void spread_t(fipi_ctx* ctx, const double* p, const double* f_pp, T* cons
 // result is deterministic) and no sort is needed; the touched nodes are
 // then converted to FP32.  The FP64 form keeps the sorted reduction in
 // ascending particle id, bit-identical to the reference.
+//
+// Between steps the accumulators are zero everywhere and the force grids are
+// zero except at the 8n nodes of the previous spread (nodes[]): the atomics
+// kernel first zeroes the grids at its particle's previous nodes, and the
+// store kernel takes each node's sum with an exchange against zero, so the
+// first of a node's duplicate slots writes the grid and the others read 0.
 constexpr double kFxScale = 4294967296.0;  // 2^32
 
-__global__ void k_spread_fx_clear(const unsigned* __restrict__ nodes, int m, size_t V, unsigned long long* acc,
-                                  float* f0, float* f1, float* f2) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= m) return;
-    const unsigned nd = nodes[s];
-    acc[nd] = 0ull;
-    acc[V + nd] = 0ull;
-    acc[2 * V + nd] = 0ull;
-    f0[nd] = 0.f;
-    f1[nd] = 0.f;
-    f2[nd] = 0.f;
-}
-
 __global__ void k_spread_fx(PC pc, const double* __restrict__ p, const double* __restrict__ f_pp, size_t V,
-                            unsigned long long* acc, unsigned* nodes) {
+                            unsigned long long* acc, unsigned* nodes, int clear_prev, float* f0, float* f1,
+                            float* f2) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = pc.n;
     if (i >= n) return;
+    if (clear_prev)
+        for (int c = 0; c < 8; ++c) {
+            const unsigned nd = nodes[8 * i + c];
+            f0[nd] = 0.f;
+            f1[nd] = 0.f;
+            f2[nd] = 0.f;
+        }
     int ix[3];
     double fr[3];
     cell_and_frac(pc, p[i], p[n + i], p[2 * n + i], ix, fr);
@@ -1084,14 +1085,16 @@ __global__ void k_spread_fx(PC pc, const double* __restrict__ p, const double* _
     }
 }
 
-__global__ void k_spread_fx_store(const unsigned* __restrict__ nodes, int m, size_t V,
-                                  const unsigned long long* __restrict__ acc, float* f0, float* f1, float* f2) {
+__global__ void k_spread_fx_store(const unsigned* __restrict__ nodes, int m, size_t V, unsigned long long* acc,
+                                  float* f0, float* f1, float* f2) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= m) return;
     const unsigned nd = nodes[s];
-    f0[nd] = (float)((double)(long long)acc[nd] / kFxScale);
-    f1[nd] = (float)((double)(long long)acc[V + nd] / kFxScale);
-    f2[nd] = (float)((double)(long long)acc[2 * V + nd] / kFxScale);
+    float* fa[3] = {f0, f1, f2};
+    for (int a = 0; a < 3; ++a) {
+        const unsigned long long v = atomicExch(acc + a * V + nd, 0ull);
+        if (v != 0ull) fa[a][nd] = (float)((double)(long long)v / kFxScale);
+    }
 }
 
 static void spread_fx(fipi_ctx* ctx) {
@@ -1102,14 +1105,15 @@ static void spread_fx(fipi_ctx* ctx) {
     float* f0 = (float*)ctx->fb.fsp[0];
     float* f1 = (float*)ctx->fb.fsp[1];
     float* f2 = (float*)ctx->fb.fsp[2];
-    if (b.sp_prev_valid) {
-        LaunchScope ls_(ctx, "spread clear", 0.0);
-        k_spread_fx_clear<<<(m + 255) / 256, 256, 0, ctx->stream>>>(b.sp_prev, m, V, b.sp_acc, f0, f1, f2);
-    } else {
+    if (!b.sp_prev_valid) {
         cudaMemsetAsync(b.sp_acc, 0, sizeof(unsigned long long) * 3 * V, ctx->stream);
         for (int a = 0; a < 3; ++a) cudaMemsetAsync(ctx->fb.fsp[a], 0, sizeof(float) * V, ctx->stream);
     }
-    { LaunchScope ls_(ctx, "spread fixed-point atomics", 0.0); k_spread_fx<<<(n + kPT - 1) / kPT, kPT, 0, ctx->stream>>>(pc, b.p, b.f_pp, V, b.sp_acc, b.sp_prev); }
+    {
+        LaunchScope ls_(ctx, "spread fixed-point atomics", 0.0);
+        k_spread_fx<<<(n + kPT - 1) / kPT, kPT, 0, ctx->stream>>>(pc, b.p, b.f_pp, V, b.sp_acc, b.sp_prev,
+                                                                  b.sp_prev_valid, f0, f1, f2);
+    }
     { LaunchScope ls_(ctx, "spread store", 0.0); k_spread_fx_store<<<(m + 255) / 256, 256, 0, ctx->stream>>>(b.sp_prev, m, V, b.sp_acc, f0, f1, f2); }
     b.sp_prev_valid = 1;
 }

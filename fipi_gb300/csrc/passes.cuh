@@ -250,6 +250,12 @@ template <typename T, int NF, int NT> struct XMinBlocks {
     static constexpr int value = sizeof(T) == 4 ? (NF <= 3 ? 4 : 3) : (NF <= 3 ? 3 : 2);
 };
 
+// op.prefetch_rows(z, y0, rows): L2 prefetches of the real rows the point
+// operation reads, issued by one thread with the tile loads.
+template <class O, class = void> struct HasRowPrefetch : std::false_type {};
+template <class O>
+struct HasRowPrefetch<O, std::void_t<decltype(std::declval<const O&>().prefetch_rows(0, 0, 0))>> : std::true_type {};
+
 template <typename T, int NIN, int NOUT, bool REDUCE, int M, class Op, int NT = kThreads>
 __global__ void __launch_bounds__(NT, XMinBlocks<T, (NIN > NOUT ? NIN : NOUT), NT>::value)
     k_xpass_acc(Geom g, const cplx<T>* __restrict__ twx, Op op, double* partials) {
@@ -271,19 +277,37 @@ __global__ void __launch_bounds__(NT, XMinBlocks<T, (NIN > NOUT ? NIN : NOUT), N
     const int tyl = tid % TY, kx0 = tid / TY;
     const size_t gbase = (size_t)z * H * g.ny + y0 + tyl;
     if constexpr (NIN > 0) {
-        // every element of the tile is requested before any is waited for
+        // every element of the tile is requested before any is waited for,
+        // one cp.async group per field
 #pragma unroll
         for (int f = 0; f < NIN; ++f) {
             const C* src = op.in(f) + gbase;
             for (int kx = kx0; kx < H; kx += KS) cp_async<sizeof(C)>(&s[idx(f * TY + tyl, kx)], src + (size_t)kx * g.ny);
+            cp_async_commit();
         }
-        cp_async_wait_all();
-        __syncthreads();
-        c2r_pre<T, M, NIN * TY, NT>(s, idx, twx, tid);
-        __syncthreads();
-        for (int r0 = 0; r0 < NIN * TY; r0 += rpr) {
-            const int row = r0 + tid / Tn;
-            smem_fft2<T, +1, M, EM>(s, idx, row, tid % Tn, row < NIN * TY, twx, 2);
+        if constexpr (HasRowPrefetch<Op>::value)
+            if (tid == 0) op.prefetch_rows(z, y0, TY);
+        if constexpr (TY % rpr == 0) {
+            // FFT rounds align with fields: field f is pre-processed and
+            // transformed while the later fields are still in flight
+#pragma unroll
+            for (int f = 0; f < NIN; ++f) {
+                cp_async_wait_pending(NIN - 1 - f);
+                __syncthreads();
+                C* sf = s + (size_t)f * TY * idx.pitch;
+                c2r_pre<T, M, TY, NT>(sf, idx, twx, tid);
+                __syncthreads();
+                for (int r0 = 0; r0 < TY; r0 += rpr) smem_fft2<T, +1, M, EM>(sf, idx, r0 + tid / Tn, tid % Tn, true, twx, 2);
+            }
+        } else {
+            cp_async_wait_all();
+            __syncthreads();
+            c2r_pre<T, M, NIN * TY, NT>(s, idx, twx, tid);
+            __syncthreads();
+            for (int r0 = 0; r0 < NIN * TY; r0 += rpr) {
+                const int row = r0 + tid / Tn;
+                smem_fft2<T, +1, M, EM>(s, idx, row, tid % Tn, row < NIN * TY, twx, 2);
+            }
         }
     }
     const T invV = T(1) / T(g.V);
@@ -363,17 +387,15 @@ __global__ void __launch_bounds__(XStreamShape<T, M>::NT,
     const int z = blockIdx.y, y0 = blockIdx.x * TY;
     const int tid = threadIdx.x;
     {
+        // one cp.async group per field; each round waits for its own field
         const int tyl = tid % TY, kx0 = tid / TY;
         const size_t gbase = (size_t)z * H * g.ny + y0 + tyl;
 #pragma unroll
         for (int f = 0; f < NIN; ++f) {
             const C* src = op.in(f) + gbase;
             for (int kx = kx0; kx < H; kx += NT / TY) cp_async<sizeof(C)>(&s[idx(f * TY + tyl, kx)], src + (size_t)kx * g.ny);
+            cp_async_commit();
         }
-        cp_async_wait_all();
-        __syncthreads();
-        c2r_pre<T, M, NIN * TY, NT>(s, idx, twx, tid);
-        __syncthreads();
     }
     const int ty = tid / Tn, t = tid % Tn;
     using IO = FftIO<T, +1, M, EM>;
@@ -386,6 +408,11 @@ __global__ void __launch_bounds__(XStreamShape<T, M>::NT,
     C* sr = s + (size_t)NF * TY * xpass_pitch(M);
     static_for<0, NIN>([&](auto FC) {
         constexpr int f = decltype(FC)::value;
+        C* sf = s + (size_t)f * TY * idx.pitch;
+        cp_async_wait_pending(NIN - 1 - f);
+        __syncthreads();
+        c2r_pre<T, M, TY, NT>(sf, idx, twx, tid);
+        __syncthreads();
         if constexpr (Op::kStaged) {
             const C* src = reinterpret_cast<const C*>(op.template staged_src<f>() + ((size_t)z * g.ny + y0) * g.nx);
             for (int e = tid; e < TY * M; e += NT) {
