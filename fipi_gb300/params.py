@@ -144,6 +144,10 @@ WORKLOADS = {
                     note="32^3 parity case with contact forces active from the first step"),
     "t32_aniso": Workload("t32_aniso", 32, 16, 8, 32.0, 16.0, 8.0, n_p=20, r_p=0.5,
                           t_end=10, steps=3, note="anisotropic 32x16x8 grid"),
+    "t256x": Workload("t256x", 256, 16, 16, 256.0, 16.0, 16.0, n_p=24, r_p=1.0, t_end=10, steps=3,
+                      note="256x16x16: rows of 128 complex pairs along x"),
+    "t512x": Workload("t512x", 512, 16, 16, 512.0, 16.0, 16.0, n_p=40, r_p=1.0, t_end=10, steps=2,
+                      note="512x16x16: rows of 256 complex pairs along x"),
     "t32_2pi": Workload("t32_2pi", 32, 32, 32, 2 * REF_PI, 2 * REF_PI, 2 * REF_PI, n_p=30,
                         r_p=0.06, sigma=0.07, epsilon=0.15, mobility=0.02, mu=1e-3,
                         t_end=10, steps=3, phi_amp=0.1,

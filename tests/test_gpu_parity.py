@@ -12,7 +12,7 @@ from conftest import rel_l2, seeded_state
 
 pytestmark = pytest.mark.gpu
 
-SMALL = ["t16", "t32", "t32_aniso", "t32_2pi"]
+SMALL = ["t16", "t32", "t32_aniso", "t32_2pi", "t256x", "t512x"]
 
 
 def half_spectrum_from_numpy(x, P):
@@ -178,7 +178,7 @@ def test_step_fp64_matches_oracle(fipi, oracle_mod, name):
         assert abs(s.packing_tau() - port.tau()) <= 1e-9 * max(1.0, abs(port.tau()))
 
 
-@pytest.mark.parametrize("name", ["t32", "t32_2pi", "cfg1_64"])
+@pytest.mark.parametrize("name", ["t32", "t32_2pi", "cfg1_64", "t256x"])
 def test_step_mixed_close_to_fp64(fipi, name):
     w = fipi.workload(name)
     P, c, p, r, ct = seeded_state(w, 22)
