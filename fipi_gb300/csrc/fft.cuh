@@ -303,7 +303,9 @@ __global__ void __launch_bounds__(kThreads) k_zpass(Geom g, const cplx<T>* __res
 // Z pass with a round trip: the NF loaded fields are transformed along z
 // in direction DIR; op.mid() maps each mode's NF values to NB values
 // (writing whatever state it owns) that are transformed back in the other
-// direction and handed to op.store2().  It replaces a forward Z pass and the
+// direction and stored output by output with op.rr_store(b, gi, v)
+// (k_zpass_rt; k_zpass_rt_t hands a mode's NB values to op.store2()).  It
+// replaces a forward Z pass and the
 // inverse Z pass that read its output again (one write and one read of
 // every intermediate spectrum less).  COLS ky columns per block (a run of
 // COLS complex values per kz).
