@@ -144,6 +144,9 @@ WORKLOADS = {
                     note="32^3 parity case with contact forces active from the first step"),
     "t32_aniso": Workload("t32_aniso", 32, 16, 8, 32.0, 16.0, 8.0, n_p=20, r_p=0.5,
                           t_end=10, steps=3, note="anisotropic 32x16x8 grid"),
+    "t32_bo": Workload("t32_bo", 32, 32, 32, 32.0, 32.0, 32.0, n_p=40, r_p=1.2, t_end=10, steps=3,
+                       rho2=5e-2, note="32^3 with a density contrast (rho2 != rho1: the buoyancy "
+                                       "is not a constant the projection removes)"),
     "t256x": Workload("t256x", 256, 16, 16, 256.0, 16.0, 16.0, n_p=24, r_p=1.0, t_end=10, steps=3,
                       note="256x16x16: rows of 128 complex pairs along x"),
     "t512x": Workload("t512x", 512, 16, 16, 512.0, 16.0, 16.0, n_p=40, r_p=1.0, t_end=10, steps=2,

@@ -12,7 +12,7 @@ from conftest import rel_l2, seeded_state
 
 pytestmark = pytest.mark.gpu
 
-SMALL = ["t16", "t32", "t32_aniso", "t32_2pi", "t256x", "t512x"]
+SMALL = ["t16", "t32", "t32_aniso", "t32_2pi", "t32_bo", "t256x", "t512x"]
 
 
 def half_spectrum_from_numpy(x, P):

@@ -94,7 +94,7 @@ def _ref_or_skip(oracle_mod):
         pytest.skip("reference sources not present on this host")
 
 
-@pytest.mark.parametrize("name", GOLDEN + ["t256x", "t512x"])
+@pytest.mark.parametrize("name", GOLDEN + ["t256x", "t512x", "t32_bo"])
 def test_oracle_bit_exact_with_live_reference(oracle_mod, name):
     _ref_or_skip(oracle_mod)
     from fipi_gb300.params import workload
