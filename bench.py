@@ -27,6 +27,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -142,13 +143,14 @@ def timed_steps(sim, n, torch):
 
 
 def adjoint_ratio(F, P, c, p, r, ct, device, torch, steps, traj_steps):
-    """FP64 adjoint cost against the FP64 forward step on the same state.
+    """FP64 adjoint cost against the FP64 forward step on the same state,
+    both timed with CUDA events on the library's stream.
 
     adjoint_step: one fipi_adjoint_step (checkpoint load, the step recomputed
-    with its intermediates kept, the reverse pass), host wall time of the
-    synchronous call; forward: CUDA-event time of one plain FP64 step.
-    trajectory: fipi_trajectory_forward + fipi_trajectory_backward over
-    `traj_steps` steps (sqrt(N) checkpoints) against as many plain steps."""
+    with its intermediates kept, the reverse pass); forward: one plain FP64
+    step.  trajectory: fipi_trajectory_forward + fipi_trajectory_backward
+    over `traj_steps` steps (sqrt(N) checkpoints) against as many plain
+    steps."""
     import numpy as np
 
     s = F.Simulation(P, "fp64", device=device)
@@ -161,26 +163,31 @@ def adjoint_ratio(F, P, c, p, r, ct, device, torch, steps, traj_steps):
     s.step(1)
     s.checkpoint_save(1)
     dc = np.random.default_rng(0).standard_normal(s.V)
+    stream = torch.cuda.ExternalStream(s.stream())
+
+    def on_stream(fn):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        s.sync()
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        s.sync()
+        return e0.elapsed_time(e1) / 1e3
+
     times = []
     for _ in range(steps + 1):
         s.checkpoint_load(1)
         s.adjoint_seed(dc)
-        t0 = time.perf_counter()
-        s.adjoint_step(0)
-        times.append(time.perf_counter() - t0)
+        times.append(on_stream(lambda: s.adjoint_step(0)))
     adj = statistics.median(times[1:])
     s.checkpoint_load(0)
-    s.sync()
-    t0 = time.perf_counter()
-    s.trajectory_forward(traj_steps)
-    s.sync()
-    tf = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    s.trajectory_backward(dc)
-    tb = time.perf_counter() - t0
+    tf = on_stream(lambda: s.trajectory_forward(traj_steps))
+    tb = on_stream(lambda: s.trajectory_backward(dc))
     s.close()
     stride = int(np.ceil(np.sqrt(traj_steps)))
-    return {"form": "fp64", "forward_ms": fwd * 1e3, "adjoint_step_ms": adj * 1e3,
+    return {"form": "fp64", "clock": "CUDA events on the library stream (forward and adjoint)",
+            "forward_ms": fwd * 1e3, "adjoint_step_ms": adj * 1e3,
             "adjoint_step_over_forward": adj / fwd,
             "trajectory": {"steps": traj_steps, "stride": stride,
                            "slots": -(-traj_steps // stride) + stride,
@@ -214,44 +221,120 @@ def committed_traffic(kernel, workload):
     return None
 
 
-def cpu_baseline(w, seed, steps=1):
-    """The CPU oracle (C restatement of the reference step) on the same workload."""
-    sys.path.insert(0, str(REPO / "oracle"))
-    import oracle as O
+# FFT threads of the reference's CPU step: fftw_plan_with_nthreads(4)
+# (main.cpp:70 of the reference); everything else there is single-threaded.
+CPU_FFT_THREADS = 4
 
-    threads = os.cpu_count() or 1
-    P, c, p, r, ct = seeded(w, seed)
-    port = O.Port(P, threads=threads)
-    port.set_state(c, p, r, ct)
-    port.step(1)  # t = 0 (IMEX start) as warm-up
+
+class CpuStep:
+    """The reference's CPU step on one workload: the reference itself,
+    compiled in place into oracle/_ref where its sources are present
+    (kind "reference"), else the oracle's C restatement of it (kind
+    "port").  Inputs come from the oracle's restatement of the seeded
+    generators, so nothing here loads the CUDA library."""
+
+    def __init__(self, w, threads=CPU_FFT_THREADS):
+        sys.path.insert(0, str(REPO / "oracle"))
+        import oracle as O
+
+        self.O, self.w, self.threads = O, w, threads
+        self.kind, self.ref = "port", None
+        if O.reference_available() and w.radius_range is None and w.theta_range_deg is None:
+            try:
+                self.ref = O.Ref(w.name)
+                self.kind = "reference"
+            except Exception:
+                self.ref = None
+        if self.ref is None:
+            self.port = O.Port(w.params(), threads=threads)
+
+    def seeded(self, seed):
+        return self.O.seeded_state(self.w, seed)
+
+    def set_state(self, c, p, r, ct):
+        if self.ref is not None:
+            self.ref.init(c, p, r)
+        else:
+            self.port.set_state(c, p, r, ct)
+
+    def step(self, n):
+        st = (self.ref or self.port).step(n)
+        if st != 0:
+            raise RuntimeError(f"CPU step failed with status {st}")
+
+    def state(self):
+        e = self.ref or self.port
+        return e.phase(), e.velocity(), e.particles()[0]
+
+    def describe(self):
+        if self.kind == "reference":
+            return "the reference's own step (compiled in place, FFTW-API shim)"
+        return "C restatement of the reference step (full-complex C2C FFTs as the reference)"
+
+
+def cpu_baseline(w, seed, steps=1):
+    """The reference's CPU step on the same workload and seed, 1 warm-up step
+    (t = 0, the IMEX start) and `steps` timed steps.  Returns the baseline
+    record and the CPU state after those steps (the oracle's end state the
+    GPU forms are compared with)."""
+    eng = CpuStep(w)
+    P, c, p, r, ct = eng.seeded(seed)
+    eng.set_state(c, p, r, ct)
+    eng.step(1)
     t0 = time.perf_counter()
-    port.step(steps)
+    eng.step(steps)
     dt = time.perf_counter() - t0
-    return {"value": steps / dt, "unit": "steps/s", "cores": threads, "kind": "port",
-            "sample": f"{steps} step(s) of the {w.name} workload after 1 warm-up step; C restatement "
-                      f"of the reference (full-complex C2C FFTs as the reference), {threads} OpenMP "
-                      f"threads in the transforms"}
+    rec = {"value": steps / dt, "unit": "steps/s", "cores": eng.threads, "kind": eng.kind,
+           "sample": f"{steps} step(s) of the {w.name} workload after 1 warm-up step; {eng.describe()}; "
+                     f"{eng.threads} threads in the transforms as the reference configures FFTW "
+                     f"(main.cpp:70), the rest single-threaded"}
+    return rec, eng.state(), 1 + steps
+
+
+def error_vs_oracle(F, w, P, c, p, r, ct, device, ref_state, nsteps):
+    """Both GPU forms after `nsteps` steps from the seeded state, against the
+    CPU oracle's state after the same steps: relative L2 of phi, u and
+    positions, and the largest position difference."""
+    import numpy as np
+
+    rc, ru, rp = ref_state
+    L = np.array([P.lx, P.ly, P.lz])
+    out = {"steps": nsteps, "oracle": "CPU step of the reference (bench cpu_baseline leg)"}
+    for prec in ("fp64", "mixed"):
+        with F.Simulation(P, prec, device=device) as s:
+            s.set_phase(c)
+            s.set_particles(p, r, ct)
+            s.step(nsteps)
+            gc, gu, gp = s.get_phase(), s.get_velocity(), s.get_particles()[0]
+        dp = np.abs(gp - rp).reshape(-1, 3)
+        dp = np.minimum(dp, L - dp)
+        out[prec] = {"phi_rel_l2": float(np.linalg.norm(gc - rc) / np.linalg.norm(rc)),
+                     "u_rel_l2": float(np.linalg.norm(gu - ru) / max(np.linalg.norm(ru), 1e-300)),
+                     "pos_rel_l2": float(np.linalg.norm(dp) / np.linalg.norm(rp)),
+                     "pos_max_abs": float(dp.max()) if dp.size else 0.0}
+    return out
 
 
 def run_reference(args):
+    """The reference's CPU path on the host cores (the oracle's C
+    restatement, or the reference compiled in place where its sources are
+    present), on the same workload, seed and metric as the GPU arm.  Loads
+    no part of the CUDA library: the workload table is plain Python and the
+    inputs come from the oracle's restatement of the seeded generators."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return 0
-    import fipi_gb300 as F
+    from fipi_gb300.params import workload
 
-    w = F.workload(args.workload)
+    w = workload(args.workload)
     warm = min(args.warmup, 1)
     steps = max(1, min(args.steps, 2))
-    sys.path.insert(0, str(REPO / "oracle"))
-    import oracle as O
-
-    threads = os.cpu_count() or 1
-    P, c, p, r, ct = seeded(w, 1)
-    port = O.Port(P, threads=threads)
-    port.set_state(c, p, r, ct)
-    port.step(warm)
+    eng = CpuStep(w)
+    P, c, p, r, ct = eng.seeded(1)
+    eng.set_state(c, p, r, ct)
+    eng.step(warm)
     t0 = time.perf_counter()
-    port.step(steps)
+    eng.step(steps)
     dt = time.perf_counter() - t0
     v = steps / dt
     line = {
@@ -259,10 +342,10 @@ def run_reference(args):
         "steps": steps, "warmup": warm, "ms_per_step": 1e3 * dt / steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": w.name, "grid": f"{w.nx}x{w.ny}x{w.nz}", "particles": w.n_p},
-        "cpu_baseline": {"value": v, "unit": "steps/s", "cores": threads, "kind": "port",
-                         "sample": f"{steps} timed step(s) after {warm} warm-up of the {w.name} workload "
-                                   f"(C restatement of the reference step; the reference's own build "
-                                   f"needs its sources, absent on this host)"},
+        "cpu_baseline": {"value": v, "unit": "steps/s", "cores": eng.threads, "kind": eng.kind,
+                         "sample": f"{steps} timed step(s) after {warm} warm-up of the {w.name} workload; "
+                                   f"{eng.describe()}; {eng.threads} threads in the transforms as the "
+                                   f"reference configures FFTW (main.cpp:70), the rest single-threaded"},
         "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -368,6 +451,28 @@ def run_gpu(args):
         s.close()
     a, b = res["mixed"], res["fp64"]
 
+    # ---- the same runs in the mass-conserving mode (fipi_set_mass_conserving)
+    drift_on = {}
+    for prec in ("fp64", "mixed"):
+        with F.Simulation(P, prec, device=local) as s:
+            s.set_phase(c)
+            s.set_particles(p, r, ct)
+            s.set_mass_conserving(True)
+            m0 = s.mass()
+            s.step(args.err_steps)
+            drift_on[prec] = abs(s.mass() - m0) / (np.abs(c).sum() * P.lx * P.ly * P.lz / w.V)
+
+    # ---- the FP64 form against its own roof: the FP64 FMA pipe (measured
+    # here) at the nominal 13 R2C/C2R transforms x 2.5 V log2 V FLOP per step
+    fp64_peak = F.fma_peak(local, fp64=True)
+    fp32_peak = F.fma_peak(local, fp64=False)
+    fp64_flop = 13 * 2.5 * w.V * math.log2(w.V)
+    fp64_roof = {"bound": "fp64 pipe", "model": "13 transforms x 2.5 V log2 V FLOP per step",
+                 "flop_per_step": fp64_flop, "achieved": fp64_flop * fp64_rate / 1e12,
+                 "peak": fp64_peak, "unit": "TFLOP/s", "frac": fp64_flop * fp64_rate / 1e12 / fp64_peak,
+                 "peak_source": "measured here: fipi_fma_peak (FP64 FMA chains on every SM, FMA = 2 FLOP)",
+                 "fp32_fma_peak_tflops": fp32_peak}
+
     def rl2(x, y):
         return float(np.linalg.norm(x - y) / np.linalg.norm(y))
 
@@ -382,6 +487,7 @@ def run_gpu(args):
         "free_energy_rel": abs(a[5] - b[5]) / abs(b[5]),
         "mass_drift_mixed": abs(a[3] - a[4]) / (np.abs(c).sum() * P.lx * P.ly * P.lz / w.V),
         "mass_drift_fp64": abs(b[3] - b[4]) / (np.abs(c).sum() * P.lx * P.ly * P.lz / w.V),
+        "mass_drift_mass_conserving": drift_on,
     }
 
     # ---- roofline of the dominant kernel
@@ -421,9 +527,10 @@ def run_gpu(args):
     if args.adj_steps > 0:
         adj = adjoint_ratio(F, P, c, p, r, ct, local, torch, args.adj_steps, args.traj_steps)
 
-    cpu = None
+    cpu = err_oracle = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(w, seed)
+        cpu, ref_state, nref = cpu_baseline(w, seed)
+        err_oracle = error_vs_oracle(F, w, P, c, p, r, ct, local, ref_state, nref)
 
     if rank == 0:
         line = {
@@ -435,8 +542,10 @@ def run_gpu(args):
                        "form": "mixed", "parallelism": f"replicas x{ws}",
                        "l2": "working set > L2 (inputs larger than L2; no flush needed)"},
             "particle_updates_per_s": value * w.n_p,
-            "fp64": {"steps_per_s": fp64_rate * ws, "mixed_over_fp64": value / (fp64_rate * ws)},
+            "fp64": {"steps_per_s": fp64_rate * ws, "mixed_over_fp64": value / (fp64_rate * ws),
+                     "roofline": fp64_roof},
             "error_mixed_vs_fp64": err,
+            "error_vs_oracle": err_oracle,
             "adjoint_over_forward": adj["adjoint_step_over_forward"] if adj else None,
             "adjoint": adj,
             "e2e": {"value": e2e_val, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},

@@ -10,6 +10,7 @@ from .lib import (  # noqa: F401
     Simulation,
     cell_geometry,
     declared_symbols,
+    fma_peak,
     load,
     reference_initial_state,
     reference_params,
@@ -22,6 +23,6 @@ from .lib import (  # noqa: F401
 
 __all__ = [
     "FipiParams", "Workload", "WORKLOADS", "workload", "reference_head", "FipiError",
-    "Simulation", "cell_geometry", "declared_symbols", "load", "reference_params",
+    "Simulation", "cell_geometry", "declared_symbols", "fma_peak", "load", "reference_params",
     "reference_initial_state", "seed_particles", "seed_phase", "vtk_write_field", "vtk_write_particles", "free_energy_density",
 ]

@@ -26,6 +26,7 @@ UNITS = {
     "particles.cu": ["-fmad=false"],
     "vtk.cu": ["-Xcompiler", "-ffp-contract=off"],
     "initial.cu": ["-Xcompiler", "-ffp-contract=off"],
+    "probe.cu": [],
 }
 
 

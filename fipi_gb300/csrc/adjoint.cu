@@ -54,7 +54,8 @@ template <typename T> struct OpAdjStokes {
     int nx, ny;
     __device__ const C* in(int f) const { return S[f]; }
     __device__ C* out(int f) const { return S[f]; }
-    template <class A> __device__ void point(int z, int y, int n, C* v, A&) const {
+    // acc: <L_mu, mu> (mu = lambda (k^2 c_hat)^ + f is linear in lambda: d mu / d lambda = mu / lambda)
+    template <class A> __device__ void point(int z, int y, int n, C* v, A& acc) const {
         const size_t row = ((size_t)z * ny + y) * nx;
         const C lf[3] = {v[0], v[1], v[2]};
         C gd[3];
@@ -67,6 +68,7 @@ template <typename T> struct OpAdjStokes {
         const C cc = reinterpret_cast<const C*>(c + row)[n];
         const T lmx = lf[0].x * gd[0].x + lf[1].x * gd[1].x + lf[2].x * gd[2].x;
         const T lmy = lf[0].y * gd[0].y + lf[1].y * gd[1].y + lf[2].y * gd[2].y;
+        acc += lmx * m.x + lmy * m.y;
         T lcx = lam_eps * (T(3) * cc.x * cc.x - T(1)) * lmx + bz * lf[2].x;
         T lcy = lam_eps * (T(3) * cc.y * cc.y - T(1)) * lmy + bz * lf[2].y;
         C lg[3];
@@ -104,10 +106,12 @@ template <typename T> struct OpAdjCH {
     int nx, ny;
     __device__ const C* in(int f) const { return S[f]; }
     __device__ C* out(int f) const { return S[f]; }
-    template <class A> __device__ void point(int z, int y, int n, C* v, A&) const {
+    // acc: <lam_f, c^3 - c> (f^n = (lambda/eps^2)(c^3 - c): d f / d lambda = (c^3 - c)/eps^2)
+    template <class A> __device__ void point(int z, int y, int n, C* v, A& acc) const {
         const size_t row = ((size_t)z * ny + y) * nx;
         const C lf = v[0], lC = v[1];
         const C cc = reinterpret_cast<const C*>(c0 + row)[n];
+        acc += lf.x * (cc.x * cc.x * cc.x - cc.x) + lf.y * (cc.y * cc.y * cc.y - cc.y);
         v[0] = mkc<C>(lam_eps * (T(3) * cc.x * cc.x - T(1)) * lf.x, lam_eps * (T(3) * cc.y * cc.y - T(1)) * lf.y);
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
@@ -142,6 +146,7 @@ template <typename T> struct ZOpAdjC {
     KTabs<T> kt;
     StepConsts<T> k;
     int first;
+    int conserve;  // mass-conserving mode: the forward step took C^n(0) = 0
     __device__ const C* src(int f) const { return S[f]; }
     __device__ void load(int, int, int, size_t gi, C* v) const {
 #pragma unroll
@@ -179,11 +184,70 @@ template <typename T> struct ZOpAdjC {
             la_fo[gi] = mkc<C>(a2 * L.x, a2 * L.y);
             la_Co[gi] = mkc<C>(c2 * L.x, c2 * L.y);
         }
+        if (conserve && gi == 0) lC = mkc<C>(T(0), T(0));
         la_c[gi] = lc;
         S[0][gi] = lf;
         S[1][gi] = lC;
+        S[2][gi] = L;  // the cotangent of c_hat^{n+1}, for the parameter cotangents (read before S[2] is reused)
     }
 };
+
+// Cotangents of the mobility and of lambda through the CH update
+// (main.cpp:95-138), c_hat^{n+1} = N / D:
+//   SBDF2: N = 4 c^n - c^{n-1} - 4 dt M k^2 f^n + 2 dt M k^2 f^{n-1} - ...,
+//          D = 3 + 2 dt M lambda k^4
+//          dc/dM = (-4 dt k^2 f^n + 2 dt k^2 f^{n-1} - 2 dt lambda k^4 c^{n+1}) / D
+//          dc/dlambda = -2 dt M k^4 c^{n+1} / D
+//   IMEX (t = 0): N = c^0 - dt M k^2 f^0 - dt C^0, D = 1 + dt M lambda k^4
+//          dc/dM = (-dt k^2 f^0 - dt lambda k^4 c^1) / D,  dc/dlambda = -dt M k^4 c^1 / D
+// With L = R2C of the real cotangent of c^{n+1}, <lambda_c, dc> = (1/V) sum
+// over the full spectrum of Re(conj(L) dc_hat), i.e. over the half spectrum
+// with weight 2 off the kx = 0 and kx = nx/2 planes.  Per-block sums of the
+// two inner products go to part[0][blk] and part[1][blk].
+__global__ void k_adj_param_ch(const cplx<double>* __restrict__ L, const cplx<double>* __restrict__ c1,
+                               const cplx<double>* __restrict__ fn, const cplx<double>* __restrict__ fo,
+                               KTabs<double> kt, StepConsts<double> k, double M, int first, int ny, int h,
+                               size_t SH, double* part) {
+    double sM = 0.0, sL = 0.0;
+    for (size_t gi = (size_t)blockIdx.x * blockDim.x + threadIdx.x; gi < SH; gi += (size_t)gridDim.x * blockDim.x) {
+        const int iy = (int)(gi % ny);
+        const size_t q = gi / ny;
+        const int ix = (int)(q % h), iz = (int)(q / h);
+        const double w = (ix == 0 || ix == k.m) ? 1.0 : 2.0;
+        const double k2 = kt.k2(ix, iy, iz), k4 = k2 * k2;
+        const cplx<double> l = L[gi], c = c1[gi], f = fn[gi];
+        double dMx, dMy, dLx, dLy;
+        if (first) {
+            const double den = 1.0 + k.s2 * k4;
+            dMx = (-k.dt * k2 * f.x - k.dt * k.lam * k4 * c.x) / den;
+            dMy = (-k.dt * k2 * f.y - k.dt * k.lam * k4 * c.y) / den;
+            dLx = -k.dt * M * k4 * c.x / den;
+            dLy = -k.dt * M * k4 * c.y / den;
+        } else {
+            const cplx<double> g = fo[gi];
+            const double den = 3.0 + k.s3 * k4;
+            dMx = (k2 * (-4.0 * k.dt * f.x + 2.0 * k.dt * g.x) - 2.0 * k.dt * k.lam * k4 * c.x) / den;
+            dMy = (k2 * (-4.0 * k.dt * f.y + 2.0 * k.dt * g.y) - 2.0 * k.dt * k.lam * k4 * c.y) / den;
+            dLx = -2.0 * k.dt * M * k4 * c.x / den;
+            dLy = -2.0 * k.dt * M * k4 * c.y / den;
+        }
+        sM += w * (l.x * dMx + l.y * dMy);
+        sL += w * (l.x * dLx + l.y * dLy);
+    }
+    sM = block_sum(sM);
+    sL = block_sum(sL);
+    if (threadIdx.x == 0) {
+        part[blockIdx.x] = sM;
+        part[gridDim.x + blockIdx.x] = sL;
+    }
+}
+
+__global__ void k_param_acc(const double* __restrict__ part, int np, double scale, double* dst) {
+    double s = 0.0;
+    for (int i = threadIdx.x; i < np; i += blockDim.x) s += part[i];
+    s = block_sum(s);
+    if (threadIdx.x == 0) *dst += scale * s;
+}
 
 // la_c += X0 - i k . (X1, X2, X3)
 template <typename T> struct ZOpAdjAcc {
@@ -213,6 +277,11 @@ namespace {
 
 using D = double;
 using CD = cplx<double>;
+
+constexpr int kParamBlocks = 304;  // blocks of the spectral parameter reduction
+
+// Blocks of an FP64 X pass (one partial sum each when it reduces).
+int x_blocks(const Geom& g) { return (g.ny / x_rows_of(sizeof(double), g.m)) * g.nz; }
 
 CD* sp(void* p) { return (CD*)p; }
 
@@ -255,8 +324,13 @@ fipi_status adjoint_alloc(fipi_ctx* ctx) {
         }
         return e;
     };
-    void** specs[] = {&a.la_c, &a.la_co, &a.la_fo, &a.la_Co, &a.AS[0], &a.AS[1], &a.AS[2], &a.AS[3], &a.AS[4]};
+    void** specs[] = {&a.la_c, &a.la_co, &a.la_fo, &a.la_Co, &a.AS[0], &a.AS[1], &a.AS[2], &a.AS[3], &a.AS[4],
+                      &a.tfo};
     for (void** p : specs) FIPI_CUDA(ctx, A(p, sizeof(CD) * SH));
+    // partial sums: one per X-pass block, or two per block of the spectral reduction
+    a.pg_nparts = std::max(x_blocks(g), 2 * kParamBlocks);
+    FIPI_CUDA(ctx, A((void**)&a.pg, sizeof(D) * kParamGrads));
+    FIPI_CUDA(ctx, A((void**)&a.pg_part, sizeof(D) * (size_t)a.pg_nparts));
     FIPI_CUDA(ctx, A((void**)&a.la_u, sizeof(D) * 3 * V));
     FIPI_CUDA(ctx, A((void**)&a.lamF, sizeof(D) * 3 * V));
     FIPI_CUDA(ctx, A((void**)&a.part, sizeof(D) * 4 * V));
@@ -429,11 +503,24 @@ void adjoint_fields(fipi_ctx* ctx, bool first) {
                       P.gravity * (P.rho1 - P.rho2) / 2.0,
                       g.nx,
                       g.ny};
-    launch_x<D, 3, 5, false>(ctx, "adjoint: X Stokes", particles_on(ctx) ? 12 : 8, os);
+    launch_x<D, 3, 5, true>(ctx, "adjoint: X Stokes", particles_on(ctx) ? 12 : 8, os, a.pg_part);
+    // lambda through mu^{n+1}: <L_mu, mu> / lambda
+    param_acc(ctx, a.pg_part, x_blocks(g), P.lambda != 0.0 ? 1.0 / P.lambda : 0.0, a.pg + kPgLambda);
     launch_y<D>(ctx, 5, Sv, Sv, -1);
     ZOpAdjC<D> zc{{S[0], S[1], S[2], S[3], S[4]}, sp(a.la_c), sp(a.la_co), sp(a.la_fo), sp(a.la_Co), kt, k,
-                  first ? 1 : 0};
+                  first ? 1 : 0, ctx->conserve_mass};
     launch_z<D, 5, -1>(ctx, "adjoint: Z forward + CH", 13, zc);
+    {
+        // mobility and lambda through the CH update (c_hat^{n+1} = chat, f^n = fhat_old after the
+        // recomputed step, f^{n-1} taped before it)
+        LaunchScope ls(ctx, "adjoint: CH parameter sums", 4.0 * g.SH * sizeof(CD));
+        k_adj_param_ch<<<kParamBlocks, 256, 0, ctx->stream>>>(S[2], sp(ctx->fb.chat), sp(ctx->fb.fhat_old),
+                                                               sp(a.tfo), kt, k, P.mobility, first ? 1 : 0, g.ny,
+                                                               g.h, (size_t)g.SH, a.pg_part);
+    }
+    const double invV = 1.0 / (double)g.V;
+    param_acc(ctx, a.pg_part, kParamBlocks, invV, a.pg + kPgMobility);
+    param_acc(ctx, a.pg_part + kParamBlocks, kParamBlocks, invV, a.pg + kPgLambda);
     if (particles_on(ctx)) particles_adjoint_spread(ctx);
     // lam_f, lam_C real; la_u; 4 forward transforms into la_c
     ZOpStore<D, 2> zi2{{S[0], S[1]}, {S[0], S[1]}, 0};
@@ -447,7 +534,9 @@ void adjoint_fields(fipi_ctx* ctx, bool first) {
                   k.lam_eps,
                   g.nx,
                   g.ny};
-    launch_x<D, 2, 4, false>(ctx, "adjoint: X CH", 10, oc);
+    launch_x<D, 2, 4, true>(ctx, "adjoint: X CH", 10, oc, a.pg_part);
+    // lambda through f^n = (lambda / eps^2)(c^3 - c): <lam_f, c^3 - c> / eps^2
+    param_acc(ctx, a.pg_part, x_blocks(g), 1.0 / (P.epsilon * P.epsilon), a.pg + kPgLambda);
     launch_y<D>(ctx, 4, Sv, Sv, -1);
     ZOpAdjAcc<D> za{{S[0], S[1], S[2], S[3]}, sp(a.la_c), kt, g.m, g.ny / 2, g.nz / 2};
     launch_z<D, 4, -1>(ctx, "adjoint: Z forward + accumulate", 6, za);
@@ -467,6 +556,9 @@ fipi_status adjoint_step_impl(fipi_ctx* ctx, int slot) {
     // the forward step's intermediates that the reverse pass reads
     FieldBufs& b = ctx->fb;
     FIPI_CUDA(ctx, cudaMemcpyAsync(a.tc0, b.c, sizeof(D) * V, cudaMemcpyDeviceToDevice, ctx->stream));
+    if (n > 0)  // f_hat^{n-1}: the recomputed step overwrites it (the mobility cotangent reads it)
+        FIPI_CUDA(ctx, cudaMemcpyAsync(a.tfo, b.fhat_old, sizeof(CD) * (size_t)g.SH, cudaMemcpyDeviceToDevice,
+                                       ctx->stream));
     for (int d = 0; d < 3; ++d)
         FIPI_CUDA(ctx, cudaMemcpyAsync(a.tg0 + d * V, b.g[d], sizeof(D) * V, cudaMemcpyDeviceToDevice, ctx->stream));
     const bool parts = particles_on(ctx);
@@ -515,6 +607,8 @@ fipi_status adjoint_seed_impl(fipi_ctx* ctx, const double* dc, const double* du,
     }
     void* hist[3] = {a.la_co, a.la_fo, a.la_Co};
     for (void* h : hist) FIPI_CUDA(ctx, cudaMemsetAsync(h, 0, sizeof(CD) * SH, ctx->stream));
+    FIPI_CUDA(ctx, cudaMemsetAsync(a.pg, 0, sizeof(D) * kParamGrads, ctx->stream));
+    if (n > 0) FIPI_CUDA(ctx, cudaMemsetAsync(a.dct, 0, sizeof(D) * n, ctx->stream));
     if (du) FIPI_CUDA(ctx, cudaMemcpyAsync(a.la_u, du, sizeof(D) * 3 * V, cudaMemcpyHostToDevice, ctx->stream));
     else FIPI_CUDA(ctx, cudaMemsetAsync(a.la_u, 0, sizeof(D) * 3 * V, ctx->stream));
     if (n > 0) {
@@ -549,10 +643,15 @@ fipi_status adjoint_ready(fipi_ctx* ctx) {
 
 }  // namespace
 
+void param_acc(fipi_ctx* ctx, const double* part, int np, double scale, double* dst) {
+    LaunchScope ls(ctx, "adjoint: parameter sum", 0.0);
+    k_param_acc<<<1, 256, 0, ctx->stream>>>(part, np, scale, dst);
+}
+
 void adjoint_free(fipi_ctx* ctx) {
     AdjBufs& a = ctx->ad;
     void* all[] = {a.la_c, a.la_co, a.la_fo, a.la_Co, a.AS[0], a.AS[1], a.AS[2], a.AS[3], a.AS[4],
-                   a.la_u, a.lamF, a.part, a.tc0, a.tg0, a.tu, a.tmu};
+                   a.la_u, a.lamF, a.part, a.tc0, a.tg0, a.tu, a.tmu, a.pg, a.pg_part, a.tfo};
     for (void* p : all)
         if (p) cudaFree(p);
     particles_adjoint_free(ctx);
@@ -678,6 +777,31 @@ fipi_status fipi_adjoint_get(fipi_ctx* ctx, double* dc, double* du, double* dp, 
         st = download_soa(ctx, a.la_fpp, df_pp, n);
         if (st != FIPI_OK) return st;
     }
+    return check_status(ctx);
+}
+
+fipi_status fipi_adjoint_get_params(fipi_ctx* ctx, fipi_param_grads* out, double* dcos_theta) {
+    if (!ctx) return set_error(ctx, FIPI_ERR_BAD_ARG, "ctx is NULL");
+    FIPI_CUDA(ctx, cudaSetDevice(ctx->device));
+    fipi_status st = adjoint_ready(ctx);
+    if (st != FIPI_OK) return st;
+    const fipi_params& P = ctx->P;
+    AdjBufs& a = ctx->ad;
+    if (out) {
+        if (P.lambda == 0.0)
+            return set_error(ctx, FIPI_ERR_UNSUPPORTED, "the lambda (and sigma) cotangents need lambda != 0");
+        double pg[kParamGrads];
+        FIPI_CUDA(ctx, d2h(ctx, pg, a.pg, sizeof(pg)));
+        out->mobility = pg[kPgMobility];
+        out->lambda = pg[kPgLambda];
+        out->k_n = pg[kPgKn];
+        out->sigma_attach = pg[kPgSigmaAttach];
+        // lambda = sigma eps 3 / 2 / sqrt 2 (head.hpp:47), k_n = 0.5 sigma (parameter.hpp:18)
+        out->sigma = pg[kPgSigmaAttach] + pg[kPgLambda] * (P.epsilon * 3.0 / 2.0 / std::sqrt(2.0)) +
+                     pg[kPgKn] * 0.5;
+    }
+    const int n = ctx->pb.n;
+    if (dcos_theta && n > 0) FIPI_CUDA(ctx, d2h(ctx, dcos_theta, a.dct, sizeof(D) * (size_t)n));
     return check_status(ctx);
 }
 

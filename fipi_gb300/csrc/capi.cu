@@ -100,9 +100,11 @@ static fipi_status validate(const fipi_params* P, fipi_precision prec) {
     if (P->n_p < 0) return set_error(nullptr, FIPI_ERR_BAD_PARAMS, "n_p < 0");
     if (P->n_p > (1 << 28)) return set_error(nullptr, FIPI_ERR_UNSUPPORTED, "n_p too large");
     if (P->n_p > 0 && P->switch_particle) {
+        if (!(P->r_eq > 0 && P->r_c > 0)) return set_error(nullptr, FIPI_ERR_BAD_PARAMS, "r_eq, r_c must be positive");
         int nc[3];
         double dc[3];
-        fipi_cell_geometry(P, nc, dc);
+        const fipi_status gs = fipi_cell_geometry(P, nc, dc);
+        if (gs != FIPI_OK) return gs;
         if (nc[0] < 3 || nc[1] < 3 || nc[2] < 3)
             return set_error(nullptr, FIPI_ERR_UNSUPPORTED,
                              "the cell grid needs at least 3 cells per axis (L/r_c >= 3); with fewer the "
@@ -152,6 +154,15 @@ fipi_status fipi_params_reference(fipi_params* o) {
 fipi_status fipi_cell_geometry(const fipi_params* P, int n_cell[3], double d_cell[3]) {
     if (!P || !n_cell || !d_cell) return set_error(nullptr, FIPI_ERR_BAD_ARG, "NULL argument");
     const double L[3] = {P->lx, P->ly, P->lz};
+    // the cell counts are converted to int below: r_c must be finite and
+    // positive and every L / r_c within the int range first
+    if (!(P->r_c > 0) || !std::isfinite(P->r_c) || !std::isfinite(P->margin))
+        return set_error(nullptr, FIPI_ERR_BAD_PARAMS, "r_c must be finite and positive (and margin finite)");
+    for (int a = 0; a < 3; ++a) {
+        const double q = std::floor(L[a] / P->r_c + 2 * P->margin / P->r_c);
+        if (!(q >= 0.0 && q <= 1073741824.0))
+            return set_error(nullptr, FIPI_ERR_BAD_PARAMS, "cell count L / r_c outside [0, 2^30]");
+    }
     for (int a = 0; a < 3; ++a) {
         n_cell[a] = (int)std::floor(L[a] / P->r_c + 2 * P->margin / P->r_c);  // cluster.cpp:26-28
         d_cell[a] = n_cell[a] > 0 ? std::fmod(L[a] + 2 * P->margin, P->r_c) / n_cell[a] + P->r_c : 0.0;
@@ -246,8 +257,11 @@ fipi_status fipi::check_status(fipi_ctx* ctx) {
     FIPI_CUDA(ctx, cudaGetLastError());
     if (st) {
         FIPI_CUDA(ctx, cudaMemsetAsync(ctx->status, 0, sizeof(int), ctx->stream));
-        if (st & ERR_TMA_TIMEOUT) return set_error(ctx, FIPI_ERR_CUDA, "a bulk-copy wait timed out in an FFT pass");
+        if (st & ERR_TMA_TIMEOUT) return set_error(ctx, FIPI_ERR_TIMEOUT, "a bulk-copy wait timed out in an FFT pass");
         if (st & ERR_NONFINITE) return set_error(ctx, FIPI_ERR_NONFINITE, "non-finite particle position");
+        if (st & ERR_SPREAD_RANGE)
+            return set_error(ctx, FIPI_ERR_RANGE, "a spread force density left the range of the fixed-point "
+                                                  "accumulators (|sum| >= 2^31 per node)");
         return set_error(ctx, FIPI_ERR_OUT_OF_RANGE, "particle out of sorting range (cluster.cpp:144-163)");
     }
     return FIPI_OK;
@@ -705,6 +719,32 @@ fipi_status fipi_set_brownian(fipi_ctx* ctx, double kt, uint64_t seed) {
     ctx->noise_seed = seed;
     graphs_reset(ctx);
     return particles_ext_alloc(ctx);
+}
+
+fipi_status fipi_set_mass_conserving(fipi_ctx* ctx, int on) {
+    NEED(ctx);
+    if (ctx->substep != 0) return set_error(ctx, FIPI_ERR_STATE, "the mode changes between iterations only");
+    FIPI_CUDA(ctx, cudaSetDevice(ctx->device));
+    FIPI_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->conserve_mass = on ? 1 : 0;
+    graphs_reset(ctx);
+    return FIPI_OK;
+}
+
+fipi_status fipi_set_debug(fipi_ctx* ctx, int what, long long value) {
+    NEED(ctx);
+    FIPI_CUDA(ctx, cudaSetDevice(ctx->device));
+    FIPI_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    switch (what) {
+        case FIPI_DEBUG_FFT_FIRST_WAIT_POLLS:
+            if (value < -1 || value > (1 << 22)) return set_error(ctx, FIPI_ERR_BAD_ARG, "polls must be -1 or in [0, 2^22]");
+            ctx->debug_first_wait = (int)value;
+            break;
+        default:
+            return set_error(ctx, FIPI_ERR_BAD_ARG, "unknown debug setting");
+    }
+    graphs_reset(ctx);
+    return FIPI_OK;
 }
 
 fipi_status fipi_fft_r2c(fipi_ctx* ctx, const double* in, double* out) {

@@ -35,6 +35,7 @@ enum : int {
     ERR_OUT_OF_RANGE = 1,  // particle outside the cell grid (cluster.cpp:144-163)
     ERR_NONFINITE = 2,     // NaN/Inf seen in a particle position
     ERR_TMA_TIMEOUT = 4,   // a bounded wait for a bulk copy gave up
+    ERR_SPREAD_RANGE = 8,  // a fixed-point spread sum left the int64 range
 };
 
 __host__ __device__ __forceinline__ int ilog2i(int n) {

@@ -133,7 +133,17 @@ struct AdjBufs {
     unsigned* rv2 = nullptr;
     double* rw = nullptr;      // 14n: fractions (3) and cotangents (4) of 2n interpolations
     double* rmp = nullptr;     // 1: ramp factor of the reversed step
+    // parameter cotangents, summed from fipi_adjoint_seed over every reversed step
+    double* pg = nullptr;       // kParamGrads doubles: mobility, lambda, k_n, sigma through f_pi
+    double* pg_part = nullptr;  // per-block partial sums of one reduction
+    int pg_nparts = 0;
+    void* tfo = nullptr;        // SH tape: f_hat^{n-1} (the start state's f_hat history)
+    double* dct = nullptr;      // n: cotangent of each particle's cos(theta)
+    double* pp_sig = nullptr;   // n: per-particle terms of the sigma (f_pi) cotangent of one step
+    double* pp_kn = nullptr;    // n: per-particle terms of the k_n cotangent of one step
 };
+// Slots of AdjBufs::pg.
+enum : int { kPgMobility = 0, kPgLambda = 1, kPgKn = 2, kPgSigmaAttach = 3, kParamGrads = 4 };
 
 }  // namespace fipi
 
@@ -193,6 +203,8 @@ struct fipi_ctx {
     double* pin_dev = nullptr; // the same buffer as a device pointer (mapped pinned memory)
     bool have_phase = false;
     int couple_u = 0;          // fluid coupling: uf = u interpolated at the particle
+    int conserve_mass = 0;     // the k = 0 mode of u . grad c taken as 0 (exact mass conservation)
+    int debug_first_wait = -1; // test hook: polls of each Y-pass block's first copy wait (-1: normal)
     double brown_kt = 0.0;     // Brownian force strength kT (0: off)
     uint64_t noise_seed = 0;   // Philox key of the Brownian force
     bool track_tau = true;     // packing energy during the step (cluster.cpp:256-259)
@@ -302,6 +314,8 @@ fipi_status download_soa(fipi_ctx* ctx, const double* d, double* h, int n);
 void graphs_reset(fipi_ctx* ctx);
 // adjoint.cu: frees checkpoint slots and adjoint buffers.
 void adjoint_free(fipi_ctx* ctx);
+// *dst += scale * (sum of part[0..np)), one block in a fixed order (deterministic).
+void param_acc(fipi_ctx* ctx, const double* part, int np, double scale, double* dst);
 
 }  // namespace fipi
 

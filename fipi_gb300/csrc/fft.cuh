@@ -103,9 +103,11 @@ template <typename T> struct YGroups {
     static constexpr int value = 1;
 };
 
+// first_wait: polls of the block's first copy wait (-1: the normal bound);
+// a test hook that lets the bounded-wait error path run (fipi_set_debug).
 template <typename T, int DIR, int N>
 __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 3 : 2) k_ypass_tma(Geom g, const cplx<T>* __restrict__ twy, FieldPtrs<T> fp,
-                                                       int fields, int* status) {
+                                                       int fields, int* status, int first_wait) {
     using C = cplx<T>;
     constexpr int EM = YE<T>::value;
     using IO = FftIO<T, DIR, N, EM>;
@@ -152,7 +154,8 @@ __global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 3 : 2) k_ypass_tma(
         const int f = (int)(tile / tiles_f);
         const long long r0 = (tile - (long long)f * tiles_f) * RB;
         const int rows = (int)min((long long)RB, rows_f - r0);
-        const bool ok = mbar_wait(&bar[b], (parity >> b) & 1u);
+        const int limit = (first_wait >= 0 && tile == blockIdx.x) ? first_wait : kSpinLimit;
+        const bool ok = mbar_wait(&bar[b], (parity >> b) & 1u, limit);
         if (ok) {
             parity ^= 1u << b;
             inflight &= ~(1u << b);

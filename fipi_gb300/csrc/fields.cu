@@ -215,7 +215,8 @@ template <typename T, bool MIXED> struct ZOpCH {
     C* Chat_old;  // in: C^{n-1}; out: C^n
     KTabs<T> kt;
     StepConsts<T> k;
-    int first;  // t == 0
+    int first;     // t == 0
+    int conserve;  // mass-conserving mode: the k = 0 mode of C^n is taken as 0
     __device__ void load(int, int, int, size_t gi, C* v) const { v[0] = conv[gi]; }
     __device__ void store(int ix, int iy, int iz, size_t gi, const C* v) const {
         Pre p;
@@ -235,7 +236,8 @@ template <typename T, bool MIXED> struct ZOpCH {
         }
     }
     // Writes c_hat^{n+1} and C^n at gi and returns c_hat^{n+1}.
-    __device__ C update(int ix, int iy, int iz, size_t gi, const C Cn, const Pre& p) const {
+    __device__ C update(int ix, int iy, int iz, size_t gi, C Cn, const Pre& p) const {
+        if (conserve && gi == 0) Cn = mkc<C>(T(0), T(0));
         const C c = p.c;
         const C f = p.f;
         const T k2 = kt.k2(ix, iy, iz);
@@ -277,10 +279,11 @@ template <typename T, bool MIXED> struct ZOpCH {
 // per-block sums of conv.  k0 = [c0, c0_old, C0_old, C0_cur].
 // All threads of one block call it.
 __device__ __forceinline__ void k0_update_block(double* k0, const double* partials, int np, int first, double dt,
-                                                double invV) {
+                                                double invV, int conserve) {
     double s = 0.0;
     for (int i = threadIdx.x; i < np; i += blockDim.x) s += partials[i];
     s = block_sum(s);
+    if (conserve) s = 0.0;  // mass-conserving mode: C(0) = 0
     if (threadIdx.x == 0) {
         const double c0 = k0[0], c0o = k0[1], C0o = k0[2];
         double nw;
@@ -314,7 +317,8 @@ template <typename T, bool MIXED> struct ZOpCHRt {
     int np;
     double dt, invV;
     __device__ void prologue() const {
-        if (MIXED && blockIdx.x == 0 && blockIdx.y == 0) k0_update_block(k0, partials, np, ch.first, dt, invV);
+        if (MIXED && blockIdx.x == 0 && blockIdx.y == 0)
+            k0_update_block(k0, partials, np, ch.first, dt, invV, ch.conserve);
     }
     __device__ void load(int, int, int, size_t gi, C* v) const { v[0] = ch.conv[gi]; }
     __device__ const C* src(int) const { return ch.conv; }
@@ -797,7 +801,7 @@ template <typename T, bool MIXED> static void step_ch_t(fipi_ctx* ctx, int t) {
     void* s1[1] = {b.S[3]};
     launch_y<T>(ctx, 1, s1, s1, -1);
     ZOpCH<T, MIXED> zc{F<T>::S(ctx, 3), F<T>::sp(b.chat), F<T>::sp(b.chat_old), F<T>::sp(b.fhat),
-                       F<T>::sp(b.fhat_old), F<T>::sp(b.Chat_old), kt, k, t == 0 ? 1 : 0};
+                       F<T>::sp(b.fhat_old), F<T>::sp(b.Chat_old), kt, k, t == 0 ? 1 : 0, ctx->conserve_mass};
     ZOpCHRt<T, MIXED> zcr{zc, F<T>::S(ctx, 0), ctx->k0, ctx->partials, (g.ny / x_rows_of(sizeof(T), g.m)) * g.nz,
                           ctx->P.dt, 1.0 / (double)g.V};
     launch_zrt<T, 1, 1, -1, 16 / (sizeof(T) / 4), true>(ctx, t == 0 ? "Z forward + IMEX update + inverse" : "Z forward + SBDF2 update + inverse",

@@ -1053,9 +1053,16 @@ static void spread_t(fipi_ctx* ctx, const double* p, const double* f_pp, T* cons
 // first of a node's duplicate slots writes the grid and the others read 0.
 constexpr double kFxScale = 4294967296.0;  // 2^32
 
+// Range of the fixed-point sums: a contribution must stay below 2^30 force
+// units per dx^3 (|v| 2^32 < 2^62), and a node's running sum must not wrap
+// the signed 64-bit accumulator (|sum| < 2^31 units).  Either failure sets
+// ERR_SPREAD_RANGE; an out-of-range contribution is left out.  (A running
+// sum that wraps and later returns into range is still reported.)
+constexpr float kFxMaxContribution = 1073741824.0f;  // 2^30
+
 __global__ void k_spread_fx(PC pc, const double* __restrict__ p, const double* __restrict__ f_pp, size_t V,
                             unsigned long long* acc, unsigned* nodes, int clear_prev, float* f0, float* f1,
-                            float* f2) {
+                            float* f2, int* status) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = pc.n;
     if (i >= n) return;
@@ -1080,7 +1087,14 @@ __global__ void k_spread_fx(PC pc, const double* __restrict__ p, const double* _
         nodes[8 * i + c] = node;
         for (int a = 0; a < 3; ++a) {
             const float v = corner_value<float>(f[a], c, o, pp, q);
-            atomicAdd(acc + a * V + node, (unsigned long long)llrint((double)v * kFxScale));
+            if (!(fabsf(v) < kFxMaxContribution)) {  // also NaN
+                atomicOr(status, ERR_SPREAD_RANGE);
+                continue;
+            }
+            const unsigned long long add = (unsigned long long)llrint((double)v * kFxScale);
+            const unsigned long long old = atomicAdd(acc + a * V + node, add);
+            const unsigned long long sum = old + add;
+            if ((~(old ^ add) & (old ^ sum)) >> 63) atomicOr(status, ERR_SPREAD_RANGE);  // signed wrap
         }
     }
 }
@@ -1112,7 +1126,7 @@ static void spread_fx(fipi_ctx* ctx) {
     {
         LaunchScope ls_(ctx, "spread fixed-point atomics", 0.0);
         k_spread_fx<<<(n + kPT - 1) / kPT, kPT, 0, ctx->stream>>>(pc, b.p, b.f_pp, V, b.sp_acc, b.sp_prev,
-                                                                  b.sp_prev_valid, f0, f1, f2);
+                                                                  b.sp_prev_valid, f0, f1, f2, ctx->status);
     }
     { LaunchScope ls_(ctx, "spread store", 0.0); k_spread_fx_store<<<(m + 255) / 256, 256, 0, ctx->stream>>>(b.sp_prev, m, V, b.sp_acc, f0, f1, f2); }
     b.sp_prev_valid = 1;
@@ -1715,17 +1729,21 @@ __device__ __forceinline__ void interp_grad(const PC& pc, double x, double y, do
     g[2] = dd / pc.dz;
 }
 
-// Adjoint of f_pi_of: lf = cotangent of f_pi -> cotangents of phi and grad c.
+// Adjoint of f_pi_of: lf = cotangent of f_pi -> cotangents of phi and grad c,
+// and of the parameters: lct (the particle's cos theta: df_pi/dct = A pi r
+// sigma n) and lsig (sigma through f_pi alone: df_pi/dsigma = -A pi (d - r ct) n).
 __device__ __forceinline__ void f_pi_adj(const PC& pc, double phi, double gx, double gy, double gz, double r, double ct,
-                                         const double lf[3], double* lphi, double lg[3]) {
+                                         const double lf[3], double* lphi, double lg[3], double* lct, double* lsig) {
     const double gn = sqrt(gx * gx + gy * gy + gz * gz);
     *lphi = 0.0;
+    *lct = *lsig = 0.0;
     lg[0] = lg[1] = lg[2] = 0.0;
     if (!(fabs(phi) <= pc.tanh2 && gn != 0.0)) return;
     const double s2e = 1.4142135623730951 * pc.epsilon;
     const double d = 0.5 * log((1.0 + phi) / (1.0 - phi)) * s2e;
     double f_mag = 0.0, dmag = 0.0;
-    if (fabs(d) < r) {
+    const bool on = fabs(d) < r;
+    if (on) {
         f_mag = -pc.A * pc.pi * (d - r * ct) * pc.sigma;
         dmag = -pc.A * pc.pi * pc.sigma * s2e / (1.0 - phi * phi);  // d(d)/d(phi) = sqrt2 eps / (1 - phi^2)
     }
@@ -1733,6 +1751,10 @@ __device__ __forceinline__ void f_pi_adj(const PC& pc, double phi, double gx, do
     const double s = nh[0] * lf[0] + nh[1] * lf[1] + nh[2] * lf[2];
     *lphi = s * dmag;
     for (int a = 0; a < 3; ++a) lg[a] = f_mag / gn * (lf[a] - nh[a] * s);
+    if (on) {
+        *lct = s * pc.A * pc.pi * r * pc.sigma;
+        *lsig = s * (-pc.A * pc.pi * (d - r * ct));
+    }
 }
 
 // Forward recompute of one stage's interpolation (c, grad c) and f_pi.
@@ -1778,7 +1800,8 @@ __global__ void k_adj_stage(PC pc, int stage, const double* __restrict__ p, cons
                             const double* __restrict__ g2, const double* __restrict__ loc,
                             const double* __restrict__ r, const double* __restrict__ cth,
                             const double* lp_end, const double* __restrict__ lfpp_end,
-                            const double* __restrict__ lam_p1_in, double* lamF, double* lamloc, double* lam_p) {
+                            const double* __restrict__ lam_p1_in, double* lamF, double* lamloc, double* lam_p,
+                            double* dct, double* psig) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = pc.n;
     if (i >= n) return;
@@ -1790,8 +1813,10 @@ __global__ void k_adj_stage(PC pc, int stage, const double* __restrict__ p, cons
         lf[a] = kappa * lv[a];
         lamF[a * n + i] = lf[a] + (stage == 2 ? lfpp_end[a * n + i] : 0.0);
     }
-    double lphi, lg[3];
-    f_pi_adj(pc, loc[i], loc[n + i], loc[2 * n + i], loc[3 * n + i], r[i], cth[i], lf, &lphi, lg);
+    double lphi, lg[3], lct, lsig;
+    f_pi_adj(pc, loc[i], loc[n + i], loc[2 * n + i], loc[3 * n + i], r[i], cth[i], lf, &lphi, lg, &lct, &lsig);
+    dct[i] += lct;
+    psig[i] += lsig;
     lamloc[i] = lphi;
     for (int a = 0; a < 3; ++a) lamloc[(1 + a) * n + i] = lg[a];
     const double x = p[i], y = p[n + i], z = p[2 * n + i];
@@ -1814,11 +1839,14 @@ __global__ void k_adj_stage(PC pc, int stage, const double* __restrict__ p, cons
 // forward evaluation (same cells, minimum-image rule of cluster.cpp:225-232
 // and |d| < r_eq test), lam_p[i] += J(d) (lamF[i] - lamF[j]) with
 // J = ramp k_n ((r_eq/|d| - 1) I - r_eq d d^T / |d|^3), which is even in d.
+// With respect to k_n: pkn[i] += lamF[i] . (force on i) / k_n, the force on
+// i being +F(d) when i < j and -F(d) otherwise (f_pp[it] += F, f_pp[id] -= F,
+// cluster.cpp:246-255), F(d) = (r_eq - |d|) ramp k_n d / |d|.
 // Warp per home cell, lane per home particle as in k_f_pp; coincident pairs
 // (random separation in the reference) contribute nothing.
 __global__ void k_f_pp_adj(PC pc, const double* __restrict__ p, const unsigned* __restrict__ ids,
                            const int* __restrict__ off, const double* __restrict__ rmp_p,
-                           const double* __restrict__ lamF, double* lam_p) {
+                           const double* __restrict__ lamF, double* lam_p, double* pkn) {
     const int lane = threadIdx.x & 31;
     const int cell = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int ncells = pc.nc[0] * pc.nc[1] * pc.nc[2];
@@ -1835,6 +1863,7 @@ __global__ void k_f_pp_adj(PC pc, const double* __restrict__ p, const unsigned* 
         const double xi = p[i], yi = p[n + i], zi = p[2 * n + i];
         const double li[3] = {lamF[i], lamF[n + i], lamF[2 * n + i]};
         double acc[3] = {0.0, 0.0, 0.0};
+        double acc_kn = 0.0;
         for (int dk = -1; dk <= 1; ++dk)
             for (int dj = -1; dj <= 1; ++dj)
                 for (int di = -1; di <= 1; ++di) {
@@ -1866,10 +1895,14 @@ __global__ void k_f_pp_adj(PC pc, const double* __restrict__ p, const unsigned* 
                         const double a = pc.r_eq / dn - 1.0;
                         const double b = pc.r_eq / (dn * dn * dn) * (d[0] * dl[0] + d[1] * dl[1] + d[2] * dl[2]);
                         for (int e = 0; e < 3; ++e) acc[e] += sc * (a * dl[e] - b * d[e]);
+                        const double fk = (pc.r_eq - dn) * (*rmp_p) / dn * (d[0] * li[0] + d[1] * li[1] + d[2] * li[2]);
+                        acc_kn += (i < j) ? fk : -fk;
                     }
                 }
-        if (active)
+        if (active) {
             for (int e = 0; e < 3; ++e) lam_p[e * n + i] += acc[e];
+            pkn[i] += acc_kn;
+        }
     }
 }
 
@@ -1954,6 +1987,8 @@ fipi_status particles_adjoint_alloc(fipi_ctx* ctx) {
     const size_t b3 = sizeof(double) * 3 * n;
     double** v3[] = {&a.la_p, &a.la_fpp, &a.tp0, &a.tfpp0, &a.p1, &a.fpi1, &a.fpp1, &a.lamF1, &a.lamF2, &a.lam_p1};
     for (double** q : v3) FIPI_CUDA(ctx, A((void**)q, b3));
+    double** v1[] = {&a.dct, &a.pp_sig, &a.pp_kn};
+    for (double** q : v1) FIPI_CUDA(ctx, A((void**)q, sizeof(double) * n));
     FIPI_CUDA(ctx, A((void**)&a.loc, sizeof(double) * 8 * n));
     FIPI_CUDA(ctx, A((void**)&a.lamloc, sizeof(double) * 8 * n));
     unsigned** r16[] = {&a.rk, &a.rv, &a.rk2, &a.rv2};
@@ -1966,10 +2001,11 @@ fipi_status particles_adjoint_alloc(fipi_ctx* ctx) {
 void particles_adjoint_free(fipi_ctx* ctx) {
     AdjBufs& a = ctx->ad;
     void* all[] = {a.la_p, a.la_fpp, a.tp0, a.tfpp0, a.p1, a.fpi1, a.fpp1, a.lamF1, a.lamF2, a.lam_p1,
-                   a.loc, a.lamloc, a.rk, a.rv, a.rk2, a.rv2, a.rw, a.rmp};
+                   a.loc, a.lamloc, a.rk, a.rv, a.rk2, a.rv2, a.rw, a.rmp, a.dct, a.pp_sig, a.pp_kn};
     for (void* p : all)
         if (p) cudaFree(p);
     a.la_p = a.la_fpp = a.tp0 = a.tfpp0 = a.p1 = a.fpi1 = a.fpp1 = a.lamF1 = a.lamF2 = a.lam_p1 = nullptr;
+    a.dct = a.pp_sig = a.pp_kn = nullptr;
     a.loc = a.lamloc = a.rw = a.rmp = nullptr;
     a.rk = a.rv = a.rk2 = a.rv2 = nullptr;
 }
@@ -1994,13 +2030,18 @@ fipi_status particles_adjoint(fipi_ctx* ctx) {
     { LaunchScope ls_(ctx, "adjoint: advect", 0.0); k_adj_advect1<<<nb, 256, 0, ctx->stream>>>(pc, a.tp0, a.fpi1, a.fpp1, b.r, a.p1); }
     { LaunchScope ls_(ctx, "adjoint: interpolate", 0.0); k_adj_interp<<<nb, 256, 0, ctx->stream>>>(pc, a.p1, c, g0, g1, g2, b.r, b.cth, a.loc + 4 * n, nullptr); }
     // stage 2 reversed at p1
-    { LaunchScope ls_(ctx, "adjoint: stage", 0.0); k_adj_stage<<<nb, 256, 0, ctx->stream>>>(pc, 2, a.p1, c, g0, g1, g2, a.loc + 4 * n, b.r, b.cth, a.la_p, a.la_fpp, nullptr, a.lamF2, a.lamloc + 4 * n, a.lam_p1); }
+    // per-particle terms of this step's sigma (f_pi) and k_n cotangents
+    FIPI_CUDA(ctx, cudaMemsetAsync(a.pp_sig, 0, sizeof(double) * n, ctx->stream));
+    FIPI_CUDA(ctx, cudaMemsetAsync(a.pp_kn, 0, sizeof(double) * n, ctx->stream));
+    { LaunchScope ls_(ctx, "adjoint: stage", 0.0); k_adj_stage<<<nb, 256, 0, ctx->stream>>>(pc, 2, a.p1, c, g0, g1, g2, a.loc + 4 * n, b.r, b.cth, a.la_p, a.la_fpp, nullptr, a.lamF2, a.lamloc + 4 * n, a.lam_p1, a.dct, a.pp_sig); }
     build_cells(ctx, a.p1);
-    { LaunchScope ls_(ctx, "adjoint: contact forces", 0.0); k_f_pp_adj<<<cells_blocks, 256, 0, ctx->stream>>>(pc, a.p1, b.ids, b.cell_off, a.rmp, a.lamF2, a.lam_p1); }
+    { LaunchScope ls_(ctx, "adjoint: contact forces", 0.0); k_f_pp_adj<<<cells_blocks, 256, 0, ctx->stream>>>(pc, a.p1, b.ids, b.cell_off, a.rmp, a.lamF2, a.lam_p1, a.pp_kn); }
     // stage 1 reversed at p^n (la_p becomes the start-state cotangent)
-    { LaunchScope ls_(ctx, "adjoint: stage", 0.0); k_adj_stage<<<nb, 256, 0, ctx->stream>>>(pc, 1, a.tp0, c, g0, g1, g2, a.loc, b.r, b.cth, a.la_p, nullptr, a.lam_p1, a.lamF1, a.lamloc, a.la_p); }
+    { LaunchScope ls_(ctx, "adjoint: stage", 0.0); k_adj_stage<<<nb, 256, 0, ctx->stream>>>(pc, 1, a.tp0, c, g0, g1, g2, a.loc, b.r, b.cth, a.la_p, nullptr, a.lam_p1, a.lamF1, a.lamloc, a.la_p, a.dct, a.pp_sig); }
     build_cells(ctx, a.tp0);
-    { LaunchScope ls_(ctx, "adjoint: contact forces", 0.0); k_f_pp_adj<<<cells_blocks, 256, 0, ctx->stream>>>(pc, a.tp0, b.ids, b.cell_off, a.rmp, a.lamF1, a.la_p); }
+    { LaunchScope ls_(ctx, "adjoint: contact forces", 0.0); k_f_pp_adj<<<cells_blocks, 256, 0, ctx->stream>>>(pc, a.tp0, b.ids, b.cell_off, a.rmp, a.lamF1, a.la_p, a.pp_kn); }
+    param_acc(ctx, a.pp_sig, n, 1.0, a.pg + kPgSigmaAttach);
+    param_acc(ctx, a.pp_kn, n, 1.0, a.pg + kPgKn);
     // interpolation adjoint onto the grid: part = [c, g0, g1, g2] cotangents
     const int m = 16 * n;
     { LaunchScope ls_(ctx, "adjoint: records", 0.0); k_adj_records<<<(2 * n + 255) / 256, 256, 0, ctx->stream>>>(pc, a.tp0, a.p1, a.lamloc, a.rk, a.rv, a.rw); }
@@ -2071,8 +2112,9 @@ extern "C" fipi_status fipi_cells_build_noalloc(const fipi_params* P, const doub
                              "-particle scratch of fipi_cells_build_noalloc");
     int nc[3];
     double dc[3];
-    fipi_cell_geometry(P, nc, dc);
-    if (nc[0] < 1 || nc[1] < 1 || nc[2] < 1 || !(P->r_c > 0))
+    const fipi_status gs = fipi_cell_geometry(P, nc, dc);  // checks r_c and the cell counts' range
+    if (gs != FIPI_OK) return gs;
+    if (nc[0] < 1 || nc[1] < 1 || nc[2] < 1)
         return set_error(nullptr, FIPI_ERR_BAD_PARAMS, "empty cell grid (r_c larger than the box)");
     const long long ncells = (long long)nc[0] * nc[1] * nc[2];
     if (ncells > (1ll << 30)) return set_error(nullptr, FIPI_ERR_UNSUPPORTED, "too many cells");

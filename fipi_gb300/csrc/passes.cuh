@@ -641,7 +641,8 @@ template <typename T> void launch_y(fipi_ctx* ctx, int nf, void* const* in, void
         const long long tiles = ((long long)g.nz * g.h + rb - 1) / rb * nf;
         long long grid = (long long)ctx->num_sms * blocks_per_sm[di];
         if (grid > tiles) grid = tiles;
-        kern<<<(unsigned)grid, kThreads, smem, ctx->stream>>>(g, (const cplx<T>*)ctx->fb.twy, fp, nf, ctx->status);
+        kern<<<(unsigned)grid, kThreads, smem, ctx->stream>>>(g, (const cplx<T>*)ctx->fb.twy, fp, nf, ctx->status,
+                                                              ctx->debug_first_wait);
     });
 }
 

@@ -23,11 +23,22 @@ _vp = ctypes.c_void_p
 
 FIPI_FP64 = 0
 FIPI_MIXED = 1
+FIPI_DEBUG_FFT_FIRST_WAIT_POLLS = 1
 STATUS = {
     0: "FIPI_OK", 1: "FIPI_ERR_BAD_PARAMS", 2: "FIPI_ERR_BAD_ARG", 3: "FIPI_ERR_CUDA",
     4: "FIPI_ERR_OUT_OF_RANGE", 5: "FIPI_ERR_NONFINITE", 6: "FIPI_ERR_NO_DEVICE",
-    7: "FIPI_ERR_STATE", 8: "FIPI_ERR_UNSUPPORTED",
+    7: "FIPI_ERR_STATE", 8: "FIPI_ERR_UNSUPPORTED", 9: "FIPI_ERR_RANGE", 10: "FIPI_ERR_TIMEOUT",
 }
+
+
+class ParamGrads(ctypes.Structure):
+    """ctypes image of `struct fipi_param_grads` (include/fipi.h)."""
+
+    _fields_ = [("mobility", ctypes.c_double), ("sigma", ctypes.c_double), ("lambda_", ctypes.c_double),
+                ("k_n", ctypes.c_double), ("sigma_attach", ctypes.c_double)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class FipiError(RuntimeError):
@@ -69,6 +80,8 @@ _SIGS = {
     "fipi_get_velocity_device": (ctypes.c_int, [_vp, _vp]),
     "fipi_get_particles_device": (ctypes.c_int, [_vp, _vp, _vp, _vp]),
     "fipi_set_brownian": (ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_uint64]),
+    "fipi_set_mass_conserving": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "fipi_set_debug": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_longlong]),
     "fipi_interpolate2": (ctypes.c_int, [_vp, _dp, ctypes.c_int, _dp, _dp]),
     "fipi_div": (ctypes.c_int, [_vp, _dp, _dp]),
     "fipi_sync": (ctypes.c_int, [_vp]),
@@ -92,6 +105,7 @@ _SIGS = {
     "fipi_kernel_stats": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_char_p, ctypes.c_int,
                                          ctypes.POINTER(ctypes.c_longlong), _dp, _dp]),
     "fipi_launch_count": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_longlong)]),
+    "fipi_fma_peak": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _dp]),
     "fipi_vtk_write_field": (ctypes.c_int, [ctypes.POINTER(FipiParams), ctypes.c_char_p, ctypes.c_char_p,
                                             ctypes.c_int, _dp]),
     "fipi_vtk_write_particles": (ctypes.c_int, [ctypes.POINTER(FipiParams), ctypes.c_char_p, ctypes.c_int, _dp,
@@ -108,6 +122,7 @@ _SIGS = {
     "fipi_adjoint_step": (ctypes.c_int, [_vp, ctypes.c_int]),
     "fipi_adjoint_get": (ctypes.c_int, [_vp, _dp, _dp, _dp, _dp]),
     "fipi_adjoint_get_history": (ctypes.c_int, [_vp, _dp, _dp, _dp]),
+    "fipi_adjoint_get_params": (ctypes.c_int, [_vp, ctypes.c_void_p, _dp]),
     "fipi_trajectory_forward": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int]),
     "fipi_trajectory_backward": (ctypes.c_int, [_vp, _dp, _dp, _dp, _dp]),
     "fipi_seed_phase": (ctypes.c_int, [ctypes.POINTER(FipiParams), ctypes.c_uint64, ctypes.c_double,
@@ -207,6 +222,13 @@ def seed_phase(params: FipiParams, seed: int, mean: float = 0.0, amp: float = 0.
     c = np.empty(V)
     _check(load().fipi_seed_phase(ctypes.byref(params), seed, mean, amp, _d(c)))
     return c
+
+
+def fma_peak(device: int = 0, fp64: bool = True) -> float:
+    """Measured FMA throughput of the device in TFLOP/s (FMA = 2 FLOPs)."""
+    v = ctypes.c_double()
+    _check(load().fipi_fma_peak(device, 1 if fp64 else 0, ctypes.byref(v)))
+    return v.value
 
 
 def vtk_write_field(params: FipiParams, path, name: str, values, components: int = 1):
@@ -375,6 +397,14 @@ class Simulation:
         """Brownian force sqrt(12 pi r mu kt / dt) g per step (kt = 0: off)."""
         _check(self.lib.fipi_set_brownian(self.h, kt, seed))
 
+    def set_mass_conserving(self, on: bool = True):
+        """The k = 0 mode of u . grad c taken as 0 (off: the reference's drift)."""
+        _check(self.lib.fipi_set_mass_conserving(self.h, 1 if on else 0))
+
+    def set_debug(self, what: int, value: int):
+        """Test hooks of the bounded device waits (fipi_set_debug)."""
+        _check(self.lib.fipi_set_debug(self.h, what, value))
+
     def wrap(self, p) -> np.ndarray:
         out = _f64(p, 3 * self.n).copy()
         _check(self.lib.fipi_wrap(self.h, _d(out)))
@@ -485,6 +515,15 @@ class Simulation:
         a, b, c = np.empty(self.V), np.empty(self.V), np.empty(self.V)
         _check(self.lib.fipi_adjoint_get_history(self.h, _d(a), _d(b), _d(c)))
         return a, b, c
+
+    def adjoint_get_params(self):
+        """Parameter cotangents summed over the reversed steps: a dict with
+        mobility, sigma (lambda and k_n following it), lambda_, k_n,
+        sigma_attach, and the per-particle cos(theta) cotangents."""
+        g = ParamGrads()
+        dct = np.empty(self.n)
+        _check(self.lib.fipi_adjoint_get_params(self.h, ctypes.byref(g), _d(dct) if self.n else None))
+        return g.as_dict(), dct
 
     def trajectory_forward(self, nsteps: int, stride: int = 0):
         _check(self.lib.fipi_trajectory_forward(self.h, nsteps, stride))

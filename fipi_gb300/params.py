@@ -151,6 +151,10 @@ WORKLOADS = {
                       note="256x16x16: rows of 128 complex pairs along x"),
     "t512x": Workload("t512x", 512, 16, 16, 512.0, 16.0, 16.0, n_p=40, r_p=1.0, t_end=10, steps=2,
                       note="512x16x16: rows of 256 complex pairs along x"),
+    "t256yz": Workload("t256yz", 16, 256, 256, 16.0, 256.0, 256.0, n_p=400, r_p=1.0, t_end=10, steps=3,
+                       note="16x256x256: the 256-point y and z transforms of the 256^3 workload"),
+    "t512yz": Workload("t512yz", 16, 512, 512, 16.0, 512.0, 512.0, n_p=800, r_p=1.0, t_end=10, steps=2,
+                       note="16x512x512: the 512-point y and z transforms of the 512^3 workload"),
     "t32_2pi": Workload("t32_2pi", 32, 32, 32, 2 * REF_PI, 2 * REF_PI, 2 * REF_PI, n_p=30,
                         r_p=0.06, sigma=0.07, epsilon=0.15, mobility=0.02, mu=1e-3,
                         t_end=10, steps=3, phi_amp=0.1,

@@ -49,7 +49,11 @@ typedef enum fipi_status {
     FIPI_ERR_NONFINITE = 5,     /* NaN/Inf detected in the state              */
     FIPI_ERR_NO_DEVICE = 6,     /* no CUDA device visible                     */
     FIPI_ERR_STATE = 7,         /* call out of order (e.g. step before state) */
-    FIPI_ERR_UNSUPPORTED = 8    /* configuration outside what is built        */
+    FIPI_ERR_UNSUPPORTED = 8,   /* configuration outside what is built        */
+    FIPI_ERR_RANGE = 9,         /* a value outside what an accumulator holds
+                                   (mixed-form fixed-point spreading)         */
+    FIPI_ERR_TIMEOUT = 10       /* a bounded device wait gave up; the work of
+                                   that call is incomplete, the context usable */
 } fipi_status;
 
 typedef enum fipi_precision {
@@ -182,6 +186,11 @@ fipi_status fipi_kernel_stats(fipi_ctx* ctx, int i, char* name, int name_cap, lo
                               double* total_ms, double* bytes_per_launch);
 /* Kernels launched by this context since creation. */
 fipi_status fipi_launch_count(const fipi_ctx* ctx, long long* n);
+/* Fused multiply-add throughput of `device` in TFLOP/s (an FMA counted as
+ * two FLOPs), FP64 (fp64 != 0) or FP32, measured with a kernel of
+ * independent FMA chains on every SM (about 20 ms of device time).  The FP64
+ * form of the step is bound by this rate, not by HBM, on GB300. */
+fipi_status fipi_fma_peak(int device, int fp64, double* tflops);
 
 /* ------------------------------------------ fine-grained parity entry points
  * One call per reference function, on host arrays; they use the context's
@@ -336,6 +345,29 @@ fipi_status fipi_adjoint_seed(fipi_ctx* ctx, const double* dc, const double* du,
 fipi_status fipi_adjoint_step(fipi_ctx* ctx, int slot);
 /* The cotangent (any pointer may be NULL): dc V, du 3 x V, dp, df_pp n_p x 3. */
 fipi_status fipi_adjoint_get(fipi_ctx* ctx, double* dc, double* du, double* dp, double* df_pp);
+/* Cotangents of the step's parameters, summed over every step reversed
+ * since fipi_adjoint_seed (after fipi_trajectory_backward: the gradient of
+ * the trajectory's loss with respect to parameters that are constant along
+ * it).  The mobility enters the CH update (main.cpp:106-127), lambda the
+ * bulk potential f = (lambda/eps^2)(c^3 - c) (main.cpp:81), mu_hat = lambda
+ * k^2 c_hat + f_hat (main.cpp:153) and the CH denominators, k_n the contact
+ * forces (cluster.cpp:246-255) and sigma the attachment force f_pi
+ * (element.cpp:89).  `sigma` is the total derivative with lambda =
+ * 3 sigma eps / (2 sqrt 2) (head.hpp:47) and k_n = sigma / 2
+ * (parameter.hpp:18) following sigma; the partial derivatives are given
+ * too.  dcos_theta (n_p, may be NULL): the cotangent of each particle's
+ * wettability cos(theta) of the contact-angle extension of f_pi.  The
+ * history terms of the trajectory's start state (its c_hat, f_hat and C_hat
+ * histories) are held fixed, except f_hat, which is a function of c there.
+ * Needs lambda != 0 (FIPI_ERR_UNSUPPORTED otherwise). */
+typedef struct fipi_param_grads {
+    double mobility;     /* dL/dM                                           */
+    double sigma;        /* dL/dsigma (lambda and k_n following sigma)       */
+    double lambda;       /* partial dL/dlambda                               */
+    double k_n;          /* partial dL/dk_n                                  */
+    double sigma_attach; /* partial dL/dsigma through f_pi alone              */
+} fipi_param_grads;
+fipi_status fipi_adjoint_get_params(fipi_ctx* ctx, fipi_param_grads* out, double* dcos_theta);
 /* Cotangents of the SBDF2 histories as real fields (V each, NULL = skip). */
 fipi_status fipi_adjoint_get_history(fipi_ctx* ctx, double* dc_old, double* df_old, double* dconv_old);
 /* Whole-trajectory gradient with sqrt(N) checkpointing.
@@ -389,6 +421,27 @@ fipi_status fipi_seed_particles(const fipi_params* p, uint64_t seed, double r_mi
  * instead of rand().  kt = 0 switches it off. */
 fipi_status fipi_set_fluid_coupling(fipi_ctx* ctx, int on);
 fipi_status fipi_set_brownian(fipi_ctx* ctx, double kt, uint64_t seed);
+
+/* Mass-conserving mode (off by default: the step is then the reference's).
+ * The reference's wave vector takes +N/2 at the Nyquist index for a mode and
+ * its mirror alike (field.cpp:108-115), so the projected velocity is not
+ * exactly divergence-free against the Nyquist-zeroed gradient and the k = 0
+ * mode of the advection term u . grad c (main.cpp:88-92) is not zero: the
+ * integral of phi drifts (about 4e-11 of sum |phi| dV over 1000 steps at
+ * 256^3).  With on != 0 that mode is taken as 0 in the Cahn-Hilliard update
+ * of both forms (and in the adjoint), so the integral of phi stays constant
+ * to rounding; every other mode is unchanged. */
+fipi_status fipi_set_mass_conserving(fipi_ctx* ctx, int on);
+
+/* Test hooks of the bounded device waits (not for production runs).
+ * FIPI_DEBUG_FFT_FIRST_WAIT_POLLS: the number of polls the first bulk-copy
+ * wait of every Y-pass block makes before it gives up (-1 restores the
+ * normal bound of 2^22 polls; 0 gives up at once).  A block that gives up
+ * sets the device error word, waits (with the normal bound) for its copies
+ * in flight and returns, so the call reports FIPI_ERR_TIMEOUT and the
+ * context stays usable.  Later waits of the block keep the normal bound. */
+#define FIPI_DEBUG_FFT_FIRST_WAIT_POLLS 1
+fipi_status fipi_set_debug(fipi_ctx* ctx, int what, long long value);
 
 /* The reference's own initial state for a given seed (host only): srand(seed)
  * (main.cpp:24 seeds from the clock), then the phase field's V draws

@@ -46,6 +46,9 @@ struct oracle {
     double kt;
     unsigned long long seed;
     double *uf, *f_rand; /* n x 3 */
+    /* mass-conserving mode of the library (not in the reference): the k = 0
+     * mode of the advection spectrum taken as 0 */
+    int conserve;
 };
 
 void oracle_set_threads(int n) { offt_set_threads(n); }
@@ -714,6 +717,8 @@ void oracle_brownian_normals(unsigned long long seed, unsigned id, unsigned t, d
     }
 }
 
+void oracle_set_mass_conserving(oracle* o, int on) { o->conserve = on ? 1 : 0; }
+
 void oracle_set_extensions(oracle* o, int couple, double kt, unsigned long long seed) {
     o->couple = couple;
     o->kt = kt;
@@ -833,6 +838,7 @@ int oracle_step(oracle* o) {
                 o->conv[2 * it + 1] = 0.0;
             }
             fft(o, o->conv); /* main.cpp:92 */
+            if (o->conserve) o->conv[0] = o->conv[1] = 0.0;
         }
         if (t == 0) { /* main.cpp:95-114 */
             memcpy(o->c_old, o->c, sizeof(double) * 2 * (size_t)V);
@@ -1099,4 +1105,128 @@ int oracle_reference_initial_state(const fipi_params* P, unsigned int seed, doub
     if (pos) memcpy(pos, p, sizeof(double) * 3 * (size_t)n);
     free(p);
     return FIPI_OK;
+}
+
+/* ------------------------------------------------ seeded synthetic inputs
+ * Restatement of the library's own input generators fipi_seed_phase and
+ * fipi_seed_particles (the reference draws from unseeded rand() instead,
+ * field.cpp:96, cluster.cpp:59-89), so that the CPU baselines can build the
+ * same inputs without loading the library.  splitmix64 (Steele, Lea, Flood
+ * 2014) drives both: 53-bit uniforms in [0, 1).  Equal to the library's
+ * draws bit for bit (tests/test_capi_cpu.py). */
+static uint64_t sm64_next(uint64_t* s) {
+    uint64_t z = (*s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+static double sm64_u01(uint64_t* s) { return (double)(sm64_next(s) >> 11) * 0x1.0p-53; }
+
+void oracle_seed_phase(const fipi_params* P, unsigned long long seed, double mean, double amp, double* c) {
+    uint64_t s = (uint64_t)seed * 0x2545F4914F6CDD1Dull + 1;
+    const long V = (long)P->nx * P->ny * P->nz;
+    for (long i = 0; i < V; ++i) c[i] = mean + amp * (2.0 * sm64_u01(&s) - 1.0);
+}
+
+static double seed_wrapd(double d, double l) {
+    if (d > 0.5 * l) d -= l;
+    else if (d < -0.5 * l) d += l;
+    return d;
+}
+
+/* Random sequential addition with the periodic minimum-image test
+ * |x_i - x_j| >= r_i + r_j over a hash grid of cells >= 2 r_max (every
+ * particle closer than r_i + r_j lies in one of the 27 cells around the
+ * candidate); candidates are drawn until one fits, at most 200000 times. */
+int oracle_seed_particles(const fipi_params* P, unsigned long long seed, double r_min, double r_max,
+                          double theta_min_deg, double theta_max_deg, int allow_overlap, double* pos, double* r,
+                          double* cos_theta) {
+    const int n = P->n_p;
+    if (n <= 0) return FIPI_OK;
+    uint64_t s = (uint64_t)seed * 0x9E3779B97F4A7C15ull + 7;
+    const double L[3] = {P->lx, P->ly, P->lz};
+    int gc[3];
+    double gs[3];
+    for (int a = 0; a < 3; ++a) {
+        gc[a] = (int)floor(L[a] / (2.0 * r_max));
+        if (gc[a] < 1) gc[a] = 1;
+        gs[a] = L[a] / gc[a];
+    }
+    const long ncell = (long)gc[0] * gc[1] * gc[2];
+    /* per-cell singly linked lists in insertion order (head, tail, next) */
+    int* head = (int*)malloc(sizeof(int) * (size_t)ncell);
+    int* tail = (int*)malloc(sizeof(int) * (size_t)ncell);
+    int* next = (int*)malloc(sizeof(int) * (size_t)n);
+    double* rr = (double*)malloc(sizeof(double) * (size_t)n);
+    for (long q = 0; q < ncell; ++q) head[q] = tail[q] = -1;
+    for (int i = 0; i < n; ++i) rr[i] = r_min + (r_max - r_min) * sm64_u01(&s);
+    int status = FIPI_OK;
+    for (int i = 0; i < n && status == FIPI_OK; ++i) {
+        double x[3];
+        int ok = 0;
+        for (long tries = 0; tries < 200000 && !ok; ++tries) {
+            for (int a = 0; a < 3; ++a) {
+                x[a] = L[a] * sm64_u01(&s);
+                if (x[a] >= L[a]) x[a] = 0.0;
+            }
+            if (allow_overlap) {
+                ok = 1;
+                break;
+            }
+            int ci[3];
+            for (int a = 0; a < 3; ++a) {
+                ci[a] = (int)(x[a] / gs[a]);
+                if (ci[a] > gc[a] - 1) ci[a] = gc[a] - 1;
+            }
+            ok = 1;
+            for (int dk = -1; dk <= 1 && ok; ++dk)
+                for (int dj = -1; dj <= 1 && ok; ++dj)
+                    for (int di = -1; di <= 1 && ok; ++di) {
+                        const long c = (long)((ci[0] + di + gc[0]) % gc[0]) +
+                                       (long)((ci[1] + dj + gc[1]) % gc[1]) * gc[0] +
+                                       (long)((ci[2] + dk + gc[2]) % gc[2]) * gc[0] * gc[1];
+                        for (int j = head[c]; j >= 0; j = next[j]) {
+                            double d2 = 0.0;
+                            for (int a = 0; a < 3; ++a) {
+                                const double d = seed_wrapd(x[a] - pos[3 * j + a], L[a]);
+                                d2 += d * d;
+                            }
+                            const double rs = rr[i] + rr[j];
+                            if (d2 < rs * rs) {
+                                ok = 0;
+                                break;
+                            }
+                        }
+                    }
+        }
+        if (!ok) {
+            status = FIPI_ERR_BAD_PARAMS;
+            break;
+        }
+        for (int a = 0; a < 3; ++a) pos[3 * i + a] = x[a];
+        int ci[3];
+        for (int a = 0; a < 3; ++a) {
+            ci[a] = (int)(x[a] / gs[a]);
+            if (ci[a] > gc[a] - 1) ci[a] = gc[a] - 1;
+        }
+        const long c = (long)ci[0] + (long)ci[1] * gc[0] + (long)ci[2] * gc[0] * gc[1];
+        next[i] = -1;
+        if (tail[c] < 0) head[c] = i;
+        else next[tail[c]] = i;
+        tail[c] = i;
+    }
+    if (status == FIPI_OK) {
+        if (r)
+            for (int i = 0; i < n; ++i) r[i] = rr[i];
+        if (cos_theta)
+            for (int i = 0; i < n; ++i) {
+                const double th = theta_min_deg + (theta_max_deg - theta_min_deg) * sm64_u01(&s);
+                cos_theta[i] = (th == 90.0) ? 0.0 : cos(th * 3.14159265358979323846 / 180.0);
+            }
+    }
+    free(head);
+    free(tail);
+    free(next);
+    free(rr);
+    return status;
 }

@@ -72,6 +72,9 @@ void oracle_spread(const fipi_params* P, int n, const double* p, const double* f
  * interpolated, element.cpp:38-52) and the Brownian force of
  * element.cpp:109-144 drawn from Philox-4x32-10. */
 void oracle_set_extensions(oracle* o, int couple, double kt, unsigned long long seed);
+/* The library's mass-conserving mode (fipi_set_mass_conserving): the k = 0
+ * mode of the advection spectrum (main.cpp:92) taken as 0. */
+void oracle_set_mass_conserving(oracle* o, int on);
 void oracle_philox4x32(const unsigned ctr[4], unsigned k0, unsigned k1, unsigned out[4]);
 void oracle_brownian_normals(unsigned long long seed, unsigned id, unsigned t, double pi, double g[3]);
 /* srand(seed) (main.cpp:24), the phase field's draws (field.cpp:85-99) and
@@ -81,6 +84,12 @@ int oracle_reference_initial_state(const fipi_params* P, unsigned int seed, doub
                                    long max_candidates);
 double oracle_free_energy(const oracle* o);
 double oracle_mass(const oracle* o);
+/* The library's seeded input generators (fipi_seed_phase,
+ * fipi_seed_particles of include/fipi.h) restated, same draws bit for bit. */
+void oracle_seed_phase(const fipi_params* P, unsigned long long seed, double mean, double amp, double* c);
+int oracle_seed_particles(const fipi_params* P, unsigned long long seed, double r_min, double r_max,
+                          double theta_min_deg, double theta_max_deg, int allow_overlap, double* pos, double* r,
+                          double* cos_theta);
 
 #ifdef __cplusplus
 }

@@ -79,6 +79,7 @@ def port_lib():
         lib.oracle_mass.restype = ctypes.c_double
         lib.oracle_mass.argtypes = [ctypes.c_void_p]
         lib.oracle_set_extensions.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_ulonglong]
+        lib.oracle_set_mass_conserving.argtypes = [ctypes.c_void_p, ctypes.c_int]
         lib.oracle_philox4x32.argtypes = [ctypes.POINTER(ctypes.c_uint), ctypes.c_uint, ctypes.c_uint,
                                           ctypes.POINTER(ctypes.c_uint)]
         lib.oracle_brownian_normals.argtypes = [ctypes.c_ulonglong, ctypes.c_uint, ctypes.c_uint, ctypes.c_double,
@@ -98,6 +99,9 @@ def port_lib():
         lib.oracle_cell_geometry.argtypes = [P, _ip, _dp]
         lib.oracle_reference_initial_state.argtypes = [P, ctypes.c_uint, _dp, _dp, ctypes.c_long]
         lib.oracle_params_ok.argtypes = [P]
+        lib.oracle_seed_phase.argtypes = [P, ctypes.c_ulonglong, ctypes.c_double, ctypes.c_double, _dp]
+        lib.oracle_seed_particles.argtypes = [P, ctypes.c_ulonglong, ctypes.c_double, ctypes.c_double,
+                                              ctypes.c_double, ctypes.c_double, ctypes.c_int, _dp, _dp, _dp]
         _port_lib = lib
     return _port_lib
 
@@ -140,6 +144,9 @@ class Port:
 
     def set_extensions(self, couple: bool = False, kt: float = 0.0, seed: int = 0):
         self.lib.oracle_set_extensions(self.h, 1 if couple else 0, kt, seed)
+
+    def set_mass_conserving(self, on: bool = True):
+        self.lib.oracle_set_mass_conserving(self.h, 1 if on else 0)
 
     def step(self, n: int = 1):
         for _ in range(n):
@@ -235,6 +242,45 @@ def reference_initial_state(params, seed: int, max_candidates: int = 10**7):
     pos = np.zeros(3 * max(params.n_p, 0))
     st = port_lib().oracle_reference_initial_state(ctypes.byref(params), seed, _d(c), _d(pos), max_candidates)
     return st, c, pos
+
+
+def seed_phase(params, seed: int, mean: float = 0.0, amp: float = 0.05):
+    """The library's fipi_seed_phase draws, restated (no library load)."""
+    V = params.nx * params.ny * params.nz
+    c = np.empty(V)
+    port_lib().oracle_seed_phase(ctypes.byref(params), seed, mean, amp, _d(c))
+    return c
+
+
+def seed_particles(params, seed: int, r_range=None, theta_range_deg=None, allow_overlap: bool = False):
+    """The library's fipi_seed_particles draws, restated (no library load)."""
+    n = max(params.n_p, 0)
+    pos, r, ct = np.empty(3 * n), np.empty(n), np.empty(n)
+    rmin, rmax = r_range if r_range else (params.r_p, params.r_p)
+    tmin, tmax = theta_range_deg if theta_range_deg else (90.0, 90.0)
+    st = port_lib().oracle_seed_particles(ctypes.byref(params), seed, rmin, rmax, tmin, tmax,
+                                          1 if allow_overlap else 0, _d(pos), _d(r), _d(ct))
+    if st != 0:
+        raise ValueError("random non-overlapping placement did not converge")
+    return pos, r, ct
+
+
+def seeded_state(w, seed: int):
+    """Seeded initial state of a workload as the benchmark draws it
+    (phase field from `seed`, particles from `seed + 1000`); r and cos_theta
+    are None where the workload keeps the reference's single radius / 90
+    degrees."""
+    P = w.params()
+    c = seed_phase(P, seed, w.phi_mean, w.phi_amp)
+    p = r = ct = None
+    if w.n_p > 0:
+        p, r, ct = seed_particles(P, seed + 1000, w.radius_range, w.theta_range_deg,
+                                  allow_overlap=w.radius_range is not None)
+        if w.radius_range is None:
+            r = None
+        if w.theta_range_deg is None:
+            ct = None
+    return P, c, p, r, ct
 
 
 def sorting(params, p):

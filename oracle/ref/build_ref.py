@@ -1,7 +1,8 @@
 """TEST INFRASTRUCTURE ONLY (oracle recipe).
 
 Compiles the reference FIPI sources, unmodified and where they lie
-(`/root/reference/src/{field,cluster,element,linked_list,primitive}.cpp`),
+(`$FIPI_REFERENCE_SRC`, else the reference checkout mounted beside this
+repository: `../reference/src/{field,cluster,element,linked_list,primitive}.cpp`),
 into one shared library per configuration under `oracle/_ref/`:
 
   g++ -include oracle/_ref/cfg_<name>.hpp -I oracle/ref -I <ref>/src ...
@@ -27,7 +28,9 @@ HERE = Path(__file__).resolve().parent
 ORACLE = HERE.parent
 REPO = ORACLE.parent
 OUT = ORACLE / "_ref"
-REF_SRC = Path(os.environ.get("FIPI_REFERENCE_SRC", "/root/reference/src"))
+# the reference's sources: $FIPI_REFERENCE_SRC, else the checkout mounted beside
+# this repository; where neither exists nothing here runs
+REF_SRC = Path(os.environ.get("FIPI_REFERENCE_SRC", str(REPO.parent / "reference" / "src")))
 REF_UNITS = ["field.cpp", "cluster.cpp", "element.cpp", "linked_list.cpp", "primitive.cpp"]
 
 sys.path.insert(0, str(REPO))

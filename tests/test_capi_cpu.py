@@ -96,6 +96,25 @@ def test_seeded_generators(fipi):
     assert ct2.min() >= np.cos(np.radians(120)) - 1e-12 and ct2.max() <= 0.5 + 1e-12
 
 
+@pytest.mark.parametrize("name", ["t32", "cfg1_64", "cfg2_256", "cfg3_512", "t32_aniso"])
+def test_oracle_seeding_equals_library(fipi, oracle_mod, name):
+    """The CPU baselines draw their inputs with the oracle's restatement of
+    the seeded generators (no library load); it must give the library's
+    draws bit for bit, including the rejection sampling of the
+    non-overlapping placement and the radius / contact-angle draws."""
+    w = fipi.workload(name)
+    P = w.params()
+    if name == "cfg3_512":
+        P.nx = P.ny = P.nz = 8  # the particle draws use only the box; keep the phase field small
+    a = fipi.seed_phase(P, 17, w.phi_mean, w.phi_amp)
+    b = oracle_mod.seed_phase(P, 17, w.phi_mean, w.phi_amp)
+    assert np.array_equal(a, b)
+    ov = w.radius_range is not None
+    pa, ra, ca = fipi.seed_particles(P, 1017, w.radius_range, w.theta_range_deg, allow_overlap=ov)
+    pb, rb, cb = oracle_mod.seed_particles(P, 1017, w.radius_range, w.theta_range_deg, allow_overlap=ov)
+    assert np.array_equal(pa, pb) and np.array_equal(ra, rb) and np.array_equal(ca, cb)
+
+
 def test_cpp_header_compiles(tmp_path):
     src = tmp_path / "use_fipi.cpp"
     src.write_text("""

@@ -5,6 +5,8 @@ spreading; relative L2 <= 1e-10 (plain FP64) for phase field, velocity and
 positions after several steps; FFT against numpy to ~1e-14 (FP64) and
 ~1e-6 (FP32).
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -13,6 +15,10 @@ from conftest import rel_l2, seeded_state
 pytestmark = pytest.mark.gpu
 
 SMALL = ["t16", "t32", "t32_aniso", "t32_2pi", "t32_bo", "t256x", "t512x"]
+# y and z lengths of the 256^3 and 512^3 workloads (the 256- and 512-point
+# Y / Z codelets and tile shapes), plus the CPU-runnable 64^3 case
+HEADLINE = ["cfg1_64", "t256yz", "t512yz"]
+THREADS = os.cpu_count() or 1  # the oracle's transforms are threaded over independent lines
 
 
 def half_spectrum_from_numpy(x, P):
@@ -38,6 +44,38 @@ def test_fft_r2c_c2r(fipi, name, prec):
         assert rel_l2(X.view(np.float64), ref.view(np.float64)) < tol
         y = s.fft_c2r(ref)
         assert rel_l2(y, x) < tol
+
+
+@pytest.mark.parametrize("shape", [(16, 256, 16), (16, 16, 256), (16, 512, 16), (16, 16, 512),
+                                   (16, 256, 256), (256, 256, 256)])
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_fft_headline_shapes(fipi, shape, prec):
+    """R2C / C2R against numpy.rfftn on the axis lengths the 256^3 and
+    512^3 workloads transform (the field::fft / ifft of main.cpp:72-73 is
+    one 3-D plan over all axes), with the small grids' tolerances."""
+    nx, ny, nz = shape
+    w = fipi.workload("t32").with_(name="fft", nx=nx, ny=ny, nz=nz, lx=float(nx), ly=float(ny), lz=float(nz),
+                                   n_p=0)
+    P = w.params()
+    rng = np.random.default_rng(nx + 3 * ny + 7 * nz)
+    x = rng.standard_normal(w.V)
+    with fipi.Simulation(P, prec) as s:
+        X = s.fft_r2c(x)
+        ref = half_spectrum_from_numpy(x, P)
+        tol = 1e-14 if prec == "fp64" else 2e-6
+        assert rel_l2(X.view(np.float64), ref.view(np.float64)) < tol
+        y = s.fft_c2r(ref)
+        assert rel_l2(y, x) < tol
+        # a single mode at the largest wave numbers below Nyquist: V/2 at
+        # (kx, ky, kz) of the half spectrum and nothing else
+        kx, ky, kz = nx // 2 - 1, ny // 2 - 1, nz // 2 - 1
+        k, j, i = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+        m = np.cos(2 * np.pi * (kx * i / nx + ky * j / ny + kz * k / nz)).ravel()
+        M = s.fft_r2c(m).reshape(nz, nx // 2 + 1, ny)
+        bar = (1e-13 if prec == "fp64" else 2e-6) * w.V
+        assert abs(M[kz, kx, ky] - w.V / 2) < bar
+        M[kz, kx, ky] = 0
+        assert np.abs(M).max() < bar
 
 
 @pytest.mark.parametrize("prec", ["fp64", "mixed"])
@@ -152,11 +190,12 @@ def test_interpolate_f_pi_advect_spread(fipi, oracle_mod, name):
         assert np.array_equal(sp, oracle_mod.spread(P, p, fpp))
 
 
-@pytest.mark.parametrize("name", SMALL)
+@pytest.mark.parametrize("name", SMALL + HEADLINE)
 def test_step_fp64_matches_oracle(fipi, oracle_mod, name):
     w = fipi.workload(name)
+    w = w.with_(steps=min(w.steps, 3))
     P, c, p, r, ct = seeded_state(w, 21)
-    port = oracle_mod.Port(P)
+    port = oracle_mod.Port(P, threads=THREADS)
     port.set_state(c, p, r, ct)
     with fipi.Simulation(P, "fp64") as s:
         s.set_phase(c)
@@ -176,6 +215,42 @@ def test_step_fp64_matches_oracle(fipi, oracle_mod, name):
         assert abs(s.free_energy() - port.free_energy()) <= 1e-10 * abs(port.free_energy())
         assert abs(s.mass() - port.mass()) <= 1e-12 * np.abs(c).sum()
         assert abs(s.packing_tau() - port.tau()) <= 1e-9 * max(1.0, abs(port.tau()))
+
+
+def test_cfg2_256_matches_oracle(fipi, oracle_mod):
+    """The 256^3, 20,000-sphere workload itself, two steps (the IMEX start
+    and the first SBDF2 step) from the seeded state: the FP64 form within
+    the parity bars of the oracle, the mixed form within its stated error."""
+    w = fipi.workload("cfg2_256")
+    P, c, p, r, ct = seeded_state(w, 1)
+    port = oracle_mod.Port(P, threads=THREADS)
+    port.set_state(c, p, r, ct)
+    sims = {prec: fipi.Simulation(P, prec) for prec in ("fp64", "mixed")}
+    try:
+        for s in sims.values():
+            s.set_phase(c)
+            s.set_particles(p, r, ct)
+        for step in range(2):
+            assert port.step(1) == 0
+            pc, pu = port.phase(), port.velocity()
+            pp, pf, _ = port.particles()
+            for s in sims.values():
+                s.step(1)
+            g = sims["fp64"]
+            gp, gf, _ = g.get_particles()
+            assert rel_l2(g.get_phase(), pc) < 1e-10, step
+            assert rel_l2(g.get_velocity(), pu) < 1e-10, step
+            assert rel_l2(gp, pp) < 1e-12, step
+            assert rel_l2(gf, pf) < 1e-10, step
+            m = sims["mixed"]
+            assert rel_l2(m.get_phase(), pc) < 1e-5, step
+            assert rel_l2(m.get_velocity(), pu) < 1e-3, step
+            assert rel_l2(m.get_particles()[0], pp) < 1e-8, step
+        assert abs(g.mass() - port.mass()) <= 1e-12 * np.abs(c).sum()
+        assert abs(g.free_energy() - port.free_energy()) <= 1e-10 * abs(port.free_energy())
+    finally:
+        for s in sims.values():
+            s.close()
 
 
 @pytest.mark.parametrize("name", ["t32", "t32_2pi", "cfg1_64", "t256x"])

@@ -94,7 +94,7 @@ def _ref_or_skip(oracle_mod):
         pytest.skip("reference sources not present on this host")
 
 
-@pytest.mark.parametrize("name", GOLDEN + ["t256x", "t512x", "t32_bo"])
+@pytest.mark.parametrize("name", GOLDEN + ["t256x", "t512x", "t32_bo", "t256yz"])
 def test_oracle_bit_exact_with_live_reference(oracle_mod, name):
     _ref_or_skip(oracle_mod)
     from fipi_gb300.params import workload
@@ -194,3 +194,27 @@ def test_div_and_interpolate2_bit_exact_with_reference(oracle_mod, name):
     fld = rng.standard_normal(w.V)
     p = (rng.random((50, 3)) * np.array([P.lx, P.ly, P.lz])).ravel()
     assert np.array_equal(oracle_mod.interpolate2(P, fld, p), ref.interpolate2(fld, p))
+
+
+def test_oracle_mass_conserving_mode(oracle_mod):
+    """The library's mass-conserving mode restated in the oracle: without it
+    the reference's Nyquist drift of the integral of phi is there, with it
+    the integral stays constant to rounding."""
+    from fipi_gb300.params import workload
+
+    w = workload("t32")
+    P = w.params()
+    rng = np.random.default_rng(12)
+    c0 = rng.uniform(-0.05, 0.05, w.V)
+    p0 = (rng.uniform(0, 1, (w.n_p, 3)) * [w.lx, w.ly, w.lz]).ravel()
+    dv = w.lx * w.ly * w.lz / w.V
+    drift = {}
+    for on in (False, True):
+        port = oracle_mod.Port(P)
+        port.set_state(c0, p0)
+        port.set_mass_conserving(on)
+        m0 = port.mass()
+        assert port.step(8) == 0
+        drift[on] = abs(port.mass() - m0) / (np.abs(c0).sum() * dv)
+    assert drift[True] <= 1e-14, drift
+    assert drift[False] > 1e-13, drift

@@ -45,6 +45,31 @@ def test_noalloc_cells_match_context_entry_point(fipi):
         assert np.array_equal(d_off.cpu().numpy(), off), name
 
 
+def test_noalloc_cells_at_the_scratch_bound(fipi):
+    """Exactly FIPI_NOALLOC_MAX_PARTICLES particles: every histogram block
+    and the whole position region of the scratch in use."""
+    torch = pytest.importorskip("torch")
+    lib = fipi.load()
+    stream = torch.cuda.current_stream().cuda_stream
+    w = fipi.workload("cfg1_64")
+    P = w.params()
+    n = P.n_p = 65536
+    rng = np.random.default_rng(n)
+    p = (rng.random((n, 3)) * np.array([P.lx, P.ly, P.lz])).ravel()
+    with fipi.Simulation(P, "fp64") as s:
+        keys, srt, off = s.cells_build(p)
+    d_pos = torch.tensor(p, dtype=torch.float64, device="cuda")
+    d_keys = torch.full((n,), -7, dtype=torch.int32, device="cuda")
+    d_sorted = torch.full((n,), -7, dtype=torch.int32, device="cuda")
+    d_off = torch.full((off.size,), -7, dtype=torch.int32, device="cuda")
+    for _ in range(2):
+        st = _call(lib, P, d_pos, d_keys, d_sorted, d_off, stream)
+        assert st == 0, lib.fipi_last_error_string()
+        assert np.array_equal(d_keys.cpu().numpy(), keys)
+        assert np.array_equal(d_sorted.cpu().numpy(), srt)
+        assert np.array_equal(d_off.cpu().numpy(), off)
+
+
 def test_noalloc_rejects_sizes_beyond_its_scratch(fipi):
     torch = pytest.importorskip("torch")
     lib = fipi.load()
