@@ -195,6 +195,93 @@ def adjoint_ratio(F, P, c, p, r, ct, device, torch, steps, traj_steps):
                            "gradient_over_forward": (tf + tb) / (traj_steps * fwd)}}
 
 
+def grad_bench(F, name, device, torch, steps=None, fd_h=None, fd=("phi0", "mobility", "sigma", "cos_theta")):
+    """Gradient benchmark of a workload through the FP64 adjoint with sqrt(N)
+    checkpointing (fipi_gradient harness, torch loss on the GPU):
+
+      cfg4_128  128^3, 2000 spheres, 200 steps, a checkpoint every 20 steps;
+                loss ||S(k) - S_target(k)||^2, the target from a second seed;
+                gradients w.r.t. phi0, M, sigma and every cos theta
+      cfg5_256  the coated droplet (256^3, 20,000 spheres, g along -z),
+                1000 steps, ceil(sqrt(1000)) = 32 checkpoints; loss
+                interfacial area + centroid height; gradients w.r.t. sigma
+                and every cos theta; the mixed forward against the FP64 one
+
+    Reports the gradient's wall time over the plain FP64 forward's (both
+    host wall clocks around synchronous calls), the device memory the
+    context holds with its checkpoint slots, and the central-difference
+    agreement of each gradient (relative step h)."""
+    import numpy as np
+
+    from fipi_gb300 import gradcheck as G
+    from fipi_gb300 import inputs
+
+    w = F.workload(name)
+    nsteps = steps or w.steps
+    dev = f"cuda:{device}"
+    if name == "cfg5_256":
+        P, c0, p0, r, ct = inputs.initial_state(w, 1)
+        stride = 0  # ceil(sqrt(N))
+        h = fd_h or 1e-5
+        which = tuple(x for x in fd if x in ("sigma", "cos_theta"))
+
+        def loss_fn(c):
+            return G.area_plus_height(c, P)
+    else:
+        P, c0, p0, r, ct = seeded(w, 1)
+        stride = 20
+        h = fd_h or 1e-6
+        which = fd
+        with F.Simulation(P, "fp64", device=device) as s:  # the target: the same run from a second seed
+            Pt, ct0, pt, rt, ctt = seeded(w, 2)
+            s.set_phase(ct0)
+            s.set_particles(pt, rt, ctt)
+            s.step(nsteps)
+            target = G.structure_factor(torch.from_numpy(s.get_phase()).to(dev), (P.nz, P.ny, P.nx))
+
+        def loss_fn(c):
+            return G.structure_loss(c, target, (P.nz, P.ny, P.nx))
+    init = G.InitialState(p0=p0, r=r, cos_theta=np.zeros(w.n_p) if ct is None else ct)
+    out = {"workload": name, "steps": nsteps, "grid": f"{w.nx}x{w.ny}x{w.nz}", "particles": w.n_p,
+           "loss": "interfacial area + centroid height" if name == "cfg5_256" else "||S(k) - S_target(k)||^2"}
+    with F.Simulation(P, "fp64", device=device) as s:
+        G._start(s, c0, init)
+        s.sync()
+        t0 = time.perf_counter()
+        s.step(nsteps)
+        fwd = time.perf_counter() - t0
+        end64 = (s.get_phase(), s.get_velocity(), s.get_particles()[0])
+        t0 = time.perf_counter()
+        L0, g_c, g_th, g_ct = G.loss_and_grads(s, c0, init, nsteps, loss_fn, stride, dev)
+        s.sync()
+        tg = time.perf_counter() - t0
+        ck = s.checkpoint_bytes()
+        hbm = s.device_bytes()
+        slots = -(-nsteps // (stride or int(np.ceil(np.sqrt(nsteps))))) + (stride or int(np.ceil(np.sqrt(nsteps))))
+        out.update({"forward_s": fwd, "gradient_s": tg, "gradient_over_forward": tg / fwd,
+                    "checkpoint_stride": stride or int(np.ceil(np.sqrt(nsteps))), "checkpoint_slots": slots,
+                    "checkpoint_slot_bytes": ck, "device_bytes": hbm, "loss_value": L0,
+                    "grad_norms": {"phi0": float(np.linalg.norm(g_c)), "mobility": float(g_th[0]),
+                                   "sigma": float(g_th[1]), "cos_theta": float(np.linalg.norm(g_ct))}})
+        if which:
+            chk = G.fd_all(s, c0, init, nsteps, loss_fn, h, stride, seed=7, device=dev, which=which)
+            out["fd"] = {k: v for k, v in chk.items() if k != "loss"}
+            out["fd_max_rel"] = max(v["rel"] for k, v in chk.items() if k != "loss")
+    if name == "cfg5_256":
+        with F.Simulation(P, "mixed", device=device) as s:
+            G._start(s, c0, init)
+            s.step(nsteps)
+            a = (s.get_phase(), s.get_velocity(), s.get_particles()[0])
+        L = np.array([P.lx, P.ly, P.lz])
+        dp = np.abs(a[2] - end64[2]).reshape(-1, 3)
+        dp = np.minimum(dp, L - dp)
+        out["mixed_vs_fp64"] = {"steps": nsteps,
+                                "phi_rel_l2": float(np.linalg.norm(a[0] - end64[0]) / np.linalg.norm(end64[0])),
+                                "u_rel_l2": float(np.linalg.norm(a[1] - end64[1]) / np.linalg.norm(end64[1])),
+                                "pos_max_abs": float(dp.max())}
+    return out
+
+
 def kernel_stats(sim):
     return sim.kernel_stats()
 
@@ -527,6 +614,11 @@ def run_gpu(args):
     if args.adj_steps > 0:
         adj = adjoint_ratio(F, P, c, p, r, ct, local, torch, args.adj_steps, args.traj_steps)
 
+    grads = {}
+    if rank == 0 and args.grad != "none":
+        for name in (("cfg4_128", "cfg5_256") if args.grad == "all" else (args.grad,)):
+            grads[name] = grad_bench(F, name, local, torch, steps=args.grad_steps or None)
+
     cpu = err_oracle = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         cpu, ref_state, nref = cpu_baseline(w, seed)
@@ -548,6 +640,7 @@ def run_gpu(args):
             "error_vs_oracle": err_oracle,
             "adjoint_over_forward": adj["adjoint_step_over_forward"] if adj else None,
             "adjoint": adj,
+            "gradients": grads,
             "e2e": {"value": e2e_val, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,
             "roofline": roof,
@@ -578,6 +671,9 @@ def main():
     ap.add_argument("--adj-steps", type=int, default=5, help="adjoint steps timed (0 = skip)")
     ap.add_argument("--traj-steps", type=int, default=16, help="steps of the checkpointed gradient")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--grad", default="all", choices=["all", "none", "cfg4_128", "cfg5_256"],
+                    help="gradient benchmarks of the adjoint (configs 4 and 5)")
+    ap.add_argument("--grad-steps", type=int, default=0, help="steps of the gradient benchmarks (0 = the workload's)")
     ap.add_argument("--profile", type=int, default=0, help="only run N steps (for ncu)")
     ap.add_argument("--form", default="mixed", choices=["mixed", "fp64"])
     args = ap.parse_args()

@@ -721,6 +721,31 @@ fipi_status fipi_set_brownian(fipi_ctx* ctx, double kt, uint64_t seed) {
     return particles_ext_alloc(ctx);
 }
 
+fipi_status fipi_set_params(fipi_ctx* ctx, const fipi_params* P) {
+    NEED(ctx);
+    NEED(P);
+    if (ctx->substep != 0) return set_error(ctx, FIPI_ERR_STATE, "parameters change between iterations only");
+    const fipi_params& Q = ctx->P;
+    // the grid, box, time step, particle geometry and switches the context's
+    // buffers, wave-number tables and cell grid were built for stay fixed
+    const bool same = P->nx == Q.nx && P->ny == Q.ny && P->nz == Q.nz && P->lx == Q.lx && P->ly == Q.ly &&
+                      P->lz == Q.lz && P->dt == Q.dt && P->t_end == Q.t_end && P->pi == Q.pi &&
+                      P->margin == Q.margin && P->r_p == Q.r_p && P->r_eq == Q.r_eq && P->r_c == Q.r_c &&
+                      P->n_p == Q.n_p && P->switch_particle == Q.switch_particle && P->switch_ch == Q.switch_ch &&
+                      P->switch_ns == Q.switch_ns;
+    if (!same)
+        return set_error(ctx, FIPI_ERR_BAD_PARAMS,
+                         "only sigma, epsilon, lambda, mobility, mu, rho1, rho2, gravity, A and k_n can change "
+                         "on a live context");
+    fipi_status st = validate(P, ctx->prec);
+    if (st != FIPI_OK) return st;
+    FIPI_CUDA(ctx, cudaSetDevice(ctx->device));
+    FIPI_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->P = *P;
+    graphs_reset(ctx);
+    return FIPI_OK;
+}
+
 fipi_status fipi_set_mass_conserving(fipi_ctx* ctx, int on) {
     NEED(ctx);
     if (ctx->substep != 0) return set_error(ctx, FIPI_ERR_STATE, "the mode changes between iterations only");
@@ -752,7 +777,8 @@ fipi_status fipi_fft_r2c(fipi_ctx* ctx, const double* in, double* out) {
     NEED(in);
     NEED(out);
     FIPI_CUDA(ctx, cudaSetDevice(ctx->device));
-    return fields_fft_r2c(ctx, in, out);
+    const fipi_status st = fields_fft_r2c(ctx, in, out);
+    return st != FIPI_OK ? st : check_status(ctx);  // the transforms' device error word (bounded copy waits)
 }
 
 fipi_status fipi_fft_c2r(fipi_ctx* ctx, const double* in, double* out) {
@@ -760,7 +786,8 @@ fipi_status fipi_fft_c2r(fipi_ctx* ctx, const double* in, double* out) {
     NEED(in);
     NEED(out);
     FIPI_CUDA(ctx, cudaSetDevice(ctx->device));
-    return fields_fft_c2r(ctx, in, out);
+    const fipi_status st = fields_fft_c2r(ctx, in, out);
+    return st != FIPI_OK ? st : check_status(ctx);  // the transforms' device error word (bounded copy waits)
 }
 
 fipi_status fipi_grad(fipi_ctx* ctx, const double* c, double* g) {
@@ -768,7 +795,8 @@ fipi_status fipi_grad(fipi_ctx* ctx, const double* c, double* g) {
     NEED(c);
     NEED(g);
     FIPI_CUDA(ctx, cudaSetDevice(ctx->device));
-    return fields_grad(ctx, c, g);
+    const fipi_status st = fields_grad(ctx, c, g);
+    return st != FIPI_OK ? st : check_status(ctx);  // the transforms' device error word (bounded copy waits)
 }
 
 fipi_status fipi_cells_build(fipi_ctx* ctx, const double* p, int* keys, int* sorted_ids, int* cell_offsets) {
@@ -847,7 +875,8 @@ fipi_status fipi_interpolate2(fipi_ctx* ctx, const double* fields, int nfields, 
 fipi_status fipi_div(fipi_ctx* ctx, const double* v, double* out) {
     if (!ctx || !v || !out) return set_error(ctx, FIPI_ERR_BAD_ARG, "NULL argument");
     FIPI_CUDA(ctx, cudaSetDevice(ctx->device));
-    return fields_div(ctx, v, out);
+    const fipi_status st = fields_div(ctx, v, out);
+    return st != FIPI_OK ? st : check_status(ctx);  // the transforms' device error word (bounded copy waits)
 }
 
 fipi_status fipi_wrap(fipi_ctx* ctx, double* p) {

@@ -81,6 +81,7 @@ _SIGS = {
     "fipi_get_particles_device": (ctypes.c_int, [_vp, _vp, _vp, _vp]),
     "fipi_set_brownian": (ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_uint64]),
     "fipi_set_mass_conserving": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "fipi_set_params": (ctypes.c_int, [_vp, ctypes.POINTER(FipiParams)]),
     "fipi_set_debug": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_longlong]),
     "fipi_interpolate2": (ctypes.c_int, [_vp, _dp, ctypes.c_int, _dp, _dp]),
     "fipi_div": (ctypes.c_int, [_vp, _dp, _dp]),
@@ -396,6 +397,12 @@ class Simulation:
     def set_brownian(self, kt: float, seed: int = 0):
         """Brownian force sqrt(12 pi r mu kt / dt) g per step (kt = 0: off)."""
         _check(self.lib.fipi_set_brownian(self.h, kt, seed))
+
+    def set_params(self, params: FipiParams):
+        """New physical constants (sigma, epsilon, lambda, mobility, mu,
+        densities, gravity, A, k_n) for the next steps; the state is kept."""
+        _check(self.lib.fipi_set_params(self.h, ctypes.byref(params)))
+        self.params = params
 
     def set_mass_conserving(self, on: bool = True):
         """The k = 0 mode of u . grad c taken as 0 (off: the reference's drift)."""

@@ -137,6 +137,12 @@ WORKLOADS = {
     "cfg4_128": Workload("cfg4_128", 128, 128, 128, 128.0, 128.0, 128.0, n_p=2000, r_p=4.0,
                          t_end=200, steps=200,
                          note="128^3, 2000 spheres r=4, 200 steps (gradient-check case)"),
+    "cfg5_256": Workload("cfg5_256", 256, 256, 256, 256.0, 256.0, 256.0, n_p=20000, r_p=3.0,
+                         t_end=1000, steps=1000, rho1=2.0, rho2=1.0, gravity=-1e-4,
+                         extra={"init": "droplet", "radius": 64.0},
+                         note="256^3, one droplet of radius 64 (phi = +1 inside, tanh profile of width eps), "
+                              "20,000 spheres r=3 on its interface (overlap allowed: a monolayer holds ~1650), "
+                              "g = 1e-4 along -z with rho1 = 2 inside and rho2 = 1 outside, 1000 steps"),
     # Small grids the CPU oracle finishes in seconds (parity cases).
     "t16": Workload("t16", 16, 16, 16, 16.0, 16.0, 16.0, n_p=6, r_p=1.0, t_end=20, steps=4,
                     note="16^3 parity case"),

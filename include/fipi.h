@@ -110,6 +110,13 @@ fipi_status fipi_create(const fipi_params* p, fipi_precision prec, int device, f
 fipi_status fipi_destroy(fipi_ctx* ctx);
 /* Bytes of device memory held by the context. */
 fipi_status fipi_device_bytes(const fipi_ctx* ctx, size_t* out);
+/* Replaces the physical constants of a live context (the reference fixes
+ * them at compile time, head.hpp:44-58, parameter.hpp:18): sigma, epsilon,
+ * lambda, mobility, mu, rho1, rho2, gravity, A and k_n; they take effect at
+ * the next step.  Everything else must equal the context's parameters
+ * (FIPI_ERR_BAD_PARAMS otherwise).  The state is kept, so a sensitivity
+ * study or a finite-difference check needs no new context. */
+fipi_status fipi_set_params(fipi_ctx* ctx, const fipi_params* p);
 
 /* ----------------------------------------------------------------- state */
 /* Initial phase field (field.cpp:85-99 drew it from rand()); resets t = 0

@@ -154,3 +154,39 @@ def test_mass_conserving_adjoint_matches_fd(fipi):
     fd = (run(c0 + h * d) - run(c0 - h * d)) / (2 * h)
     ad = float(np.dot(dc, d))
     assert abs(ad - fd) <= 1e-5 * abs(fd), (ad, fd)
+
+
+@pytest.mark.parametrize("init", ["noise", "droplet"])
+def test_harness_gradients_match_fd(fipi, init):
+    """The torch.autograd.Function of the harness on the two gradient-check
+    losses of the benchmark (structure factor against a second seed's, and
+    interfacial area + centroid height of a coated droplet): d/dphi0, dM,
+    dsigma and d/dcos(theta) against central differences (h = 1e-6)."""
+    torch = pytest.importorskip("torch")
+    from fipi_gb300 import gradcheck as G
+    from fipi_gb300 import inputs
+
+    w = fipi.workload("t32")
+    rng = np.random.default_rng(65)
+    if init == "droplet":
+        P = w.params()
+        P.rho1, P.rho2, P.gravity = 2.0, 1.0, -1e-2
+        c0 = inputs.droplet_phase(P, 8.0)
+        p0 = inputs.interface_particles(P, w.n_p, 8.0, 3)
+        r = None
+
+        def loss_fn(c):
+            return G.area_plus_height(c, P)
+    else:
+        P, c0, p0, r, _ = seeded_state(w, 64)
+        Pt, ct0, _, _, _ = seeded_state(w, 66)
+        target = G.structure_factor(torch.from_numpy(ct0), (P.nz, P.ny, P.nx))
+
+        def loss_fn(c):
+            return G.structure_loss(c, target, (P.nz, P.ny, P.nx))
+    ct = rng.uniform(-0.5, 0.5, w.n_p)
+    start = G.InitialState(p0=p0, r=r, cos_theta=ct)
+    with fipi.Simulation(P, "fp64") as s:
+        res = G.fd_all(s, c0, start, 5, loss_fn, 1e-6, stride=2, seed=3)
+    for k in ("phi0", "mobility", "sigma", "cos_theta"):
+        assert res[k]["rel"] < 1e-3, (k, res[k])
