@@ -218,31 +218,32 @@ def fd_check(sim: Simulation, c0: np.ndarray, init: InitialState, nsteps: int, t
     return {"loss": L0, "adjoint": ad, "fd": fd, "rel": abs(ad - fd) / max(abs(fd), 1e-300), "grad": g}
 
 
-def fd_all(sim: Simulation, c0: np.ndarray, init: InitialState, nsteps: int, loss_fn, h: float, stride: int = 0,
+def fd_all(sim: Simulation, c0: np.ndarray, init: InitialState, nsteps: int, loss_fn, h, stride: int = 0,
            seed: int = 0, device: str = "cpu", which=("phi0", "mobility", "sigma", "cos_theta")) -> dict:
     """Adjoint gradients of `loss_fn` against central differences with
-    relative step h: along a random direction in c0 and in cos theta, and
-    in M and sigma."""
+    relative step h (a number, or a dict per gradient): along a random
+    direction in c0 and in cos theta, and in M and sigma."""
     P = sim.params
     L0, g_c, g_th, g_ct = loss_and_grads(sim, c0, init, nsteps, loss_fn, stride, device)
     rng = np.random.default_rng(seed)
     ct0 = init.cos_theta if init.cos_theta is not None else np.zeros(sim.n)
     out = {"loss": L0}
     for what in which:
+        h_w = h[what] if isinstance(h, dict) else h
         if what == "phi0":
             d = rng.standard_normal(c0.size)
-            ad, hh = float(np.dot(g_c, d)), h
+            ad, hh = float(np.dot(g_c, d)), h_w
             lp = loss_only(sim, c0 + hh * d, init, nsteps, loss_fn, device=device)
             lm = loss_only(sim, c0 - hh * d, init, nsteps, loss_fn, device=device)
         elif what == "cos_theta":
             d = rng.standard_normal(sim.n)
-            ad, hh = float(np.dot(g_ct, d)), h
+            ad, hh = float(np.dot(g_ct, d)), h_w
             lp = loss_only(sim, c0, init, nsteps, loss_fn, cos_theta=ct0 + hh * d, device=device)
             lm = loss_only(sim, c0, init, nsteps, loss_fn, cos_theta=ct0 - hh * d, device=device)
         else:
             i = 0 if what == "mobility" else 1
             base = P.mobility if i == 0 else P.sigma
-            ad, hh = float(g_th[i]), h * base
+            ad, hh = float(g_th[i]), h_w * base
             kw = "mobility" if i == 0 else "sigma"
             lp = loss_only(sim, c0, init, nsteps, loss_fn, P=with_physics(P, **{kw: base + hh}), device=device)
             lm = loss_only(sim, c0, init, nsteps, loss_fn, P=with_physics(P, **{kw: base - hh}), device=device)

