@@ -190,7 +190,7 @@ def adjoint_ratio(F, P, c, p, r, ct, device, torch, steps, traj_steps):
             "forward_ms": fwd * 1e3, "adjoint_step_ms": adj * 1e3,
             "adjoint_step_over_forward": adj / fwd,
             "trajectory": {"steps": traj_steps, "stride": stride,
-                           "slots": -(-traj_steps // stride) + stride,
+                           "slots": -(-traj_steps // stride) + stride + 1,
                            "forward_s": tf, "backward_s": tb,
                            "gradient_over_forward": (tf + tb) / (traj_steps * fwd)}}
 
@@ -264,7 +264,7 @@ def grad_bench(F, name, device, torch, steps=None, fd_steps=None, fd=("phi0", "m
         tg = time.perf_counter() - t0
         ck = s.checkpoint_bytes()
         hbm = s.device_bytes()
-        slots = -(-nsteps // (stride or int(np.ceil(np.sqrt(nsteps))))) + (stride or int(np.ceil(np.sqrt(nsteps))))
+        slots = -(-nsteps // (stride or int(np.ceil(np.sqrt(nsteps))))) + (stride or int(np.ceil(np.sqrt(nsteps)))) + 1
         out.update({"forward_s": fwd, "gradient_s": tg, "gradient_over_forward": tg / fwd,
                     "checkpoint_stride": stride or int(np.ceil(np.sqrt(nsteps))), "checkpoint_slots": slots,
                     "checkpoint_slot_bytes": ck, "device_bytes": hbm, "loss_value": L0,

@@ -585,6 +585,49 @@ fipi_status adjoint_step_impl(fipi_ctx* ctx, int slot) {
     return check_status(ctx);
 }
 
+// Reverses step n without recomputing it: slot_n holds the state at the
+// start of the step, slot_n1 the state after it, and tape the u^n and
+// mu^{n+1} the step wrote when it ran (4V doubles) -- what the trajectory's
+// segment sweep leaves.  Gives the same cotangents as adjoint_step_impl,
+// which recomputes the step from slot_n to obtain the same inputs.
+fipi_status adjoint_reverse_pair(fipi_ctx* ctx, int slot_n, int slot_n1, const double* tape) {
+    AdjBufs& a = ctx->ad;
+    const Geom& g = ctx->g;
+    const size_t V = (size_t)g.V, SH = (size_t)g.SH;
+    const int n = ctx->ck.t[slot_n];
+    if (n != a.t - 1 || ctx->ck.t[slot_n1] != a.t)
+        return set_error(ctx, FIPI_ERR_STATE, "the slots must hold the states before and after the reversed step");
+    const CkLayout L = ck_layout(ctx);
+    const unsigned char* sn = ctx->ck.base + (size_t)slot_n * ctx->ck.bytes;
+    const bool parts = particles_on(ctx);
+    // inputs of the reverse pass from the step's start state
+    FIPI_CUDA(ctx, cudaMemcpyAsync(a.tc0, sn + L.c, sizeof(D) * V, cudaMemcpyDeviceToDevice, ctx->stream));
+    FIPI_CUDA(ctx, cudaMemcpyAsync(a.tg0, sn + L.g, sizeof(D) * 3 * V, cudaMemcpyDeviceToDevice, ctx->stream));
+    if (n > 0)  // f_hat^{n-1}: the start state's f_hat history (spectral region 3 of the slot)
+        FIPI_CUDA(ctx, cudaMemcpyAsync(a.tfo, sn + L.spec + 3 * 2 * sizeof(D) * SH, sizeof(CD) * SH,
+                                       cudaMemcpyDeviceToDevice, ctx->stream));
+    if (parts) {
+        const size_t b3 = sizeof(D) * 3 * (size_t)ctx->pb.n;
+        FIPI_CUDA(ctx, cudaMemcpyAsync(a.tp0, sn + L.p, b3, cudaMemcpyDeviceToDevice, ctx->stream));
+        FIPI_CUDA(ctx, cudaMemcpyAsync(a.tfpp0, sn + L.fpp, b3, cudaMemcpyDeviceToDevice, ctx->stream));
+        set_tick(ctx, n);  // ramp(n + 1, 0.2 t_end) of the reversed step
+        FIPI_CUDA(ctx, cudaMemcpyAsync(a.rmp, ctx->d_rmp, sizeof(D), cudaMemcpyDeviceToDevice, ctx->stream));
+    }
+    FIPI_CUDA(ctx, cudaMemcpyAsync(a.tu, tape, sizeof(D) * 3 * V, cudaMemcpyDeviceToDevice, ctx->stream));
+    FIPI_CUDA(ctx, cudaMemcpyAsync(a.tmu, tape + 3 * V, sizeof(D) * V, cudaMemcpyDeviceToDevice, ctx->stream));
+    // the step's end state, as the recomputed step would have left it
+    fipi_status st = ck_load(ctx, slot_n1);
+    if (st != FIPI_OK) return st;
+    if (parts) {
+        st = particles_adjoint(ctx);
+        if (st != FIPI_OK) return st;
+    }
+    adjoint_fields(ctx, n == 0);
+    FIPI_CUDA(ctx, cudaGetLastError());
+    a.t = n;
+    return FIPI_OK;
+}
+
 fipi_status adjoint_seed_impl(fipi_ctx* ctx, const double* dc, const double* du, const double* dp,
                               const double* dfpp) {
     if (ctx->prec != FIPI_FP64)
@@ -651,7 +694,7 @@ void param_acc(fipi_ctx* ctx, const double* part, int np, double scale, double* 
 void adjoint_free(fipi_ctx* ctx) {
     AdjBufs& a = ctx->ad;
     void* all[] = {a.la_c, a.la_co, a.la_fo, a.la_Co, a.AS[0], a.AS[1], a.AS[2], a.AS[3], a.AS[4],
-                   a.la_u, a.lamF, a.part, a.tc0, a.tg0, a.tu, a.tmu, a.pg, a.pg_part, a.tfo};
+                   a.la_u, a.lamF, a.part, a.tc0, a.tg0, a.tu, a.tmu, a.pg, a.pg_part, a.tfo, a.seg_tape};
     for (void* p : all)
         if (p) cudaFree(p);
     particles_adjoint_free(ctx);
@@ -833,7 +876,7 @@ fipi_status fipi_trajectory_forward(fipi_ctx* ctx, int nsteps, int stride) {
     tr.s = stride > 0 ? stride : (int)std::ceil(std::sqrt((double)nsteps));
     if (tr.s > nsteps) tr.s = nsteps;
     tr.K = (nsteps + tr.s - 1) / tr.s;
-    fipi_status st = ck_reserve(ctx, tr.K + tr.s);
+    fipi_status st = ck_reserve(ctx, tr.K + tr.s + 1);
     if (st != FIPI_OK) return st;
     for (int k = 0; k < tr.K; ++k) {
         st = ck_save(ctx, k);
@@ -854,9 +897,26 @@ fipi_status fipi_trajectory_backward(fipi_ctx* ctx, const double* dc, const doub
     if (tr->t0 < 0) return set_error(ctx, FIPI_ERR_STATE, "fipi_trajectory_forward must come first");
     if (ctx->t != tr->t0 + tr->n)
         return set_error(ctx, FIPI_ERR_STATE, "the state moved since fipi_trajectory_forward");
-    if (ctx->ck.slots < tr->K + tr->s) return set_error(ctx, FIPI_ERR_STATE, "checkpoint slots were released");
+    if (ctx->ck.slots < tr->K + tr->s + 1) return set_error(ctx, FIPI_ERR_STATE, "checkpoint slots were released");
     fipi_status st = adjoint_seed_impl(ctx, dc, du, dp, df_pp);
     if (st != FIPI_OK) return st;
+    // per-step tapes of one segment: u^n and mu^{n+1} (4V doubles per step)
+    AdjBufs& a = ctx->ad;
+    const size_t V = (size_t)ctx->g.V;
+    if (a.seg_tape_steps < tr->s) {
+        if (a.seg_tape) {
+            cudaFree(a.seg_tape);
+            ctx->device_bytes -= sizeof(D) * 4 * V * (size_t)a.seg_tape_steps;
+            a.seg_tape = nullptr;
+            a.seg_tape_steps = 0;
+        }
+        FIPI_CUDA(ctx, cudaMalloc((void**)&a.seg_tape, sizeof(D) * 4 * V * (size_t)tr->s));
+        a.seg_tape_steps = tr->s;
+        ctx->device_bytes += sizeof(D) * 4 * V * (size_t)tr->s;
+    }
+    // Each segment is run once more from its checkpoint with its tapes kept
+    // and its states (the one after the last step too) in the slots K..K+len;
+    // its steps are then reversed from those without recomputing them.
     for (int k = tr->K - 1; k >= 0; --k) {
         const int len = std::min(tr->s, tr->n - k * tr->s);
         st = ck_load(ctx, k);
@@ -864,15 +924,25 @@ fipi_status fipi_trajectory_backward(fipi_ctx* ctx, const double* dc, const doub
         for (int j = 0; j < len; ++j) {
             st = ck_save(ctx, tr->K + j);
             if (st != FIPI_OK) return st;
-            if (j + 1 < len) {
-                st = fipi_step(ctx, 1);
-                if (st != FIPI_OK) return st;
-            }
+            double* tp = a.seg_tape + 4 * V * (size_t)j;
+            ctx->tape_u[0] = tp;
+            ctx->tape_u[1] = tp + V;
+            ctx->tape_u[2] = tp + 2 * V;
+            ctx->tape_mu = tp + 3 * V;
+            enqueue_step(ctx);  // direct launches: the step graphs hold no tape
+            ctx->tape_u[0] = ctx->tape_u[1] = ctx->tape_u[2] = nullptr;
+            ctx->tape_mu = nullptr;
         }
+        st = ck_save(ctx, tr->K + len);
+        if (st != FIPI_OK) return st;
+        st = check_status(ctx);
+        if (st != FIPI_OK) return st;
         for (int j = len - 1; j >= 0; --j) {
-            st = adjoint_step_impl(ctx, tr->K + j);
+            st = adjoint_reverse_pair(ctx, tr->K + j, tr->K + j + 1, a.seg_tape + 4 * V * (size_t)j);
             if (st != FIPI_OK) return st;
         }
+        st = check_status(ctx);
+        if (st != FIPI_OK) return st;
     }
     tr->t0 = -1;  // the state is no longer the trajectory's end
     return FIPI_OK;

@@ -141,6 +141,9 @@ struct AdjBufs {
     double* dct = nullptr;      // n: cotangent of each particle's cos(theta)
     double* pp_sig = nullptr;   // n: per-particle terms of the sigma (f_pi) cotangent of one step
     double* pp_kn = nullptr;    // n: per-particle terms of the k_n cotangent of one step
+    // per-step tapes of a trajectory segment (u^n, mu^{n+1}: 4V doubles each)
+    double* seg_tape = nullptr;
+    int seg_tape_steps = 0;
 };
 // Slots of AdjBufs::pg.
 enum : int { kPgMobility = 0, kPgLambda = 1, kPgKn = 2, kPgSigmaAttach = 3, kParamGrads = 4 };

@@ -380,12 +380,15 @@ fipi_status fipi_adjoint_get_history(fipi_ctx* ctx, double* dc_old, double* df_o
 /* Whole-trajectory gradient with sqrt(N) checkpointing.
  * fipi_trajectory_forward advances nsteps from the current state, saving a
  * checkpoint every `stride` steps (stride <= 0: ceil(sqrt(nsteps))) into
- * slots it reserves (ceil(nsteps/stride) + stride of them).
+ * slots it reserves (ceil(nsteps/stride) + stride + 1 of them).
  * fipi_trajectory_backward seeds the cotangent of the final state and
- * reverses every step: each segment is recomputed once from its
- * checkpoint, its states kept in slots, then reversed step by step.  The
- * gradient with respect to the trajectory's first state is then read with
- * fipi_adjoint_get. */
+ * reverses every step: each segment is run once more from its checkpoint
+ * with its states kept in slots and the velocity and chemical potential
+ * each step forms kept in a per-segment tape (4 V doubles per step, stride
+ * steps; allocated on the first call), then reversed step by step from
+ * those without recomputing the steps again.  The gradient with respect to
+ * the trajectory's first state is then read with fipi_adjoint_get, and with
+ * respect to the parameters with fipi_adjoint_get_params. */
 fipi_status fipi_trajectory_forward(fipi_ctx* ctx, int nsteps, int stride);
 fipi_status fipi_trajectory_backward(fipi_ctx* ctx, const double* dc, const double* du, const double* dp,
                                      const double* df_pp);
