@@ -195,7 +195,8 @@ def adjoint_ratio(F, P, c, p, r, ct, device, torch, steps, traj_steps):
                            "gradient_over_forward": (tf + tb) / (traj_steps * fwd)}}
 
 
-def grad_bench(F, name, device, torch, steps=None, fd_steps=None, fd=("phi0", "mobility", "sigma", "cos_theta")):
+def grad_bench(F, name, device, torch, steps=None, fd_steps=None, fd_h=None,
+               fd=("phi0", "mobility", "sigma", "cos_theta")):
     """Gradient benchmark of a workload through the FP64 adjoint with sqrt(N)
     checkpointing (fipi_gradient harness, torch loss on the GPU):
 
@@ -215,7 +216,9 @@ def grad_bench(F, name, device, torch, steps=None, fd_steps=None, fd=("phi0", "m
     whole rollout particles cross the attachment force's jump at |d| = r
     (element.cpp:84-89: f_mag drops from -A pi r sigma to 0), where the
     trajectory is not differentiable and a central difference across the
-    jump measures the jump, not the derivative."""
+    jump measures the jump, not the derivative (over all 1000 steps the
+    differences converge to the adjoint's values as h shrinks: run with
+    --grad cfg5_256 --grad-fd-steps 1000 --grad-fd-h 1e-7)."""
     import numpy as np
 
     from fipi_gb300 import gradcheck as G
@@ -227,7 +230,7 @@ def grad_bench(F, name, device, torch, steps=None, fd_steps=None, fd=("phi0", "m
     if name == "cfg5_256":
         P, c0, p0, r, ct = inputs.initial_state(w, 1)
         stride = 0  # ceil(sqrt(N))
-        h = {"sigma": 1e-6, "cos_theta": 1e-4}
+        h = fd_h or {"sigma": 1e-6, "cos_theta": 1e-4}
         which = tuple(x for x in fd if x in ("sigma", "cos_theta"))
         fd_n = fd_steps or min(nsteps, 100)
 
@@ -236,7 +239,7 @@ def grad_bench(F, name, device, torch, steps=None, fd_steps=None, fd=("phi0", "m
     else:
         P, c0, p0, r, ct = seeded(w, 1)
         stride = 20
-        h = 1e-6
+        h = fd_h or 1e-6
         which = fd
         fd_n = fd_steps or nsteps
         with F.Simulation(P, "fp64", device=device) as s:  # the target: the same run from a second seed
@@ -272,7 +275,7 @@ def grad_bench(F, name, device, torch, steps=None, fd_steps=None, fd=("phi0", "m
                                    "sigma": float(g_th[1]), "cos_theta": float(np.linalg.norm(g_ct))}})
         if which:
             chk = G.fd_all(s, c0, init, fd_n, loss_fn, h, stride if fd_n == nsteps else 0, seed=7, device=dev,
-                           which=which)
+                           which=which, grads=(L0, g_c, g_th, g_ct) if fd_n == nsteps else None)
             out["fd"] = {k: v for k, v in chk.items() if k != "loss"}
             out["fd_steps"] = fd_n
             out["fd_max_rel"] = max(v["rel"] for k, v in chk.items() if k != "loss")
@@ -627,7 +630,7 @@ def run_gpu(args):
     if rank == 0 and args.grad != "none":
         for name in (("cfg4_128", "cfg5_256") if args.grad == "all" else (args.grad,)):
             grads[name] = grad_bench(F, name, local, torch, steps=args.grad_steps or None,
-                                     fd_steps=args.grad_fd_steps or None)
+                                     fd_steps=args.grad_fd_steps or None, fd_h=args.grad_fd_h or None)
 
     cpu = err_oracle = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
@@ -686,6 +689,8 @@ def main():
     ap.add_argument("--grad-steps", type=int, default=0, help="steps of the gradient benchmarks (0 = the workload's)")
     ap.add_argument("--grad-fd-steps", type=int, default=0,
                     help="steps of the finite-difference checks (0: config 4 all, config 5 the first 100)")
+    ap.add_argument("--grad-fd-h", type=float, default=0.0,
+                    help="relative step of the finite differences (0: 1e-6; config 5: 1e-6 sigma, 1e-4 cos theta)")
     ap.add_argument("--profile", type=int, default=0, help="only run N steps (for ncu)")
     ap.add_argument("--form", default="mixed", choices=["mixed", "fp64"])
     args = ap.parse_args()

@@ -193,19 +193,8 @@ fipi_status fipi_create(const fipi_params* P, fipi_precision prec, int device, f
     if (cudaSetDevice(device) != cudaSuccess) return fail(cuda_check(ctx, cudaGetLastError(), "cudaSetDevice"));
     cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
     if (ctx->num_sms < 1) ctx->num_sms = 1;
-    // FIPI_PARTICLE_STREAM: 0 = one stream; 1 = particle stream below the
-    // grid passes' priority; 2 = above it; 3 = both at the default priority
-    int pmode = 0;
-    if (const char* ev = std::getenv("FIPI_PARTICLE_STREAM")) pmode = std::atoi(ev);
-    int prio_lo = 0, prio_hi = 0;
-    cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
-    cudaError_t e = cudaStreamCreateWithPriority(&ctx->stream, cudaStreamNonBlocking, pmode == 1 ? prio_hi : prio_lo);
+    cudaError_t e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) return fail(cuda_check(ctx, e, "cudaStreamCreate"));
-    if (pmode >= 1 && pmode <= 3) {
-        e = cudaStreamCreateWithPriority(&ctx->pstream, cudaStreamNonBlocking, pmode == 2 ? prio_hi : prio_lo);
-        for (int i = 0; i < 4 && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&ctx->pev[i], cudaEventDisableTiming);
-        if (e != cudaSuccess) return fail(cuda_check(ctx, e, "particle stream"));
-    }
     e = cudaMalloc(&ctx->status, sizeof(int));
     if (e != cudaSuccess) return fail(cuda_check(ctx, e, "cudaMalloc(status)"));
     e = cudaMalloc(&ctx->d_t, sizeof(int));
@@ -248,12 +237,6 @@ fipi_status fipi_destroy(fipi_ctx* ctx) {
     fields_free(ctx);
     particles_free(ctx);
     if (ctx->status) cudaFree(ctx->status);
-    if (ctx->pstream) {
-        cudaStreamSynchronize(ctx->pstream);
-        cudaStreamDestroy(ctx->pstream);
-    }
-    for (cudaEvent_t e : ctx->pev)
-        if (e) cudaEventDestroy(e);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return FIPI_OK;
@@ -518,44 +501,13 @@ void fipi::graphs_reset(fipi_ctx* ctx) {
 
 
 // One iteration of main.cpp:75-219, enqueued on the context stream.
-// With a particle stream the spreading (it reads only the previous step's
-// particles) runs beside the Cahn-Hilliard part, and the particle stages
-// (they read c^{n+1} and grad c^{n+1}, written by the force X pass) beside
-// the velocity's Y pass and projection; the step ends when both streams
-// have finished.  The launches go to the particle stream by pointing the
-// context's stream at it while they are enqueued.
 void fipi::enqueue_step(fipi_ctx* ctx) {
     const int t = ctx->t;
-    const bool split = ctx->pstream && !ctx->couple_u && !ctx->kt.enabled && ctx->pb.n > 0 &&
-                       ctx->P.switch_particle;
-    if (!split) {
-        fields_step_ch(ctx, t);      // main.cpp:79-141
-        particles_spread(ctx);       // main.cpp:169 (compute_f_r of the previous step's state)
-        fields_step_stokes(ctx);     // main.cpp:146-181
-        particles_step(ctx);         // main.cpp:186-219
-        step_tick(ctx);
-        ctx->t = t + 1;
-        return;
-    }
-    cudaStream_t main_s = ctx->stream, side = ctx->pstream;
-    cudaEventRecord(ctx->pev[0], main_s);
-    cudaStreamWaitEvent(side, ctx->pev[0], 0);
-    ctx->stream = side;
-    particles_spread(ctx);
-    cudaEventRecord(ctx->pev[1], side);
-    ctx->stream = main_s;
-    fields_step_ch(ctx, t);
-    cudaStreamWaitEvent(main_s, ctx->pev[1], 0);
-    fields_step_stokes_part(ctx, 1);
-    cudaEventRecord(ctx->pev[2], main_s);
-    cudaStreamWaitEvent(side, ctx->pev[2], 0);
-    ctx->stream = side;
-    particles_step(ctx);
+    fields_step_ch(ctx, t);      // main.cpp:79-141
+    particles_spread(ctx);       // main.cpp:169 (compute_f_r of the previous step's state)
+    fields_step_stokes(ctx);     // main.cpp:146-181
+    particles_step(ctx);         // main.cpp:186-219
     step_tick(ctx);
-    cudaEventRecord(ctx->pev[3], side);
-    ctx->stream = main_s;
-    fields_step_stokes_part(ctx, 2);
-    cudaStreamWaitEvent(main_s, ctx->pev[3], 0);
     ctx->t = t + 1;
 }
 
@@ -586,7 +538,7 @@ static fipi_status graph_step(fipi_ctx* ctx, bool* done) {
             e = cudaStreamEndCapture(ctx->stream, &graph);
         }
         cudaGraphExec_t exec = nullptr;
-        if (e == cudaSuccess) e = cudaGraphInstantiateWithFlags(&exec, graph, cudaGraphInstantiateFlagUseNodePriority);
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
         if (graph) cudaGraphDestroy(graph);
         const fipi::FieldBufs fb1 = ctx->fb;
         const fipi::ParticleBufs pb1 = ctx->pb;

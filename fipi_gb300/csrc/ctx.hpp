@@ -201,10 +201,6 @@ struct fipi_ctx {
         long long launches = 0;
     } graphs[2];
     bool use_graphs = true;
-    // particle stream: the spreading and the two particle stages run on it
-    // beside the grid passes they do not depend on (enqueue_step); 0 = off
-    cudaStream_t pstream = nullptr;
-    cudaEvent_t pev[4] = {};
     int substep = 0;           // 1 after fipi_step_ch, 2 after fipi_step_stokes
     double* pin = nullptr;     // pinned host staging of the particle state, 12 n doubles
     double* pin_dev = nullptr; // the same buffer as a device pointer (mapped pinned memory)
@@ -240,9 +236,6 @@ fipi_status fields_get_velocity(fipi_ctx* ctx, double* u, bool dev = false);
 // The three grid sub-steps of one iteration (enqueue only).
 void fields_step_ch(fipi_ctx* ctx, int t);        // conv, CH update, c, f
 void fields_step_stokes(fipi_ctx* ctx);           // mu, grad c, force, projection
-// The two halves of fields_step_stokes: part 1 = Y inverse of mu, grad c and
-// the force X pass (grad c^{n+1} written), part 2 = Y forward + projection.
-void fields_step_stokes_part(fipi_ctx* ctx, int part);
 fipi_status fields_get_grad(fipi_ctx* ctx, double* g_host);  // grad c of the state, 3 x V
 fipi_status fields_mass(fipi_ctx* ctx, double* out);
 fipi_status fields_free_energy(fipi_ctx* ctx, double* out);

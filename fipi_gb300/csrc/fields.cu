@@ -831,12 +831,11 @@ void fields_step_ch(fipi_ctx* ctx, int t) {
 // C: Y inverse of mu, grad c; X inverse with grad c stored and
 //    F = mu grad c + spread + buoyancy, R2C of F; Y forward; Z forward +
 //    projection (u_hat stored) + Z inverse of u_hat for the next step.
-template <typename T> static void step_stokes_t(fipi_ctx* ctx, int part) {
+template <typename T> static void step_stokes_t(fipi_ctx* ctx) {
     const Geom& g = ctx->g;
     FieldBufs& b = ctx->fb;
     const StepConsts<T> k = make_consts<T>(ctx);
     const KTabs<T> kt = F<T>::ktabs(ctx);
-    if (part != 2) {
     void* s4[4] = {b.S[0], b.S[1], b.S[2], b.S[3]};
     launch_y<T>(ctx, 4, s4, s4, +1);
     OpForce<T> of{{F<T>::S(ctx, 0), F<T>::S(ctx, 1), F<T>::S(ctx, 2), F<T>::S(ctx, 3)},
@@ -848,8 +847,6 @@ template <typename T> static void step_stokes_t(fipi_ctx* ctx, int part) {
     // real arrays: grad c written; the spread grid and c (buoyancy) read when they matter
     const int nreal = 3 + (of.spread ? 3 : 0) + (ctx->P.gravity != 0.0 ? 1 : 0);
     launch_x<T, 4, 3, false>(ctx, "X inverse mu,grad, force, forward", nreal, of);
-    }
-    if (part == 1) return;
     void* s3[3] = {b.S[0], b.S[1], b.S[2]};
     launch_y<T>(ctx, 3, s3, s3, -1);
     ZOpProj<T> zp{{F<T>::S(ctx, 0), F<T>::S(ctx, 1), F<T>::S(ctx, 2)}, {nullptr, nullptr, nullptr}, kt, k.mu, g.m,
@@ -859,11 +856,9 @@ template <typename T> static void step_stokes_t(fipi_ctx* ctx, int part) {
 }
 
 
-void fields_step_stokes(fipi_ctx* ctx) { fields_step_stokes_part(ctx, 0); }
-
-void fields_step_stokes_part(fipi_ctx* ctx, int part) {
-    if (ctx->prec == FIPI_MIXED) step_stokes_t<float>(ctx, part);
-    else step_stokes_t<double>(ctx, part);
+void fields_step_stokes(fipi_ctx* ctx) {
+    if (ctx->prec == FIPI_MIXED) step_stokes_t<float>(ctx);
+    else step_stokes_t<double>(ctx);
 }
 
 // ------------------------------------------------------------ diagnostics

@@ -219,12 +219,15 @@ def fd_check(sim: Simulation, c0: np.ndarray, init: InitialState, nsteps: int, t
 
 
 def fd_all(sim: Simulation, c0: np.ndarray, init: InitialState, nsteps: int, loss_fn, h, stride: int = 0,
-           seed: int = 0, device: str = "cpu", which=("phi0", "mobility", "sigma", "cos_theta")) -> dict:
+           seed: int = 0, device: str = "cpu", which=("phi0", "mobility", "sigma", "cos_theta"),
+           grads=None) -> dict:
     """Adjoint gradients of `loss_fn` against central differences with
     relative step h (a number, or a dict per gradient): along a random
-    direction in c0 and in cos theta, and in M and sigma."""
+    direction in c0 and in cos theta, and in M and sigma.  `grads`: the
+    result of loss_and_grads for the same trajectory, if already known."""
     P = sim.params
-    L0, g_c, g_th, g_ct = loss_and_grads(sim, c0, init, nsteps, loss_fn, stride, device)
+    L0, g_c, g_th, g_ct = grads if grads is not None else loss_and_grads(sim, c0, init, nsteps, loss_fn, stride,
+                                                                          device)
     rng = np.random.default_rng(seed)
     ct0 = init.cos_theta if init.cos_theta is not None else np.zeros(sim.n)
     out = {"loss": L0}

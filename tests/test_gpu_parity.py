@@ -445,23 +445,3 @@ def test_div_and_interpolate2(fipi, oracle_mod, name, prec):
     else:
         assert rel_l2(d, d_ref) < 1e-5
         assert rel_l2(i2, i_ref) < 1e-6
-
-
-@pytest.mark.parametrize("mode", ["1", "2", "3"])
-@pytest.mark.parametrize("prec", ["fp64", "mixed"])
-def test_particle_stream_gives_the_same_steps(fipi, monkeypatch, mode, prec):
-    """The step with its particle work on a second stream (spreading beside
-    the Cahn-Hilliard part, the particle stages beside the projection) is the
-    same computation: bit-identical states, through the CUDA graph too."""
-    w = fipi.workload("cfg1_64")
-    P, c, p, r, ct = seeded_state(w, 71)
-    out = {}
-    for m in ("0", mode):
-        monkeypatch.setenv("FIPI_PARTICLE_STREAM", m)
-        with fipi.Simulation(P, prec) as s:
-            s.set_phase(c)
-            s.set_particles(p, r, ct)
-            s.step(6)
-            out[m] = (s.get_phase(), s.get_velocity(), *s.get_particles())
-    for a, b in zip(out["0"], out[mode]):
-        assert np.array_equal(a, b)
