@@ -522,11 +522,14 @@ def run_gpu(args):
     cc = ct if ct is not None else np.zeros(w.n_p)
     sim.sync()
     e2e_steps = max(1, min(args.steps, args.e2e_steps))
+    # the step is enqueued without waiting; the particle read that follows
+    # synchronises and reports any device error of the step
+    outs = (np.empty(3 * w.n_p), np.empty(3 * w.n_p), np.empty(3 * w.n_p))
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         sim.set_particles(pos, rr, cc, fpp)
-        sim.step(1)
-        pos, fpp, fpi = sim.get_particles()
+        sim.step_async(1)
+        pos, fpp, fpi = sim.get_particles(outs)  # set_particles has consumed the last ones
         sim.mass()
     e2e_dt = time.perf_counter() - t0
     e2e_val = ws * e2e_steps / e2e_dt

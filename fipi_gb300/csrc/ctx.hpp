@@ -63,6 +63,7 @@ struct ParticleBufs {
     unsigned* sp_vals_alt = nullptr;  // 8n
     unsigned* sp_prev = nullptr;      // 8n nodes written by the previous spread
     unsigned long long* sp_acc = nullptr;  // mixed form: 3 x V fixed-point spread accumulators
+    float* sp_mag = nullptr;               // mixed form: V sums of |contribution| (range bound)
     int sp_prev_valid = 0;
     // radix sort scratch
     unsigned* hist = nullptr;  // 256 * max_blocks

@@ -1053,16 +1053,20 @@ static void spread_t(fipi_ctx* ctx, const double* p, const double* f_pp, T* cons
 // first of a node's duplicate slots writes the grid and the others read 0.
 constexpr double kFxScale = 4294967296.0;  // 2^32
 
-// Range of the fixed-point sums: a contribution must stay below 2^30 force
-// units per dx^3 (|v| 2^32 < 2^62), and a node's running sum must not wrap
-// the signed 64-bit accumulator (|sum| < 2^31 units).  Either failure sets
-// ERR_SPREAD_RANGE; an out-of-range contribution is left out.  (A running
-// sum that wraps and later returns into range is still reported.)
-constexpr float kFxMaxContribution = 1073741824.0f;  // 2^30
+// Range of the fixed-point sums: a node's running sums must stay inside the
+// signed 64-bit accumulators, |sum| < 2^31 units.  Each node also sums the
+// magnitudes of its contributions (|v_x| + |v_y| + |v_z|, FP32, a fire-and-
+// forget atomic like the sums), which bounds every running sum of every
+// component; the store kernel reports ERR_SPREAD_RANGE when that bound
+// reaches kFxMaxNodeMagnitude (2^31 less a margin for the FP32 rounding of
+// the bound), and a single contribution of 2^30 units or more (or NaN) is
+// reported and left out at once.
+constexpr float kFxMaxContribution = 1073741824.0f;   // 2^30
+constexpr float kFxMaxNodeMagnitude = 2.1e9f;         // < 2^31 = 2.147e9
 
 __global__ void k_spread_fx(PC pc, const double* __restrict__ p, const double* __restrict__ f_pp, size_t V,
-                            unsigned long long* acc, unsigned* nodes, int clear_prev, float* f0, float* f1,
-                            float* f2, int* status) {
+                            unsigned long long* acc, float* mag, unsigned* nodes, int clear_prev, float* f0,
+                            float* f1, float* f2, int* status) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = pc.n;
     if (i >= n) return;
@@ -1085,25 +1089,26 @@ __global__ void k_spread_fx(PC pc, const double* __restrict__ p, const double* _
         const int z = (ix[2] + c_corner[c][2]) % pc.N[2];
         const unsigned node = (unsigned)(x + (size_t)y * pc.N[0] + (size_t)z * pc.N[0] * pc.N[1]);
         nodes[8 * i + c] = node;
+        float m = 0.f;
         for (int a = 0; a < 3; ++a) {
             const float v = corner_value<float>(f[a], c, o, pp, q);
             if (!(fabsf(v) < kFxMaxContribution)) {  // also NaN
                 atomicOr(status, ERR_SPREAD_RANGE);
                 continue;
             }
-            const unsigned long long add = (unsigned long long)llrint((double)v * kFxScale);
-            const unsigned long long old = atomicAdd(acc + a * V + node, add);
-            const unsigned long long sum = old + add;
-            if ((~(old ^ add) & (old ^ sum)) >> 63) atomicOr(status, ERR_SPREAD_RANGE);  // signed wrap
+            m += fabsf(v);
+            atomicAdd(acc + a * V + node, (unsigned long long)llrint((double)v * kFxScale));
         }
+        if (m != 0.f) atomicAdd(mag + node, m);
     }
 }
 
 __global__ void k_spread_fx_store(const unsigned* __restrict__ nodes, int m, size_t V, unsigned long long* acc,
-                                  float* f0, float* f1, float* f2) {
+                                  float* mag, float* f0, float* f1, float* f2, int* status) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= m) return;
     const unsigned nd = nodes[s];
+    if (atomicExch(mag + nd, 0.f) >= kFxMaxNodeMagnitude) atomicOr(status, ERR_SPREAD_RANGE);
     float* fa[3] = {f0, f1, f2};
     for (int a = 0; a < 3; ++a) {
         const unsigned long long v = atomicExch(acc + a * V + nd, 0ull);
@@ -1121,14 +1126,16 @@ static void spread_fx(fipi_ctx* ctx) {
     float* f2 = (float*)ctx->fb.fsp[2];
     if (!b.sp_prev_valid) {
         cudaMemsetAsync(b.sp_acc, 0, sizeof(unsigned long long) * 3 * V, ctx->stream);
+        cudaMemsetAsync(b.sp_mag, 0, sizeof(float) * V, ctx->stream);
         for (int a = 0; a < 3; ++a) cudaMemsetAsync(ctx->fb.fsp[a], 0, sizeof(float) * V, ctx->stream);
     }
     {
         LaunchScope ls_(ctx, "spread fixed-point atomics", 0.0);
-        k_spread_fx<<<(n + kPT - 1) / kPT, kPT, 0, ctx->stream>>>(pc, b.p, b.f_pp, V, b.sp_acc, b.sp_prev,
+        k_spread_fx<<<(n + kPT - 1) / kPT, kPT, 0, ctx->stream>>>(pc, b.p, b.f_pp, V, b.sp_acc, b.sp_mag, b.sp_prev,
                                                                   b.sp_prev_valid, f0, f1, f2, ctx->status);
     }
-    { LaunchScope ls_(ctx, "spread store", 0.0); k_spread_fx_store<<<(m + 255) / 256, 256, 0, ctx->stream>>>(b.sp_prev, m, V, b.sp_acc, f0, f1, f2); }
+    { LaunchScope ls_(ctx, "spread store", 0.0); k_spread_fx_store<<<(m + 255) / 256, 256, 0, ctx->stream>>>(b.sp_prev, m, V, b.sp_acc, b.sp_mag, f0, f1, f2,
+                                                                                                     ctx->status); }
     b.sp_prev_valid = 1;
 }
 
@@ -1308,8 +1315,10 @@ fipi_status particles_alloc(fipi_ctx* ctx) {
     FIPI_CUDA(ctx, A((void**)&b.sp_vals, sizeof(unsigned) * 8 * n));
     FIPI_CUDA(ctx, A((void**)&b.sp_vals_alt, sizeof(unsigned) * 8 * n));
     FIPI_CUDA(ctx, A((void**)&b.sp_prev, sizeof(unsigned) * 8 * n));
-    if (ctx->prec == FIPI_MIXED && b.n > 0)
+    if (ctx->prec == FIPI_MIXED && b.n > 0) {
         FIPI_CUDA(ctx, A((void**)&b.sp_acc, sizeof(unsigned long long) * 3 * (size_t)P.nx * P.ny * P.nz));
+        FIPI_CUDA(ctx, A((void**)&b.sp_mag, sizeof(float) * (size_t)P.nx * P.ny * P.nz));
+    }
     b.hist_cap = 256 * ((16 * n + RS_TILE - 1) / RS_TILE + 1);  // up to 16 records per particle (adjoint)
     FIPI_CUDA(ctx, A((void**)&b.hist, sizeof(unsigned) * b.hist_cap));
     FIPI_CUDA(ctx, A((void**)&b.tau_part, sizeof(double) * n));
@@ -1331,7 +1340,7 @@ void particles_free(fipi_ctx* ctx) {
     ParticleBufs& b = ctx->pb;
     void* all[] = {b.p, b.p_old, b.u_old, b.f_pp, b.f_pi, b.r, b.cth, b.keys, b.keys_alt, b.ids, b.ids_alt,
                    b.cell_off, b.cell_cnt, b.sp_keys, b.sp_keys_alt, b.sp_vals, b.sp_vals_alt, b.sp_prev,
-                   b.hist, b.tau_part, b.it_mark, b.tau, b.spos, b.sp_fw, b.ymax, b.sp_acc, b.uf, b.f_rand};
+                   b.hist, b.tau_part, b.it_mark, b.tau, b.spos, b.sp_fw, b.ymax, b.sp_acc, b.sp_mag, b.uf, b.f_rand};
     for (void* p : all)
         if (p) cudaFree(p);
     b = ParticleBufs{};

@@ -331,9 +331,17 @@ class Simulation:
         _check(self.lib.fipi_get_velocity(self.h, _d(out)))
         return out
 
-    def get_particles(self):
+    def get_particles(self, out=None):
+        """(positions, f_pp, f_pi), n_p x 3 each; `out`: three float64 arrays
+        of 3 n_p values to fill instead of new ones."""
         n = self.n
-        p, fpp, fpi = np.empty(3 * n), np.empty(3 * n), np.empty(3 * n)
+        if out is None:
+            p, fpp, fpi = np.empty(3 * n), np.empty(3 * n), np.empty(3 * n)
+        else:
+            p, fpp, fpi = out
+            for a in out:
+                if a.dtype != np.float64 or a.size != 3 * n or not a.flags.c_contiguous:
+                    raise ValueError(f"out arrays must be contiguous float64 of {3 * n} values")
         _check(self.lib.fipi_get_particles(self.h, _d(p), _d(fpp), _d(fpi)))
         return p, fpp, fpi
 

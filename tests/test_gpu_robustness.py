@@ -85,6 +85,17 @@ def test_spread_range_guard(fipi):
         s.set_particles(p, r, ct)
         s.step(2)
         assert np.isfinite(s.get_phase()).all()
+    # contributions each inside the bound whose sum at one node is not:
+    # every particle on the same grid node (weight 1 there) with 1e8 units
+    pile = np.tile(np.array([8.0, 8.0, 8.0]), n)
+    fx = np.zeros(3 * n)
+    fx[0::3] = 1e8
+    with fipi.Simulation(P, "mixed") as s:
+        s.set_phase(c)
+        s.set_particles(pile, r, ct, fx)
+        with pytest.raises(fipi.FipiError) as e:
+            s.step(1)
+        assert e.value.code == FIPI_ERR_RANGE
     # a force the accumulators do hold gives the FP64 form's spread
     ok = np.zeros(3 * n)
     ok[3 * 5 + 2] = 1e6
