@@ -204,15 +204,24 @@ template <typename T> struct OpForce {
 // ------------------------------------------------------------ Z-pass ops
 // Z forward with the Cahn-Hilliard update (main.cpp:95-138) fused.
 // The conv spectrum C^n is the transformed input; c_hat^{n+1} is written
-// over c_hat^{n-1} and C^n over C^{n-1} at the same index.
+// over c_hat^{n-1} at the same index.
+//
+// FP64 form: the reference's histories and evaluation order (bit parity):
+// C^n is written over C^{n-1}.
+// Mixed form: the three histories enter the SBDF2 numerator only as
+// H^n = -c_hat^{n-1} + 2 dt M k^2 f_hat^{n-1} + 2 dt C^{n-1}, so the step
+// stores H^{n+1} = -c_hat^n + 2 dt M k^2 f_hat^n + 2 dt C^n (in the C^{n-1}
+// array) and reads it back at the next step instead of the three arrays:
+// two spectral reads fewer per step.  (The history term carries the
+// mobility of the step that stored it.)
 template <typename T, bool MIXED> struct ZOpCH {
     using C = cplx<T>;
     const C* conv;
     const C* chat;
-    C* chat_old;  // in: c^{n-1}; out: c^{n+1}
+    C* chat_old;  // in: c^{n-1} (FP64); out: c^{n+1}
     const C* fhat;
     const C* fhat_old;
-    C* Chat_old;  // in: C^{n-1}; out: C^n
+    C* Chat_old;  // FP64: in C^{n-1}, out C^n;  mixed: in H^n, out H^{n+1}
     KTabs<T> kt;
     StepConsts<T> k;
     int first;     // t == 0
@@ -224,18 +233,20 @@ template <typename T, bool MIXED> struct ZOpCH {
         update(ix, iy, iz, gi, v[0], p);
     }
     struct Pre {
-        C c, f, co, fo, Co;
+        C c, f, co, fo, Co;  // mixed: Co holds H^n, co and fo unused
     };
     __device__ void pre(size_t gi, Pre& p) const {
         p.c = chat[gi];
         p.f = fhat[gi];
         if (!first) {
-            p.co = chat_old[gi];
-            p.fo = fhat_old[gi];
+            if constexpr (!MIXED) {
+                p.co = chat_old[gi];
+                p.fo = fhat_old[gi];
+            }
             p.Co = Chat_old[gi];
         }
     }
-    // Writes c_hat^{n+1} and C^n at gi and returns c_hat^{n+1}.
+    // Writes c_hat^{n+1} and the history at gi and returns c_hat^{n+1}.
     __device__ C update(int ix, int iy, int iz, size_t gi, C Cn, const Pre& p) const {
         if (conserve && gi == 0) Cn = mkc<C>(T(0), T(0));
         const C c = p.c;
@@ -250,7 +261,7 @@ template <typename T, bool MIXED> struct ZOpCH {
             im -= Cn.y * k.dt;
             const T den = k4 * k.s2 + T(1);
             out = mkc<C>(re / den, im / den);
-        } else {
+        } else if constexpr (!MIXED) {
             const C co = p.co;
             const C fo = p.fo;
             const C Co = p.Co;
@@ -266,10 +277,24 @@ template <typename T, bool MIXED> struct ZOpCH {
             im += Co.y * k.s2c;
             const T den = k4 * k.s3 + T(3);
             out = mkc<C>(re / den, im / den);
+        } else {
+            const T a4 = k2 * k.s4;
+            T re = c.x * T(4) + p.Co.x, im = c.y * T(4) + p.Co.y;
+            re -= a4 * f.x;
+            im -= a4 * f.y;
+            re -= Cn.x * k.s4c;
+            im -= Cn.y * k.s4c;
+            const T den = k4 * k.s3 + T(3);
+            out = mkc<C>(re / den, im / den);
         }
         if (MIXED && gi == 0) out = mkc<C>(T(0), T(0));  // k = 0 lives in FP64 scalars
         chat_old[gi] = out;
-        Chat_old[gi] = Cn;
+        if constexpr (MIXED) {
+            const T a2 = k2 * k.s2m;  // H^{n+1} = -c^n + 2 dt M k^2 f^n + 2 dt C^n
+            Chat_old[gi] = mkc<C>(a2 * f.x + k.s2c * Cn.x - c.x, a2 * f.y + k.s2c * Cn.y - c.y);
+        } else {
+            Chat_old[gi] = Cn;
+        }
         return out;
     }
 };
@@ -804,8 +829,10 @@ template <typename T, bool MIXED> static void step_ch_t(fipi_ctx* ctx, int t) {
                        F<T>::sp(b.fhat_old), F<T>::sp(b.Chat_old), kt, k, t == 0 ? 1 : 0, ctx->conserve_mass};
     ZOpCHRt<T, MIXED> zcr{zc, F<T>::S(ctx, 0), ctx->k0, ctx->partials, (g.ny / x_rows_of(sizeof(T), g.m)) * g.nz,
                           ctx->P.dt, 1.0 / (double)g.V};
+    // spectral arrays: conv, c, f read, c^{n+1}, history, Z^-1 c^{n+1} written; for
+    // t > 0 also the history (mixed: H) or the three histories (FP64) read
     launch_zrt<T, 1, 1, -1, 16 / (sizeof(T) / 4), true>(ctx, t == 0 ? "Z forward + IMEX update + inverse" : "Z forward + SBDF2 update + inverse",
-                                t == 0 ? 6 : 9, zcr);
+                                t == 0 ? 6 : (MIXED ? 7 : 9), zcr);
     std::swap(b.chat, b.chat_old);  // chat = c^{n+1}, chat_old = c^n
     // B: Y inverse; X inverse c^{n+1} (stored) with f = (lambda/eps^2)(c^3 - c) and its
     //    R2C; Y forward; Z forward f (f_hat^{n+1} stored) + Z inverse of mu_hat, i k c_hat
