@@ -107,10 +107,12 @@ __device__ __forceinline__ void plane_y(cplx<float>* buf, int rows, const cplx<f
 
 // One cluster per z plane (blockIdx.x = z * CS + rank).  Op: the X pass's
 // op (in(f), out(f), point(z, y, n, v, acc)); in(f) / out(f) are the
-// spectral arrays before the Y inverse / after the Y forward.
-template <int NIN, int NOUT, int M, int NY, class Op>
+// spectral arrays before the Y inverse / after the Y forward.  REDUCE: the
+// FP64 sum of each CTA's point accumulator goes to partials[z * CS + rank]
+// (the X pass's block index: plane z, tile of rows `rank`).
+template <int NIN, int NOUT, bool REDUCE, int M, int NY, class Op>
 __global__ void __launch_bounds__(256) k_plane_yx(Geom g, const cplx<float>* __restrict__ twx,
-                                                  const cplx<float>* __restrict__ twy, Op op) {
+                                                  const cplx<float>* __restrict__ twy, Op op, double* partials) {
     using T = float;
     using C = cplx<T>;
     using SH = PlaneShape<M, NY>;
@@ -176,6 +178,10 @@ __global__ void __launch_bounds__(256) k_plane_yx(Geom g, const cplx<float>* __r
         op.point(z, y0 + ty, n, v, acc);
 #pragma unroll
         for (int f = 0; f < NOUT; ++f) s[idx(f * TY + ty, n)] = v[f];
+    }
+    if constexpr (REDUCE) {
+        const double bs = block_sum((double)acc);
+        if (tid == 0) partials[(size_t)z * CS + rank] = bs;
     }
     __syncthreads();
 #pragma unroll
