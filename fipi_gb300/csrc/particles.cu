@@ -1180,21 +1180,12 @@ __global__ void k_spread_fx_store(const unsigned* __restrict__ nodes, int m, siz
                                   float* mag, float* f0, float* f1, float* f2, int* status) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= m) return;
-    // A node appears once per particle that touches it.  Every slot of the
-    // node reads the sums and writes the same grid value and the same zeros
-    // (or, once another slot has zeroed them, reads 0 and writes nothing),
-    // so plain L2 loads and stores give the outcome exchanges would.
     const unsigned nd = nodes[s];
-    if (__ldcg(mag + nd) >= kFxMaxNodeMagnitude) atomicOr(status, ERR_SPREAD_RANGE);
-    __stcg(mag + nd, 0.f);
+    if (atomicExch(mag + nd, 0.f) >= kFxMaxNodeMagnitude) atomicOr(status, ERR_SPREAD_RANGE);
     float* fa[3] = {f0, f1, f2};
     for (int a = 0; a < 3; ++a) {
-        unsigned long long* q = acc + a * V + nd;
-        const unsigned long long v = __ldcg(q);
-        if (v != 0ull) {
-            fa[a][nd] = (float)((double)(long long)v / kFxScale);
-            __stcg(q, 0ull);
-        }
+        const unsigned long long v = atomicExch(acc + a * V + nd, 0ull);
+        if (v != 0ull) fa[a][nd] = (float)((double)(long long)v / kFxScale);
     }
 }
 

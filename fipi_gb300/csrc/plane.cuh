@@ -44,9 +44,12 @@ __device__ __forceinline__ uint32_t cluster_addr(const void* p, unsigned rank) {
     asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(smem_addr(p)), "r"(rank));
     return r;
 }
+// No memory clobber: the loads of a gather are independent and issue back
+// to back; the cluster barriers (which clobber memory) order them against
+// the stores of the other phases.
 __device__ __forceinline__ float2 ld_cluster(uint32_t a) {
     float2 v;
-    asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(a) : "memory");
+    asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(a));
     return v;
 }
 __device__ __forceinline__ void st_cluster(uint32_t a, float2 v) {
@@ -150,13 +153,25 @@ __global__ void __launch_bounds__(256) k_plane_yx(Geom g, const cplx<float>* __r
 
     // B: gather this CTA's y rows (y0 = rank * TY) of every kx, X pass
     const int y0 = (int)rank * TY;
+    // all of a thread's remote loads of a field are issued before any of
+    // their values is stored
+    constexpr int PER = (TY * H + NT - 1) / NT;
 #pragma unroll
     for (int f = 0; f < NIN; ++f) {
         const C* buf = ybuf + (size_t)f * SH::YBUF;
-        for (int e = tid; e < TY * H; e += NT) {
-            const int yl = e % TY, kx = e / TY;
-            const float2 v = ld_cluster(cluster_addr(buf + (kx / CS) * NY + y0 + yl, (unsigned)(kx % CS)));
-            s[idx(f * TY + yl, kx)] = mkc<C>(v.x, v.y);
+        float2 r[PER];
+#pragma unroll
+        for (int k = 0; k < PER; ++k) {
+            const int e = tid + k * NT;
+            if (e < TY * H) {
+                const int yl = e % TY, kx = e / TY;
+                r[k] = ld_cluster(cluster_addr(buf + (kx / CS) * NY + y0 + yl, (unsigned)(kx % CS)));
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < PER; ++k) {
+            const int e = tid + k * NT;
+            if (e < TY * H) s[idx(f * TY + e % TY, e / TY)] = mkc<C>(r[k].x, r[k].y);
         }
     }
     __syncthreads();
