@@ -499,8 +499,6 @@ def run_gpu(args):
 
     # ---- headline: mixed form, inputs resident
     sim = F.Simulation(P, "mixed", device=local)
-    if args.no_plane_fusion:
-        sim.set_debug(F.lib.FIPI_DEBUG_PLANE_FUSION, 0)
     sim.set_phase(c)
     sim.set_particles(p, r, ct)
     sim.step(args.warmup)
@@ -689,8 +687,6 @@ def main():
     ap.add_argument("--adj-steps", type=int, default=5, help="adjoint steps timed (0 = skip)")
     ap.add_argument("--traj-steps", type=int, default=16, help="steps of the checkpointed gradient")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-plane-fusion", action="store_true",
-                    help="run the mixed form's Y and X passes as separate kernels (comparison)")
     ap.add_argument("--grad", default="all", choices=["all", "none", "cfg4_128", "cfg5_256"],
                     help="gradient benchmarks of the adjoint (configs 4 and 5)")
     ap.add_argument("--grad-steps", type=int, default=0, help="steps of the gradient benchmarks (0 = the workload's)")

@@ -766,9 +766,6 @@ fipi_status fipi_set_debug(fipi_ctx* ctx, int what, long long value) {
             if (value < -1 || value > (1 << 22)) return set_error(ctx, FIPI_ERR_BAD_ARG, "polls must be -1 or in [0, 2^22]");
             ctx->debug_first_wait = (int)value;
             break;
-        case FIPI_DEBUG_PLANE_FUSION:
-            ctx->plane_fusion = value ? 1 : 0;
-            break;
         default:
             return set_error(ctx, FIPI_ERR_BAD_ARG, "unknown debug setting");
     }

@@ -210,7 +210,6 @@ struct fipi_ctx {
     int couple_u = 0;          // fluid coupling: uf = u interpolated at the particle
     int conserve_mass = 0;     // the k = 0 mode of u . grad c taken as 0 (exact mass conservation)
     int debug_first_wait = -1; // test hook: polls of each Y-pass block's first copy wait (-1: normal)
-    int plane_fusion = 1;      // cluster-fused Y + X passes where the grid allows (0: separate passes)
     double brown_kt = 0.0;     // Brownian force strength kT (0: off)
     uint64_t noise_seed = 0;   // Philox key of the Brownian force
     bool track_tau = true;     // packing energy during the step (cluster.cpp:256-259)

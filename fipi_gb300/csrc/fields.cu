@@ -19,7 +19,6 @@
 
 #include "ctx.hpp"
 #include "passes.cuh"
-#include "plane.cuh"
 
 
 namespace fipi {
@@ -809,47 +808,6 @@ fipi_status fields_get_velocity(fipi_ctx* ctx, double* u, bool dev) {
 }
 
 // ------------------------------------------------------------ the step
-// One launch of the cluster-fused Y inverse + X pass + Y forward of every z
-// plane (plane.cuh) in place of three passes: FP32 grids of 256 x 256 in
-// x and y, where the device takes clusters of kPlaneCS CTAs (checked once;
-// otherwise the three passes run).  Returns whether it launched.
-template <int NIN, int NOUT, bool REDUCE, class Op>
-static bool launch_plane(fipi_ctx* ctx, const char* name, int nreal, const Op& op, double* partials = nullptr) {
-    const Geom& g = ctx->g;
-    if (ctx->prec != FIPI_MIXED || !ctx->plane_fusion || g.nx != 256 || g.ny != 256) return false;
-    constexpr int M = 128, NY = 256;
-    using SH = PlaneShape<M, NY>;
-    auto kern = k_plane_yx<NIN, NOUT, REDUCE, M, NY, Op>;
-    const size_t smem = SH::smem(NIN);
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = SH::CS;
-    at[0].val.clusterDim.y = 1;
-    at[0].val.clusterDim.z = 1;
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)(g.nz * SH::CS));
-    cfg.blockDim = dim3(SH::NT);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = ctx->stream;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    static int usable = 0;  // 0: not yet checked, 1: yes, -1: no
-    if (usable == 0) {
-        usable = -1;
-        int nc = 0;
-        if (cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess &&
-            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) == cudaSuccess &&
-            cudaOccupancyMaxActiveClusters(&nc, kern, &cfg) == cudaSuccess && nc > 0)
-            usable = 1;
-        cudaGetLastError();
-    }
-    if (usable < 0) return false;
-    LaunchScope ls(ctx, name,
-                   (double)(NIN + NOUT) * g.SH * sizeof(cplx<float>) + (double)nreal * g.V * sizeof(float));
-    cudaLaunchKernelEx(&cfg, kern, g, (const cplx<float>*)ctx->fb.twx, (const cplx<float>*)ctx->fb.twy, op, partials);
-    return true;
-}
-
 template <typename T, bool MIXED> static void step_ch_t(fipi_ctx* ctx, int t) {
     const Geom& g = ctx->g;
     FieldBufs& b = ctx->fb;
@@ -860,23 +818,13 @@ template <typename T, bool MIXED> static void step_ch_t(fipi_ctx* ctx, int t) {
     //    Z forward + CH update + Z inverse of c_hat^{n+1}
     void* up[3] = {b.upre[0], b.upre[1], b.upre[2]};
     void* s3[3] = {b.S[0], b.S[1], b.S[2]};
-    bool fused = false;
-    if constexpr (MIXED) {
-        // one kernel per plane from the velocity state (Z^-1 u_hat) to the Y-forwarded conv
-        OpConv<T, MIXED> ocp{{F<T>::sp(b.upre[0]), F<T>::sp(b.upre[1]), F<T>::sp(b.upre[2])},
-                             {(const T*)b.g[0], (const T*)b.g[1], (const T*)b.g[2]}, F<T>::S(ctx, 3), ctx->partials,
-                             {nullptr, nullptr, nullptr}, g.nx, g.ny};
-        fused = launch_plane<3, 1, true>(ctx, "Y inverse u, X u, conv, Y forward (cluster)", 3, ocp, ctx->partials);
-    }
-    if (!fused) {
-        launch_y<T>(ctx, 3, up, s3, +1);
-        OpConv<T, MIXED> oc{{F<T>::S(ctx, 0), F<T>::S(ctx, 1), F<T>::S(ctx, 2)},
-                            {(const T*)b.g[0], (const T*)b.g[1], (const T*)b.g[2]}, F<T>::S(ctx, 3), ctx->partials,
-                            {(T*)ctx->tape_u[0], (T*)ctx->tape_u[1], (T*)ctx->tape_u[2]}, g.nx, g.ny};
-        launch_xs<T, 3, 1, MIXED>(ctx, "X inverse u, conv, forward", 3, oc, ctx->partials);
-        void* s1[1] = {b.S[3]};
-        launch_y<T>(ctx, 1, s1, s1, -1);
-    }
+    launch_y<T>(ctx, 3, up, s3, +1);
+    OpConv<T, MIXED> oc{{F<T>::S(ctx, 0), F<T>::S(ctx, 1), F<T>::S(ctx, 2)},
+                        {(const T*)b.g[0], (const T*)b.g[1], (const T*)b.g[2]}, F<T>::S(ctx, 3), ctx->partials,
+                        {(T*)ctx->tape_u[0], (T*)ctx->tape_u[1], (T*)ctx->tape_u[2]}, g.nx, g.ny};
+    launch_xs<T, 3, 1, MIXED>(ctx, "X inverse u, conv, forward", 3, oc, ctx->partials);
+    void* s1[1] = {b.S[3]};
+    launch_y<T>(ctx, 1, s1, s1, -1);
     ZOpCH<T, MIXED> zc{F<T>::S(ctx, 3), F<T>::sp(b.chat), F<T>::sp(b.chat_old), F<T>::sp(b.fhat),
                        F<T>::sp(b.fhat_old), F<T>::sp(b.Chat_old), kt, k, t == 0 ? 1 : 0, ctx->conserve_mass};
     ZOpCHRt<T, MIXED> zcr{zc, F<T>::S(ctx, 0), ctx->k0, ctx->partials, (g.ny / x_rows_of(sizeof(T), g.m)) * g.nz,
@@ -889,16 +837,12 @@ template <typename T, bool MIXED> static void step_ch_t(fipi_ctx* ctx, int t) {
     // B: Y inverse; X inverse c^{n+1} (stored) with f = (lambda/eps^2)(c^3 - c) and its
     //    R2C; Y forward; Z forward f (f_hat^{n+1} stored) + Z inverse of mu_hat, i k c_hat
     void* s0[1] = {b.S[0]};
+    launch_y<T>(ctx, 1, s0, s0, +1);
     OpCF<T, MIXED> ocf{F<T>::S(ctx, 0), (T*)b.c, F<T>::S(ctx, 1), reinterpret_cast<const float*>(ctx->k0 + 4),
                        k.lam_eps, g.nx, g.ny};
-    bool fused_cf = false;
-    if constexpr (MIXED) fused_cf = launch_plane<1, 1, false>(ctx, "Y inverse c, X c, f, Y forward (cluster)", 1, ocf);
-    if (!fused_cf) {
-        launch_y<T>(ctx, 1, s0, s0, +1);
-        launch_xs<T, 1, 1, false>(ctx, "X inverse c, f, forward", 1, ocf);
-        void* s1b[1] = {b.S[1]};
-        launch_y<T>(ctx, 1, s1b, s1b, -1);
-    }
+    launch_xs<T, 1, 1, false>(ctx, "X inverse c, f, forward", 1, ocf);
+    void* s1b[1] = {b.S[1]};
+    launch_y<T>(ctx, 1, s1b, s1b, -1);
     ZOpFRt<T> zf{F<T>::S(ctx, 1), F<T>::sp(b.fhat_old), F<T>::sp(b.chat),
                  {F<T>::S(ctx, 0), F<T>::S(ctx, 1), F<T>::S(ctx, 2), F<T>::S(ctx, 3)}, kt, k.lam, g.m, g.ny / 2,
                  g.nz / 2};

@@ -24,7 +24,6 @@ _vp = ctypes.c_void_p
 FIPI_FP64 = 0
 FIPI_MIXED = 1
 FIPI_DEBUG_FFT_FIRST_WAIT_POLLS = 1
-FIPI_DEBUG_PLANE_FUSION = 2
 STATUS = {
     0: "FIPI_OK", 1: "FIPI_ERR_BAD_PARAMS", 2: "FIPI_ERR_BAD_ARG", 3: "FIPI_ERR_CUDA",
     4: "FIPI_ERR_OUT_OF_RANGE", 5: "FIPI_ERR_NONFINITE", 6: "FIPI_ERR_NO_DEVICE",

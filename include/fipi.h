@@ -451,10 +451,6 @@ fipi_status fipi_set_mass_conserving(fipi_ctx* ctx, int on);
  * in flight and returns, so the call reports FIPI_ERR_TIMEOUT and the
  * context stays usable.  Later waits of the block keep the normal bound. */
 #define FIPI_DEBUG_FFT_FIRST_WAIT_POLLS 1
-/* FIPI_DEBUG_PLANE_FUSION: 0 runs the mixed form's Y and X passes as
- * separate kernels where it would otherwise fuse them over a thread-block
- * cluster (1, the default); the results are the same. */
-#define FIPI_DEBUG_PLANE_FUSION 2
 fipi_status fipi_set_debug(fipi_ctx* ctx, int what, long long value);
 
 /* The reference's own initial state for a given seed (host only): srand(seed)

@@ -446,29 +446,3 @@ def test_div_and_interpolate2(fipi, oracle_mod, name, prec):
         assert rel_l2(d, d_ref) < 1e-5
         assert rel_l2(i2, i_ref) < 1e-6
 
-
-def test_plane_fusion_gives_the_same_steps(fipi):
-    """The mixed form's cluster-fused Y inverse + X pass + Y forward (one
-    kernel per z plane over a cluster's distributed shared memory) runs the
-    same transforms as the three separate passes (256 x 256 x 64, the grids
-    it applies to).  The X work runs through shared memory where the
-    separate pass keeps it in registers, and the per-block partial sums of
-    u . grad c add in another order, so the states agree to FP32 rounding
-    rather than bit for bit."""
-    w = fipi.workload("cfg1_64").with_(name="fuse", nx=256, ny=256, lx=256.0, ly=256.0, n_p=600)
-    P, c, p, r, ct = seeded_state(w, 81)
-    out = {}
-    for fused in (1, 0):
-        with fipi.Simulation(P, "mixed") as s:
-            s.set_debug(fipi.lib.FIPI_DEBUG_PLANE_FUSION, fused)
-            s.set_phase(c)
-            s.set_particles(p, r, ct)
-            s.step(4)
-            out[fused] = (s.get_phase(), s.get_velocity(), *s.get_particles())
-    (c1, u1, p1, f1, _), (c0, u0, p0, f0, _) = out[1], out[0]
-    # FP32 rounding of the mixed form (its own bar against FP64 after five
-    # steps is 1e-5 on phi)
-    assert rel_l2(c1, c0) < 5e-6
-    assert rel_l2(u1, u0) < 5e-5
-    assert np.abs(p1 - p0).max() < 1e-8
-    assert rel_l2(f1, f0) < 5e-5
