@@ -55,8 +55,7 @@ struct ParticleBufs {
     unsigned* ids = nullptr;       // n (sorted particle ids)
     unsigned* ids_alt = nullptr;   // n
     int* cell_off = nullptr;       // ncells + 1
-    int* cell_cnt = nullptr;       // ncells (zero between builds)
-    unsigned* cnt_done = nullptr;  // 1: blocks of the counting kernel done (zero between builds)
+    int* cell_cnt = nullptr;       // ncells
     // spreading records (8 per particle)
     unsigned* sp_keys = nullptr;      // 8n node index
     unsigned* sp_keys_alt = nullptr;  // 8n

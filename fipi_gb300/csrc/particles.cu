@@ -40,7 +40,6 @@ constexpr int kPT = 64;
 
 struct PC {
     int n;
-    int ncells;
     int nc[3];
     double dc[3];
     double margin;
@@ -55,7 +54,6 @@ static PC make_pc(const fipi_ctx* ctx) {
     const fipi_params& P = ctx->P;
     PC c;
     c.n = P.n_p;
-    c.ncells = ctx->pb.ncells;
     for (int a = 0; a < 3; ++a) {
         c.nc[a] = ctx->pb.ncell[a];
         c.dc[a] = ctx->pb.dcell[a];
@@ -244,24 +242,18 @@ __global__ void k_cell_offsets(const unsigned* __restrict__ keys, int n, int* of
 // not depend on the order of the atomics.  With `ymax` the same kernels
 // find it_mark of cluster.cpp:128-138 (the first id with the largest
 // p_y > 0; unchanged when there is none).
-// Cell key and arrival slot of particle i at (x, y, z); returns the bits of
-// y for the it_mark search (0 unless y > 0).
-__device__ __forceinline__ unsigned long long cells_count_one(const PC& pc, int i, double x, double y, double z,
-                                                             unsigned* keys, unsigned* slot, int* cnt, int* status) {
-    const unsigned key = cell_key(pc, x, y, z, status);
-    keys[i] = key;
-    slot[i] = (unsigned)atomicAdd(&cnt[key], 1);
-    return (y > 0.0) ? (unsigned long long)__double_as_longlong(y) : 0ull;
-}
-
-// End of a counting kernel; every thread of every block calls it after its
-// count.  The largest y bits go to ymax[0]; then the last block to finish
-// (a ticket taken after a memory fence, so every block's counts are in)
-// turns the counts into offsets off[0..ncells] (exclusive scan) and zeroes
-// the counts and the ticket for the next build.  No block waits for another.
-// For kernels of kPT threads per block.
-__device__ __forceinline__ void cells_count_finish(unsigned long long yb, unsigned long long* ymax, int* cnt,
-                                                   int ncells, int* off, unsigned* done) {
+__global__ void k_cells_count(PC pc, const double* __restrict__ p, unsigned* keys, unsigned* slot, int* cnt,
+                              unsigned long long* ymax, int* status) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = pc.n;
+    unsigned long long yb = 0;
+    if (i < n) {
+        const double y = p[n + i];
+        const unsigned key = cell_key(pc, p[i], y, p[2 * n + i], status);
+        keys[i] = key;
+        slot[i] = (unsigned)atomicAdd(&cnt[key], 1);
+        yb = (y > 0.0) ? (unsigned long long)__double_as_longlong(y) : 0ull;
+    }
     if (ymax) {
         for (int o = 16; o > 0; o >>= 1) {
             const unsigned long long x = __shfl_down_sync(0xffffffffu, yb, o);
@@ -269,22 +261,19 @@ __device__ __forceinline__ void cells_count_finish(unsigned long long yb, unsign
         }
         if ((threadIdx.x & 31) == 0 && yb) atomicMax(&ymax[0], yb);
     }
-    __shared__ int last;
-    __shared__ int part[kPT];
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) last = (atomicAdd(done, 1u) == gridDim.x - 1);
-    __syncthreads();
-    if (!last) return;
-    __threadfence();
-    const int t = threadIdx.x, nt = blockDim.x;
-    const int chunk = (ncells + nt - 1) / nt;
-    const int b = min(ncells, t * chunk), e = min(ncells, b + chunk);
+}
+
+// Exclusive scan of ncells counts into off[0..ncells] (one block).
+__global__ void k_cells_scan(const int* __restrict__ cnt, int ncells, int* off) {
+    __shared__ int part[1024];
+    const int t = threadIdx.x;
+    const int chunk = (ncells + 1023) / 1024;
+    const int b = t * chunk, e = min(ncells, b + chunk);
     int s = 0;
-    for (int i = b; i < e; ++i) s += __ldcg(cnt + i);
+    for (int i = b; i < e; ++i) s += cnt[i];
     part[t] = s;
     __syncthreads();
-    for (int o = 1; o < nt; o <<= 1) {
+    for (int o = 1; o < 1024; o <<= 1) {
         const int v = (t >= o) ? part[t - o] : 0;
         __syncthreads();
         part[t] += v;
@@ -292,25 +281,10 @@ __device__ __forceinline__ void cells_count_finish(unsigned long long yb, unsign
     }
     int run = part[t] - s;
     for (int i = b; i < e; ++i) {
-        const int c = __ldcg(cnt + i);
         off[i] = run;
-        run += c;
-        cnt[i] = 0;
+        run += cnt[i];
     }
-    if (t == nt - 1) {
-        off[ncells] = part[nt - 1];
-        *done = 0u;
-    }
-}
-
-__global__ void __launch_bounds__(kPT) k_cells_count(PC pc, const double* __restrict__ p, unsigned* keys,
-                                                     unsigned* slot, int* cnt, int* off, unsigned* done,
-                                                     unsigned long long* ymax, int* status) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int n = pc.n;
-    unsigned long long yb = 0;
-    if (i < n) yb = cells_count_one(pc, i, p[i], p[n + i], p[2 * n + i], keys, slot, cnt, status);
-    cells_count_finish(yb, ymax, cnt, pc.ncells, off, done);
+    if (t == 1023) off[ncells] = part[1023];
 }
 
 __global__ void k_cells_place(PC pc, const double* __restrict__ p, const unsigned* __restrict__ keys,
@@ -361,22 +335,8 @@ __global__ void k_cells_order(PC pc, const double* __restrict__ p, const int* __
     }
 }
 
-// The second half of the cell list, once the keys, arrival slots and offsets
-// of the particles at p_dev are in (k_cells_count, or a step kernel that
-// counts as it moves the particles): placement and the per-cell id order.
 // Returns true when it also computed it_mark (asked for by `want_it_mark`).
 // With spos the sorted FP32 positions of the mixed-form contact forces too.
-static bool cells_place_order(fipi_ctx* ctx, const double* p_dev, bool want_it_mark, float4* spos) {
-    ParticleBufs& b = ctx->pb;
-    const PC pc = make_pc(ctx);
-    const int nb = (b.n + kPT - 1) / kPT;
-    unsigned long long* ym = want_it_mark ? b.ymax : nullptr;
-    { LaunchScope ls_(ctx, "cell placement", 0.0); k_cells_place<<<nb, kPT, 0, ctx->stream>>>(pc, p_dev, b.keys_alt, b.ids_alt, b.cell_off, b.keys, ym); }
-    { LaunchScope ls_(ctx, "cell order", 0.0); k_cells_order<<<(b.ncells * 32 + 255) / 256, 256, 0, ctx->stream>>>(pc, p_dev, b.cell_off, b.ncells, b.keys, b.ids, b.keys_alt, ym, b.it_mark, spos); }
-    std::swap(b.keys, b.keys_alt);  // sorted keys now in keys
-    return want_it_mark;
-}
-
 static bool build_cells(fipi_ctx* ctx, const double* p_dev, bool want_it_mark = false, float4* spos = nullptr) {
     ParticleBufs& b = ctx->pb;
     const PC pc = make_pc(ctx);
@@ -384,10 +344,14 @@ static bool build_cells(fipi_ctx* ctx, const double* p_dev, bool want_it_mark = 
     if (n <= 0) return false;
     const int nb = (n + kPT - 1) / kPT;
     unsigned long long* ym = want_it_mark ? b.ymax : nullptr;
-    // keys_alt holds the per-particle keys (by id), ids_alt the arrival slots, then the placed ids;
-    // the counts are zero between builds (the scanning block clears them)
-    { LaunchScope ls_(ctx, "cell keys + counts + offsets", 0.0); k_cells_count<<<nb, kPT, 0, ctx->stream>>>(pc, p_dev, b.keys_alt, b.ids_alt, b.cell_cnt, b.cell_off, b.cnt_done, ym, ctx->status); }
-    return cells_place_order(ctx, p_dev, want_it_mark, spos);
+    // keys_alt holds the per-particle keys (by id), ids_alt the arrival slots, then the placed ids
+    cudaMemsetAsync(b.cell_cnt, 0, sizeof(int) * (b.ncells + 1), ctx->stream);
+    { LaunchScope ls_(ctx, "cell keys + counts", 0.0); k_cells_count<<<nb, kPT, 0, ctx->stream>>>(pc, p_dev, b.keys_alt, b.ids_alt, b.cell_cnt, ym, ctx->status); }
+    { LaunchScope ls_(ctx, "cell offsets", 0.0); k_cells_scan<<<1, 1024, 0, ctx->stream>>>(b.cell_cnt, b.ncells, b.cell_off); }
+    { LaunchScope ls_(ctx, "cell placement", 0.0); k_cells_place<<<nb, kPT, 0, ctx->stream>>>(pc, p_dev, b.keys_alt, b.ids_alt, b.cell_off, b.keys, ym); }
+    { LaunchScope ls_(ctx, "cell order", 0.0); k_cells_order<<<(b.ncells * 32 + 255) / 256, 256, 0, ctx->stream>>>(pc, p_dev, b.cell_off, b.ncells, b.keys, b.ids, b.keys_alt, ym, b.it_mark, spos); }
+    std::swap(b.keys, b.keys_alt);  // sorted keys now in keys
+    return want_it_mark;
 }
 
 // ------------------------------------------------------------ contact forces
@@ -886,103 +850,66 @@ __device__ __forceinline__ void ext_load(const PExt& ex, int n, int i, double* u
 
 // Stage part 1: interpolate c, grad c at the stage-start positions and form
 // f_pi (cluster::interpolate_local_variables + compute_f_pi).
-// Cell-list counting carried by the stage kernels (cells_count_one /
-// cells_count_finish): keys and arrival slots by id, counts, offsets.
-struct CellCount {
-    unsigned* keys;
-    unsigned* slot;
-    int* cnt;
-    int* off;
-    unsigned* done;
-    unsigned long long* ymax;  // NULL: no it_mark search
-};
-
-// Stage 1's interpolation of c, grad c and f_pi at p^n, and the counting
-// part of stage 1's cell list at the same positions.
 template <typename TF, typename TA>
-__global__ void __launch_bounds__(kPT) k_stage_fpi(PC pc, const TF* __restrict__ c, const TF* __restrict__ g0,
-                                                   const TF* __restrict__ g1, const TF* __restrict__ g2,
-                                                   const double* __restrict__ p, double* f_pi,
-                                                   const double* __restrict__ r, const double* __restrict__ cth,
-                                                   PExt ex, CellCount cc, int* status) {
+__global__ void k_stage_fpi(PC pc, const TF* __restrict__ c, const TF* __restrict__ g0, const TF* __restrict__ g1,
+                            const TF* __restrict__ g2, const double* __restrict__ p, double* f_pi,
+                            const double* __restrict__ r, const double* __restrict__ cth, PExt ex) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = pc.n;
-    unsigned long long yb = 0;
-    if (i < n) {
-        const double x = p[i], y = p[n + i], z = p[2 * n + i];
-        const TF* fl[4] = {c, g0, g1, g2};
-        TA vals[4];
-        interp_fields<TF, TA>(pc, x, y, z, fl, 4, vals);
-        double fpi[3];
-        f_pi_of(pc, (double)vals[0], (double)vals[1], (double)vals[2], (double)vals[3], r[i], cth[i], fpi);
-        for (int a = 0; a < 3; ++a) f_pi[a * n + i] = fpi[a];
-        stage_ext<TF, TA>(pc, ex, i, x, y, z, r[i], true);
-        yb = cells_count_one(pc, i, x, y, z, cc.keys, cc.slot, cc.cnt, status);
-    }
-    cells_count_finish(yb, cc.ymax, cc.cnt, pc.ncells, cc.off, cc.done);
+    if (i >= n) return;
+    const TF* fl[4] = {c, g0, g1, g2};
+    TA vals[4];
+    interp_fields<TF, TA>(pc, p[i], p[n + i], p[2 * n + i], fl, 4, vals);
+    double fpi[3];
+    f_pi_of(pc, (double)vals[0], (double)vals[1], (double)vals[2], (double)vals[3], r[i], cth[i], fpi);
+    for (int a = 0; a < 3; ++a) f_pi[a * n + i] = fpi[a];
+    stage_ext<TF, TA>(pc, ex, i, p[i], p[n + i], p[2 * n + i], r[i], true);
 }
 
 // Stage 1's advection and wrap followed, for the same particle, by stage 2's
 // interpolation of c, grad c and f_pi at the new position (k_stage_advect
 // with stage = 1, then k_stage_fpi).
-// Stage 1's advection and wrap, then for the new position stage 2's
-// interpolation and f_pi and the counting part of stage 2's cell list.
 template <typename TF, typename TA>
-__global__ void __launch_bounds__(kPT) k_stage_advect1_fpi2(PC pc, double* p, double* p_old, double* u_old,
-                                                            double* f_pi, const double* __restrict__ f_pp,
-                                                            const double* __restrict__ r,
-                                                            const double* __restrict__ cth, const TF* __restrict__ c,
-                                                            const TF* __restrict__ g0, const TF* __restrict__ g1,
-                                                            const TF* __restrict__ g2, int* status, PExt ex,
-                                                            CellCount cc) {
+__global__ void k_stage_advect1_fpi2(PC pc, double* p, double* p_old, double* u_old, double* f_pi,
+                                     const double* __restrict__ f_pp, const double* __restrict__ r,
+                                     const double* __restrict__ cth, const TF* __restrict__ c,
+                                     const TF* __restrict__ g0, const TF* __restrict__ g1,
+                                     const TF* __restrict__ g2, int* status, PExt ex) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = pc.n;
-    unsigned long long yb = 0;
-    if (i < n) {
-        double pp[3] = {p[i], p[n + i], p[2 * n + i]};
-        double po[3], uo[3];
-        const double fpi[3] = {f_pi[i], f_pi[n + i], f_pi[2 * n + i]};
-        const double fpp[3] = {f_pp[i], f_pp[n + i], f_pp[2 * n + i]};
-        double ufv[3], frv[3];
-        const double *puf, *pfr;
-        ext_load(ex, n, i, ufv, frv, puf, pfr);
-        advect_one(pc, 1, fpi, fpp, r[i], pp, po, uo, puf, pfr);
-        for (int a = 0; a < 3; ++a) {
-            p[a * n + i] = pp[a];
-            p_old[a * n + i] = po[a];
-            u_old[a * n + i] = uo[a];
-        }
-        if (!(isfinite(pp[0]) && isfinite(pp[1]) && isfinite(pp[2]))) {
-            atomicOr(status, ERR_NONFINITE);
-        } else {
-            const TF* fl[4] = {c, g0, g1, g2};
-            TA vals[4];
-            interp_fields<TF, TA>(pc, pp[0], pp[1], pp[2], fl, 4, vals);
-            double f2[3];
-            f_pi_of(pc, (double)vals[0], (double)vals[1], (double)vals[2], (double)vals[3], r[i], cth[i], f2);
-            for (int a = 0; a < 3; ++a) f_pi[a * n + i] = f2[a];
-            stage_ext<TF, TA>(pc, ex, i, pp[0], pp[1], pp[2], r[i], false);
-        }
-        yb = cells_count_one(pc, i, pp[0], pp[1], pp[2], cc.keys, cc.slot, cc.cnt, status);
+    if (i >= n) return;
+    double pp[3] = {p[i], p[n + i], p[2 * n + i]};
+    double po[3], uo[3];
+    const double fpi[3] = {f_pi[i], f_pi[n + i], f_pi[2 * n + i]};
+    const double fpp[3] = {f_pp[i], f_pp[n + i], f_pp[2 * n + i]};
+    double ufv[3], frv[3];
+    const double *puf, *pfr;
+    ext_load(ex, n, i, ufv, frv, puf, pfr);
+    advect_one(pc, 1, fpi, fpp, r[i], pp, po, uo, puf, pfr);
+    for (int a = 0; a < 3; ++a) {
+        p[a * n + i] = pp[a];
+        p_old[a * n + i] = po[a];
+        u_old[a * n + i] = uo[a];
     }
-    cells_count_finish(yb, cc.ymax, cc.cnt, pc.ncells, cc.off, cc.done);
+    if (!(isfinite(pp[0]) && isfinite(pp[1]) && isfinite(pp[2]))) {
+        atomicOr(status, ERR_NONFINITE);
+        return;
+    }
+    const TF* fl[4] = {c, g0, g1, g2};
+    TA vals[4];
+    interp_fields<TF, TA>(pc, pp[0], pp[1], pp[2], fl, 4, vals);
+    double f2[3];
+    f_pi_of(pc, (double)vals[0], (double)vals[1], (double)vals[2], (double)vals[3], r[i], cth[i], f2);
+    for (int a = 0; a < 3; ++a) f_pi[a * n + i] = f2[a];
+    stage_ext<TF, TA>(pc, ex, i, pp[0], pp[1], pp[2], r[i], false);
 }
 
 // Stage part 2: advect with this stage's f_pi + f_pp, then wrap.
-// tick (d_t non-NULL): the step's tick of the device step counter and
-// ramp factor (k_step_tick), by the first thread; no kernel of this launch
-// reads them.
 __global__ void k_stage_advect(PC pc, int stage, double* p, double* p_old, double* u_old,
                                const double* __restrict__ f_pi, const double* __restrict__ f_pp,
-                               const double* __restrict__ r, int* status, PExt ex, int* d_t, double* d_rmp,
-                               double thr) {
+                               const double* __restrict__ r, int* status, PExt ex) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = pc.n;
-    if (d_t && i == 0) {
-        const int t = ++(*d_t);
-        const double x = (double)(t + 1);
-        *d_rmp = (x < 0) ? 0.0 : (x < thr ? x / thr : 1.0);
-    }
     if (i >= n) return;
     double pp[3] = {p[i], p[n + i], p[2 * n + i]};
     double po[3] = {p_old[i], p_old[n + i], p_old[2 * n + i]};
@@ -1315,28 +1242,21 @@ template <typename T> static void step_t(fipi_ctx* ctx) {
     // per stage: interpolate_local_variables, sorting, compute_f_pi,
     // compute_f_pp(t+1), compute_f_ext (zero), advect, enforce_bc
     // (main.cpp:198-217); the ramp(t+1, 0.2 t_end) factor is kept on the
-    // device.  The interpolation kernels also count the cell list of the
-    // positions they hold (keys, slots, offsets), stage 1's advection and
-    // stage 2's interpolation run in one kernel, and stage 2's advection
-    // ticks the device step counter.
+    // device (step_tick).  Stage 1's advection and stage 2's interpolation
+    // run in one kernel.
     const PExt ex = particle_ext(ctx);
-    auto counts = [&]() {
-        return CellCount{b.keys_alt, b.ids_alt, b.cell_cnt, b.cell_off, b.cnt_done,
-                         ctx->track_tau ? b.ymax : nullptr};
-    };
-    { LaunchScope ls_(ctx, "stage interpolate + f_pi + cell counts", 0.0); k_stage_fpi<T, T><<<nb, kPT, 0, ctx->stream>>>(pc, c, g0, g1, g2, b.p, b.f_pi, b.r, b.cth, ex, counts(), ctx->status); }
+    { LaunchScope ls_(ctx, "stage interpolate + f_pi", 0.0); k_stage_fpi<T, T><<<nb, kPT, 0, ctx->stream>>>(pc, c, g0, g1, g2, b.p, b.f_pi, b.r, b.cth, ex); }
     for (int stage = 1; stage <= 2; ++stage) {
-        const bool im = cells_place_order(ctx, b.p, ctx->track_tau, spos);
+        const bool im = build_cells(ctx, b.p, ctx->track_tau, spos);
         f_pp_launch<T>(ctx, b.p, ctx->d_rmp, b.f_pi, b.f_pp, ctx->track_tau, im, spos != nullptr);
         if (stage == 1) {
-            LaunchScope ls_(ctx, "stage advect + interpolate + f_pi + cell counts", 0.0);
+            LaunchScope ls_(ctx, "stage advect + interpolate + f_pi", 0.0);
             k_stage_advect1_fpi2<T, T><<<nb, kPT, 0, ctx->stream>>>(pc, b.p, b.p_old, b.u_old, b.f_pi, b.f_pp, b.r,
-                                                                     b.cth, c, g0, g1, g2, ctx->status, ex,
-                                                                     counts());
+                                                                     b.cth, c, g0, g1, g2, ctx->status, ex);
         } else {
-            LaunchScope ls_(ctx, "stage advect + wrap + tick", 0.0);
+            LaunchScope ls_(ctx, "stage advect + wrap", 0.0);
             k_stage_advect<<<nb, kPT, 0, ctx->stream>>>(pc, 2, b.p, b.p_old, b.u_old, b.f_pi, b.f_pp, b.r, ctx->status,
-                                                        ex, ctx->d_t, ctx->d_rmp, 0.2 * ctx->P.t_end);
+                                                        ex);
         }
     }
 }
@@ -1356,9 +1276,7 @@ __global__ void k_step_tick(int* d_t, double* d_rmp, double thr) {
     *d_rmp = (x < 0) ? 0.0 : (x < thr ? x / thr : 1.0);
 }
 
-// The step's tick when particles_step did not run (it ticks in its last kernel).
 void step_tick(fipi_ctx* ctx) {
-    if (ctx->pb.n > 0 && ctx->P.switch_particle) return;
     LaunchScope ls_(ctx, "step tick", 0.0);
     k_step_tick<<<1, 1, 0, ctx->stream>>>(ctx->d_t, ctx->d_rmp, 0.2 * ctx->P.t_end);
 }
@@ -1392,7 +1310,6 @@ fipi_status particles_alloc(fipi_ctx* ctx) {
     FIPI_CUDA(ctx, A((void**)&b.ids_alt, sizeof(unsigned) * n));
     FIPI_CUDA(ctx, A((void**)&b.cell_off, sizeof(int) * (b.ncells + 1)));
     FIPI_CUDA(ctx, A((void**)&b.cell_cnt, sizeof(int) * (b.ncells + 1)));
-    FIPI_CUDA(ctx, A((void**)&b.cnt_done, sizeof(unsigned)));
     FIPI_CUDA(ctx, A((void**)&b.sp_keys, sizeof(unsigned) * 8 * n));
     FIPI_CUDA(ctx, A((void**)&b.sp_keys_alt, sizeof(unsigned) * 8 * n));
     FIPI_CUDA(ctx, A((void**)&b.sp_vals, sizeof(unsigned) * 8 * n));
@@ -1422,7 +1339,7 @@ fipi_status particles_alloc(fipi_ctx* ctx) {
 void particles_free(fipi_ctx* ctx) {
     ParticleBufs& b = ctx->pb;
     void* all[] = {b.p, b.p_old, b.u_old, b.f_pp, b.f_pi, b.r, b.cth, b.keys, b.keys_alt, b.ids, b.ids_alt,
-                   b.cell_off, b.cell_cnt, b.cnt_done, b.sp_keys, b.sp_keys_alt, b.sp_vals, b.sp_vals_alt, b.sp_prev,
+                   b.cell_off, b.cell_cnt, b.sp_keys, b.sp_keys_alt, b.sp_vals, b.sp_vals_alt, b.sp_prev,
                    b.hist, b.tau_part, b.it_mark, b.tau, b.spos, b.sp_fw, b.ymax, b.sp_acc, b.sp_mag, b.uf, b.f_rand};
     for (void* p : all)
         if (p) cudaFree(p);
