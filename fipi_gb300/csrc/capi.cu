@@ -506,8 +506,8 @@ void fipi::enqueue_step(fipi_ctx* ctx) {
     fields_step_ch(ctx, t);      // main.cpp:79-141
     particles_spread(ctx);       // main.cpp:169 (compute_f_r of the previous step's state)
     fields_step_stokes(ctx);     // main.cpp:146-181
-    particles_step(ctx);         // main.cpp:186-219
-    step_tick(ctx);
+    if (!particles_step(ctx))    // main.cpp:186-219
+        step_tick(ctx);
     ctx->t = t + 1;
 }
 
@@ -626,8 +626,8 @@ fipi_status fipi_step_particles(fipi_ctx* ctx) {
     if (!ctx) return set_error(ctx, FIPI_ERR_BAD_ARG, "ctx is NULL");
     if (ctx->substep != 2) return set_error(ctx, FIPI_ERR_STATE, "fipi_step_particles must follow fipi_step_stokes");
     FIPI_CUDA(ctx, cudaSetDevice(ctx->device));
-    particles_step(ctx);        // main.cpp:186-219
-    step_tick(ctx);
+    if (!particles_step(ctx))   // main.cpp:186-219
+        step_tick(ctx);
     ctx->t += 1;
     ctx->substep = 0;
     return check_status(ctx);

@@ -190,7 +190,7 @@ struct fipi_ctx {
     int* status = nullptr;       // device error word
     double* scratch_d = nullptr; // small FP64 device scratch (reductions)
     int t = 0;
-    int* d_t = nullptr;          // device copy of t (advanced by step_tick)
+    int* d_t = nullptr;          // device copy of t (advanced by step_tick or the last advection)
     double* d_rmp = nullptr;     // ramp(t + 1, 0.2 t_end) for the next step
     // CUDA graphs of one step (t >= 1) for each of the two states of the
     // ping-pong buffers; `after` is the host-side buffer state the step leaves
@@ -255,7 +255,9 @@ void particles_free(fipi_ctx* ctx);
 // Spread f_pp at p onto the dense spread grid (enqueue).
 void particles_spread(fipi_ctx* ctx);
 // Two Heun stages (enqueue); the ramp factor is read from ctx->d_rmp.
-void particles_step(fipi_ctx* ctx);
+// Returns true when its last kernel also ended the step (step_tick's
+// update); otherwise the caller enqueues step_tick.
+bool particles_step(fipi_ctx* ctx);
 fipi_status particles_ext_alloc(fipi_ctx* ctx);
 void fields_velocity_real(fipi_ctx* ctx);  // fb.ureal = u (the fluid-coupling extension)
 // t += 1 on the device and the next step's ramp factor.

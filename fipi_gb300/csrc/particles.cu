@@ -30,6 +30,7 @@
 #include <vector>
 
 #include "ctx.hpp"
+#include "fixed_point.cuh"
 
 namespace fipi {
 
@@ -48,6 +49,15 @@ struct PC {
     double dx, dy, dz;
     int N[3];
     double tanh2;  // tanh(2.0), element.cpp:84
+    // Constants of the mixed form's particle arithmetic.  GB300 issues FP64
+    // at about 1/70 of the FP32 rate, so the mixed form multiplies by
+    // reciprocals instead of dividing, forms f_pi in FP32 and converts its
+    // fixed-point sums with integer operations; positions stay FP64.
+    double inv_d[3];   // 1/dx, 1/dy, 1/dz
+    double inv_dc[3];  // 1/d_cell
+    double mdc[3];     // margin/d_cell
+    double drag;       // 6 pi mu: the Stokes drag is drag * r
+    float f_req, f_req2, f_kn, f_dc[3], f_inv_vol, f_tanh2, f_dscale, f_apisig;
 };
 
 static PC make_pc(const fipi_ctx* ctx) {
@@ -78,6 +88,21 @@ static PC make_pc(const fipi_ctx* ctx) {
     c.N[1] = P.ny;
     c.N[2] = P.nz;
     c.tanh2 = std::tanh(2.0);
+    const double d[3] = {c.dx, c.dy, c.dz};
+    for (int a = 0; a < 3; ++a) {
+        c.inv_d[a] = 1.0 / d[a];
+        c.inv_dc[a] = 1.0 / c.dc[a];
+        c.mdc[a] = c.margin / c.dc[a];
+        c.f_dc[a] = (float)c.dc[a];
+    }
+    c.drag = 6.0 * c.pi * c.mu;
+    c.f_req = (float)c.r_eq;
+    c.f_req2 = c.f_req * c.f_req;
+    c.f_kn = (float)c.k_n;
+    c.f_inv_vol = (float)(1.0 / (c.dx * c.dy * c.dz));
+    c.f_tanh2 = (float)c.tanh2;
+    c.f_dscale = (float)(0.5 * 1.4142135623730951 * c.epsilon);
+    c.f_apisig = (float)(c.A * c.pi * c.sigma);
     return c;
 }
 
@@ -198,19 +223,37 @@ __device__ __forceinline__ int cell_coord(double x, double dcell, double margin)
     return (int)floor(x / dcell + margin / dcell);  // cluster.cpp:140-142
 }
 
+// x != 0.0 on the bits (true for NaN, false for -0.0), integer operations only
+__device__ __forceinline__ bool nonzero_bits(double x) {
+    return (__double_as_longlong(x) << 1) != 0;
+}
+
+// isfinite(x) from the exponent bits (integer operations only)
+__device__ __forceinline__ bool finite_bits(double x) {
+    return ((__double_as_longlong(x) >> 52) & 0x7ff) != 0x7ff;
+}
+
 // Cell key of one position (cluster.cpp:140-163); out-of-range or
 // non-finite positions are clamped and reported through the error word.
+// FAST (mixed form): floor(x (1/d_cell) + margin/d_cell), one product
+// instead of two divisions; a position within rounding of a cell face may
+// land in the neighbouring cell, which changes no pair (the cells are
+// wider than r_eq by more than that).
+template <bool FAST = false>
 __device__ __forceinline__ unsigned cell_key(const PC& pc, double x, double y, double z, int* status) {
-    int c[3] = {cell_coord(x, pc.dc[0], pc.margin), cell_coord(y, pc.dc[1], pc.margin),
-                cell_coord(z, pc.dc[2], pc.margin)};
-    bool bad = !(isfinite(x) && isfinite(y) && isfinite(z));
+    const double xs[3] = {x, y, z};
+    int c[3];
+    for (int a = 0; a < 3; ++a)
+        c[a] = FAST ? (int)floor(fma(xs[a], pc.inv_dc[a], pc.mdc[a])) : cell_coord(xs[a], pc.dc[a], pc.margin);
+    const bool fin = finite_bits(x) && finite_bits(y) && finite_bits(z);
+    bool bad = !fin;
     for (int a = 0; a < 3; ++a) {
         if (c[a] < 0 || c[a] >= pc.nc[a]) {
             bad = true;
             c[a] = c[a] < 0 ? 0 : pc.nc[a] - 1;
         }
     }
-    if (bad) atomicOr(status, isfinite(x) && isfinite(y) && isfinite(z) ? ERR_OUT_OF_RANGE : ERR_NONFINITE);
+    if (bad) atomicOr(status, fin ? ERR_OUT_OF_RANGE : ERR_NONFINITE);
     return (unsigned)(c[0] + c[1] * pc.nc[0] + c[2] * pc.nc[0] * pc.nc[1]);
 }
 
@@ -242,6 +285,7 @@ __global__ void k_cell_offsets(const unsigned* __restrict__ keys, int n, int* of
 // not depend on the order of the atomics.  With `ymax` the same kernels
 // find it_mark of cluster.cpp:128-138 (the first id with the largest
 // p_y > 0; unchanged when there is none).
+template <bool FAST>
 __global__ void k_cells_count(PC pc, const double* __restrict__ p, unsigned* keys, unsigned* slot, int* cnt,
                               unsigned long long* ymax, int* status) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -249,10 +293,12 @@ __global__ void k_cells_count(PC pc, const double* __restrict__ p, unsigned* key
     unsigned long long yb = 0;
     if (i < n) {
         const double y = p[n + i];
-        const unsigned key = cell_key(pc, p[i], y, p[2 * n + i], status);
+        const unsigned key = cell_key<FAST>(pc, p[i], y, p[2 * n + i], status);
         keys[i] = key;
         slot[i] = (unsigned)atomicAdd(&cnt[key], 1);
-        yb = (y > 0.0) ? (unsigned long long)__double_as_longlong(y) : 0ull;
+        // y > 0.0 on the bits: positive, at most +inf (NaN and -0.0 excluded)
+        const long long b = __double_as_longlong(y);
+        yb = (b > 0 && b <= 0x7ff0000000000000ll) ? (unsigned long long)b : 0ull;
     }
     if (ymax) {
         for (int o = 16; o > 0; o >>= 1) {
@@ -324,11 +370,11 @@ __global__ void k_cells_order(PC pc, const double* __restrict__ p, const int* __
         for (int j = beg; j < end; ++j) r += tmp[j] < id;
         ids[beg + r] = id;
         skeys[beg + r] = (unsigned)cell;
-        if (spos) {
+        if (spos) {  // mixed form only: one fused multiply-add per axis
             float4 v;
-            v.x = (float)(p[id] - cx * pc.dc[0]);
-            v.y = (float)(p[n + id] - cy * pc.dc[1]);
-            v.z = (float)(p[2 * n + id] - cz * pc.dc[2]);
+            v.x = (float)fma((double)-cx, pc.dc[0], p[id]);
+            v.y = (float)fma((double)-cy, pc.dc[1], p[n + id]);
+            v.z = (float)fma((double)-cz, pc.dc[2], p[2 * n + id]);
             v.w = __int_as_float((int)id);
             spos[beg + r] = v;
         }
@@ -336,8 +382,10 @@ __global__ void k_cells_order(PC pc, const double* __restrict__ p, const int* __
 }
 
 // Returns true when it also computed it_mark (asked for by `want_it_mark`).
-// With spos the sorted FP32 positions of the mixed-form contact forces too.
-static bool build_cells(fipi_ctx* ctx, const double* p_dev, bool want_it_mark = false, float4* spos = nullptr) {
+// With spos the sorted FP32 positions of the mixed-form contact forces too;
+// `fast` takes the mixed form's cell keys (cell_key<true>).
+static bool build_cells(fipi_ctx* ctx, const double* p_dev, bool want_it_mark = false, float4* spos = nullptr,
+                        bool fast = false) {
     ParticleBufs& b = ctx->pb;
     const PC pc = make_pc(ctx);
     const int n = b.n;
@@ -346,7 +394,11 @@ static bool build_cells(fipi_ctx* ctx, const double* p_dev, bool want_it_mark = 
     unsigned long long* ym = want_it_mark ? b.ymax : nullptr;
     // keys_alt holds the per-particle keys (by id), ids_alt the arrival slots, then the placed ids
     cudaMemsetAsync(b.cell_cnt, 0, sizeof(int) * (b.ncells + 1), ctx->stream);
-    { LaunchScope ls_(ctx, "cell keys + counts", 0.0); k_cells_count<<<nb, kPT, 0, ctx->stream>>>(pc, p_dev, b.keys_alt, b.ids_alt, b.cell_cnt, ym, ctx->status); }
+    {
+        LaunchScope ls_(ctx, "cell keys + counts", 0.0);
+        auto kern = fast ? k_cells_count<true> : k_cells_count<false>;
+        kern<<<nb, kPT, 0, ctx->stream>>>(pc, p_dev, b.keys_alt, b.ids_alt, b.cell_cnt, ym, ctx->status);
+    }
     { LaunchScope ls_(ctx, "cell offsets", 0.0); k_cells_scan<<<1, 1024, 0, ctx->stream>>>(b.cell_cnt, b.ncells, b.cell_off); }
     { LaunchScope ls_(ctx, "cell placement", 0.0); k_cells_place<<<nb, kPT, 0, ctx->stream>>>(pc, p_dev, b.keys_alt, b.ids_alt, b.cell_off, b.keys, ym); }
     { LaunchScope ls_(ctx, "cell order", 0.0); k_cells_order<<<(b.ncells * 32 + 255) / 256, 256, 0, ctx->stream>>>(pc, p_dev, b.cell_off, b.ncells, b.keys, b.ids, b.keys_alt, ym, b.it_mark, spos); }
@@ -531,13 +583,16 @@ __global__ void __launch_bounds__(32 * kFppRows) k_f_pp_fast(PC pc, const float4
     const int ci = cell % pc.nc[0], cj = (cell / pc.nc[0]) % pc.nc[1], ck = cell / (pc.nc[0] * pc.nc[1]);
     const int dk = w / 3 - 1, dj = w % 3 - 1;
     const int beg = off[cell], end = off[cell + 1];
-    const float req = (float)pc.r_eq, req2 = req * req, kn = (float)pc.k_n;
-    const float rmp = (float)*rmp_p;
-    const float dcx = (float)pc.dc[0], dcy = (float)pc.dc[1], dcz = (float)pc.dc[2];
+    // FP32 constants from the host; the ramp is converted once per warp
+    const float req = pc.f_req, req2 = pc.f_req2, kn = pc.f_kn;
+    float rmp = 0.f;
+    if (lane == 0) rmp = (float)*rmp_p;
+    rmp = __shfl_sync(0xffffffffu, rmp, 0);
+    const float dcx = pc.f_dc[0], dcy = pc.f_dc[1], dcz = pc.f_dc[2];
     bool mark_ok = false;
     if (f_pi != nullptr) {
         const int m = *it_mark;
-        if (m >= 0) mark_ok = f_pi[m] != 0.0 || f_pi[n + m] != 0.0 || f_pi[2 * n + m] != 0.0;
+        if (m >= 0) mark_ok = nonzero_bits(f_pi[m]) || nonzero_bits(f_pi[n + m]) || nonzero_bits(f_pi[2 * n + m]);
     }
     const int rowbase = (cj + dj + pc.nc[1]) % pc.nc[1] * pc.nc[0] + (ck + dk + pc.nc[2]) % pc.nc[2] * pc.nc[0] * pc.nc[1];
     // L lanes per home particle when the cell holds few (L = 1, 2 or 4): the
@@ -553,7 +608,8 @@ __global__ void __launch_bounds__(32 * kFppRows) k_f_pp_fast(PC pc, const float4
         const float4 h = active ? spos[s] : make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
         const int i = __float_as_int(h.w);
         bool own_ok = false;
-        if (f_pi != nullptr && active) own_ok = f_pi[i] != 0.0 || f_pi[n + i] != 0.0 || f_pi[2 * n + i] != 0.0;
+        if (f_pi != nullptr && active)
+            own_ok = nonzero_bits(f_pi[i]) || nonzero_bits(f_pi[n + i]) || nonzero_bits(f_pi[2 * n + i]);
         float ax = 0.f, ay = 0.f, az = 0.f, tau = 0.f;
         for (int di = -1; di <= 1; ++di) {
             const int co = (ci + di + pc.nc[0]) % pc.nc[0] + rowbase;
@@ -704,6 +760,28 @@ __device__ __forceinline__ void interp_fields(const PC& pc, double x, double y, 
     for (int q = 0; q < nf; ++q) out[q] = interp<TF, TA>(f[q], i, j, k, i1, j1, k1, m, nn, o, pc.N[0], pc.N[1]);
 }
 
+// Node index (wrapped into [0, n)) and FP32 fraction of a coordinate, x (1/dx)
+// split by floor: the mixed form's cell_and_frac / interpolation index.
+__device__ __forceinline__ void node_frac_fast(double x, double inv, int n, int& i, float& fr) {
+    const double q = x * inv;
+    const double fq = floor(q);
+    i = wrapi((int)fq, n);
+    fr = (float)(q - fq);
+}
+
+// Mixed form: interp_fields with the index arithmetic of node_frac_fast.
+template <typename TF>
+__device__ __forceinline__ void interp_fields_fast(const PC& pc, double x, double y, double z, const TF* const* f,
+                                                   int nf, float* out) {
+    int i, j, k;
+    float m, nn, o;
+    node_frac_fast(x, pc.inv_d[0], pc.N[0], i, m);
+    node_frac_fast(y, pc.inv_d[1], pc.N[1], j, nn);
+    node_frac_fast(z, pc.inv_d[2], pc.N[2], k, o);
+    const int i1 = i + 1 == pc.N[0] ? 0 : i + 1, j1 = j + 1 == pc.N[1] ? 0 : j + 1, k1 = k + 1 == pc.N[2] ? 0 : k + 1;
+    for (int q = 0; q < nf; ++q) out[q] = interp<TF, float>(f[q], i, j, k, i1, j1, k1, m, nn, o, pc.N[0], pc.N[1]);
+}
+
 // element::get_f_pi (element.cpp:75-97) with f_mag = -A pi (d - r cos_theta) sigma.
 __device__ __forceinline__ void f_pi_of(const PC& pc, double phi, double gx, double gy, double gz, double r, double ct,
                                         double* f) {
@@ -716,6 +794,25 @@ __device__ __forceinline__ void f_pi_of(const PC& pc, double phi, double gx, dou
         f[0] = gx / gn * f_mag;
         f[1] = gy / gn * f_mag;
         f[2] = gz / gn * f_mag;
+    } else {
+        f[0] = f[1] = f[2] = 0.0;
+    }
+}
+
+// Mixed form: get_f_pi in FP32 from the FP32 interpolated phi and grad phi
+// (d = 0.5 ln((1+phi)/(1-phi)) sqrt(2) eps, f_mag = -A pi sigma (d - r cos_theta)),
+// stored as FP64 for the FP64 advection.
+__device__ __forceinline__ void f_pi_fast(const PC& pc, float phi, float gx, float gy, float gz, double r_d,
+                                          double ct_d, double* f) {
+    const float gn = sqrtf(gx * gx + gy * gy + gz * gz);
+    if (fabsf(phi) <= pc.f_tanh2 && gn != 0.f) {
+        const float r = (float)r_d, ct = (float)ct_d;
+        const float d = logf((1.f + phi) / (1.f - phi)) * pc.f_dscale;
+        const float f_mag = fabsf(d) < r ? -pc.f_apisig * (d - r * ct) : 0.f;
+        const float sc = f_mag / gn;
+        f[0] = (double)(gx * sc);
+        f[1] = (double)(gy * sc);
+        f[2] = (double)(gz * sc);
     } else {
         f[0] = f[1] = f[2] = 0.0;
     }
@@ -786,6 +883,20 @@ struct PExt {
     double kt;
 };
 
+// fmod(x + L, L) (enforce_bc, element.cpp:177-185), bit for bit, without
+// the FP64 remainder loop where x + L lies in [0, 2L): there the result is
+// x + L or (x + L) - L, and the subtraction is exact (Sterbenz: L <= q <= 2L).
+// The range tests compare bit patterns (non-negative doubles order like
+// their bits).
+__device__ __forceinline__ double wrap_exact(double x, double L) {
+    const double q = x + L;
+    const long long qb = __double_as_longlong(q), lb = __double_as_longlong(L);
+    const long long l2b = lb + (1ll << 52);  // 2L: the exponent field plus one (L > 0 and normal)
+    if (qb >= 0 && qb < lb) return q;
+    if (qb >= lb && qb < l2b) return q - L;
+    return fmod(q, L);
+}
+
 // element::advect (element.cpp:156-173) and enforce_bc (element.cpp:177-185)
 // for one particle; f_ext = 0 as in the reference, uf = 0 unless fluid
 // coupling is on, and f_rand only with a Brownian force.
@@ -809,7 +920,32 @@ __device__ __forceinline__ void advect_one(const PC& pc, int stage, const double
         const double hdt = 0.5 * pc.dt;
         for (int a = 0; a < 3; ++a) p[a] = po[a] + (uo[a] + v[a]) * hdt;
     }
-    for (int a = 0; a < 3; ++a) p[a] = fmod(p[a] + pc.L[a], pc.L[a]);
+    for (int a = 0; a < 3; ++a) p[a] = wrap_exact(p[a], pc.L[a]);
+}
+
+// Mixed form: the same update with the drag as one reciprocal,
+// v = F / (6 pi mu r), instead of four divisions per component.
+__device__ __forceinline__ void advect_fast(const PC& pc, int stage, const double* fpi, const double* fpp, double r,
+                                            double* p, double* po, double* uo, const double* uf = nullptr,
+                                            const double* fr = nullptr) {
+    const double mob = 1.0 / (pc.drag * r);
+    double v[3];
+    for (int a = 0; a < 3; ++a) {
+        double F = fpi[a] + fpp[a];
+        if (fr) F = F + fr[a];
+        v[a] = uf ? fma(F, mob, uf[a]) : F * mob;
+    }
+    if (stage == 1) {
+        for (int a = 0; a < 3; ++a) {
+            uo[a] = v[a];
+            po[a] = p[a];
+            p[a] = fma(v[a], pc.dt, p[a]);
+        }
+    } else {
+        const double hdt = 0.5 * pc.dt;
+        for (int a = 0; a < 3; ++a) p[a] = fma(uo[a] + v[a], hdt, po[a]);
+    }
+    for (int a = 0; a < 3; ++a) p[a] = wrap_exact(p[a], pc.L[a]);
 }
 
 // Extension work of a stage for particle i at (x, y, z): uf from the fluid
@@ -859,9 +995,14 @@ __global__ void k_stage_fpi(PC pc, const TF* __restrict__ c, const TF* __restric
     if (i >= n) return;
     const TF* fl[4] = {c, g0, g1, g2};
     TA vals[4];
-    interp_fields<TF, TA>(pc, p[i], p[n + i], p[2 * n + i], fl, 4, vals);
     double fpi[3];
-    f_pi_of(pc, (double)vals[0], (double)vals[1], (double)vals[2], (double)vals[3], r[i], cth[i], fpi);
+    if constexpr (std::is_same<TA, float>::value) {  // mixed form
+        interp_fields_fast<TF>(pc, p[i], p[n + i], p[2 * n + i], fl, 4, vals);
+        f_pi_fast(pc, vals[0], vals[1], vals[2], vals[3], r[i], cth[i], fpi);
+    } else {
+        interp_fields<TF, TA>(pc, p[i], p[n + i], p[2 * n + i], fl, 4, vals);
+        f_pi_of(pc, (double)vals[0], (double)vals[1], (double)vals[2], (double)vals[3], r[i], cth[i], fpi);
+    }
     for (int a = 0; a < 3; ++a) f_pi[a * n + i] = fpi[a];
     stage_ext<TF, TA>(pc, ex, i, p[i], p[n + i], p[2 * n + i], r[i], true);
 }
@@ -885,31 +1026,47 @@ __global__ void k_stage_advect1_fpi2(PC pc, double* p, double* p_old, double* u_
     double ufv[3], frv[3];
     const double *puf, *pfr;
     ext_load(ex, n, i, ufv, frv, puf, pfr);
-    advect_one(pc, 1, fpi, fpp, r[i], pp, po, uo, puf, pfr);
+    constexpr bool FAST = std::is_same<TA, float>::value;  // mixed form
+    if constexpr (FAST) advect_fast(pc, 1, fpi, fpp, r[i], pp, po, uo, puf, pfr);
+    else advect_one(pc, 1, fpi, fpp, r[i], pp, po, uo, puf, pfr);
     for (int a = 0; a < 3; ++a) {
         p[a * n + i] = pp[a];
         p_old[a * n + i] = po[a];
         u_old[a * n + i] = uo[a];
     }
-    if (!(isfinite(pp[0]) && isfinite(pp[1]) && isfinite(pp[2]))) {
+    if (!(finite_bits(pp[0]) && finite_bits(pp[1]) && finite_bits(pp[2]))) {
         atomicOr(status, ERR_NONFINITE);
         return;
     }
     const TF* fl[4] = {c, g0, g1, g2};
     TA vals[4];
-    interp_fields<TF, TA>(pc, pp[0], pp[1], pp[2], fl, 4, vals);
     double f2[3];
-    f_pi_of(pc, (double)vals[0], (double)vals[1], (double)vals[2], (double)vals[3], r[i], cth[i], f2);
+    if constexpr (FAST) {
+        interp_fields_fast<TF>(pc, pp[0], pp[1], pp[2], fl, 4, vals);
+        f_pi_fast(pc, vals[0], vals[1], vals[2], vals[3], r[i], cth[i], f2);
+    } else {
+        interp_fields<TF, TA>(pc, pp[0], pp[1], pp[2], fl, 4, vals);
+        f_pi_of(pc, (double)vals[0], (double)vals[1], (double)vals[2], (double)vals[3], r[i], cth[i], f2);
+    }
     for (int a = 0; a < 3; ++a) f_pi[a * n + i] = f2[a];
     stage_ext<TF, TA>(pc, ex, i, pp[0], pp[1], pp[2], r[i], false);
 }
 
-// Stage part 2: advect with this stage's f_pi + f_pp, then wrap.
+// Stage part 2: advect with this stage's f_pi + f_pp, then wrap (FAST: the
+// mixed form's advect_fast).  With d_t the first thread also ends the step
+// (k_step_tick's update; no thread of this kernel reads d_t or d_rmp).
+template <bool FAST>
 __global__ void k_stage_advect(PC pc, int stage, double* p, double* p_old, double* u_old,
                                const double* __restrict__ f_pi, const double* __restrict__ f_pp,
-                               const double* __restrict__ r, int* status, PExt ex) {
+                               const double* __restrict__ r, int* status, PExt ex, int* d_t, double* d_rmp,
+                               double thr) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = pc.n;
+    if (d_t && i == 0) {
+        const int t = ++(*d_t);
+        const double x = (double)(t + 1);
+        *d_rmp = (x < 0) ? 0.0 : (x < thr ? x / thr : 1.0);
+    }
     if (i >= n) return;
     double pp[3] = {p[i], p[n + i], p[2 * n + i]};
     double po[3] = {p_old[i], p_old[n + i], p_old[2 * n + i]};
@@ -919,13 +1076,14 @@ __global__ void k_stage_advect(PC pc, int stage, double* p, double* p_old, doubl
     double ufv[3], frv[3];
     const double *puf, *pfr;
     ext_load(ex, n, i, ufv, frv, puf, pfr);
-    advect_one(pc, stage, fpi, fpp, r[i], pp, po, uo, puf, pfr);
+    if constexpr (FAST) advect_fast(pc, stage, fpi, fpp, r[i], pp, po, uo, puf, pfr);
+    else advect_one(pc, stage, fpi, fpp, r[i], pp, po, uo, puf, pfr);
     for (int a = 0; a < 3; ++a) {
         p[a * n + i] = pp[a];
         p_old[a * n + i] = po[a];
         u_old[a * n + i] = uo[a];
     }
-    if (!(isfinite(pp[0]) && isfinite(pp[1]) && isfinite(pp[2]))) atomicOr(status, ERR_NONFINITE);
+    if (!(finite_bits(pp[0]) && finite_bits(pp[1]) && finite_bits(pp[2]))) atomicOr(status, ERR_NONFINITE);
 }
 
 // ------------------------------------------------------------ spreading
@@ -1051,7 +1209,6 @@ static void spread_t(fipi_ctx* ctx, const double* p, const double* f_pp, T* cons
 // kernel first zeroes the grids at its particle's previous nodes, and the
 // store kernel takes each node's sum with an exchange against zero, so the
 // first of a node's duplicate slots writes the grid and the others read 0.
-constexpr double kFxScale = 4294967296.0;  // 2^32
 
 // Range of the fixed-point sums: a node's running sums must stay inside the
 // signed 64-bit accumulators, |sum| < 2^31 units.  Each node also sums the
@@ -1063,6 +1220,7 @@ constexpr double kFxScale = 4294967296.0;  // 2^32
 // reported and left out at once.
 constexpr float kFxMaxContribution = 1073741824.0f;   // 2^30
 constexpr float kFxMaxNodeMagnitude = 2.1e9f;         // < 2^31 = 2.147e9
+
 
 __global__ void k_spread_fx(PC pc, const double* __restrict__ p, const double* __restrict__ f_pp, size_t V,
                             unsigned long long* acc, float* mag, unsigned* nodes, int clear_prev, float* f0,
@@ -1077,12 +1235,14 @@ __global__ void k_spread_fx(PC pc, const double* __restrict__ p, const double* _
             f1[nd] = 0.f;
             f2[nd] = 0.f;
         }
+    // the weights' fractions as in cell_and_frac, the force density in FP32
     int ix[3];
-    double fr[3];
-    cell_and_frac(pc, p[i], p[n + i], p[2 * n + i], ix, fr);
+    float o, pp, q;
+    node_frac_fast(p[i], pc.inv_d[0], pc.N[0], ix[0], o);
+    node_frac_fast(p[n + i], pc.inv_d[1], pc.N[1], ix[1], pp);
+    node_frac_fast(p[2 * n + i], pc.inv_d[2], pc.N[2], ix[2], q);
     float f[3];
-    for (int a = 0; a < 3; ++a) f[a] = (float)((f_pp[a * n + i] + 0.0) / pc.dx / pc.dy / pc.dz);
-    const float o = (float)fr[0], pp = (float)fr[1], q = (float)fr[2];
+    for (int a = 0; a < 3; ++a) f[a] = (float)f_pp[a * n + i] * pc.f_inv_vol;
     for (int c = 0; c < 8; ++c) {
         const int x = (ix[0] + c_corner[c][0]) % pc.N[0];
         const int y = (ix[1] + c_corner[c][1]) % pc.N[1];
@@ -1097,7 +1257,7 @@ __global__ void k_spread_fx(PC pc, const double* __restrict__ p, const double* _
                 continue;
             }
             m += fabsf(v);
-            atomicAdd(acc + a * V + node, (unsigned long long)llrint((double)v * kFxScale));
+            atomicAdd(acc + a * V + node, (unsigned long long)fx_units(v));
         }
         if (m != 0.f) atomicAdd(mag + node, m);
     }
@@ -1112,7 +1272,7 @@ __global__ void k_spread_fx_store(const unsigned* __restrict__ nodes, int m, siz
     float* fa[3] = {f0, f1, f2};
     for (int a = 0; a < 3; ++a) {
         const unsigned long long v = atomicExch(acc + a * V + nd, 0ull);
-        if (v != 0ull) fa[a][nd] = (float)((double)(long long)v / kFxScale);
+        if (v != 0ull) fa[a][nd] = fx_to_float((long long)v);
     }
 }
 
@@ -1230,6 +1390,7 @@ fipi_status particles_ext_alloc(fipi_ctx* ctx) {
 }
 
 template <typename T> static void step_t(fipi_ctx* ctx) {
+    constexpr bool FAST = sizeof(T) == sizeof(float);  // mixed form
     ParticleBufs& b = ctx->pb;
     const PC pc = make_pc(ctx);
     const int n = b.n;
@@ -1238,16 +1399,17 @@ template <typename T> static void step_t(fipi_ctx* ctx) {
     const T* g0 = (const T*)ctx->fb.g[0];
     const T* g1 = (const T*)ctx->fb.g[1];
     const T* g2 = (const T*)ctx->fb.g[2];
-    float4* spos = f_pp_fast_path(ctx, sizeof(T) == sizeof(float)) ? b.spos : nullptr;
+    float4* spos = f_pp_fast_path(ctx, FAST) ? b.spos : nullptr;
     // per stage: interpolate_local_variables, sorting, compute_f_pi,
     // compute_f_pp(t+1), compute_f_ext (zero), advect, enforce_bc
     // (main.cpp:198-217); the ramp(t+1, 0.2 t_end) factor is kept on the
-    // device (step_tick).  Stage 1's advection and stage 2's interpolation
-    // run in one kernel.
+    // device: the last advection kernel advances it with t (step_tick's
+    // update).  Stage 1's advection and stage 2's interpolation run in one
+    // kernel.
     const PExt ex = particle_ext(ctx);
     { LaunchScope ls_(ctx, "stage interpolate + f_pi", 0.0); k_stage_fpi<T, T><<<nb, kPT, 0, ctx->stream>>>(pc, c, g0, g1, g2, b.p, b.f_pi, b.r, b.cth, ex); }
     for (int stage = 1; stage <= 2; ++stage) {
-        const bool im = build_cells(ctx, b.p, ctx->track_tau, spos);
+        const bool im = build_cells(ctx, b.p, ctx->track_tau, spos, FAST);
         f_pp_launch<T>(ctx, b.p, ctx->d_rmp, b.f_pi, b.f_pp, ctx->track_tau, im, spos != nullptr);
         if (stage == 1) {
             LaunchScope ls_(ctx, "stage advect + interpolate + f_pi", 0.0);
@@ -1255,17 +1417,19 @@ template <typename T> static void step_t(fipi_ctx* ctx) {
                                                                      b.cth, c, g0, g1, g2, ctx->status, ex);
         } else {
             LaunchScope ls_(ctx, "stage advect + wrap", 0.0);
-            k_stage_advect<<<nb, kPT, 0, ctx->stream>>>(pc, 2, b.p, b.p_old, b.u_old, b.f_pi, b.f_pp, b.r, ctx->status,
-                                                        ex);
+            k_stage_advect<FAST><<<nb, kPT, 0, ctx->stream>>>(pc, 2, b.p, b.p_old, b.u_old, b.f_pi, b.f_pp, b.r,
+                                                              ctx->status, ex, ctx->d_t, ctx->d_rmp,
+                                                              0.2 * ctx->P.t_end);
         }
     }
 }
 
-void particles_step(fipi_ctx* ctx) {
-    if (ctx->pb.n <= 0 || !ctx->P.switch_particle) return;
+bool particles_step(fipi_ctx* ctx) {
+    if (ctx->pb.n <= 0 || !ctx->P.switch_particle) return false;
     if (ctx->couple_u) fields_velocity_real(ctx);  // u^{n+1} at the particles (get_local_u)
     if (ctx->prec == FIPI_MIXED) step_t<float>(ctx);
     else step_t<double>(ctx);
+    return true;
 }
 
 // End of a step: t += 1 and the next step's ramp(t + 1, 0.2 t_end)
@@ -1391,7 +1555,7 @@ static fipi_status read_status(fipi_ctx* ctx) {
 __global__ void k_wrap_many(PC pc, double* p) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= pc.n) return;
-    for (int a = 0; a < 3; ++a) p[3 * i + a] = fmod(p[3 * i + a] + pc.L[a], pc.L[a]);  // element.cpp:177-185
+    for (int a = 0; a < 3; ++a) p[3 * i + a] = wrap_exact(p[3 * i + a], pc.L[a]);  // element.cpp:177-185
 }
 
 fipi_status particles_wrap(fipi_ctx* ctx, double* p_host) {
