@@ -62,8 +62,10 @@ struct ParticleBufs {
     unsigned* sp_vals = nullptr;      // 8n record id = particle*8 + corner
     unsigned* sp_vals_alt = nullptr;  // 8n
     unsigned* sp_prev = nullptr;      // 8n nodes written by the previous spread
-    unsigned long long* sp_acc = nullptr;  // mixed form: 3 x V fixed-point spread accumulators
-    float* sp_mag = nullptr;               // mixed form: V sums of |contribution| (range bound)
+    // mixed form: per node 32 bytes, the three fixed-point spread sums and,
+    // in the low half of the fourth word, the FP32 sum of |contribution|
+    // (the range bound): one 32-byte sector per touched node
+    unsigned long long* sp_acc = nullptr;
     int sp_prev_valid = 0;
     // radix sort scratch
     unsigned* hist = nullptr;  // 256 * max_blocks

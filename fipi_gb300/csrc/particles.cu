@@ -574,15 +574,37 @@ __global__ void __launch_bounds__(32 * kFppRows) k_f_pp_fast(PC pc, const float4
                                                              const double* __restrict__ f_pi,
                                                              const int* __restrict__ it_mark, double* f_pp,
                                                              double* tau_part) {
-    __shared__ float4 stage[kFppRows][32];
-    __shared__ float part[kFppRows][4][32];  // fx, fy, fz, tau per row warp and lane
+    __shared__ float4 stage[kFppRows][3][32];  // per row warp: a chunk of each of its three cells
+    __shared__ float part[kFppRows][4][32];    // fx, fy, fz, tau per row warp and lane
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int cell = blockIdx.x;
-    float4* buf = stage[w];
     const int n = pc.n;
     const int ci = cell % pc.nc[0], cj = (cell / pc.nc[0]) % pc.nc[1], ck = cell / (pc.nc[0] * pc.nc[1]);
     const int dk = w / 3 - 1, dj = w % 3 - 1;
+    const int rowbase = (cj + dj + pc.nc[1]) % pc.nc[1] * pc.nc[0] + (ck + dk + pc.nc[2]) % pc.nc[2] * pc.nc[0] * pc.nc[1];
+    // The home range and the ranges of the row's three cells are loaded
+    // together (lanes 0-2 the starts, 3-5 the ends), then the first 32
+    // candidates of each of the three cells: two dependent loads before the
+    // pair loop instead of two per cell.
+    const int cw = (ci + (lane % 3) - 1 + pc.nc[0]) % pc.nc[0] + rowbase;
+    const int r6 = lane < 6 ? off[cw + (lane >= 3 ? 1 : 0)] : 0;
     const int beg = off[cell], end = off[cell + 1];
+    int qb[3], qe[3], held[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        qb[c] = __shfl_sync(0xffffffffu, r6, c);
+        qe[c] = __shfl_sync(0xffffffffu, r6, c + 3);
+        held[c] = qb[c];  // first candidate of the chunk staged for cell c
+    }
+    {
+        float4 v[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+            if (lane < qe[c] - qb[c]) v[c] = spos[qb[c] + lane];
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+            if (lane < qe[c] - qb[c]) stage[w][c][lane] = v[c];
+    }
     // FP32 constants from the host; the ramp is converted once per warp
     const float req = pc.f_req, req2 = pc.f_req2, kn = pc.f_kn;
     float rmp = 0.f;
@@ -594,7 +616,7 @@ __global__ void __launch_bounds__(32 * kFppRows) k_f_pp_fast(PC pc, const float4
         const int m = *it_mark;
         if (m >= 0) mark_ok = nonzero_bits(f_pi[m]) || nonzero_bits(f_pi[n + m]) || nonzero_bits(f_pi[2 * n + m]);
     }
-    const int rowbase = (cj + dj + pc.nc[1]) % pc.nc[1] * pc.nc[0] + (ck + dk + pc.nc[2]) % pc.nc[2] * pc.nc[0] * pc.nc[1];
+    __syncwarp();
     // L lanes per home particle when the cell holds few (L = 1, 2 or 4): the
     // L lanes take every L-th candidate and their sums meet by shuffles in a
     // fixed order (deterministic)
@@ -611,19 +633,22 @@ __global__ void __launch_bounds__(32 * kFppRows) k_f_pp_fast(PC pc, const float4
         if (f_pi != nullptr && active)
             own_ok = nonzero_bits(f_pi[i]) || nonzero_bits(f_pi[n + i]) || nonzero_bits(f_pi[2 * n + i]);
         float ax = 0.f, ay = 0.f, az = 0.f, tau = 0.f;
-        for (int di = -1; di <= 1; ++di) {
-            const int co = (ci + di + pc.nc[0]) % pc.nc[0] + rowbase;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const int di = c - 1;
             // home particle relative to the neighbour cell's origin (home frame)
             const float hx = h.x - di * dcx, hy = h.y - dj * dcy, hz = h.z - dk * dcz;
-            const int qb = off[co], qe = off[co + 1];
-            for (int q0 = qb; q0 < qe; q0 += 32) {
-                __syncwarp();
-                if (q0 + lane < qe) buf[lane] = spos[q0 + lane];
-                __syncwarp();
-                const int cnt = min(32, qe - q0);
+            for (int q0 = qb[c]; q0 < qe[c]; q0 += 32) {
+                if (q0 != held[c]) {  // a cell of more than 32 particles: stage its next chunk
+                    __syncwarp();
+                    if (q0 + lane < qe[c]) stage[w][c][lane] = spos[q0 + lane];
+                    held[c] = q0;
+                    __syncwarp();
+                }
+                const int cnt = min(32, qe[c] - q0);
                 if (!active) continue;
                 for (int q = sub; q < cnt; q += L) {
-                    const float4 cd = buf[q];
+                    const float4 cd = stage[w][c][q];
                     const int j = __float_as_int(cd.w);
                     float dx = hx - cd.x, dy = hy - cd.y, dz = hz - cd.z;
                     float d2 = dx * dx + dy * dy + dz * dz;
@@ -1222,9 +1247,9 @@ constexpr float kFxMaxContribution = 1073741824.0f;   // 2^30
 constexpr float kFxMaxNodeMagnitude = 2.1e9f;         // < 2^31 = 2.147e9
 
 
-__global__ void k_spread_fx(PC pc, const double* __restrict__ p, const double* __restrict__ f_pp, size_t V,
-                            unsigned long long* acc, float* mag, unsigned* nodes, int clear_prev, float* f0,
-                            float* f1, float* f2, int* status) {
+__global__ void k_spread_fx(PC pc, const double* __restrict__ p, const double* __restrict__ f_pp,
+                            unsigned long long* acc, unsigned* nodes, int clear_prev, float* f0, float* f1,
+                            float* f2, int* status) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = pc.n;
     if (i >= n) return;
@@ -1249,6 +1274,7 @@ __global__ void k_spread_fx(PC pc, const double* __restrict__ p, const double* _
         const int z = (ix[2] + c_corner[c][2]) % pc.N[2];
         const unsigned node = (unsigned)(x + (size_t)y * pc.N[0] + (size_t)z * pc.N[0] * pc.N[1]);
         nodes[8 * i + c] = node;
+        unsigned long long* slot = acc + 4 * (size_t)node;
         float m = 0.f;
         for (int a = 0; a < 3; ++a) {
             const float v = corner_value<float>(f[a], c, o, pp, q);
@@ -1257,21 +1283,22 @@ __global__ void k_spread_fx(PC pc, const double* __restrict__ p, const double* _
                 continue;
             }
             m += fabsf(v);
-            atomicAdd(acc + a * V + node, (unsigned long long)fx_units(v));
+            atomicAdd(slot + a, (unsigned long long)fx_units(v));
         }
-        if (m != 0.f) atomicAdd(mag + node, m);
+        if (m != 0.f) atomicAdd(reinterpret_cast<float*>(slot + 3), m);
     }
 }
 
-__global__ void k_spread_fx_store(const unsigned* __restrict__ nodes, int m, size_t V, unsigned long long* acc,
-                                  float* mag, float* f0, float* f1, float* f2, int* status) {
+__global__ void k_spread_fx_store(const unsigned* __restrict__ nodes, int m, unsigned long long* acc, float* f0,
+                                  float* f1, float* f2, int* status) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= m) return;
     const unsigned nd = nodes[s];
-    if (atomicExch(mag + nd, 0.f) >= kFxMaxNodeMagnitude) atomicOr(status, ERR_SPREAD_RANGE);
+    unsigned long long* slot = acc + 4 * (size_t)nd;
+    if (atomicExch(reinterpret_cast<float*>(slot + 3), 0.f) >= kFxMaxNodeMagnitude) atomicOr(status, ERR_SPREAD_RANGE);
     float* fa[3] = {f0, f1, f2};
     for (int a = 0; a < 3; ++a) {
-        const unsigned long long v = atomicExch(acc + a * V + nd, 0ull);
+        const unsigned long long v = atomicExch(slot + a, 0ull);
         if (v != 0ull) fa[a][nd] = fx_to_float((long long)v);
     }
 }
@@ -1285,16 +1312,15 @@ static void spread_fx(fipi_ctx* ctx) {
     float* f1 = (float*)ctx->fb.fsp[1];
     float* f2 = (float*)ctx->fb.fsp[2];
     if (!b.sp_prev_valid) {
-        cudaMemsetAsync(b.sp_acc, 0, sizeof(unsigned long long) * 3 * V, ctx->stream);
-        cudaMemsetAsync(b.sp_mag, 0, sizeof(float) * V, ctx->stream);
+        cudaMemsetAsync(b.sp_acc, 0, sizeof(unsigned long long) * 4 * V, ctx->stream);
         for (int a = 0; a < 3; ++a) cudaMemsetAsync(ctx->fb.fsp[a], 0, sizeof(float) * V, ctx->stream);
     }
     {
         LaunchScope ls_(ctx, "spread fixed-point atomics", 0.0);
-        k_spread_fx<<<(n + kPT - 1) / kPT, kPT, 0, ctx->stream>>>(pc, b.p, b.f_pp, V, b.sp_acc, b.sp_mag, b.sp_prev,
+        k_spread_fx<<<(n + kPT - 1) / kPT, kPT, 0, ctx->stream>>>(pc, b.p, b.f_pp, b.sp_acc, b.sp_prev,
                                                                   b.sp_prev_valid, f0, f1, f2, ctx->status);
     }
-    { LaunchScope ls_(ctx, "spread store", 0.0); k_spread_fx_store<<<(m + 255) / 256, 256, 0, ctx->stream>>>(b.sp_prev, m, V, b.sp_acc, b.sp_mag, f0, f1, f2,
+    { LaunchScope ls_(ctx, "spread store", 0.0); k_spread_fx_store<<<(m + 255) / 256, 256, 0, ctx->stream>>>(b.sp_prev, m, b.sp_acc, f0, f1, f2,
                                                                                                      ctx->status); }
     b.sp_prev_valid = 1;
 }
@@ -1480,8 +1506,7 @@ fipi_status particles_alloc(fipi_ctx* ctx) {
     FIPI_CUDA(ctx, A((void**)&b.sp_vals_alt, sizeof(unsigned) * 8 * n));
     FIPI_CUDA(ctx, A((void**)&b.sp_prev, sizeof(unsigned) * 8 * n));
     if (ctx->prec == FIPI_MIXED && b.n > 0) {
-        FIPI_CUDA(ctx, A((void**)&b.sp_acc, sizeof(unsigned long long) * 3 * (size_t)P.nx * P.ny * P.nz));
-        FIPI_CUDA(ctx, A((void**)&b.sp_mag, sizeof(float) * (size_t)P.nx * P.ny * P.nz));
+        FIPI_CUDA(ctx, A((void**)&b.sp_acc, sizeof(unsigned long long) * 4 * (size_t)P.nx * P.ny * P.nz));
     }
     b.hist_cap = 256 * ((16 * n + RS_TILE - 1) / RS_TILE + 1);  // up to 16 records per particle (adjoint)
     FIPI_CUDA(ctx, A((void**)&b.hist, sizeof(unsigned) * b.hist_cap));
@@ -1504,7 +1529,7 @@ void particles_free(fipi_ctx* ctx) {
     ParticleBufs& b = ctx->pb;
     void* all[] = {b.p, b.p_old, b.u_old, b.f_pp, b.f_pi, b.r, b.cth, b.keys, b.keys_alt, b.ids, b.ids_alt,
                    b.cell_off, b.cell_cnt, b.sp_keys, b.sp_keys_alt, b.sp_vals, b.sp_vals_alt, b.sp_prev,
-                   b.hist, b.tau_part, b.it_mark, b.tau, b.spos, b.sp_fw, b.ymax, b.sp_acc, b.sp_mag, b.uf, b.f_rand};
+                   b.hist, b.tau_part, b.it_mark, b.tau, b.spos, b.sp_fw, b.ymax, b.sp_acc, b.uf, b.f_rand};
     for (void* p : all)
         if (p) cudaFree(p);
     b = ParticleBufs{};
