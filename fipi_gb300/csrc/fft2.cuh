@@ -164,7 +164,14 @@ template <int N, int EM> struct FftPlan {
 // (row, t); E/R groups per thread.  With IN the stage's inputs are already
 // in v (slot q*R + m holds element g + m N/R, g = t + Tn q); with OUT its
 // outputs stay in v (slot q*R + j holds element (g - k) R + k + j p).
-template <typename T, int R, int DIR, int N, int P, bool IN, bool OUT, int EM, class Idx>
+// Barrier between the reads and the writes of a stage: the whole block, or
+// only the warp when every row is owned by the lanes of one warp (WS).
+template <bool WS> __device__ __forceinline__ void stage_sync() {
+    if constexpr (WS) __syncwarp();
+    else __syncthreads();
+}
+
+template <typename T, int R, int DIR, int N, int P, bool IN, bool OUT, int EM, bool WS, class Idx>
 __device__ __forceinline__ void fft_stage(cplx<T>* s, const Idx& idx, int row, int t, bool act,
                                           const cplx<T>* __restrict__ tw, int ts, cplx<T>* v) {
     using PL = FftPlan<N, EM>;
@@ -179,7 +186,7 @@ __device__ __forceinline__ void fft_stage(cplx<T>* s, const Idx& idx, int row, i
                 for (int m = 0; m < R; ++m) v[q * R + m] = s[idx(row, g + m * NR)];
             }
         }
-        __syncthreads();
+        stage_sync<WS>();
     }
     if (act) {
 #pragma unroll
@@ -199,17 +206,17 @@ __device__ __forceinline__ void fft_stage(cplx<T>* s, const Idx& idx, int row, i
             }
         }
     }
-    if constexpr (!OUT) __syncthreads();
+    if constexpr (!OUT) stage_sync<WS>();
 }
 
-template <typename T, int DIR, int N, int S, int P, bool IN, bool OUT, int EM, class Idx>
+template <typename T, int DIR, int N, int S, int P, bool IN, bool OUT, int EM, bool WS, class Idx>
 __device__ __forceinline__ void fft_stages(cplx<T>* s, const Idx& idx, int row, int t, bool act,
                                            const cplx<T>* __restrict__ tw, int ts, cplx<T>* v) {
     using PL = FftPlan<N, EM>;
     if constexpr (S < PL::NS) {
         constexpr int R = PL::radix(S, DIR);
-        fft_stage<T, R, DIR, N, P, IN && S == 0, OUT && S == PL::NS - 1, EM>(s, idx, row, t, act, tw, ts, v);
-        fft_stages<T, DIR, N, S + 1, P * R, IN, OUT, EM>(s, idx, row, t, act, tw, ts, v);
+        fft_stage<T, R, DIR, N, P, IN && S == 0, OUT && S == PL::NS - 1, EM, WS>(s, idx, row, t, act, tw, ts, v);
+        fft_stages<T, DIR, N, S + 1, P * R, IN, OUT, EM, WS>(s, idx, row, t, act, tw, ts, v);
     }
 }
 
@@ -230,19 +237,23 @@ template <typename T, int DIR, int N, int EM = FftE<T>::value> struct FftIO {
 
 // In-place N-point FFT of one row per participating thread group, held in
 // shared memory through `idx`.  tw[q*ts] = exp(-2 pi i q / N) for q < N.
-// Every thread of the block must call it (it contains block barriers).
+// Every thread of the block must call it (it contains block barriers; with
+// WS only warp barriers, for callers whose rows each lie within one warp,
+// which then synchronise the block themselves where their own thread
+// mapping changes).
 // IN: the first stage's inputs are in v (FftIO::in_elem order) instead of
 // shared memory; OUT: the results stay in v (FftIO::out_elem order).
-template <typename T, int DIR, int N, bool IN = false, bool OUT = false, int EM = FftE<T>::value, class Idx>
+template <typename T, int DIR, int N, bool IN = false, bool OUT = false, int EM = FftE<T>::value, bool WS = false,
+          class Idx>
 __device__ __forceinline__ void smem_fft2(cplx<T>* s, const Idx& idx, int row, int t, bool act,
                                           const cplx<T>* __restrict__ tw, int ts, cplx<T>* v) {
-    fft_stages<T, DIR, N, 0, 1, IN, OUT, EM>(s, idx, row, t, act, tw, ts, v);
+    fft_stages<T, DIR, N, 0, 1, IN, OUT, EM, WS>(s, idx, row, t, act, tw, ts, v);
 }
-template <typename T, int DIR, int N, int EM = FftE<T>::value, class Idx>
+template <typename T, int DIR, int N, int EM = FftE<T>::value, bool WS = false, class Idx>
 __device__ __forceinline__ void smem_fft2(cplx<T>* s, const Idx& idx, int row, int t, bool act,
                                           const cplx<T>* __restrict__ tw, int ts) {
     cplx<T> v[FftPlan<N, EM>::E];
-    fft_stages<T, DIR, N, 0, 1, false, false, EM>(s, idx, row, t, act, tw, ts, v);
+    fft_stages<T, DIR, N, 0, 1, false, false, EM, WS>(s, idx, row, t, act, tw, ts, v);
 }
 
 // Calls f(std::integral_constant<int, n>) for a power of two n in [8, 512].

@@ -243,6 +243,13 @@ __host__ __device__ constexpr int x_rows_of(int elem_bytes, int m) {
 }
 template <typename T, int M> constexpr int x_rows = x_rows_of(sizeof(T), M);
 
+// The FFT rows of an X pass lie within one warp each (Tn = M / E <= 32
+// threads per row, rows of consecutive threads), so the stages between the
+// split processing steps synchronise the warp only; the block synchronises
+// where the thread mapping changes (tile loads, split processing, point
+// loop, tile stores).
+constexpr bool kXWarpSync = true;
+
 // Elements per thread (radix of the register codelets) of the X pass.
 template <typename T, int NIN, int NOUT> constexpr int x_elems = FftE<T>::value;
 
@@ -297,7 +304,8 @@ __global__ void __launch_bounds__(NT, XMinBlocks<T, (NIN > NOUT ? NIN : NOUT), N
                 C* sf = s + (size_t)f * TY * idx.pitch;
                 c2r_pre<T, M, TY, NT>(sf, idx, twx, tid);
                 __syncthreads();
-                for (int r0 = 0; r0 < TY; r0 += rpr) smem_fft2<T, +1, M, EM>(sf, idx, r0 + tid / Tn, tid % Tn, true, twx, 2);
+                for (int r0 = 0; r0 < TY; r0 += rpr)
+                    smem_fft2<T, +1, M, EM, kXWarpSync>(sf, idx, r0 + tid / Tn, tid % Tn, true, twx, 2);
             }
         } else {
             cp_async_wait_all();
@@ -306,9 +314,10 @@ __global__ void __launch_bounds__(NT, XMinBlocks<T, (NIN > NOUT ? NIN : NOUT), N
             __syncthreads();
             for (int r0 = 0; r0 < NIN * TY; r0 += rpr) {
                 const int row = r0 + tid / Tn;
-                smem_fft2<T, +1, M, EM>(s, idx, row, tid % Tn, row < NIN * TY, twx, 2);
+                smem_fft2<T, +1, M, EM, kXWarpSync>(s, idx, row, tid % Tn, row < NIN * TY, twx, 2);
             }
         }
+        if constexpr (kXWarpSync) __syncthreads();  // the point loop walks rows across warps
     }
     const T invV = T(1) / T(g.V);
     T acc = T(0);  // per-thread partial sum in the arithmetic type (FP64 only per block)
@@ -330,8 +339,9 @@ __global__ void __launch_bounds__(NT, XMinBlocks<T, (NIN > NOUT ? NIN : NOUT), N
     if constexpr (NOUT > 0) {
         for (int r0 = 0; r0 < NOUT * TY; r0 += rpr) {
             const int row = r0 + tid / Tn;
-            smem_fft2<T, -1, M, EM>(s, idx, row, tid % Tn, row < NOUT * TY, twx, 2);
+            smem_fft2<T, -1, M, EM, kXWarpSync>(s, idx, row, tid % Tn, row < NOUT * TY, twx, 2);
         }
+        if constexpr (kXWarpSync) __syncthreads();  // the split post-processing walks rows across warps
         r2c_post<T, M, NOUT * TY, NT>(s, idx, twx, tid);
         __syncthreads();
 #pragma unroll
@@ -421,7 +431,7 @@ __global__ void __launch_bounds__(XStreamShape<T, M>::NT,
             }
         }
         C v[E];
-        smem_fft2<T, +1, M, false, true, EM>(s, idx, f * TY + ty, t, true, twx, 2, v);
+        smem_fft2<T, +1, M, false, true, EM, kXWarpSync>(s, idx, f * TY + ty, t, true, twx, 2, v);
         if constexpr (Op::kStaged) {
             cp_async_wait_all();
             __syncthreads();
@@ -433,7 +443,7 @@ __global__ void __launch_bounds__(XStreamShape<T, M>::NT,
             v[i] = op.template take<f>(z, y0 + ty, n, cscale(v[i], invV), in2, st[i], acc);
         }
         constexpr int d = Op::emit_after(f);
-        if constexpr (d >= 0) smem_fft2<T, -1, M, true, false, EM>(s, idx, d * TY + ty, t, true, twx, 2, v);
+        if constexpr (d >= 0) smem_fft2<T, -1, M, true, false, EM, kXWarpSync>(s, idx, d * TY + ty, t, true, twx, 2, v);
         if constexpr (Op::kStaged) __syncthreads();  // the tile is read before the next copy overwrites it
     });
     if constexpr (REDUCE) {
