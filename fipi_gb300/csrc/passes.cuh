@@ -227,6 +227,80 @@ __device__ __forceinline__ void r2c_post(cplx<T>* s, const Idx& idx, const cplx<
     for (int row = tid; row < ROWS; row += NT) pair(row, HM, Wh, Wh);
 }
 
+template <int I, int N, class F> __device__ __forceinline__ void static_for(F&& f) {
+    if constexpr (I < N) {
+        f(std::integral_constant<int, I>{});
+        static_for<I + 1, N>(f);
+    }
+}
+
+// The same split processing for one row by the Tn = M / E threads that
+// transform it (thread t takes k = t + Tn j, j < E/2, and thread 0 also the
+// self-paired k = M/2), so a warp that owns whole rows needs no block
+// barrier around it.  Wt = twx[t]; the other twiddles follow by one
+// rotation each: W_{t + Tn j} = W_t exp(-2 pi i j / (2E)) and
+// W_{M-k} = -conj(W_k).
+// exp(-2 pi i j / (2E)) for j < E/2 (E = 4 or 8): an eighth of a turn or
+// less, from the sixteenth-turn cosines (the product with j = 0 is exact).
+template <typename T, int E> __device__ __forceinline__ cplx<T> xsplit_rot(int j) {
+    static_assert(E == 4 || E == 8, "X-pass split twiddles: E = 4 or 8");
+    const int e = j * (8 / E);
+    const T c = e == 0 ? T(1) : e == 1 ? T(cos16(1)) : e == 2 ? T(cos16(2)) : T(cos16(3));
+    const T sn = e == 0 ? T(0) : e == 1 ? T(cos16(3)) : e == 2 ? T(cos16(2)) : T(cos16(1));
+    return mkc<cplx<T>>(c, -sn);
+}
+template <typename T, int M, int E, class Idx>
+__device__ __forceinline__ void c2r_pre_row(cplx<T>* s, const Idx& idx, int row, int t, cplx<T> Wt) {
+    using C = cplx<T>;
+    constexpr int Tn = M / E, HM = M / 2;
+    auto pair = [&](int k, const C Wk, const C Wm) {
+        const int km = M - k;
+        const C Xk = s[idx(row, k)], Xm = s[idx(row, km)];
+        const C A = cadd(Xk, cconj(Xm)), B = csub(Xk, cconj(Xm));
+        const C A2 = cadd(Xm, cconj(Xk)), B2 = csub(Xm, cconj(Xk));
+        s[idx(row, k)] = cadd(A, cmul_i(cmul(B, cconj(Wk)), +1));
+        if (km != k) s[idx(row, km)] = cadd(A2, cmul_i(cmul(B2, cconj(Wm)), +1));
+    };
+#pragma unroll 1
+    for (int j = 0; j < E / 2; ++j) {
+        const int k = t + Tn * j;
+        const C Wk = cmul(Wt, xsplit_rot<T, E>(j));
+        if (k == 0) {
+            const T a = s[idx(row, 0)].x, c = s[idx(row, M)].x;
+            s[idx(row, 0)] = mkc<C>(a + c, a - c);
+        } else {
+            pair(k, Wk, mkc<C>(-Wk.x, Wk.y));
+        }
+    }
+    if (t == 0) pair(HM, mkc<C>(T(0), T(-1)), mkc<C>(T(0), T(-1)));
+}
+template <typename T, int M, int E, class Idx>
+__device__ __forceinline__ void r2c_post_row(cplx<T>* s, const Idx& idx, int row, int t, cplx<T> Wt) {
+    using C = cplx<T>;
+    constexpr int Tn = M / E, HM = M / 2;
+    auto pair = [&](int k, const C Wk, const C Wm) {
+        const int km = M - k;
+        const C Zk = s[idx(row, k)], Zm = s[idx(row, km)];
+        const C E1 = cadd(Zk, cconj(Zm)), D1 = csub(Zk, cconj(Zm));
+        const C E2 = cadd(Zm, cconj(Zk)), D2 = csub(Zm, cconj(Zk));
+        s[idx(row, k)] = cscale(csub(E1, cmul_i(cmul(Wk, D1), +1)), T(0.5));
+        if (km != k) s[idx(row, km)] = cscale(csub(E2, cmul_i(cmul(Wm, D2), +1)), T(0.5));
+    };
+#pragma unroll 1
+    for (int j = 0; j < E / 2; ++j) {
+        const int k = t + Tn * j;
+        const C Wk = cmul(Wt, xsplit_rot<T, E>(j));
+        if (k == 0) {
+            const C Z0 = s[idx(row, 0)];
+            s[idx(row, 0)] = mkc<C>(Z0.x + Z0.y, T(0));
+            s[idx(row, M)] = mkc<C>(Z0.x - Z0.y, T(0));
+        } else {
+            pair(k, Wk, mkc<C>(-Wk.x, Wk.y));
+        }
+    }
+    if (t == 0) pair(HM, mkc<C>(T(0), T(-1)), mkc<C>(T(0), T(-1)));
+}
+
 // X pass: one block = TY consecutive rows y0..y0+TY-1 of plane z, NIN
 // spectral inputs (transposed runs of TY along y, C2R) and NOUT spectral
 // outputs (R2C, transposed store); point() does the fused real-space work
@@ -278,11 +352,19 @@ __global__ void __launch_bounds__(NT, XMinBlocks<T, (NIN > NOUT ? NIN : NOUT), N
     constexpr int EM = x_elems<T, NIN, NOUT>;
     constexpr int Tn = FftPlan<M, EM>::Tn;
     constexpr int rpr = NT / Tn;  // row FFTs per round
+    // WL: one round covers the TY rows of a field, so every row of every
+    // field belongs to one warp from the split processing through the
+    // point loop; the block synchronises only after each field's tile
+    // load and before the tile stores
+    constexpr bool WL = kXWarpSync && TY * Tn == NT && M >= 32;
     // Loads and stores walk the tile field by field with ty fastest (a
     // run of TY along y per kx): each thread keeps one ty and steps kx.
     constexpr int KS = NT / TY;
     const int tyl = tid % TY, kx0 = tid / TY;
     const size_t gbase = (size_t)z * H * g.ny + y0 + tyl;
+    const int rrow = tid / Tn, rt = tid % Tn;  // WL: the row of a field this thread transforms
+    C Wt{};
+    if constexpr (WL) Wt = twx[rt];
     if constexpr (NIN > 0) {
         // every element of the tile is requested before any is waited for,
         // one cp.async group per field
@@ -294,7 +376,17 @@ __global__ void __launch_bounds__(NT, XMinBlocks<T, (NIN > NOUT ? NIN : NOUT), N
         }
         if constexpr (HasRowPrefetch<Op>::value)
             if (tid == 0) op.prefetch_rows(z, y0, TY);
-        if constexpr (TY % rpr == 0) {
+        if constexpr (WL) {
+#pragma unroll
+            for (int f = 0; f < NIN; ++f) {
+                cp_async_wait_pending(NIN - 1 - f);
+                __syncthreads();
+                C* sf = s + (size_t)f * TY * idx.pitch;
+                c2r_pre_row<T, M, EM>(sf, idx, rrow, rt, Wt);
+                __syncwarp();
+                smem_fft2<T, +1, M, EM, true>(sf, idx, rrow, rt, true, twx, 2);
+            }
+        } else if constexpr (TY % rpr == 0) {
             // FFT rounds align with fields: field f is pre-processed and
             // transformed while the later fields are still in flight
 #pragma unroll
@@ -317,45 +409,56 @@ __global__ void __launch_bounds__(NT, XMinBlocks<T, (NIN > NOUT ? NIN : NOUT), N
                 smem_fft2<T, +1, M, EM, kXWarpSync>(s, idx, row, tid % Tn, row < NIN * TY, twx, 2);
             }
         }
-        if constexpr (kXWarpSync) __syncthreads();  // the point loop walks rows across warps
+        if constexpr (kXWarpSync && !WL) __syncthreads();  // the point loop walks rows across warps
     }
     const T invV = T(1) / T(g.V);
     T acc = T(0);  // per-thread partial sum in the arithmetic type (FP64 only per block)
-    for (int i = tid; i < TY * M; i += NT) {
-        const int n = i % M;
-        const int ty = i / M;
+    auto point = [&](int ty, int n) {
         C v[NF];
 #pragma unroll
         for (int f = 0; f < NIN; ++f) v[f] = cscale(s[idx(f * TY + ty, n)], invV);
         op.point(z, y0 + ty, n, v, acc);
 #pragma unroll
         for (int f = 0; f < NOUT; ++f) s[idx(f * TY + ty, n)] = v[f];
+    };
+    if constexpr (WL) {
+        // the warp's own rows, 32 consecutive x pairs per step (coalesced
+        // global accesses of the point operation)
+        constexpr int RPW = 32 / Tn;
+        const int lane = tid & 31, w = tid >> 5;
+#pragma unroll
+        for (int r = 0; r < RPW; ++r)
+            for (int n = lane; n < M; n += 32) point(w * RPW + r, n);
+    } else {
+        for (int i = tid; i < TY * M; i += NT) point(i / M, i % M);
     }
     if constexpr (REDUCE) {
         const double bs = block_sum((double)acc);
         if (tid == 0) partials[(size_t)blockIdx.y * gridDim.x + blockIdx.x] = bs;
     }
-    __syncthreads();
+    if constexpr (WL) __syncwarp();
+    else __syncthreads();
     if constexpr (NOUT > 0) {
-        for (int r0 = 0; r0 < NOUT * TY; r0 += rpr) {
-            const int row = r0 + tid / Tn;
-            smem_fft2<T, -1, M, EM, kXWarpSync>(s, idx, row, tid % Tn, row < NOUT * TY, twx, 2);
+        if constexpr (WL) {
+#pragma unroll
+            for (int f = 0; f < NOUT; ++f) {
+                smem_fft2<T, -1, M, EM, true>(s, idx, f * TY + rrow, rt, true, twx, 2);
+                r2c_post_row<T, M, EM>(s, idx, f * TY + rrow, rt, Wt);
+            }
+        } else {
+            for (int r0 = 0; r0 < NOUT * TY; r0 += rpr) {
+                const int row = r0 + tid / Tn;
+                smem_fft2<T, -1, M, EM, kXWarpSync>(s, idx, row, tid % Tn, row < NOUT * TY, twx, 2);
+            }
+            if constexpr (kXWarpSync) __syncthreads();  // the split post-processing walks rows across warps
+            r2c_post<T, M, NOUT * TY, NT>(s, idx, twx, tid);
         }
-        if constexpr (kXWarpSync) __syncthreads();  // the split post-processing walks rows across warps
-        r2c_post<T, M, NOUT * TY, NT>(s, idx, twx, tid);
         __syncthreads();
 #pragma unroll
         for (int f = 0; f < NOUT; ++f) {
             C* dst = op.out(f) + gbase;
             for (int kx = kx0; kx < H; kx += KS) dst[(size_t)kx * g.ny] = s[idx(f * TY + tyl, kx)];
         }
-    }
-}
-
-template <int I, int N, class F> __device__ __forceinline__ void static_for(F&& f) {
-    if constexpr (I < N) {
-        f(std::integral_constant<int, I>{});
-        static_for<I + 1, N>(f);
     }
 }
 
@@ -409,6 +512,11 @@ __global__ void __launch_bounds__(XStreamShape<T, M>::NT,
     }
     const int ty = tid / Tn, t = tid % Tn;
     using IO = FftIO<T, +1, M, EM>;
+    // WL: a field's rows are pre-processed, transformed and post-processed
+    // by the warp that owns them (no block barrier in between); rows of 512
+    // points keep the block-wide split processing (the warp-local form
+    // spills there at the three-blocks-per-SM register budget)
+    constexpr bool WL = kXWarpSync && M >= 32 && M <= 128;
     const T invV = T(1) / T(g.V);
     T acc = T(0);
     typename Op::State st[E];
@@ -421,8 +529,13 @@ __global__ void __launch_bounds__(XStreamShape<T, M>::NT,
         C* sf = s + (size_t)f * TY * idx.pitch;
         cp_async_wait_pending(NIN - 1 - f);
         __syncthreads();
-        c2r_pre<T, M, TY, NT>(sf, idx, twx, tid);
-        __syncthreads();
+        if constexpr (WL) {
+            c2r_pre_row<T, M, EM>(sf, idx, ty, t, twx[t]);  // twiddle read at use: no register held across rounds
+            __syncwarp();
+        } else {
+            c2r_pre<T, M, TY, NT>(sf, idx, twx, tid);
+            __syncthreads();
+        }
         if constexpr (Op::kStaged) {
             const C* src = reinterpret_cast<const C*>(op.template staged_src<f>() + ((size_t)z * g.ny + y0) * g.nx);
             for (int e = tid; e < TY * M; e += NT) {
@@ -443,7 +556,10 @@ __global__ void __launch_bounds__(XStreamShape<T, M>::NT,
             v[i] = op.template take<f>(z, y0 + ty, n, cscale(v[i], invV), in2, st[i], acc);
         }
         constexpr int d = Op::emit_after(f);
-        if constexpr (d >= 0) smem_fft2<T, -1, M, true, false, EM, kXWarpSync>(s, idx, d * TY + ty, t, true, twx, 2, v);
+        if constexpr (d >= 0) {
+            smem_fft2<T, -1, M, true, false, EM, kXWarpSync>(s, idx, d * TY + ty, t, true, twx, 2, v);
+            if constexpr (WL) r2c_post_row<T, M, EM>(s, idx, d * TY + ty, t, twx[t]);
+        }
         if constexpr (Op::kStaged) __syncthreads();  // the tile is read before the next copy overwrites it
     });
     if constexpr (REDUCE) {
@@ -451,8 +567,10 @@ __global__ void __launch_bounds__(XStreamShape<T, M>::NT,
         if (tid == 0) partials[(size_t)blockIdx.y * gridDim.x + blockIdx.x] = bs;
     }
     __syncthreads();
-    r2c_post<T, M, NOUT * TY, NT>(s, idx, twx, tid);
-    __syncthreads();
+    if constexpr (!WL) {
+        r2c_post<T, M, NOUT * TY, NT>(s, idx, twx, tid);
+        __syncthreads();
+    }
     const int tyl = tid % TY, kx0 = tid / TY;
     const size_t gbase = (size_t)z * H * g.ny + y0 + tyl;
 #pragma unroll
