@@ -318,6 +318,18 @@ template <typename T, int N, int COLS, int EM = FftE<T>::value> struct ZRtShape 
     static constexpr int RC = COLS * Tn <= kThreads ? COLS : kThreads / Tn;  // columns per FFT round
     static constexpr int THREADS = RC * Tn;
     static constexpr int P = COLS + 1;  // shared-memory pitch of one kz row (odd: fewer bank conflicts)
+    // WZ (FP32, one round of column FFTs of at most a warp each): the
+    // forward transforms and the first stage of each inverse run on columns
+    // owned by single warps; the tile then adds one pad slot per 16 kz rows
+    // so that the strided writes of a column's first stage meet no bank
+    // conflicts
+    static constexpr bool WZ = sizeof(T) == 4 && RC == COLS && Tn <= 32 && FftPlan<N, EM>::NS >= 2;
+    static constexpr int FSTRIDE = N * P + (WZ ? N / 16 : 0);  // complex entries per field tile
+};
+// Z round-trip tile index: mode e of column c, with the WZ pad slots.
+template <bool PAD> struct IdxZ {
+    int cols;
+    __device__ __forceinline__ int operator()(int c, int e) const { return e * cols + c + (PAD ? (e >> 4) : 0); }
 };
 
 // The tile is COLS columns (a 128-byte run of ky per kz for FP32 and FP64)
@@ -336,8 +348,9 @@ __global__ void __launch_bounds__(kThreads) k_zpass_rt(Geom g, const cplx<T>* __
     const int tid = threadIdx.x;
     const size_t zstride = (size_t)g.h * g.ny;
     const size_t base = (size_t)kx * g.ny + ky0;
-    const IdxColumns idx{P};
-    constexpr size_t fstride = (size_t)N * P;
+    constexpr bool WZ = SH::WZ;
+    const IdxZ<WZ> idx{P};
+    constexpr size_t fstride = SH::FSTRIDE;
     op.prologue();
     if constexpr (HasSrc<Op>::value) {
         // one cp.async group per field: the transform of field f starts once
@@ -347,7 +360,7 @@ __global__ void __launch_bounds__(kThreads) k_zpass_rt(Geom g, const cplx<T>* __
             const C* src = op.src(f);
             for (int e = tid; e < ELEMS; e += NT) {
                 const int c = e % COLS, z = e / COLS;
-                cp_async<sizeof(C)>(&s[f * fstride + z * P + c], src + base + c + z * zstride);
+                cp_async<sizeof(C)>(&s[f * fstride + idx(c, z)], src + base + c + z * zstride);
             }
             cp_async_commit();
         }
@@ -357,18 +370,26 @@ __global__ void __launch_bounds__(kThreads) k_zpass_rt(Geom g, const cplx<T>* __
             C v[NF];
             op.load(kx, ky0 + c, z, base + c + z * zstride, v);
 #pragma unroll
-            for (int f = 0; f < NF; ++f) s[f * fstride + z * P + c] = v[f];
+            for (int f = 0; f < NF; ++f) s[f * fstride + idx(c, z)] = v[f];
         }
         __syncthreads();
     }
     const int cl = tid % RC, t = tid / RC;
+    // WZ: the forward transforms (and the first stage of each inverse) run
+    // on columns owned by single warps (wc = tid / Tn), synchronising only
+    // the warp; the mid operation and the inverse's last stage keep the
+    // column-fastest mapping (full 128-byte runs in global memory)
+    using PLZ = FftPlan<N, EM>;
+    const int wc = tid / PLZ::Tn, wt = tid % PLZ::Tn;
 #pragma unroll
     for (int f = 0; f < NF; ++f) {
         if constexpr (HasSrc<Op>::value) {
             cp_async_wait_pending(NF - 1 - f);
             __syncthreads();
         }
-        for (int r = 0; r < COLS; r += RC) smem_fft2<T, DIR, N, EM>(s + f * fstride + r, idx, cl, t, true, twz, 1);
+        if constexpr (WZ) smem_fft2<T, DIR, N, EM, true>(s + f * fstride, idx, wc, wt, true, twz, 1);
+        else
+            for (int r = 0; r < COLS; r += RC) smem_fft2<T, DIR, N, EM>(s + f * fstride + r, idx, cl, t, true, twz, 1);
     }
     __syncthreads();
     if constexpr (HasPre<Op>::value) {
@@ -387,10 +408,10 @@ __global__ void __launch_bounds__(kThreads) k_zpass_rt(Geom g, const cplx<T>* __
                     const int c = e % COLS, z = e / COLS;
                     C vi[NF], vo[NB];
 #pragma unroll
-                    for (int f = 0; f < NF; ++f) vi[f] = s[f * fstride + z * P + c];
+                    for (int f = 0; f < NF; ++f) vi[f] = s[f * fstride + idx(c, z)];
                     op.mid(kx, ky0 + c, z, base + c + z * zstride, vi, vo, p[u]);
 #pragma unroll
-                    for (int b = 0; b < NB; ++b) s[b * fstride + z * P + c] = vo[b];
+                    for (int b = 0; b < NB; ++b) s[b * fstride + idx(c, z)] = vo[b];
                 }
             }
         }
@@ -399,10 +420,10 @@ __global__ void __launch_bounds__(kThreads) k_zpass_rt(Geom g, const cplx<T>* __
             const int c = e % COLS, z = e / COLS;
             C vi[NF], vo[NB];
 #pragma unroll
-            for (int f = 0; f < NF; ++f) vi[f] = s[f * fstride + z * P + c];
+            for (int f = 0; f < NF; ++f) vi[f] = s[f * fstride + idx(c, z)];
             op.mid(kx, ky0 + c, z, base + c + z * zstride, vi, vo);
 #pragma unroll
-            for (int b = 0; b < NB; ++b) s[b * fstride + z * P + c] = vo[b];
+            for (int b = 0; b < NB; ++b) s[b * fstride + idx(c, z)] = vo[b];
         }
     }
     __syncthreads();
@@ -414,7 +435,14 @@ __global__ void __launch_bounds__(kThreads) k_zpass_rt(Geom g, const cplx<T>* __
     for (int b = 0; b < NB; ++b)
         for (int r = 0; r < COLS; r += RC) {
             C v[SH::E];
-            smem_fft2<T, -DIR, N, false, true, EM>(s + b * fstride + r, idx, cl, t, true, twz, 1, v);
+            if constexpr (WZ) {
+                constexpr int R0 = PLZ::radix(0, -DIR);
+                fft_stage<T, R0, -DIR, N, 1, false, false, EM, true>(s + b * fstride, idx, wc, wt, true, twz, 1, v);
+                __syncthreads();
+                fft_stages<T, -DIR, N, 1, R0, false, true, EM, false>(s + b * fstride, idx, cl, t, true, twz, 1, v);
+            } else {
+                smem_fft2<T, -DIR, N, false, true, EM>(s + b * fstride + r, idx, cl, t, true, twz, 1, v);
+            }
 #pragma unroll
             for (int i = 0; i < SH::E; ++i) op.rr_store(b, base + r + cl + (size_t)IO::out_elem(t, i) * zstride, v[i]);
         }

@@ -840,7 +840,7 @@ void launch_zrt(fipi_ctx* ctx, const char* name, int nspec, const Op& op) {
         // columns of 512 modes with three or more fields: half the tile (two blocks per SM)
         constexpr int CW = (N >= 512 && NS >= 3 && COLS > 8) ? COLS / 2 : COLS;
         using SHP = ZRtShape<T, N, CW, EM>;
-        const size_t smem = (size_t)NS * SHP::P * N * sizeof(cplx<T>);
+        const size_t smem = (size_t)NS * SHP::FSTRIDE * sizeof(cplx<T>);
         dim3 grid(g.h, g.ny / CW);
         auto kern = k_zpass_rt<T, NF, NB, DIR, N, CW, Op, EM>;
         static size_t granted = 48 * 1024;
