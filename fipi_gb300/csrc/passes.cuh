@@ -274,31 +274,72 @@ __device__ __forceinline__ void c2r_pre_row(cplx<T>* s, const Idx& idx, int row,
     }
     if (t == 0) pair(HM, mkc<C>(T(0), T(-1)), mkc<C>(T(0), T(-1)));
 }
+// Split processing between the tile and a row's FFT registers, for rows
+// owned by the Tn = M / E lanes of one warp.  Lane t holds the modes
+// k = t + Tn j (j < E): the input set of the inverse transform's first
+// stage and the output set of the forward transform's last stage.
+// Twiddles: W_{t + Tn j} = W_t exp(-2 pi i j / (2E)) from Wt = twx[t].
+template <typename T> __device__ __forceinline__ cplx<T> shfl_c(cplx<T> v, int src) {
+    return mkc<cplx<T>>(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
+}
+// slot of mode t + Tn j in a stage's register order (first stage of radix R:
+// slot = q R + m holds t + Tn q + m M / R)
+template <int E, int R> constexpr int xslot_of_j(int j) {
+    return (j % (E / R)) * R + j / (E / R);
+}
+// C2R pre-processing straight into v (the inverse plan's first-stage
+// order): Z_k = (X_k + conj X_{M-k}) + i conj(W_k) (X_k - conj X_{M-k}),
+// both modes read from the tile (M - k = M for k = 0: the X_M slot); Z_0
+// from the real parts of X_0 and X_M.  Reads the tile only.
 template <typename T, int M, int E, class Idx>
-__device__ __forceinline__ void r2c_post_row(cplx<T>* s, const Idx& idx, int row, int t, cplx<T> Wt) {
+__device__ __forceinline__ void c2r_pre_regs(const cplx<T>* s, const Idx& idx, int row, int t, cplx<T> Wt,
+                                             cplx<T>* v) {
     using C = cplx<T>;
-    constexpr int Tn = M / E, HM = M / 2;
-    auto pair = [&](int k, const C Wk, const C Wm) {
-        const int km = M - k;
-        const C Zk = s[idx(row, k)], Zm = s[idx(row, km)];
-        const C E1 = cadd(Zk, cconj(Zm)), D1 = csub(Zk, cconj(Zm));
-        const C E2 = cadd(Zm, cconj(Zk)), D2 = csub(Zm, cconj(Zk));
-        s[idx(row, k)] = cscale(csub(E1, cmul_i(cmul(Wk, D1), +1)), T(0.5));
-        if (km != k) s[idx(row, km)] = cscale(csub(E2, cmul_i(cmul(Wm, D2), +1)), T(0.5));
-    };
-#pragma unroll 1
-    for (int j = 0; j < E / 2; ++j) {
+    constexpr int Tn = M / E;
+    constexpr int R0 = FftPlan<M, E>::radix(0, +1);
+    static_for<0, E>([&](auto JC) {
+        constexpr int j = decltype(JC)::value;
         const int k = t + Tn * j;
-        const C Wk = cmul(Wt, xsplit_rot<T, E>(j));
-        if (k == 0) {
-            const C Z0 = s[idx(row, 0)];
-            s[idx(row, 0)] = mkc<C>(Z0.x + Z0.y, T(0));
-            s[idx(row, M)] = mkc<C>(Z0.x - Z0.y, T(0));
-        } else {
-            pair(k, Wk, mkc<C>(-Wk.x, Wk.y));
-        }
-    }
-    if (t == 0) pair(HM, mkc<C>(T(0), T(-1)), mkc<C>(T(0), T(-1)));
+        const C xk = s[idx(row, k)], xm = s[idx(row, M - k)];
+        const C Wk = tw16<-1, (8 * j) / E>(Wt);
+        const C A = cadd(xk, cconj(xm)), B = csub(xk, cconj(xm));
+        C z = cadd(A, cmul_i(cmul(B, cconj(Wk)), +1));
+        if constexpr (j == 0)
+            if (t == 0) z = mkc<C>(xk.x + xm.x, xk.x - xm.x);
+        v[xslot_of_j<E, R0>(j)] = z;
+    });
+}
+// R2C post-processing from v (the forward plan's last-stage order) into the
+// tile: X_k = (E - i W_k D) / 2 with E = Z_k + conj Z_{M-k}, D = Z_k - conj
+// Z_{M-k}; X_0 and X_M from Z_0.  The partner mode M - k = (Tn - t) +
+// Tn (E - 1 - j) is held by lane (Tn - t) mod Tn of the same row and arrives
+// by shuffle; lane 0 pairs k = Tn j with its own j' = E - j.  The warp's
+// lanes finish reading the tile (the last FFT stage) before any writes.
+template <typename T, int M, int E, class Idx>
+__device__ __forceinline__ void r2c_post_regs(cplx<T>* s, const Idx& idx, int row, int t, cplx<T> Wt,
+                                              const cplx<T>* v) {
+    using C = cplx<T>;
+    constexpr int Tn = M / E;
+    constexpr int RL = FftPlan<M, E>::radix(FftPlan<M, E>::NS - 1, -1);
+    const int lane = threadIdx.x & 31;
+    const int src = (lane & ~(Tn - 1)) | ((Tn - t) & (Tn - 1));
+    __syncwarp();
+    static_for<0, E>([&](auto JC) {
+        constexpr int j = decltype(JC)::value;
+        const C zk = v[xslot_of_j<E, RL>(j)];
+        C zm = shfl_c<T>(v[xslot_of_j<E, RL>(E - 1 - j)], src);
+        if constexpr (j > 0)
+            if (t == 0) zm = v[xslot_of_j<E, RL>(E - j)];
+        const C Wk = tw16<-1, (8 * j) / E>(Wt);
+        const C Ev = cadd(zk, cconj(zm)), D = csub(zk, cconj(zm));
+        C x = cscale(csub(Ev, cmul_i(cmul(Wk, D), +1)), T(0.5));
+        if constexpr (j == 0)
+            if (t == 0) {
+                x = mkc<C>(zk.x + zk.y, T(0));
+                s[idx(row, M)] = mkc<C>(zk.x - zk.y, T(0));
+            }
+        s[idx(row, t + Tn * j)] = x;
+    });
 }
 
 // X pass: one block = TY consecutive rows y0..y0+TY-1 of plane z, NIN
@@ -382,9 +423,10 @@ __global__ void __launch_bounds__(NT, XMinBlocks<T, (NIN > NOUT ? NIN : NOUT), N
                 cp_async_wait_pending(NIN - 1 - f);
                 __syncthreads();
                 C* sf = s + (size_t)f * TY * idx.pitch;
-                c2r_pre_row<T, M, EM>(sf, idx, rrow, rt, Wt);
-                __syncwarp();
-                smem_fft2<T, +1, M, EM, true>(sf, idx, rrow, rt, true, twx, 2);
+                C v[EM];
+                c2r_pre_regs<T, M, EM>(sf, idx, rrow, rt, Wt, v);
+                __syncwarp();  // the row is read before the first stage writes it
+                smem_fft2<T, +1, M, true, false, EM, true>(sf, idx, rrow, rt, true, twx, 2, v);
             }
         } else if constexpr (TY % rpr == 0) {
             // FFT rounds align with fields: field f is pre-processed and
@@ -442,8 +484,9 @@ __global__ void __launch_bounds__(NT, XMinBlocks<T, (NIN > NOUT ? NIN : NOUT), N
         if constexpr (WL) {
 #pragma unroll
             for (int f = 0; f < NOUT; ++f) {
-                smem_fft2<T, -1, M, EM, true>(s, idx, f * TY + rrow, rt, true, twx, 2);
-                r2c_post_row<T, M, EM>(s, idx, f * TY + rrow, rt, Wt);
+                C v[EM];
+                smem_fft2<T, -1, M, false, true, EM, true>(s, idx, f * TY + rrow, rt, true, twx, 2, v);
+                r2c_post_regs<T, M, EM>(s, idx, f * TY + rrow, rt, Wt, v);
             }
         } else {
             for (int r0 = 0; r0 < NOUT * TY; r0 += rpr) {
@@ -517,6 +560,10 @@ __global__ void __launch_bounds__(XStreamShape<T, M>::NT,
     // points keep the block-wide split processing (the warp-local form
     // spills there at the three-blocks-per-SM register budget)
     constexpr bool WL = kXWarpSync && M >= 32 && M <= 128;
+    // the pre-processing feeds the first FFT stage from registers for a
+    // single input; with three inputs the State kept across rounds leaves no
+    // room for it (it spills), so those rows are pre-processed in the tile
+    constexpr bool PRE_REGS = WL && NIN == 1;
     const T invV = T(1) / T(g.V);
     T acc = T(0);
     typename Op::State st[E];
@@ -529,8 +576,12 @@ __global__ void __launch_bounds__(XStreamShape<T, M>::NT,
         C* sf = s + (size_t)f * TY * idx.pitch;
         cp_async_wait_pending(NIN - 1 - f);
         __syncthreads();
-        if constexpr (WL) {
-            c2r_pre_row<T, M, EM>(sf, idx, ty, t, twx[t]);  // twiddle read at use: no register held across rounds
+        C v[E];
+        if constexpr (PRE_REGS) {
+            c2r_pre_regs<T, M, EM>(sf, idx, ty, t, twx[t], v);  // twiddle read at use: no register held across rounds
+            __syncwarp();  // the row is read before the first stage writes it
+        } else if constexpr (WL) {
+            c2r_pre_row<T, M, EM>(sf, idx, ty, t, twx[t]);
             __syncwarp();
         } else {
             c2r_pre<T, M, TY, NT>(sf, idx, twx, tid);
@@ -543,8 +594,7 @@ __global__ void __launch_bounds__(XStreamShape<T, M>::NT,
                 cp_async<sizeof(C)>(&sr[e], src + (size_t)r * (g.nx / 2) + n);
             }
         }
-        C v[E];
-        smem_fft2<T, +1, M, false, true, EM, kXWarpSync>(s, idx, f * TY + ty, t, true, twx, 2, v);
+        smem_fft2<T, +1, M, PRE_REGS, true, EM, kXWarpSync>(s, idx, f * TY + ty, t, true, twx, 2, v);
         if constexpr (Op::kStaged) {
             cp_async_wait_all();
             __syncthreads();
@@ -557,8 +607,8 @@ __global__ void __launch_bounds__(XStreamShape<T, M>::NT,
         }
         constexpr int d = Op::emit_after(f);
         if constexpr (d >= 0) {
-            smem_fft2<T, -1, M, true, false, EM, kXWarpSync>(s, idx, d * TY + ty, t, true, twx, 2, v);
-            if constexpr (WL) r2c_post_row<T, M, EM>(s, idx, d * TY + ty, t, twx[t]);
+            smem_fft2<T, -1, M, true, WL, EM, kXWarpSync>(s, idx, d * TY + ty, t, true, twx, 2, v);
+            if constexpr (WL) r2c_post_regs<T, M, EM>(s, idx, d * TY + ty, t, twx[t], v);
         }
         if constexpr (Op::kStaged) __syncthreads();  // the tile is read before the next copy overwrites it
     });
