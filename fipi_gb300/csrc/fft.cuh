@@ -586,7 +586,13 @@ __global__ void __launch_bounds__(kThreads, 2) k_zpass_rr(Geom g, const cplx<T>*
     for (int b = 0; b < NB; ++b) {
         C v[E];
 #pragma unroll
-        for (int i = 0; i < E; ++i) v[i] = op.rr_out(b, kx, ky, IOF::out_elem(t, i), st[i]);
+        for (int i = 0; i < E; ++i) {
+            const int z = IOF::out_elem(t, i);
+            // the staged aux value is read again per output instead of being
+            // kept in registers across the inverse transforms
+            if constexpr (HasAux<Op>::value) v[i] = op.rr_out(b, kx, ky, z, st[i], sa[(size_t)z * TZ + c]);
+            else v[i] = op.rr_out(b, kx, ky, z, st[i]);
+        }
         smem_fft2<T, -DIR, N, true, true, EM>(s, idx, c, t, true, twz, 1, v);
 #pragma unroll
         for (int i = 0; i < E; ++i) {

@@ -411,18 +411,18 @@ template <typename T> struct ZOpFRt {
 #pragma unroll
         for (int b = 0; b < 4; ++b) out[b][gi] = v[b];
     }
-    // register round trip (k_zpass_rr): the outputs are formed one at a time
+    // register round trip (k_zpass_rr): the outputs are formed one at a time;
+    // f_hat is kept for output 0 only, c_hat (the staged aux tile) is read
+    // again for each output
     struct State {
-        C f, c;
+        C f;
     };
     __device__ const C* aux() const { return chat; }
-    __device__ void rr_mid(int, int, int, size_t gi, const C* w, C c_hat, State& st) const {
+    __device__ void rr_mid(int, int, int, size_t gi, const C* w, C, State& st) const {
         fhat_out[gi] = w[0];
         st.f = w[0];
-        st.c = c_hat;
     }
-    __device__ C rr_out(int b, int ix, int iy, int iz, const State& st) const {
-        const C c = st.c;
+    __device__ C rr_out(int b, int ix, int iy, int iz, const State& st, C c) const {
         if (b == 0) {
             const T a = kt.k2(ix, iy, iz) * lam;
             return mkc<C>(a * c.x + st.f.x, a * c.y + st.f.y);
