@@ -85,16 +85,25 @@ template <typename T, bool MIXED> struct OpConv {
         v[0] = mkc<C>(s0, s1);
         if (MIXED) acc += s0 + s1;  // per-thread FP32 partial; FP64 from the block sum on
     }
-    // k_xpass_stream: u_f . (grad c)_f accumulated field by field
+    // k_xpass_stream: u_f . (grad c)_f accumulated field by field; the rows
+    // of grad_F c are prefetched into L2 at the start of the block and read
+    // in round F
     struct State {
         C s;
     };
     static constexpr int emit_after(int f) { return f == 2 ? 0 : -1; }
-    // grad_F c arrives through the staged tile of round F
-    static constexpr bool kStaged = true;
-    template <int F> __device__ const T* staged_src() const { return g[F]; }
-    template <int F, class A> __device__ C take(int z, int y, int n, C v, C gg, State& st, A& acc) const {
+    static constexpr bool kStaged = false;
+    template <int F> __device__ const T* staged_src() const { return nullptr; }
+    __device__ void prefetch_rows(int z, int y0, int rows) const {
+        const size_t row = ((size_t)z * ny + y0) * nx;
+        const uint32_t bytes = (uint32_t)((size_t)rows * nx * sizeof(T));
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+            if ((((uintptr_t)(g[d] + row)) | bytes) % 16 == 0) prefetch_l2_bulk(g[d] + row, bytes);
+    }
+    template <int F, class A> __device__ C take(int z, int y, int n, C v, C, State& st, A& acc) const {
         const size_t row = ((size_t)z * ny + y) * nx;
+        const C gg = reinterpret_cast<const C*>(g[F] + row)[n];
         if (tape_u[0]) reinterpret_cast<C*>(tape_u[F] + row)[n] = v;
         if (F == 0) {
             T s0 = T(0), s1 = T(0);

@@ -552,6 +552,8 @@ __global__ void __launch_bounds__(XStreamShape<T, M>::NT,
             for (int kx = kx0; kx < H; kx += NT / TY) cp_async<sizeof(C)>(&s[idx(f * TY + tyl, kx)], src + (size_t)kx * g.ny);
             cp_async_commit();
         }
+        if constexpr (HasRowPrefetch<Op>::value)
+            if (tid == 0) op.prefetch_rows(z, y0, TY);
     }
     const int ty = tid / Tn, t = tid % Tn;
     using IO = FftIO<T, +1, M, EM>;
