@@ -92,8 +92,6 @@ template <typename T, bool MIXED> struct OpConv {
         C s;
     };
     static constexpr int emit_after(int f) { return f == 2 ? 0 : -1; }
-    static constexpr bool kStaged = false;
-    template <int F> __device__ const T* staged_src() const { return nullptr; }
     __device__ void prefetch_rows(int z, int y0, int rows) const {
         const size_t row = ((size_t)z * ny + y0) * nx;
         const uint32_t bytes = (uint32_t)((size_t)rows * nx * sizeof(T));
@@ -101,7 +99,7 @@ template <typename T, bool MIXED> struct OpConv {
         for (int d = 0; d < 3; ++d)
             if ((((uintptr_t)(g[d] + row)) | bytes) % 16 == 0) prefetch_l2_bulk(g[d] + row, bytes);
     }
-    template <int F, class A> __device__ C take(int z, int y, int n, C v, C, State& st, A& acc) const {
+    template <int F, class A> __device__ C take(int z, int y, int n, C v, State& st, A& acc) const {
         const size_t row = ((size_t)z * ny + y) * nx;
         const C gg = reinterpret_cast<const C*>(g[F] + row)[n];
         if (tape_u[0]) reinterpret_cast<C*>(tape_u[F] + row)[n] = v;
@@ -143,9 +141,7 @@ template <typename T, bool MIXED> struct OpCF {
     // k_xpass_stream
     struct State {};
     static constexpr int emit_after(int f) { return f == 0 ? 0 : -1; }
-    static constexpr bool kStaged = false;
-    template <int F> __device__ const T* staged_src() const { return nullptr; }
-    template <int F, class A> __device__ C take(int z, int y, int n, C v, C, State&, A& acc) const {
+    template <int F, class A> __device__ C take(int z, int y, int n, C v, State&, A& acc) const {
         point(z, y, n, &v, acc);
         return v;
     }

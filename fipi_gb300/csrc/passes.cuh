@@ -512,7 +512,8 @@ __global__ void __launch_bounds__(NT, XMinBlocks<T, (NIN > NOUT ? NIN : NOUT), N
 // forward transform starts from the registers, exchanging through the tile
 // of field d (already consumed).  Against k_xpass_acc this drops the point
 // loop's shared-memory round trip and one exchange per field.  The op keeps
-// a State per mode between the rounds.
+// a State per mode between the rounds; real-space rows it reads in take()
+// come from global memory (op.prefetch_rows puts them in L2 at block start).
 template <typename T, int M> struct XStreamShape {
     static constexpr int TY = x_rows<T, M>;
     static constexpr int E = FftPlan<M, FftE<T>::value>::E;
@@ -569,10 +570,6 @@ __global__ void __launch_bounds__(XStreamShape<T, M>::NT,
     const T invV = T(1) / T(g.V);
     T acc = T(0);
     typename Op::State st[E];
-    // a real-space input of each round (op.staged_src<f>()) is copied with
-    // cp.async into a tile behind the spectral tiles while the round's
-    // inverse transform runs
-    C* sr = s + (size_t)NF * TY * xpass_pitch(M);
     static_for<0, NIN>([&](auto FC) {
         constexpr int f = decltype(FC)::value;
         C* sf = s + (size_t)f * TY * idx.pitch;
@@ -589,30 +586,17 @@ __global__ void __launch_bounds__(XStreamShape<T, M>::NT,
             c2r_pre<T, M, TY, NT>(sf, idx, twx, tid);
             __syncthreads();
         }
-        if constexpr (Op::kStaged) {
-            const C* src = reinterpret_cast<const C*>(op.template staged_src<f>() + ((size_t)z * g.ny + y0) * g.nx);
-            for (int e = tid; e < TY * M; e += NT) {
-                const int r = e / M, n = e - r * M;
-                cp_async<sizeof(C)>(&sr[e], src + (size_t)r * (g.nx / 2) + n);
-            }
-        }
         smem_fft2<T, +1, M, PRE_REGS, true, EM, kXWarpSync>(s, idx, f * TY + ty, t, true, twx, 2, v);
-        if constexpr (Op::kStaged) {
-            cp_async_wait_all();
-            __syncthreads();
-        }
 #pragma unroll
         for (int i = 0; i < E; ++i) {
             const int n = IO::out_elem(t, i);
-            const C in2 = Op::kStaged ? sr[ty * M + n] : C{};
-            v[i] = op.template take<f>(z, y0 + ty, n, cscale(v[i], invV), in2, st[i], acc);
+            v[i] = op.template take<f>(z, y0 + ty, n, cscale(v[i], invV), st[i], acc);
         }
         constexpr int d = Op::emit_after(f);
         if constexpr (d >= 0) {
             smem_fft2<T, -1, M, true, WL, EM, kXWarpSync>(s, idx, d * TY + ty, t, true, twx, 2, v);
             if constexpr (WL) r2c_post_regs<T, M, EM>(s, idx, d * TY + ty, t, twx[t], v);
         }
-        if constexpr (Op::kStaged) __syncthreads();  // the tile is read before the next copy overwrites it
     });
     if constexpr (REDUCE) {
         const double bs = block_sum((double)acc);
@@ -778,11 +762,10 @@ void launch_xs(fipi_ctx* ctx, const char* name, int nreal, const Op& op, double*
             const size_t smem = (size_t)NF * TY * xpass_pitch(g.m) * sizeof(cplx<T>);
             dim3 grid(g.ny / TY, g.nz);
             if constexpr (XStreamShape<T, M>::NT <= kThreads) {
-                const size_t smem_s = smem + (Op::kStaged ? (size_t)TY * M * sizeof(cplx<T>) : 0);
                 auto kern = k_xpass_stream<T, NIN, NOUT, REDUCE, M, Op>;
                 static size_t granted = 48 * 1024;
-                ensure_smem(kern, smem_s, granted);
-                kern<<<grid, XStreamShape<T, M>::NT, smem_s, ctx->stream>>>(g, (const cplx<T>*)ctx->fb.twx, op,
+                ensure_smem(kern, smem, granted);
+                kern<<<grid, XStreamShape<T, M>::NT, smem, ctx->stream>>>(g, (const cplx<T>*)ctx->fb.twx, op,
                                                                             partials);
             } else {  // rows of more than 256 points: one round per field would need > 256 threads
                 auto kern = k_xpass_acc<T, NIN, NOUT, REDUCE, M, Op>;
