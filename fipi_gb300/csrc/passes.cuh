@@ -521,9 +521,10 @@ template <typename T, int M> struct XStreamShape {
     static constexpr int NT = TY * Tn;
     // blocks per SM the register budget is set for: three (two in FP64)
     // 256-thread blocks' worth (the State of a mode stays live across
-    // rounds), four for a single field
+    // rounds); a single field five (48 registers) for rows of up to 128
+    // pairs, four for longer rows (which spill at 48)
     template <int NF> static constexpr int minb() {
-        const int b = (sizeof(T) == 4 ? (NF == 1 ? 4 : 3) : 2) * 256 / NT;
+        const int b = (sizeof(T) == 4 ? (NF == 1 ? (M <= 128 ? 5 : 4) : 3) : 2) * 256 / NT;
         return b < 1 ? 1 : (b > 8 ? 8 : b);
     }
 };
