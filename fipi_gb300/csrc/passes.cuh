@@ -150,11 +150,15 @@ template <class Op> struct NoAcc {
 };
 
 // The same access to the real inputs read straight from global memory.
+// The rows are read-only for the whole launch, so they are read through the
+// non-coherent path: the compiler may then issue a later point's loads
+// ahead of an earlier point's global stores (which it would otherwise have
+// to assume alias them).
 template <typename T, int NRF> struct XGlobalRow {
     const T* p[NRF];
     size_t row;  // element offset of the row
     __device__ __forceinline__ cplx<T> get(int f, int n) const {
-        return reinterpret_cast<const cplx<T>*>(p[f] + row)[n];
+        return __ldg(reinterpret_cast<const cplx<T>*>(p[f] + row) + n);
     }
 };
 
@@ -470,7 +474,8 @@ __global__ void __launch_bounds__(NT, XMinBlocks<T, (NIN > NOUT ? NIN : NOUT), N
         const int lane = tid & 31, w = tid >> 5;
 #pragma unroll
         for (int r = 0; r < RPW; ++r)
-            for (int n = lane; n < M; n += 32) point(w * RPW + r, n);
+#pragma unroll
+            for (int n0 = 0; n0 < M; n0 += 32) point(w * RPW + r, n0 + lane);
     } else {
         for (int i = tid; i < TY * M; i += NT) point(i / M, i % M);
     }
