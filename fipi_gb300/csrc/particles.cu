@@ -1247,46 +1247,50 @@ constexpr float kFxMaxContribution = 1073741824.0f;   // 2^30
 constexpr float kFxMaxNodeMagnitude = 2.1e9f;         // < 2^31 = 2.147e9
 
 
+// One thread per (particle, corner), the eight corners of a particle on
+// eight consecutive lanes (its position and force are loaded once per
+// warp): a launch of 8 n threads instead of n keeps every SM busy.  Corner c
+// is (c_corner[c][0..2]) as bit c of 0x1E, 0xD4 and 0xB8, and its weight
+// is the product of corner_value (x factor, then y, then z) with each factor
+// selected instead of switched on, so the lanes do not diverge.
 __global__ void k_spread_fx(PC pc, const double* __restrict__ p, const double* __restrict__ f_pp,
                             unsigned long long* acc, unsigned* nodes, int clear_prev, float* f0, float* f1,
                             float* f2, int* status) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = gid >> 3, c = gid & 7;
     const int n = pc.n;
     if (i >= n) return;
-    if (clear_prev)
-        for (int c = 0; c < 8; ++c) {
-            const unsigned nd = nodes[8 * i + c];
-            f0[nd] = 0.f;
-            f1[nd] = 0.f;
-            f2[nd] = 0.f;
-        }
+    if (clear_prev) {
+        const unsigned nd = nodes[8 * i + c];
+        f0[nd] = 0.f;
+        f1[nd] = 0.f;
+        f2[nd] = 0.f;
+    }
     // the weights' fractions as in cell_and_frac, the force density in FP32
     int ix[3];
     float o, pp, q;
     node_frac_fast(p[i], pc.inv_d[0], pc.N[0], ix[0], o);
     node_frac_fast(p[n + i], pc.inv_d[1], pc.N[1], ix[1], pp);
     node_frac_fast(p[2 * n + i], pc.inv_d[2], pc.N[2], ix[2], q);
-    float f[3];
-    for (int a = 0; a < 3; ++a) f[a] = (float)f_pp[a * n + i] * pc.f_inv_vol;
-    for (int c = 0; c < 8; ++c) {
-        const int x = (ix[0] + c_corner[c][0]) % pc.N[0];
-        const int y = (ix[1] + c_corner[c][1]) % pc.N[1];
-        const int z = (ix[2] + c_corner[c][2]) % pc.N[2];
-        const unsigned node = (unsigned)(x + (size_t)y * pc.N[0] + (size_t)z * pc.N[0] * pc.N[1]);
-        nodes[8 * i + c] = node;
-        unsigned long long* slot = acc + 4 * (size_t)node;
-        float m = 0.f;
-        for (int a = 0; a < 3; ++a) {
-            const float v = corner_value<float>(f[a], c, o, pp, q);
-            if (!(fabsf(v) < kFxMaxContribution)) {  // also NaN
-                atomicOr(status, ERR_SPREAD_RANGE);
-                continue;
-            }
-            m += fabsf(v);
-            atomicAdd(slot + a, (unsigned long long)fx_units(v));
+    const int cx = (0x1E >> c) & 1, cy = (0xD4 >> c) & 1, cz = (0xB8 >> c) & 1;
+    const int x = (ix[0] + cx) % pc.N[0];
+    const int y = (ix[1] + cy) % pc.N[1];
+    const int z = (ix[2] + cz) % pc.N[2];
+    const unsigned node = (unsigned)(x + (size_t)y * pc.N[0] + (size_t)z * pc.N[0] * pc.N[1]);
+    nodes[8 * i + c] = node;
+    const float wx = cx ? o : 1.f - o, wy = cy ? pp : 1.f - pp, wz = cz ? q : 1.f - q;
+    unsigned long long* slot = acc + 4 * (size_t)node;
+    float m = 0.f;
+    for (int a = 0; a < 3; ++a) {
+        const float v = (((float)f_pp[a * n + i] * pc.f_inv_vol) * wx * wy) * wz;
+        if (!(fabsf(v) < kFxMaxContribution)) {  // also NaN
+            atomicOr(status, ERR_SPREAD_RANGE);
+            continue;
         }
-        if (m != 0.f) atomicAdd(reinterpret_cast<float*>(slot + 3), m);
+        m += fabsf(v);
+        atomicAdd(slot + a, (unsigned long long)fx_units(v));
     }
+    if (m != 0.f) atomicAdd(reinterpret_cast<float*>(slot + 3), m);
 }
 
 __global__ void k_spread_fx_store(const unsigned* __restrict__ nodes, int m, unsigned long long* acc, float* f0,
@@ -1317,8 +1321,8 @@ static void spread_fx(fipi_ctx* ctx) {
     }
     {
         LaunchScope ls_(ctx, "spread fixed-point atomics", 0.0);
-        k_spread_fx<<<(n + kPT - 1) / kPT, kPT, 0, ctx->stream>>>(pc, b.p, b.f_pp, b.sp_acc, b.sp_prev,
-                                                                  b.sp_prev_valid, f0, f1, f2, ctx->status);
+        k_spread_fx<<<(m + 255) / 256, 256, 0, ctx->stream>>>(pc, b.p, b.f_pp, b.sp_acc, b.sp_prev, b.sp_prev_valid,
+                                                              f0, f1, f2, ctx->status);
     }
     { LaunchScope ls_(ctx, "spread store", 0.0); k_spread_fx_store<<<(m + 255) / 256, 256, 0, ctx->stream>>>(b.sp_prev, m, b.sp_acc, f0, f1, f2,
                                                                                                      ctx->status); }
