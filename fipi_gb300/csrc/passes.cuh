@@ -238,12 +238,6 @@ template <int I, int N, class F> __device__ __forceinline__ void static_for(F&& 
     }
 }
 
-// The same split processing for one row by the Tn = M / E threads that
-// transform it (thread t takes k = t + Tn j, j < E/2, and thread 0 also the
-// self-paired k = M/2), so a warp that owns whole rows needs no block
-// barrier around it.  Wt = twx[t]; the other twiddles follow by one
-// rotation each: W_{t + Tn j} = W_t exp(-2 pi i j / (2E)) and
-// W_{M-k} = -conj(W_k).
 // exp(-2 pi i j / (2E)) for j < E/2 (E = 4 or 8): an eighth of a turn or
 // less, from the sixteenth-turn cosines (the product with j = 0 is exact).
 template <typename T, int E> __device__ __forceinline__ cplx<T> xsplit_rot(int j) {
@@ -253,6 +247,14 @@ template <typename T, int E> __device__ __forceinline__ cplx<T> xsplit_rot(int j
     const T sn = e == 0 ? T(0) : e == 1 ? T(cos16(3)) : e == 2 ? T(cos16(2)) : T(cos16(1));
     return mkc<cplx<T>>(c, -sn);
 }
+// The C2R split pre-processing of c2r_pre for one row by the Tn = M / E
+// threads that transform it, in place in the tile (thread t takes the pairs
+// k = t + Tn j, j < E/2, and thread 0 also the self-paired k = M/2), so a
+// warp that owns whole rows needs no block barrier around it; used where
+// the register form below does not fit the register budget (the streamed
+// pass with three inputs).  Wt = twx[t]; the other twiddles follow by one
+// rotation each: W_{t + Tn j} = W_t exp(-2 pi i j / (2E)) and
+// W_{M-k} = -conj(W_k).
 template <typename T, int M, int E, class Idx>
 __device__ __forceinline__ void c2r_pre_row(cplx<T>* s, const Idx& idx, int row, int t, cplx<T> Wt) {
     using C = cplx<T>;
